@@ -1,0 +1,622 @@
+"""CPU oracle for the Puffin hot path (TEST INFRASTRUCTURE ONLY).
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline
+leg may import this module, and only as the checker: the GPU library never
+calls it.  It restates the reference's algorithm on the CPU:
+
+* the RK4 particle/field push (``puffin_oracle.c``, reached through ctypes);
+* the diffraction step in numpy (``diffract``), following
+  puffin/lib/diffraction/diffraction.f90:111-523, masks.f90:50-430 and
+  transforms.f90:472-590, with numpy's FFT standing in for FFTW (unnormalised
+  forward -1 / backward +1 transforms, as FFTW's are);
+* host helpers that the reference performs between kernels: the inner
+  transverse window (``get_in_node``, para_field.f90:1432-1508), the
+  inner/outer copies (para_field.f90:1352-1429) and the split-step schedule of
+  ``UndSection`` (undulator.f90:106-331).
+
+Parity status: the 1D RK4 path is pinned against the reference's golden dump
+(tests/golden/).  The 3D gather/deposit, b-field and diffraction paths have no
+golden vectors in the reference and are a restatement only (parity unpinned for
+those rows).
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+import subprocess
+from dataclasses import dataclass, field
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libpuffin_oracle.so")
+
+# puffin/lib/common/puffin_constants.f90:22 declares pi with a default-kind
+# (single precision) literal; every use of the global pi sees this value.
+PUFFIN_PI = float(np.float32(3.14159265358979323846))
+
+UND_PUFFIN, UND_HELICAL, UND_PLANEPOLE, UND_CURVED = 0, 1, 2, 3
+MESH_TEMPORAL, MESH_PERIODIC = 0, 1
+UND_NAMES = {"": UND_PUFFIN, "puffin": UND_PUFFIN, "helical": UND_HELICAL,
+             "planepole": UND_PLANEPOLE, "curved": UND_CURVED}
+
+
+class _Params(ctypes.Structure):
+    _fields_ = [
+        ("rho", ctypes.c_double), ("eta", ctypes.c_double),
+        ("kappa", ctypes.c_double), ("aw", ctypes.c_double),
+        ("gamma_r", ctypes.c_double),
+        ("fx", ctypes.c_double), ("fy", ctypes.c_double),
+        ("kx_und", ctypes.c_double), ("ky_und", ctypes.c_double),
+        ("kbxsf", ctypes.c_double), ("kbysf", ctypes.c_double),
+        ("und_type", ctypes.c_int), ("one_d", ctypes.c_int),
+        ("focusing", ctypes.c_int), ("und_ends", ctypes.c_int),
+        ("field_evolve", ctypes.c_int), ("electrons_evolve", ctypes.c_int),
+        ("coupling", ctypes.c_int),
+        ("szfs", ctypes.c_double), ("szfe", ctypes.c_double),
+        ("mesh_type", ctypes.c_int),
+        ("nz2", ctypes.c_int64), ("nix", ctypes.c_int64), ("niy", ctypes.c_int64),
+        ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz2", ctypes.c_double),
+    ]
+
+
+class _Taper(ctypes.Structure):
+    _fields_ = [("n2col", ctypes.c_double), ("n2col0", ctypes.c_double),
+                ("undgrad", ctypes.c_double)]
+
+
+class _Stage(ctypes.Structure):
+    _fields_ = [("sz", ctypes.c_double), ("n2col", ctypes.c_double),
+                ("place", ctypes.c_int)]
+
+
+_lib = None
+
+
+def build():
+    """Compile the C restatement with its committed Makefile."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        dp = ctypes.POINTER(ctypes.c_double)
+        L.or_rk4_step.argtypes = [ctypes.POINTER(_Params), ctypes.POINTER(_Taper),
+                                  ctypes.c_double, ctypes.c_double, ctypes.c_int64,
+                                  dp, dp, dp, dp, dp, dp, dp, dp, dp]
+        L.or_rk4_step.restype = ctypes.c_int
+        L.or_rhs.argtypes = [ctypes.POINTER(_Params), ctypes.POINTER(_Stage),
+                             ctypes.c_int64, dp, dp, dp, dp, dp, dp, dp, dp, dp,
+                             dp, dp, dp, dp, dp, dp, dp, dp]
+        L.or_rhs.restype = ctypes.c_int
+        L.or_stage_setup.argtypes = [ctypes.POINTER(_Params), ctypes.POINTER(_Taper),
+                                     ctypes.c_double, ctypes.POINTER(_Stage)]
+        L.or_p2.argtypes = [ctypes.c_double] * 6
+        L.or_p2.restype = ctypes.c_double
+        L.or_wrap_z2.argtypes = [ctypes.POINTER(_Params), ctypes.c_int64, dp]
+        L.or_set_threads.argtypes = [ctypes.c_int]
+        L.or_bfield.argtypes = [ctypes.POINTER(_Params), ctypes.POINTER(_Stage),
+                                ctypes.c_double, ctypes.c_double, dp, dp, dp]
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def set_threads(n: int):
+    lib().or_set_threads(int(n))
+
+
+# ---------------------------------------------------------------------------
+# Configuration (scaled units), mirroring the reference's global state.
+# ---------------------------------------------------------------------------
+@dataclass
+class Config:
+    rho: float
+    aw: float                 # peak undulator parameter (saw_G)
+    gamma_r: float
+    eta: float
+    kappa: float
+    nx: int
+    ny: int
+    nz2: int
+    dx: float
+    dy: float
+    dz2: float
+    mesh_type: int = MESH_TEMPORAL
+    und_type: int = UND_HELICAL
+    fx: float = 1.0
+    fy: float = 1.0
+    kx_und: float = 0.0
+    ky_und: float = 0.0
+    kbxsf: float = 0.0
+    kbysf: float = 0.0
+    focusing: bool = False
+    und_ends: bool = False
+    one_d: bool = False
+    field_evolve: bool = True
+    electrons_evolve: bool = True
+    coupling: bool = True
+    szfs: float = 0.0
+    szfe: float = 1.0e30
+    n2col0: float = 1.0
+    undgrad: float = 0.0
+    # diffraction
+    sbeta: float = 1.0
+    sfilt_frac: float = 0.3
+    qfilter: bool = True
+    sperwaves: float = -1.0
+    nbx: int = 16
+    nby: int = 16
+    nbz2: int = 37
+    nix: int = 0
+    niy: int = 0
+
+    @property
+    def nplanes(self):
+        return self.nz2 - 1 if self.mesh_type == MESH_PERIODIC else self.nz2
+
+    def cparams(self, nix=None, niy=None):
+        p = _Params()
+        for k in ("rho", "eta", "kappa", "aw", "gamma_r", "fx", "fy", "kx_und",
+                  "ky_und", "kbxsf", "kbysf", "szfs", "szfe", "dx", "dy", "dz2"):
+            setattr(p, k, float(getattr(self, k)))
+        p.und_type = int(self.und_type)
+        p.one_d = int(self.one_d)
+        p.focusing = int(self.focusing)
+        p.und_ends = int(self.und_ends)
+        p.field_evolve = int(self.field_evolve)
+        p.electrons_evolve = int(self.electrons_evolve)
+        p.coupling = int(self.coupling)
+        p.mesh_type = int(self.mesh_type)
+        p.nz2 = int(self.nz2)
+        p.nix = int(self.nix if nix is None else nix)
+        p.niy = int(self.niy if niy is None else niy)
+        return p
+
+
+def calc_scaling(rho, aw, gamma_r, und_type, fx=1.0, fy=1.0):
+    """eta and kappa (setup_calcs.f90 calcScaling, :722-803), with the same
+    per-type fx/fy overrides."""
+    if und_type == UND_CURVED:
+        aw_rms, fx, fy = aw / math.sqrt(2.0), 0.0, 1.0
+    elif und_type == UND_PLANEPOLE:
+        aw_rms, fx, fy = aw / math.sqrt(2.0), 0.0, 1.0
+    elif und_type == UND_HELICAL:
+        aw_rms, fx, fy = aw, 1.0, 1.0
+    else:
+        aw_rms = aw * math.sqrt(fx ** 2 + fy ** 2) / math.sqrt(2.0)
+    betaz = math.sqrt(gamma_r ** 2.0 - 1.0 - aw_rms ** 2.0) / gamma_r
+    eta = (1.0 - betaz) / betaz
+    kappa = aw / 2.0 / rho / gamma_r
+    return eta, kappa, fx, fy
+
+
+def get_in_node(cfg: Config, x, y):
+    """Inner transverse window (nspinDX, nspinDY): para_field.f90:1432-1508."""
+    if cfg.nx * cfg.ny == 1:
+        return 1, 1
+    inbuf = 3
+    if len(x) > 0:
+        smaxx, sminx = abs(np.max(x)), abs(np.min(x))
+        smaxy, sminy = abs(np.max(y)), abs(np.min(y))
+        imaxx, iminx = math.ceil(smaxx / cfg.dx), math.floor(sminx / cfg.dx)
+        imaxy, iminy = math.ceil(smaxy / cfg.dy), math.floor(sminy / cfg.dy)
+        nix = (max(imaxx, iminx) + inbuf) * 2
+        niy = (max(imaxy, iminy) + inbuf) * 2
+    else:
+        nix = niy = 2
+    if cfg.nx % 2 != nix % 2:
+        nix += 1
+    if cfg.ny % 2 != niy % 2:
+        niy += 1
+    if nix > cfg.nx or niy > cfg.ny:
+        raise ValueError(f"transverse grid not large enough: nspinDX={nix}, nspinDY={niy}")
+    return nix, niy
+
+
+def outer_to_inner(cfg: Config, re, im, nix, niy):
+    """Outer mesh (nz2, ny, nx) -> inner window (nplanes, niy, nix)."""
+    ox, oy = (cfg.nx - nix) // 2, (cfg.ny - niy) // 2
+    np_ = cfg.nplanes
+    r = np.ascontiguousarray(re.reshape(cfg.nz2, cfg.ny, cfg.nx)[:np_, oy:oy + niy, ox:ox + nix])
+    i = np.ascontiguousarray(im.reshape(cfg.nz2, cfg.ny, cfg.nx)[:np_, oy:oy + niy, ox:ox + nix])
+    return r.reshape(-1), i.reshape(-1)
+
+
+def inner_to_outer(cfg: Config, re, im, wr, wi, nix, niy):
+    """Inner window -> outer mesh (in place); periodic tail plane mirrors plane 0."""
+    ox, oy = (cfg.nx - nix) // 2, (cfg.ny - niy) // 2
+    np_ = cfg.nplanes
+    R = re.reshape(cfg.nz2, cfg.ny, cfg.nx)
+    I = im.reshape(cfg.nz2, cfg.ny, cfg.nx)
+    R[:np_, oy:oy + niy, ox:ox + nix] = wr.reshape(np_, niy, nix)
+    I[:np_, oy:oy + niy, ox:ox + nix] = wi.reshape(np_, niy, nix)
+    if cfg.mesh_type == MESH_PERIODIC:
+        R[np_] = R[0]
+        I[np_] = I[0]
+
+
+# ---------------------------------------------------------------------------
+# RK4 (C restatement)
+# ---------------------------------------------------------------------------
+@dataclass
+class Beam:
+    x: np.ndarray
+    y: np.ndarray
+    z2: np.ndarray
+    px: np.ndarray
+    py: np.ndarray   # stored as p_im = -py, as the reference's sElPY_G
+    gam: np.ndarray
+    chi: np.ndarray
+
+    def copy(self):
+        return Beam(*(np.array(getattr(self, k), dtype=np.float64, copy=True)
+                      for k in ("x", "y", "z2", "px", "py", "gam", "chi")))
+
+    def arrays(self):
+        return [self.x, self.y, self.z2, self.px, self.py, self.gam]
+
+    @property
+    def n(self):
+        return len(self.x)
+
+
+@dataclass
+class Taper:
+    n2col: float
+    n2col0: float
+    undgrad: float
+
+    def c(self):
+        return _Taper(self.n2col, self.n2col0, self.undgrad)
+
+    def update(self, t):
+        self.n2col, self.n2col0, self.undgrad = t.n2col, t.n2col0, t.undgrad
+
+
+def rk4_step(cfg: Config, taper: Taper, sz: float, h: float, beam: Beam,
+             wr: np.ndarray, wi: np.ndarray, nix: int, niy: int) -> int:
+    """One rk4par step in place on ``beam`` and the inner-window field."""
+    p = cfg.cparams(nix, niy)
+    t = taper.c()
+    st = lib().or_rk4_step(ctypes.byref(p), ctypes.byref(t), float(sz), float(h),
+                           beam.n, *(_ptr(a) for a in beam.arrays()), _ptr(beam.chi),
+                           _ptr(wr), _ptr(wi))
+    taper.update(t)
+    return st
+
+
+def stage_rhs(cfg: Config, sz: float, n2col: float, place: int, beam: Beam,
+              wr, wi, nix, niy):
+    """One getrhs evaluation; returns (status, derivs[6], dadz_r, dadz_i)."""
+    p = cfg.cparams(nix, niy)
+    st = _Stage(float(sz), float(n2col), int(place))
+    d = [np.zeros(beam.n) for _ in range(6)]
+    dr = np.zeros(len(wr))
+    di = np.zeros(len(wi))
+    s = lib().or_rhs(ctypes.byref(p), ctypes.byref(st), beam.n, _ptr(wr), _ptr(wi),
+                     *(_ptr(a) for a in beam.arrays()), _ptr(beam.chi),
+                     *(_ptr(a) for a in d), _ptr(dr), _ptr(di))
+    return s, d, dr, di
+
+
+def stage_setup(cfg: Config, taper: Taper, sz: float):
+    p = cfg.cparams(1, 1)
+    t = taper.c()
+    st = _Stage()
+    lib().or_stage_setup(ctypes.byref(p), ctypes.byref(t), float(sz), ctypes.byref(st))
+    taper.update(t)
+    return st.sz, st.n2col, st.place
+
+
+def p2(gam, px, py, cfg: Config):
+    """Vectorised getP2 (same operation order as the C restatement)."""
+    a = 1.0 / ((cfg.gamma_r * cfg.gamma_r) * (gam * gam))
+    b = 1.0 + (cfg.aw * cfg.aw) * ((px * px) + (py * py))
+    return ((1.0 / np.sqrt(1.0 - a * b)) - 1.0) / cfg.eta
+
+
+def wrap_z2(cfg: Config, z2: np.ndarray):
+    p = cfg.cparams(1, 1)
+    lib().or_wrap_z2(ctypes.byref(p), len(z2), _ptr(z2))
+
+
+# ---------------------------------------------------------------------------
+# Diffraction (numpy restatement)
+# ---------------------------------------------------------------------------
+def _linspace(a, b, n):
+    """functions linspace (base_functions.f90:67-98): xstart + i*dx."""
+    if n == 1:
+        return np.array([a])
+    d = (b - a) / float(n - 1)
+    return a + np.arange(n) * d
+
+
+def _mask1d2(x, dx, nx, nb):
+    """masks.f90 Mask1D2 (:266-302); ranges applied in the reference's order,
+    so overlapping ends keep the second (lower-end) assignment."""
+    pi = PUFFIN_PI
+    lb = (nb - 1) * dx
+    x01, x02 = x[nx - 1], x[0]
+    m = np.empty(nx)
+    hi = slice(nx - nb, nx)
+    m[hi] = np.cos(pi * (x[hi] - x01) / (2.0 * lb)) ** 2
+    lo = slice(0, nb)
+    m[lo] = np.cos(pi * (x[lo] - x02) / (2.0 * lb)) ** 2
+    if nb < nx - nb:
+        m[nb:nx - nb] = 0.0
+    return m
+
+
+def _maskf4(x, dx, nx, nb):
+    """masks.f90 Maskf4 (:329-361)."""
+    pi = PUFFIN_PI
+    lb = (nb - 1) * dx
+    x01, x02 = x[nx - nb], x[nb - 1]
+    m = np.empty(nx)
+    hi = slice(nx - nb, nx)
+    m[hi] = np.cos(pi * (x[hi] - x01) / (2.0 * lb)) ** 2
+    lo = slice(0, nb)
+    m[lo] = np.cos(pi * (x[lo] - x02) / (2.0 * lb)) ** 2
+    if nb < nx - nb:
+        m[nb:nx - nb] = 1.0
+    return m
+
+
+def transverse_mask(cfg: Config):
+    """getMask + Mask2D (masks.f90:50-189): mask(ix, iy) as a (ny, nx) array."""
+    lenx = (cfg.nx - 1) * cfg.dx
+    leny = (cfg.ny - 1) * cfg.dy
+    x = _linspace(-lenx / 2, lenx / 2, cfg.nx)
+    y = _linspace(-leny / 2, leny / 2, cfg.ny)
+    maskx = _mask1d2(x, cfg.dx, cfg.nx, cfg.nbx)
+    masky = _mask1d2(y, cfg.dy, cfg.ny, cfg.nby)
+    maskx2 = _maskf4(x, cfg.dx, cfg.nx, cfg.nbx)
+    masky2 = np.ones(cfg.ny)
+    return masky2[:, None] * maskx[None, :] + maskx2[None, :] * masky[:, None]
+
+
+def z2_mask(cfg: Config):
+    """getZ2Mask (masks.f90:366-430), including its Lf = (nx - 1*dx) form;
+    zero on the periodic mesh (diffraction.f90:447)."""
+    n = cfg.nplanes
+    if cfg.mesh_type == MESH_PERIODIC:
+        return np.zeros(n)
+    pi = PUFFIN_PI
+    dx, nx, nb = cfg.dz2, cfg.nz2, cfg.nbz2
+    x = _linspace(0.0 * dx, float(n - 1) * dx, n)
+    lb = (nb - 1) * dx
+    lf = (nx - 1 * dx)
+    x0 = lf - lb / 2.0
+    fbn = nx - nb + 1
+    m = np.zeros(n)
+    ind = np.arange(1, n + 1)
+    sel = ind >= fbn
+    m[sel] = np.cos(pi * (x[sel] - x0) / lb) ** 2
+    return m
+
+
+def k_values(cfg: Config):
+    """GetKValues (transforms.f90:472-590); note the local full-precision pi."""
+    pi = 4.0 * math.atan(1.0)
+    lx = float(cfg.nx) * cfg.dx
+    ly = float(cfg.ny) * cfg.dy
+    n = cfg.nplanes
+    lz = float(n) * cfg.dz2
+
+    def idx(m):
+        mx = math.ceil(float(m) / 2.0)
+        i = np.arange(m)
+        return np.where(i >= mx, i - m, i).astype(np.float64)
+
+    kx = 2.0 * pi * idx(cfg.nx) / lx
+    ky = 2.0 * pi * idx(cfg.ny) / ly
+    kz = 2.0 * pi * idx(n) / lz
+    return kx, ky, kz
+
+
+def filter_cutoff(cfg: Config):
+    """MultiplyExp cutoff (diffraction.f90:138-139) with sFilt from
+    setup_calcs.f90:208-210 (Lenz2 = dz2 * NZ2, lambda_r = 4*pi*rho)."""
+    lenz2 = cfg.dz2 * cfg.nz2
+    sfilt = lenz2 / (4 * PUFFIN_PI * cfg.rho) * cfg.sfilt_frac
+    cutoff = 2.0 * PUFFIN_PI * sfilt / (float(cfg.nz2) * cfg.dz2)
+    if cfg.mesh_type == MESH_PERIODIC and cfg.sperwaves <= 1.1:
+        cutoff = 0.0
+    return cutoff
+
+
+def ffact(cfg: Config):
+    return float(cfg.nx) * float(cfg.ny) * float(cfg.nplanes)
+
+
+def diffract(cfg: Config, re: np.ndarray, im: np.ndarray, h: float):
+    """DiffractionStep + AbsorptionStep on the outer mesh, in place.
+
+    re/im are flat outer-mesh arrays of nx*ny*nz2 values, x fastest."""
+    n = cfg.nplanes
+    R = re.reshape(cfg.nz2, cfg.ny, cfg.nx)
+    I = im.reshape(cfg.nz2, cfg.ny, cfg.nx)
+    A = R[:n] + 1j * I[:n]
+    kx, ky, kz = k_values(cfg)
+    ff = ffact(cfg)
+    cutoff = filter_cutoff(cfg)
+    # forward FFTW transform is the unnormalised e^{-i...} sum
+    A = np.fft.fftn(A)
+    k2 = (kx[None, None, :] ** 2 + ky[None, :, None] ** 2)
+    pass_band = (kz > cutoff) | (kz < -cutoff)
+    nz = kz != 0.0
+    with np.errstate(divide="ignore", invalid="ignore"):
+        theta = h * k2 / (2.0 * kz[:, None, None])
+    prop = np.exp(1j * theta)
+    use = (pass_band & nz)[:, None, None]
+    A = np.where(use, prop * A, A)
+    if cfg.qfilter:
+        A = np.where((~pass_band)[:, None, None], 0.0, A)
+    A = np.fft.ifftn(A) * (A.size) / ff      # unnormalised backward, then /ffact
+    # AbsorptionStep
+    mask = transverse_mask(cfg)[None, :, :]
+    mz = z2_mask(cfg)[:, None, None]
+    m = mask + mz * (1.0 - mask)
+    anb = (1.0 - m) * A
+    A = m * A
+    A = np.fft.fftn(A)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        damp = np.exp(-h * cfg.sbeta * (np.abs(kx)[None, None, :] + np.abs(ky)[None, :, None])
+                      / np.sqrt(np.abs(2.0 * kz))[:, None, None])
+    A = np.where(nz[:, None, None], damp * A, A)
+    A = np.fft.ifftn(A) * (A.size) / ff
+    A = A + anb
+    R[:n] = A.real
+    I[:n] = A.imag
+    if cfg.mesh_type == MESH_PERIODIC:
+        R[n] = R[0]
+        I[n] = I[0]
+
+
+# ---------------------------------------------------------------------------
+# Split-step schedule (UndSection, undulator.f90:106-331), without writes.
+# ---------------------------------------------------------------------------
+@dataclass
+class RunResult:
+    steps: int
+    status: int
+    retries: int = 0
+    power: list = field(default_factory=list)
+
+
+def undulator_run(cfg: Config, beam: Beam, re: np.ndarray, im: np.ndarray,
+                  h: float, nsteps: int, isteps4diff: int, qdiffraction: bool,
+                  redist_every: int = 60, taper: Taper | None = None,
+                  nix: int | None = None, niy: int | None = None,
+                  on_step=None) -> RunResult:
+    """Drive rk4_step + diffract like UndSection: a first half diffraction
+    step, merged half steps between RK4 blocks, periodic z2 wraps every
+    ``redist_every`` steps, and up to 3 retries with a recomputed inner window
+    when a particle leaves it."""
+    taper = taper or Taper(cfg.n2col0, cfg.n2col0, cfg.undgrad)
+    if nix is None:
+        nix, niy = get_in_node(cfg, beam.x, beam.y)
+    szl = 0.0
+    if qdiffraction:
+        dzds = float(isteps4diff) * h / 2.0
+        diffract(cfg, re, im, dzds)
+    wr, wi = outer_to_inner(cfg, re, im, nix, niy)
+    retries = 0
+    for istep in range(1, nsteps + 1):
+        for attempt in range(4):
+            t_before = Taper(taper.n2col, taper.n2col0, taper.undgrad)
+            st = rk4_step(cfg, taper, szl, h, beam, wr, wi, nix, niy)
+            if st == 0:
+                break
+            if st & 2:
+                return RunResult(istep - 1, st, retries)
+            taper.n2col, taper.n2col0 = t_before.n2col, t_before.n2col0
+            retries += 1
+            inner_to_outer(cfg, re, im, wr, wi, nix, niy)
+            nix, niy = get_in_node(cfg, beam.x, beam.y)
+            wrap_z2(cfg, beam.z2)
+            wr, wi = outer_to_inner(cfg, re, im, nix, niy)
+        else:
+            return RunResult(istep - 1, st, retries)
+        szl = szl + h
+        if qdiffraction and (istep % isteps4diff == 0 or istep == nsteps):
+            inner_to_outer(cfg, re, im, wr, wi, nix, niy)
+            dzdf = dzds
+            if istep == nsteps:
+                dzds = 0.0
+            elif istep + isteps4diff <= nsteps:
+                dzds = float(isteps4diff) * h / 2
+            else:
+                dzds = float(nsteps - istep) * h / 2
+            diffract(cfg, re, im, dzdf + dzds)
+            wr, wi = outer_to_inner(cfg, re, im, nix, niy)
+        if on_step is not None:
+            on_step(istep, beam, wr, wi, nix, niy)
+        if istep % redist_every == 0:
+            wrap_z2(cfg, beam.z2)
+    inner_to_outer(cfg, re, im, wr, wi, nix, niy)
+    return RunResult(nsteps, 0, retries)
+
+
+# ---------------------------------------------------------------------------
+# Undulator entry/exit matching (acc_lattice.f90:601-846, init_conds.f90:70-203)
+# ---------------------------------------------------------------------------
+def _x_offset(cfg: Config, gamma_j, px, py, n2col, sz0):
+    """xOffSet_Array (init_conds.f90:70-102): nc = aw**2."""
+    nc = cfg.aw ** 2
+    return -(cfg.fy * 4.0 * cfg.kappa * cfg.rho ** 2 / math.sqrt(cfg.eta)
+             * (cfg.gamma_r / np.sqrt(gamma_j * gamma_j - (1.0 + nc * (px * px + py * py))))
+             * n2col * math.sin(sz0 / (2.0 * cfg.rho)))
+
+
+def _y_offset(cfg: Config, gamma_j, px, py, n2col, sz0):
+    """yOffSet_Array (init_conds.f90:149-183): nc = 2 aw**2 / (ux**2 + uy**2)."""
+    nc = 2.0 * cfg.aw ** 2 / (cfg.fx ** 2 + cfg.fy ** 2)
+    return (cfg.fx * 4.0 * cfg.kappa * cfg.rho ** 2 / math.sqrt(cfg.eta)
+            * (cfg.gamma_r / np.sqrt(gamma_j * gamma_j - (1.0 + nc * (px * px + py * py))))
+            * n2col * math.cos(sz0 / (2.0 * cfg.rho)))
+
+
+def _p_offsets(cfg: Config, beam: Beam, sz, n2col):
+    pxo = -(cfg.fy * n2col * math.cos(sz / (2.0 * cfg.rho)))
+    pyo = -(cfg.fx * n2col * math.sin(sz / (2.0 * cfg.rho)))
+    n = beam.n
+    if cfg.und_type == UND_CURVED:
+        kx, ky = cfg.kx_und, cfg.ky_und
+        spx = pxo - 0.5 * kx ** 2 * beam.x ** 2 - 0.5 * ky ** 2 * beam.y ** 2
+        spy = -1.0 * (pyo - kx ** 2 * beam.x * beam.y)
+    elif cfg.und_type == UND_PLANEPOLE:
+        spx = pxo - 0.5 * (cfg.eta / (4 * cfg.rho ** 2)) * beam.x ** 2
+        spy = np.full(n, -1.0 * pyo)
+    else:
+        spx = np.full(n, pxo)
+        spy = np.full(n, -1.0 * pyo)
+    return spx, spy
+
+
+def match_in(cfg: Config, beam: Beam, sz: float, n2col: float):
+    """matchIn (acc_lattice.f90:743-846)."""
+    spx, spy = _p_offsets(cfg, beam, sz, n2col)
+    gj = cfg.gamma_r * beam.gam
+    sxo = _x_offset(cfg, gj, spx, -spy, n2col, sz)
+    syo = _y_offset(cfg, gj, spx, -spy, n2col, sz)
+    beam.x[:] = beam.x + sxo
+    beam.y[:] = beam.y + syo
+    beam.px[:] = beam.px + spx
+    beam.py[:] = beam.py + spy
+
+
+def match_out(cfg: Config, beam: Beam, sz: float, n2col: float):
+    """matchOut (acc_lattice.f90:638-741)."""
+    spx, spy = _p_offsets(cfg, beam, sz, n2col)
+    gj = cfg.gamma_r * beam.gam
+    sxo = _x_offset(cfg, gj, spx, spy, n2col, sz)
+    syo = _y_offset(cfg, gj, spx, spy, n2col, sz)
+    beam.x[:] = beam.x - sxo
+    beam.y[:] = beam.y - syo
+    beam.px[:] = beam.px - spx
+    beam.py[:] = beam.py - spy
+
+
+def correct_trans(beam: Beam):
+    """correctTrans (acc_lattice.f90:601-636): remove chi-weighted means."""
+    w = beam.chi
+    ws = np.sum(w)
+    mpx = np.sum(w * beam.px) / ws
+    mpy = np.sum(w * beam.py) / ws
+    mx = np.sum(w * beam.x) / ws
+    my = np.sum(w * beam.y) / ws
+    beam.px[:] -= mpx
+    beam.py[:] -= mpy
+    beam.x[:] -= mx
+    beam.y[:] -= my
