@@ -1,0 +1,381 @@
+#!/usr/bin/env python
+"""Benchmark of the Puffin hot path on GB300: macroparticle-RK4-steps/s.
+
+Workload (default): the large FP64 drop-in configuration -- temporal mesh
+129 x 129 x 4096 (complex FP64), planepole undulator, 2^23 macroparticles,
+24 steps per period, diffraction every 8 steps.  One "step" is one RK4 step
+over all macroparticles and the inner-window field, plus every 8th step the
+merged diffraction call (dz = 8 h), exactly as UndSection schedules them.
+
+* value  -- particle-steps/s with the state resident in HBM (CUDA events on
+            the library's stream around K steps, after W warm-up steps);
+* e2e    -- the same metric through the C ABI with host buffers: every step
+            copies the particles and the field in from pinned host memory and
+            reads both back (the drop-in call pattern of a host driver);
+* roofline -- the dominant kernel (the fused RK4 stage kernel) timed live
+            with CUDA events; algorithmic bytes 104 B per particle per stage
+            (416 B per particle-step over 4 stages);
+* cpu_baseline -- the CPU restatement of the same step (oracle/), timed on the
+            host cores on a bounded sample and extrapolated to the workload.
+
+``--impl reference`` times the CPU implementation alone (the reference is
+Fortran + MPI + FFTW-MPI + parallel HDF5 and cannot be built here, so the
+oracle restatement stands in) and prints its own line.
+
+N > 1 (torchrun): the path does not shard in this build, so N independent
+replicas run one per GPU ("replicas only"); value sums over ranks and the
+time is the maximum over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "macroparticle-RK4-steps/s: mixed vs FP64 on GB300 at stated power error"
+UNIT = "macroparticle-steps/s"
+BYTES_PER_PARTICLE_STAGE = 104          # 56 B read + 48 B write (416 B per step)
+FLOPS_PER_PARTICLE_STAGE = 166          # ~664 FP64 flop per particle-step
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=48)
+    ap.add_argument("--warmup", type=int, default=8)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--np", type=int, default=2 ** 23, help="macroparticles")
+    ap.add_argument("--e2e-steps", type=int, default=8)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.gpu)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+def cpu_baseline(w, seconds):
+    """Time the CPU restatement (oracle/) on the host cores on a bounded
+    sample of the workload and extrapolate to the full macroparticle count:
+    RK4 step time = a + b * Np from two sample sizes, plus one diffraction
+    per 8 steps (numpy restatement with scipy's multithreaded FFT)."""
+    from oracle import oracle as O
+    from tests.oracle_bridge import oracle_beam, oracle_config
+
+    cores = os.cpu_count() or 1
+    O.set_threads(cores)
+    cfg = oracle_config(w.params)
+    budget = seconds
+    samples = []
+    for frac in (1.0 / 64, 1.0 / 32):
+        n = max(1024, int(w.np * frac))
+        beam = oracle_beam({k: v[:n] for k, v in w.beam.items()})
+        beam.chi[:] = beam.chi * (w.np / n)
+        nix, niy = O.get_in_node(cfg, beam.x, beam.y)
+        re, im = (a.copy() for a in w.field)
+        wr, wi = O.outer_to_inner(cfg, re, im, nix, niy)
+        taper = O.Taper(w.params.n2col0, w.params.n2col0, w.params.undgrad)
+        t0 = time.perf_counter()
+        steps = 0
+        szl = 0.0
+        while steps < 2 or (time.perf_counter() - t0 < budget / 4 and steps < 8):
+            O.rk4_step(cfg, taper, szl, w.h, beam, wr, wi, nix, niy)
+            szl += w.h
+            steps += 1
+        samples.append((n, (time.perf_counter() - t0) / steps))
+    (n1, t1), (n2, t2) = samples
+    b = max(0.0, (t2 - t1) / (n2 - n1))
+    a = max(0.0, t1 - b * n1)
+    t_rk4 = a + b * w.np
+    re, im = (a_.copy() for a_ in w.field)
+    t_diff = 0.0
+    if w.qdiffraction:
+        try:
+            import scipy.fft as sfft
+
+            class _F:  # numpy.fft interface over scipy's threaded FFT
+                @staticmethod
+                def fftn(x):
+                    return sfft.fftn(x, workers=cores)
+
+                @staticmethod
+                def ifftn(x):
+                    return sfft.ifftn(x, workers=cores)
+            fftmod = _F
+        except Exception:
+            fftmod = None
+        t0 = time.perf_counter()
+        O.diffract(cfg, re, im, w.isteps4diff * w.h, fft=fftmod)
+        t_diff = time.perf_counter() - t0
+    per_step = t_rk4 + (t_diff / w.isteps4diff if w.qdiffraction else 0.0)
+    return {
+        "value": w.np / per_step, "unit": UNIT, "cores": cores, "kind": "port",
+        "sample": (f"CPU restatement (oracle/, C+OpenMP {cores} threads, numpy/scipy FFT): "
+                   f"RK4 steps at Np={n1} and {n2} on the full mesh fitted to a+b*Np "
+                   f"(a={a:.3f}s, b={b:.3e}s) and one diffraction ({t_diff:.1f}s) every "
+                   f"{w.isteps4diff} steps, extrapolated to Np={w.np}"),
+    }
+
+
+# ---------------------------------------------------------------------------
+def run_gpu(args, rank, world):
+    import torch
+
+    import puffin_gb300 as P
+    from puffin_gb300 import configs
+    from puffin_gb300 import lib as L
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    w = configs.config2(np_=args.np)
+    p = w.params
+    p.device = dev
+    sim = P.Puffin(p)
+    sim.set_particles(*(w.beam[k] for k in P.PARTICLE_KEYS))
+    sim.set_field(*w.field)
+    win = sim.window
+    stream = torch.cuda.ExternalStream(sim.stream_handle, device=dev)
+    every = w.isteps4diff
+    state = {"szl": 0.0, "i": 0}
+
+    def step():
+        ok = sim.rk4par(state["szl"], w.h)
+        if not ok:                      # reference behaviour: redistribute and retry
+            sim.redistribute()
+            ok = sim.rk4par(state["szl"], w.h)
+            assert ok
+        state["szl"] += w.h
+        state["i"] += 1
+        if state["i"] % every == 0:
+            sim.diffractIM(every * w.h)   # merged end + start half steps
+
+    for _ in range(args.warmup):
+        step()
+    sim.sync()
+    if world > 1:
+        torch.distributed.barrier()
+    sim.profile(True)
+    launches0 = sim.kernel_launches
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev) as clk:
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches = sim.kernel_launches - launches0
+    stage_ms, stage_n = sim.profile_read(L.PROF_STAGE)
+    nodes_ms, nodes_n = sim.profile_read(L.PROF_NODES)
+    fft_ms, fft_n = sim.profile_read(L.PROF_FFT)
+    diff_ms, diff_n = sim.profile_read(L.PROF_DIFF)
+    sim.profile(False)
+
+    # end to end through the C ABI with host buffers
+    n = w.np
+    pin = {k: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy() for k in P.PARTICLE_KEYS}
+    fre = torch.empty(sim.n_outer, dtype=torch.float64, pin_memory=True).numpy()
+    fim = torch.empty(sim.n_outer, dtype=torch.float64, pin_memory=True).numpy()
+    cur = sim.get_particles()
+    for k in P.PARTICLE_KEYS:
+        pin[k][:] = cur[k]
+    r_, i_ = sim.get_field()
+    fre[:] = r_
+    fim[:] = i_
+    lib = L.load()
+    ptrs = [pin[k].ctypes.data for k in P.PARTICLE_KEYS]
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(args.e2e_steps):
+        assert lib.pf_set_particles(sim._h, n, *ptrs) == 0
+        assert lib.pf_set_field(sim._h, fre.ctypes.data, fim.ctypes.data) == 0
+        step()
+        assert lib.pf_get_particles(sim._h, *ptrs) == 0
+        assert lib.pf_get_field(sim._h, fre.ctypes.data, fim.ctypes.data) == 0
+    t1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = t0.elapsed_time(t1)
+    h2d = 7 * 8 * n + 2 * 8 * sim.n_outer
+    d2h = h2d
+    sim.close()
+
+    times = torch.tensor([ms, e2e_ms], dtype=torch.float64, device=f"cuda:{dev}")
+    if world > 1:
+        torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
+    ms, e2e_ms = float(times[0]), float(times[1])
+    if rank != 0:
+        return None
+
+    value = world * n * args.steps / (ms * 1e-3)
+    e2e_value = world * n * args.e2e_steps / (e2e_ms * 1e-3)
+    peak, peak_kind = measured_peaks()
+    stage_avg = stage_ms / max(1, stage_n)
+    achieved = n * BYTES_PER_PARTICLE_STAGE / (stage_avg * 1e-3) / 1e9
+    # FP64 peak of this GPU, measured with a cuBLAS DGEMM
+    a = torch.randn(4096, 4096, dtype=torch.float64, device=f"cuda:{dev}")
+    torch.matmul(a, a)
+    torch.cuda.synchronize()
+    g0 = torch.cuda.Event(enable_timing=True)
+    g1 = torch.cuda.Event(enable_timing=True)
+    g0.record()
+    for _ in range(3):
+        torch.matmul(a, a)
+    g1.record()
+    torch.cuda.synchronize()
+    dgemm_tflops = 3 * 2 * 4096 ** 3 / (g0.elapsed_time(g1) * 1e-3) / 1e12
+    fp64_achieved = n * FLOPS_PER_PARTICLE_STAGE / (stage_avg * 1e-3) / 1e12
+    rec = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded beam and zero seed field; no dataset)",
+        "config": {
+            "workload": w.name, "macroparticles": n, "mesh": [p.nx, p.ny, p.nz2],
+            "inner_window": list(win),
+            "steps_per_period": 24, "diffraction_every": every, "precision": "fp64",
+            "parallelism": f"replicas x{world}",
+            "l2": "inputs larger than L2 (particle state 470 MB, field 1.09 GB per array pair)",
+        },
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "steps": args.e2e_steps},
+        "gpu_launches": launches,
+        "kernel_ms": {"stage": stage_ms, "nodes": nodes_ms, "fft": fft_ms, "diff_elementwise": diff_ms,
+                      "stage_launches": stage_n, "node_launches": nodes_n, "fft_launches": fft_n,
+                      "diff_launches": diff_n},
+        "roofline": {"kernel": "k_stage (fused RK4 stage)", "bound": "hbm", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": f"{peak_kind} copy bandwidth (burst)", "traffic": None,
+                     "fp64": {"achieved_tflops": fp64_achieved, "peak_tflops": dgemm_tflops,
+                              "peak_kind": "measured cuBLAS DGEMM 4096^3",
+                              "frac": fp64_achieved / dgemm_tflops}},
+        "clocks": clk.summary(),
+    }
+    return rec
+
+
+def run_reference(args):
+    from puffin_gb300 import configs
+    w = configs.config2(np_=args.np)
+    cb = cpu_baseline(w, args.cpu_seconds)
+    return {
+        "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * w.np / cb["value"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded beam and zero seed field; no dataset)",
+        "config": {"workload": w.name, "macroparticles": w.np, "mesh": [129, 129, 4096],
+                   "precision": "fp64", "parallelism": "host cores"},
+        "impl": "reference",
+        "cpu_baseline": cb,
+        "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "note": ("the reference is Fortran + MPI + FFTW-MPI + parallel HDF5 and no Fortran "
+                 "toolchain exists here or on the GPU host image, so the CPU restatement "
+                 "in oracle/ is timed in its place"),
+    }
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(args)), flush=True)
+        return
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    rec = run_gpu(args, rank, world)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            from puffin_gb300 import configs
+            w = configs.config2(np_=args.np)
+            rec["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds)
+        print(json.dumps(rec), flush=True)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,193 @@
+/*
+ * puffgpu — GB300 (sm_103a) library for Puffin's per-step hot path:
+ * the RK4 macroparticle push with trilinear gather/deposit between the
+ * macroparticles and the complex radiation field, and the FFT diffraction
+ * step with its absorbing boundary.
+ *
+ * C ABI only: plain pointers, sizes and int status codes, no C++ or torch
+ * types.  The array layouts are the reference's own:
+ *   particles  7 SoA FP64 arrays x, y, z2, px, py, gamma, chi of length n,
+ *              where "py" holds the stored imaginary p_perp (= -py), exactly
+ *              as sElPY_G (simple_electron_gen.f90:330);
+ *   field      2 FP64 arrays (re, im) over the outer mesh, x fastest:
+ *              idx = ix + nx*iy + nx*ny*iz (diffraction.f90:259-260), nz2
+ *              planes; on the periodic mesh the last plane mirrors the first.
+ *
+ * Every entry point returns a pf_status.  Nothing here exits or stops the
+ * process: where the reference STOPs (a particle beyond the temporal z2
+ * mesh, system_interpolation.f90:70-76) the call returns PF_OUT_OF_Z2.
+ *
+ * Reference interfaces replaced (file:line inside the Puffin project):
+ *   pf_rk4_step      rk4par(sZ, h, qD)        puffin/lib/interaction/puffin_mpi_RK4.f90:38
+ *                    -> derivs                puffin/lib/interaction/derivative.f90:36
+ *                    -> getrhs                puffin/lib/interaction/rhs.f90:60
+ *   pf_diffract      inner2Outer + diffractIM(sStep, qD, qOK) + outer2Inner
+ *                                             puffin/lib/parallel/para_field.f90:1352,1394
+ *                                             puffin/lib/diffraction/diffraction.f90:46
+ *   pf_redistribute  getInNode + getLocalFieldIndices (window + periodic z2 wrap)
+ *                                             puffin/lib/parallel/para_field.f90:1432, 83
+ *   pf_run           the RK4/diffraction loop of UndSection
+ *                                             puffin/lib/undulator.f90:182-333
+ *   pf_set/get_particles, pf_set/get_field    the module globals sElX_G..sElGam_G,
+ *                    s_chi_bar_G, ac_rfield/ac_ifield (deriv_globals.f90)
+ *   pf_set/get_taper getAlpha state n2col/n2col0/undgrad
+ *                                             puffin/lib/undulator/wiggler_taper.f90:16-53
+ */
+#ifndef PUFFGPU_H
+#define PUFFGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PUFFGPU_ABI_VERSION 1
+
+typedef enum {
+  PF_OK = 0,
+  PF_OUT_OF_WINDOW = 1,   /* a macroparticle left the inner transverse window
+                             (qInnerXYOK_G = .false.); state left unchanged */
+  PF_OUT_OF_Z2 = 2,       /* z2 node beyond the temporal mesh (the reference STOPs) */
+  PF_BAD_ARG = 3,
+  PF_CUDA_ERR = 4,
+  PF_TIMEOUT = 5,         /* a bounded device-side wait gave up */
+  PF_NO_DEVICE = 6,
+  PF_OVERFLOW = 7,        /* a deposit exceeded the fixed-point range */
+  PF_STATE = 8            /* call order error (e.g. step before set_particles) */
+} pf_status;
+
+typedef enum {
+  PF_UND_PUFFIN = 0,      /* elliptical 'puffin' undulator (zUndType = '') */
+  PF_UND_HELICAL = 1,
+  PF_UND_PLANEPOLE = 2,
+  PF_UND_CURVED = 3
+} pf_und_type;
+
+typedef enum { PF_MESH_TEMPORAL = 0, PF_MESH_PERIODIC = 1 } pf_mesh_type;
+typedef enum { PF_FP64 = 0, PF_MIXED = 1 } pf_precision;
+
+/* Scaled-unit constants and flags of one undulator module.  Names follow the
+ * reference globals they replace (deriv_globals.f90). */
+typedef struct pf_params {
+  double rho;          /* sRho_G */
+  double eta;          /* sEta_G */
+  double kappa;        /* sKappa_G */
+  double aw;           /* saw_G (peak) */
+  double gamma_r;      /* sGammaR_G */
+  double fx, fy;       /* fx_G, fy_G */
+  double kx_und, ky_und;   /* kx_und_G, ky_und_G (curved poles) */
+  double kbxsf, kbysf;     /* sKBetaXSF_G, sKBetaYSF_G (qFocussing) */
+  double szfs, szfe;   /* sZFS, sZFE: main-section bounds in local zbar */
+  double n2col0;       /* taper alpha at sZFS (mf of the module) */
+  double undgrad;      /* taper gradient d(alpha)/dzbar */
+  double dx, dy, dz2;  /* sLengthOfElm{X,Y,Z2}_G */
+  double sbeta;        /* sBeta_G: absorption coefficient */
+  double sfilt_frac;   /* sFiltFrac: high-pass cut as a fraction of the
+                          resonant frequency (the reference's default is the
+                          single-precision literal 0.3) */
+  double sperwaves;    /* sPerWaves_G (periodic cut-off rule) */
+  int32_t und_type;    /* pf_und_type */
+  int32_t mesh_type;   /* pf_mesh_type (fieldMesh) */
+  int32_t nx, ny, nz2; /* NX_G, NY_G, NZ2_G */
+  int32_t nix, niy;    /* nspinDX, nspinDY; 0 = computed from the particles
+                          the way getInNode does */
+  int32_t nbx, nby, nbz2;  /* absorbing-boundary widths (16, 16, 37) */
+  int32_t one_d;       /* qOneD (nx = ny = 1) */
+  int32_t focusing;    /* qFocussing */
+  int32_t und_ends;    /* qUndEnds */
+  int32_t field_evolve, electrons_evolve, coupling;  /* q*Evolve / coupling */
+  int32_t qfilter;     /* qFilter */
+  int32_t redist_every;/* iRedistStp_G (periodic z2 wrap cadence in pf_run) */
+  int32_t precision;   /* pf_precision */
+  int32_t device;      /* CUDA device ordinal */
+} pf_params;
+
+typedef struct pf_handle pf_handle;
+
+/* Fill *p with the reference's defaults (nb* = 16/16/37, sbeta = 1,
+ * sfilt_frac = (double)0.3f, qfilter = 1, evolve/coupling flags = 1,
+ * redist_every = 60, FP64). */
+void pf_default_params(pf_params *p);
+
+int pf_create(const pf_params *p, pf_handle **out);
+int pf_destroy(pf_handle *h);
+
+/* Particles: host arrays (copied in/out) or device arrays (device-to-device). */
+int pf_set_particles(pf_handle *h, int64_t n, const double *x, const double *y,
+                     const double *z2, const double *px, const double *py,
+                     const double *gam, const double *chi);
+int pf_get_particles(pf_handle *h, double *x, double *y, double *z2, double *px,
+                     double *py, double *gam, double *chi);
+int pf_set_particles_dev(pf_handle *h, int64_t n, const double *x, const double *y,
+                         const double *z2, const double *px, const double *py,
+                         const double *gam, const double *chi);
+int pf_get_particles_dev(pf_handle *h, double *x, double *y, double *z2, double *px,
+                         double *py, double *gam, double *chi);
+int64_t pf_num_particles(const pf_handle *h);
+
+/* Field on the outer mesh (nx*ny*nz2 values each). */
+int pf_set_field(pf_handle *h, const double *re, const double *im);
+int pf_get_field(pf_handle *h, double *re, double *im);
+int pf_set_field_dev(pf_handle *h, const double *re, const double *im);
+int pf_get_field_dev(pf_handle *h, double *re, double *im);
+
+/* Taper state (n2col, n2col0, undgrad). */
+int pf_set_taper(pf_handle *h, double n2col, double n2col0, double undgrad);
+int pf_get_taper(const pf_handle *h, double *n2col, double *n2col0, double *undgrad);
+
+/* Inner transverse window currently in use. */
+int pf_get_window(const pf_handle *h, int32_t *nix, int32_t *niy);
+
+/* One rk4par step at local zbar szl with step size h.  Returns PF_OK, or
+ * PF_OUT_OF_WINDOW / PF_OUT_OF_Z2 with the state unchanged. */
+int pf_rk4_step(pf_handle *h, double szl, double hstep);
+
+/* getInNode + getLocalFieldIndices: recompute the inner window from the
+ * particles and apply the periodic z2 wrap. */
+int pf_redistribute(pf_handle *h);
+
+/* Periodic z2 wrap alone (the part of getLocalFieldIndices that changes
+ * particle data, para_field.f90:212-215). */
+int pf_wrap_z2(pf_handle *h);
+
+/* Diffract the field over dz (inner2Outer + diffractIM + outer2Inner). */
+int pf_diffract(pf_handle *h, double dz);
+
+/* UndSection's loop for nsteps RK4 steps of size hstep starting at local
+ * zbar *szl (updated on return), diffraction every isteps4diff steps with
+ * merged half steps (qdiffraction != 0), retries with a recomputed window on
+ * PF_OUT_OF_WINDOW (up to 3, as the reference), periodic wraps every
+ * redist_every steps.  *steps_done receives the number of completed steps. */
+int pf_run(pf_handle *h, int32_t nsteps, int32_t isteps4diff, int32_t qdiffraction,
+           double hstep, double *szl, int32_t *steps_done);
+
+/* Block until all work queued by the handle is done. */
+int pf_sync(pf_handle *h);
+
+/* Number of kernels this handle has launched so far. */
+int64_t pf_kernel_launches(const pf_handle *h);
+
+/* The cudaStream_t (as void*) every kernel of this handle is launched on, so
+ * callers can order their own work and timing events against it. */
+void *pf_get_stream(const pf_handle *h);
+
+/* Per-kernel-class device timing with CUDA events recorded on the handle's
+ * stream around each launch (classes: 0 particle stage kernels, 1 field node
+ * kernels, 2 FFT passes, 3 diffraction element-wise kernels, 4 other).
+ * pf_profile(h, 1) enables and clears the counters; pf_profile_read returns
+ * the summed milliseconds and the number of timed launches of one class. */
+int pf_profile(pf_handle *h, int32_t enable);
+int pf_profile_read(pf_handle *h, int32_t kernel_class, double *ms_total, int64_t *launches);
+
+/* Human-readable text of the last error on this handle (or a global one when
+ * h is NULL). */
+const char *pf_last_error(const pf_handle *h);
+
+int pf_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -439,10 +439,12 @@ def ffact(cfg: Config):
     return float(cfg.nx) * float(cfg.ny) * float(cfg.nplanes)
 
 
-def diffract(cfg: Config, re: np.ndarray, im: np.ndarray, h: float):
+def diffract(cfg: Config, re: np.ndarray, im: np.ndarray, h: float, fft=None):
     """DiffractionStep + AbsorptionStep on the outer mesh, in place.
 
-    re/im are flat outer-mesh arrays of nx*ny*nz2 values, x fastest."""
+    re/im are flat outer-mesh arrays of nx*ny*nz2 values, x fastest.  ``fft``
+    may supply fftn/ifftn with numpy.fft's semantics (default numpy.fft)."""
+    fft = np.fft if fft is None else fft
     n = cfg.nplanes
     R = re.reshape(cfg.nz2, cfg.ny, cfg.nx)
     I = im.reshape(cfg.nz2, cfg.ny, cfg.nx)
@@ -451,30 +453,30 @@ def diffract(cfg: Config, re: np.ndarray, im: np.ndarray, h: float):
     ff = ffact(cfg)
     cutoff = filter_cutoff(cfg)
     # forward FFTW transform is the unnormalised e^{-i...} sum
-    A = np.fft.fftn(A)
+    A = fft.fftn(A)
     k2 = (kx[None, None, :] ** 2 + ky[None, :, None] ** 2)
     pass_band = (kz > cutoff) | (kz < -cutoff)
     nz = kz != 0.0
     with np.errstate(divide="ignore", invalid="ignore"):
         theta = h * k2 / (2.0 * kz[:, None, None])
-    prop = np.exp(1j * theta)
+        prop = np.exp(1j * theta)
     use = (pass_band & nz)[:, None, None]
     A = np.where(use, prop * A, A)
     if cfg.qfilter:
         A = np.where((~pass_band)[:, None, None], 0.0, A)
-    A = np.fft.ifftn(A) * (A.size) / ff      # unnormalised backward, then /ffact
+    A = fft.ifftn(A) * (A.size) / ff      # unnormalised backward, then /ffact
     # AbsorptionStep
     mask = transverse_mask(cfg)[None, :, :]
     mz = z2_mask(cfg)[:, None, None]
     m = mask + mz * (1.0 - mask)
     anb = (1.0 - m) * A
     A = m * A
-    A = np.fft.fftn(A)
+    A = fft.fftn(A)
     with np.errstate(divide="ignore", invalid="ignore"):
         damp = np.exp(-h * cfg.sbeta * (np.abs(kx)[None, None, :] + np.abs(ky)[None, :, None])
                       / np.sqrt(np.abs(2.0 * kz))[:, None, None])
     A = np.where(nz[:, None, None], damp * A, A)
-    A = np.fft.ifftn(A) * (A.size) / ff
+    A = fft.ifftn(A) * (A.size) / ff
     A = A + anb
     R[:n] = A.real
     I[:n] = A.imag

@@ -1,0 +1,689 @@
+// C ABI of puffgpu: handle life cycle, particle/field transfer, the inner
+// transverse window, the periodic z2 wrap and the UndSection-style loop.
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <string>
+
+#include "pf_internal.h"
+
+namespace {
+
+typedef unsigned long long u64;
+
+std::string g_err;
+
+// Order-preserving map of doubles onto unsigned 64-bit integers.
+__device__ __forceinline__ u64 ord_key(double v) {
+  u64 b = (u64)__double_as_longlong(v);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+__global__ void k_minmax_xy(const double *x, const double *y, int64_t n, u64 *out) {
+  // out[0] max x, out[1] min x (as keys), out[2] max y, out[3] min y
+  u64 mx = 0, mnx = ~0ull, my = 0, mny = ~0ull;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    u64 kx = ord_key(x[i]), ky = ord_key(y[i]);
+    mx = max(mx, kx);
+    mnx = min(mnx, kx);
+    my = max(my, ky);
+    mny = min(mny, ky);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    mnx = min(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
+    my = max(my, __shfl_xor_sync(0xffffffffu, my, o));
+    mny = min(mny, __shfl_xor_sync(0xffffffffu, mny, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(out + 0, mx);
+    atomicMin(out + 1, mnx);
+    atomicMax(out + 2, my);
+    atomicMin(out + 3, mny);
+  }
+}
+
+__global__ void k_absmax(const double *v, int64_t n, u64 *out) {
+  u64 m = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    m = max(m, (u64)__double_as_longlong(fabs(v[i])));
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+// outer2Inner / inner2Outer (para_field.f90:1352-1429): the window is
+// centred, offset ((nx - nix)/2, (ny - niy)/2).
+__global__ void k_window_copy(double *wr, double *wi, double *or_, double *oi, int nix, int niy,
+                              int64_t npl, int nx, int ny, int64_t nz2, int to_outer,
+                              int mirror) {
+  const int64_t nw = (int64_t)nix * niy * npl;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nw) return;
+  const int ix = (int)(t % nix);
+  const int iy = (int)((t / nix) % niy);
+  const int64_t iz = t / ((int64_t)nix * niy);
+  const int ox = (nx - nix) / 2, oy = (ny - niy) / 2;
+  const int64_t plane = (int64_t)nx * ny;
+  const int64_t o = (ix + ox) + (int64_t)nx * (iy + oy) + plane * iz;
+  if (to_outer) {
+    or_[o] = wr[t];
+    oi[o] = wi[t];
+    if (mirror && iz == 0) {
+      or_[o + plane * (nz2 - 1)] = wr[t];
+      oi[o + plane * (nz2 - 1)] = wi[t];
+    }
+  } else {
+    wr[t] = or_[o];
+    wi[t] = oi[o];
+  }
+}
+
+// Periodic wrap of z2 (para_field.f90:212-215)
+__global__ void k_wrap_z2(double *z2, int64_t n, double lenz2) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) z2[i] = z2[i] - (floor(z2[i] / lenz2) * lenz2);
+}
+
+__global__ void k_mirror_plane(double *re, double *im, int64_t plane, int64_t nz2) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < plane) {
+    re[plane * (nz2 - 1) + t] = re[t];
+    im[plane * (nz2 - 1) + t] = im[t];
+  }
+}
+
+inline unsigned grid_for(int64_t n, int threads) {
+  return (unsigned)std::max<int64_t>(1, (n + threads - 1) / threads);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// per-kernel-class timing
+void pf_prof_begin(pf_handle *h, int cls) {
+  if (!h->prof) return;
+  ProfEvent e;
+  if (!h->prof_pool.empty()) {
+    e = h->prof_pool.back();
+    h->prof_pool.pop_back();
+  } else {
+    cudaEventCreate(&e.a);
+    cudaEventCreate(&e.b);
+  }
+  e.cls = cls;
+  cudaEventRecord(e.a, h->stream);
+  h->prof_pending.push_back(e);
+  h->prof_open = (int)h->prof_pending.size() - 1;
+}
+
+void pf_prof_end(pf_handle *h) {
+  if (!h->prof || h->prof_open < 0) return;
+  cudaEventRecord(h->prof_pending[h->prof_open].b, h->stream);
+  h->prof_open = -1;
+}
+
+void pf_prof_flush(pf_handle *h) {
+  if (h->prof_pending.empty()) return;
+  for (ProfEvent &e : h->prof_pending) {
+    float ms = 0.f;
+    if (cudaEventSynchronize(e.b) == cudaSuccess && cudaEventElapsedTime(&ms, e.a, e.b) == cudaSuccess) {
+      h->prof_ms[e.cls] += ms;
+      h->prof_n[e.cls] += 1;
+    }
+    h->prof_pool.push_back(e);
+  }
+  h->prof_pending.clear();
+}
+
+static void free_particles(pf_handle *h) {
+  for (int b = 0; b < 2; ++b)
+    for (int j = 0; j < 6; ++j) cudaFree(h->y[b][j]), h->y[b][j] = nullptr;
+  for (int j = 0; j < 6; ++j) {
+    cudaFree(h->k1[j]);
+    cudaFree(h->ka[j]);
+    cudaFree(h->kb[j]);
+    h->k1[j] = h->ka[j] = h->kb[j] = nullptr;
+  }
+  cudaFree(h->chi);
+  h->chi = nullptr;
+  h->cap = 0;
+}
+
+static void free_window(pf_handle *h) {
+  double **ptrs[] = {&h->wr, &h->wi, &h->asr, &h->asi, &h->d0r, &h->d0i, &h->d12r, &h->d12i};
+  for (auto p : ptrs) {
+    cudaFree(*p);
+    *p = nullptr;
+  }
+  cudaFree(h->acc);
+  h->acc = nullptr;
+  h->wcap = 0;
+  h->nwin = 0;
+  h->window_valid = false;
+}
+
+static int alloc_particles(pf_handle *h, int64_t n) {
+  if (n <= h->cap) return PF_OK;
+  free_particles(h);
+  const size_t b = sizeof(double) * (size_t)std::max<int64_t>(n, 1);
+  for (int bb = 0; bb < 2; ++bb)
+    for (int j = 0; j < 6; ++j) PF_CUDA(cudaMalloc(&h->y[bb][j], b));
+  for (int j = 0; j < 6; ++j) {
+    PF_CUDA(cudaMalloc(&h->k1[j], b));
+    PF_CUDA(cudaMalloc(&h->ka[j], b));
+    PF_CUDA(cudaMalloc(&h->kb[j], b));
+  }
+  PF_CUDA(cudaMalloc(&h->chi, b));
+  h->cap = n;
+  return PF_OK;
+}
+
+static int alloc_window(pf_handle *h, int nix, int niy) {
+  const int64_t nw = (int64_t)nix * niy * h->npl;
+  if (nw > h->wcap) {
+    free_window(h);
+    const size_t b = sizeof(double) * (size_t)nw;
+    double **ptrs[] = {&h->wr, &h->wi, &h->asr, &h->asi, &h->d0r, &h->d0i, &h->d12r, &h->d12i};
+    for (auto p : ptrs) PF_CUDA(cudaMalloc(p, b));
+    PF_CUDA(cudaMalloc(&h->acc, 4 * b));
+    PF_CUDA(cudaMemsetAsync(h->acc, 0, 4 * b, h->stream));
+    h->wcap = nw;
+  }
+  h->nix = nix;
+  h->niy = niy;
+  h->nwin = nw;
+  return PF_OK;
+}
+
+int pf_outer_to_inner(pf_handle *h) {
+  if (h->nwin == 0) return PF_OK;
+  k_window_copy<<<grid_for(h->nwin, 256), 256, 0, h->stream>>>(
+      h->wr, h->wi, h->or_, h->oi_, h->nix, h->niy, h->npl, h->p.nx, h->p.ny, h->p.nz2, 0, 0);
+  PF_LAUNCHED(h);
+  h->window_valid = true;
+  return PF_OK;
+}
+
+int pf_inner_to_outer(pf_handle *h) {
+  if (h->nwin == 0 || !h->window_valid) return PF_OK;
+  const int mirror = (h->p.mesh_type == PF_MESH_PERIODIC);
+  k_window_copy<<<grid_for(h->nwin, 256), 256, 0, h->stream>>>(
+      h->wr, h->wi, h->or_, h->oi_, h->nix, h->niy, h->npl, h->p.nx, h->p.ny, h->p.nz2, 1,
+      mirror);
+  PF_LAUNCHED(h);
+  return PF_OK;
+}
+
+// getInNode (para_field.f90:1432-1508)
+int pf_window_from_particles(pf_handle *h, int *nix, int *niy) {
+  const pf_params &p = h->p;
+  if (p.nx * p.ny == 1) {
+    *nix = 1;
+    *niy = 1;
+    return PF_OK;
+  }
+  int ix, iy;
+  if (h->np > 0) {
+    u64 init[4] = {0ull, ~0ull, 0ull, ~0ull};
+    u64 *d = (u64 *)h->d_red;
+    PF_CUDA(cudaMemcpyAsync(d, init, sizeof(init), cudaMemcpyHostToDevice, h->stream));
+    k_minmax_xy<<<std::min<unsigned>(grid_for(h->np, 256), 4096), 256, 0, h->stream>>>(
+        h->y[h->cur][0], h->y[h->cur][1], h->np, d);
+    PF_LAUNCHED(h);
+    u64 r[4];
+    PF_CUDA(cudaMemcpyAsync(r, d, sizeof(r), cudaMemcpyDeviceToHost, h->stream));
+    PF_CUDA(cudaStreamSynchronize(h->stream));
+    auto unkey = [](u64 k) {
+      u64 b = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+      double v;
+      memcpy(&v, &b, sizeof(v));
+      return v;
+    };
+    double smaxx = fabs(unkey(r[0])), sminx = fabs(unkey(r[1]));
+    double smaxy = fabs(unkey(r[2])), sminy = fabs(unkey(r[3]));
+    long imaxx = (long)ceil(smaxx / p.dx), iminx = (long)floor(sminx / p.dx);
+    long imaxy = (long)ceil(smaxy / p.dy), iminy = (long)floor(sminy / p.dy);
+    ix = (int)((std::max(imaxx, iminx) + 3) * 2);
+    iy = (int)((std::max(imaxy, iminy) + 3) * 2);
+  } else {
+    ix = iy = 2;
+  }
+  if ((p.nx % 2) != (ix % 2)) ix += 1;
+  if ((p.ny % 2) != (iy % 2)) iy += 1;
+  if (ix > p.nx || iy > p.ny) {
+    h->err = "transverse grid not large enough for the inner window (nspinDX=" +
+             std::to_string(ix) + ", nspinDY=" + std::to_string(iy) + ")";
+    return PF_OUT_OF_WINDOW;
+  }
+  *nix = ix;
+  *niy = iy;
+  return PF_OK;
+}
+
+static int set_window(pf_handle *h, int nix, int niy) {
+  int rc = pf_inner_to_outer(h);
+  if (rc) return rc;
+  h->window_valid = false;
+  rc = alloc_window(h, nix, niy);
+  if (rc) return rc;
+  return pf_outer_to_inner(h);
+}
+
+static int choose_window(pf_handle *h) {
+  int nix = h->p.nix, niy = h->p.niy;
+  if (nix <= 0 || niy <= 0) {
+    int rc = pf_window_from_particles(h, &nix, &niy);
+    if (rc) return rc;
+  }
+  if (nix > h->p.nx || niy > h->p.ny || nix < 1 || niy < 1) {
+    h->err = "inner window larger than the mesh";
+    return PF_BAD_ARG;
+  }
+  return set_window(h, nix, niy);
+}
+
+static int status_to_rc(unsigned int st) {
+  if (st & ST_OVERFLOW) return PF_OVERFLOW;
+  if (st & ST_OUT_OF_Z2) return PF_OUT_OF_Z2;
+  if (st & ST_OUT_OF_WINDOW) return PF_OUT_OF_WINDOW;
+  return PF_OK;
+}
+
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int pf_abi_version(void) { return PUFFGPU_ABI_VERSION; }
+
+void pf_default_params(pf_params *p) {
+  memset(p, 0, sizeof(*p));
+  p->rho = 0.01;
+  p->aw = 1.0;
+  p->gamma_r = 100.0;
+  p->fx = 1.0;
+  p->fy = 1.0;
+  p->szfe = 1.0e30;
+  p->n2col0 = 1.0;
+  p->dx = p->dy = p->dz2 = 1.0;
+  p->sbeta = 1.0;
+  p->sfilt_frac = (double)0.3f;
+  p->sperwaves = -1.0;
+  p->und_type = PF_UND_PUFFIN;
+  p->mesh_type = PF_MESH_TEMPORAL;
+  p->nx = p->ny = 1;
+  p->nz2 = 2;
+  p->nbx = p->nby = 16;
+  p->nbz2 = 37;
+  p->field_evolve = p->electrons_evolve = p->coupling = 1;
+  p->qfilter = 1;
+  p->redist_every = 60;
+  p->precision = PF_FP64;
+}
+
+const char *pf_last_error(const pf_handle *h) { return h ? h->err.c_str() : g_err.c_str(); }
+
+int pf_create(const pf_params *p, pf_handle **out) {
+  if (!p || !out) return PF_BAD_ARG;
+  *out = nullptr;
+  if (p->nx < 1 || p->ny < 1 || p->nz2 < 2 || p->dz2 <= 0.0 || p->dx <= 0.0 || p->dy <= 0.0 ||
+      p->rho <= 0.0 || p->eta <= 0.0 || p->gamma_r <= 0.0) {
+    g_err = "pf_create: invalid mesh or physics constants";
+    return PF_BAD_ARG;
+  }
+  if (p->one_d && (p->nx != 1 || p->ny != 1)) {
+    g_err = "pf_create: one_d requires nx = ny = 1";
+    return PF_BAD_ARG;
+  }
+  if (p->precision != PF_FP64) {
+    g_err = "pf_create: only the FP64 path is built in this library";
+    return PF_BAD_ARG;
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    g_err = "pf_create: no CUDA device";
+    return PF_NO_DEVICE;
+  }
+  if (p->device < 0 || p->device >= ndev) {
+    g_err = "pf_create: bad device ordinal";
+    return PF_BAD_ARG;
+  }
+  pf_handle *h = new pf_handle();
+  h->p = *p;
+  h->dev = p->device;
+  h->n2col = p->n2col0;
+  h->n2col0 = p->n2col0;
+  h->undgrad = p->undgrad;
+  h->npl = (p->mesh_type == PF_MESH_PERIODIC) ? p->nz2 - 1 : p->nz2;
+  h->nouter = (int64_t)p->nx * p->ny * p->nz2;
+  auto fail = [&](cudaError_t e, const char *what) {
+    g_err = std::string("pf_create: ") + what + ": " + cudaGetErrorString(e);
+    pf_destroy(h);
+    return PF_CUDA_ERR;
+  };
+  cudaError_t e;
+  if ((e = cudaSetDevice(h->dev)) != cudaSuccess) return fail(e, "cudaSetDevice");
+  if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess)
+    return fail(e, "stream");
+  h->own_stream = true;
+  if ((e = cudaMalloc(&h->d_status, 64)) != cudaSuccess) return fail(e, "status");
+  if ((e = cudaMalloc(&h->d_red, 64)) != cudaSuccess) return fail(e, "reduction scratch");
+  if ((e = cudaMallocHost(&h->h_status, 64)) != cudaSuccess) return fail(e, "pinned status");
+  if ((e = cudaMalloc(&h->or_, sizeof(double) * h->nouter)) != cudaSuccess) return fail(e, "field");
+  if ((e = cudaMalloc(&h->oi_, sizeof(double) * h->nouter)) != cudaSuccess) return fail(e, "field");
+  cudaMemsetAsync(h->or_, 0, sizeof(double) * h->nouter, h->stream);
+  cudaMemsetAsync(h->oi_, 0, sizeof(double) * h->nouter, h->stream);
+  cudaMemsetAsync(h->d_status, 0, 64, h->stream);
+  if ((e = cudaStreamSynchronize(h->stream)) != cudaSuccess) return fail(e, "sync");
+  *out = h;
+  return PF_OK;
+}
+
+int pf_destroy(pf_handle *h) {
+  if (!h) return PF_OK;
+  cudaSetDevice(h->dev);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  pf_prof_flush(h);
+  for (ProfEvent &e : h->prof_pool) {
+    cudaEventDestroy(e.a);
+    cudaEventDestroy(e.b);
+  }
+  free_particles(h);
+  free_window(h);
+  pf_diff_destroy(h->diff);
+  cudaFree(h->or_);
+  cudaFree(h->oi_);
+  cudaFree(h->d_status);
+  cudaFree(h->d_red);
+  if (h->h_status) cudaFreeHost(h->h_status);
+  if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return PF_OK;
+}
+
+static int set_particles_impl(pf_handle *h, int64_t n, const double *const src[7],
+                              cudaMemcpyKind kind) {
+  if (!h || n < 0) return PF_BAD_ARG;
+  for (int j = 0; j < 7; ++j)
+    if (n > 0 && !src[j]) return PF_BAD_ARG;
+  cudaSetDevice(h->dev);
+  int rc = alloc_particles(h, n);
+  if (rc) return rc;
+  h->np = n;
+  const size_t b = sizeof(double) * (size_t)n;
+  if (n > 0) {
+    for (int j = 0; j < 6; ++j)
+      PF_CUDA(cudaMemcpyAsync(h->y[h->cur][j], src[j], b, kind, h->stream));
+    PF_CUDA(cudaMemcpyAsync(h->chi, src[6], b, kind, h->stream));
+  }
+  // fixed-point scale of the deposit from max |chi| / dV3
+  double chimax = 0.0;
+  if (n > 0) {
+    u64 *d = (u64 *)h->d_red;
+    PF_CUDA(cudaMemsetAsync(d, 0, sizeof(u64), h->stream));
+    k_absmax<<<std::min<unsigned>(grid_for(n, 256), 4096), 256, 0, h->stream>>>(h->chi, n, d);
+    PF_LAUNCHED(h);
+    u64 r;
+    PF_CUDA(cudaMemcpyAsync(&r, d, sizeof(r), cudaMemcpyDeviceToHost, h->stream));
+    PF_CUDA(cudaStreamSynchronize(h->stream));
+    memcpy(&chimax, &r, sizeof(r));
+  }
+  h->chi_max = chimax;
+  int lg = 0;
+  while ((int64_t(1) << lg) < 2 * n + 2) ++lg;
+  h->fix_maxexp = 126 - lg;
+  const double smax = chimax / (h->p.dx * h->p.dy * h->p.dz2);
+  const int e_s = (smax > 0.0 && isfinite(smax)) ? ilogb(smax) + 1 : 0;
+  h->fix_e = h->fix_maxexp - 16 - e_s;
+  return choose_window(h);
+}
+
+int pf_set_particles(pf_handle *h, int64_t n, const double *x, const double *y,
+                     const double *z2, const double *px, const double *py,
+                     const double *gam, const double *chi) {
+  const double *s[7] = {x, y, z2, px, py, gam, chi};
+  return set_particles_impl(h, n, s, cudaMemcpyHostToDevice);
+}
+
+int pf_set_particles_dev(pf_handle *h, int64_t n, const double *x, const double *y,
+                         const double *z2, const double *px, const double *py,
+                         const double *gam, const double *chi) {
+  const double *s[7] = {x, y, z2, px, py, gam, chi};
+  return set_particles_impl(h, n, s, cudaMemcpyDeviceToDevice);
+}
+
+static int get_particles_impl(pf_handle *h, double *const dst[7], cudaMemcpyKind kind) {
+  if (!h) return PF_BAD_ARG;
+  cudaSetDevice(h->dev);
+  const size_t b = sizeof(double) * (size_t)h->np;
+  if (h->np > 0) {
+    for (int j = 0; j < 6; ++j)
+      if (dst[j]) PF_CUDA(cudaMemcpyAsync(dst[j], h->y[h->cur][j], b, kind, h->stream));
+    if (dst[6]) PF_CUDA(cudaMemcpyAsync(dst[6], h->chi, b, kind, h->stream));
+  }
+  PF_CUDA(cudaStreamSynchronize(h->stream));
+  return PF_OK;
+}
+
+int pf_get_particles(pf_handle *h, double *x, double *y, double *z2, double *px, double *py,
+                     double *gam, double *chi) {
+  double *d[7] = {x, y, z2, px, py, gam, chi};
+  return get_particles_impl(h, d, cudaMemcpyDeviceToHost);
+}
+
+int pf_get_particles_dev(pf_handle *h, double *x, double *y, double *z2, double *px, double *py,
+                         double *gam, double *chi) {
+  double *d[7] = {x, y, z2, px, py, gam, chi};
+  return get_particles_impl(h, d, cudaMemcpyDeviceToDevice);
+}
+
+int64_t pf_num_particles(const pf_handle *h) { return h ? h->np : -1; }
+
+static int set_field_impl(pf_handle *h, const double *re, const double *im, cudaMemcpyKind kind) {
+  if (!h || !re || !im) return PF_BAD_ARG;
+  cudaSetDevice(h->dev);
+  const size_t b = sizeof(double) * (size_t)h->nouter;
+  PF_CUDA(cudaMemcpyAsync(h->or_, re, b, kind, h->stream));
+  PF_CUDA(cudaMemcpyAsync(h->oi_, im, b, kind, h->stream));
+  if (h->p.mesh_type == PF_MESH_PERIODIC) {  // pupd8: the head plane wins
+    const int64_t plane = (int64_t)h->p.nx * h->p.ny;
+    k_mirror_plane<<<grid_for(plane, 256), 256, 0, h->stream>>>(h->or_, h->oi_, plane, h->p.nz2);
+    PF_LAUNCHED(h);
+  }
+  if (h->nwin > 0) {
+    int rc = pf_outer_to_inner(h);
+    if (rc) return rc;
+  }
+  PF_CUDA(cudaStreamSynchronize(h->stream));
+  return PF_OK;
+}
+
+int pf_set_field(pf_handle *h, const double *re, const double *im) {
+  return set_field_impl(h, re, im, cudaMemcpyHostToDevice);
+}
+int pf_set_field_dev(pf_handle *h, const double *re, const double *im) {
+  return set_field_impl(h, re, im, cudaMemcpyDeviceToDevice);
+}
+
+static int get_field_impl(pf_handle *h, double *re, double *im, cudaMemcpyKind kind) {
+  if (!h || !re || !im) return PF_BAD_ARG;
+  cudaSetDevice(h->dev);
+  int rc = pf_inner_to_outer(h);
+  if (rc) return rc;
+  const size_t b = sizeof(double) * (size_t)h->nouter;
+  PF_CUDA(cudaMemcpyAsync(re, h->or_, b, kind, h->stream));
+  PF_CUDA(cudaMemcpyAsync(im, h->oi_, b, kind, h->stream));
+  PF_CUDA(cudaStreamSynchronize(h->stream));
+  return PF_OK;
+}
+
+int pf_get_field(pf_handle *h, double *re, double *im) {
+  return get_field_impl(h, re, im, cudaMemcpyDeviceToHost);
+}
+int pf_get_field_dev(pf_handle *h, double *re, double *im) {
+  return get_field_impl(h, re, im, cudaMemcpyDeviceToDevice);
+}
+
+int pf_set_taper(pf_handle *h, double n2col, double n2col0, double undgrad) {
+  if (!h) return PF_BAD_ARG;
+  h->n2col = n2col;
+  h->n2col0 = n2col0;
+  h->undgrad = undgrad;
+  return PF_OK;
+}
+
+int pf_get_taper(const pf_handle *h, double *n2col, double *n2col0, double *undgrad) {
+  if (!h) return PF_BAD_ARG;
+  if (n2col) *n2col = h->n2col;
+  if (n2col0) *n2col0 = h->n2col0;
+  if (undgrad) *undgrad = h->undgrad;
+  return PF_OK;
+}
+
+int pf_get_window(const pf_handle *h, int32_t *nix, int32_t *niy) {
+  if (!h) return PF_BAD_ARG;
+  if (nix) *nix = h->nix;
+  if (niy) *niy = h->niy;
+  return PF_OK;
+}
+
+int pf_rk4_step(pf_handle *h, double szl, double hstep) {
+  if (!h) return PF_BAD_ARG;
+  if (h->nwin == 0 || h->cap == 0) {
+    h->err = "pf_rk4_step: particles not set";
+    return PF_STATE;
+  }
+  cudaSetDevice(h->dev);
+  unsigned int st = 0;
+  int rc = pf_rk4_fp64(h, szl, hstep, &st);
+  if (rc) return rc;
+  rc = status_to_rc(st);
+  if (rc == PF_OUT_OF_Z2) h->err = "a macroparticle's z2 node lies outside the temporal mesh";
+  if (rc == PF_OUT_OF_WINDOW) h->err = "a macroparticle left the inner transverse window";
+  if (rc == PF_OVERFLOW) h->err = "deposit contribution beyond the fixed-point range";
+  return rc;
+}
+
+int pf_wrap_z2(pf_handle *h) {
+  if (!h) return PF_BAD_ARG;
+  if (h->p.mesh_type != PF_MESH_PERIODIC || h->np == 0) return PF_OK;
+  cudaSetDevice(h->dev);
+  const double lenz2 = h->p.dz2 * (double)(h->p.nz2 - 1);
+  k_wrap_z2<<<grid_for(h->np, 256), 256, 0, h->stream>>>(h->y[h->cur][2], h->np, lenz2);
+  PF_LAUNCHED(h);
+  return PF_OK;
+}
+
+int pf_redistribute(pf_handle *h) {
+  if (!h) return PF_BAD_ARG;
+  cudaSetDevice(h->dev);
+  int rc = pf_inner_to_outer(h);
+  if (rc) return rc;
+  int nix, niy;
+  rc = pf_window_from_particles(h, &nix, &niy);
+  if (rc) return rc;
+  rc = pf_wrap_z2(h);
+  if (rc) return rc;
+  h->window_valid = false;
+  rc = alloc_window(h, nix, niy);
+  if (rc) return rc;
+  rc = pf_outer_to_inner(h);
+  if (rc) return rc;
+  PF_CUDA(cudaStreamSynchronize(h->stream));
+  return PF_OK;
+}
+
+int pf_diffract(pf_handle *h, double dz) {
+  if (!h) return PF_BAD_ARG;
+  cudaSetDevice(h->dev);
+  int rc = pf_inner_to_outer(h);
+  if (rc) return rc;
+  rc = pf_diffract_outer(h, dz);
+  if (rc) return rc;
+  if (h->nwin > 0) {
+    rc = pf_outer_to_inner(h);
+    if (rc) return rc;
+  }
+  PF_CUDA(cudaStreamSynchronize(h->stream));
+  pf_prof_flush(h);
+  return PF_OK;
+}
+
+int pf_run(pf_handle *h, int32_t nsteps, int32_t isteps4diff, int32_t qdiffraction,
+           double hstep, double *szl, int32_t *steps_done) {
+  if (!h || !szl || nsteps < 0 || (qdiffraction && isteps4diff < 1)) return PF_BAD_ARG;
+  if (steps_done) *steps_done = 0;
+  cudaSetDevice(h->dev);
+  double dzds = 0.0;
+  int rc;
+  if (qdiffraction) {
+    dzds = (double)isteps4diff * hstep / 2.0;
+    rc = pf_diffract(h, dzds);
+    if (rc) return rc;
+  }
+  const int redist = h->p.redist_every > 0 ? h->p.redist_every : 60;
+  for (int istep = 1; istep <= nsteps; ++istep) {
+    int tries = 0;
+    for (;;) {
+      rc = pf_rk4_step(h, *szl, hstep);
+      if (rc == PF_OK) break;
+      if (rc != PF_OUT_OF_WINDOW || ++tries > 3) return rc;
+      rc = pf_redistribute(h);  // getInNode + getLocalFieldIndices
+      if (rc) return rc;
+    }
+    *szl = *szl + hstep;
+    if (qdiffraction && (istep % isteps4diff == 0 || istep == nsteps)) {
+      double dzdf = dzds;
+      if (istep == nsteps) dzds = 0.0;
+      else if (istep + isteps4diff <= nsteps) dzds = (double)isteps4diff * hstep / 2;
+      else dzds = (double)(nsteps - istep) * hstep / 2;
+      rc = pf_diffract(h, dzdf + dzds);
+      if (rc) return rc;
+    }
+    if (istep % redist == 0) {
+      rc = pf_wrap_z2(h);
+      if (rc) return rc;
+    }
+    if (steps_done) *steps_done = istep;
+  }
+  PF_CUDA(cudaStreamSynchronize(h->stream));
+  return PF_OK;
+}
+
+int pf_sync(pf_handle *h) {
+  if (!h) return PF_BAD_ARG;
+  cudaSetDevice(h->dev);
+  PF_CUDA(cudaStreamSynchronize(h->stream));
+  return PF_OK;
+}
+
+int64_t pf_kernel_launches(const pf_handle *h) { return h ? h->launches : -1; }
+
+void *pf_get_stream(const pf_handle *h) { return h ? (void *)h->stream : nullptr; }
+
+int pf_profile(pf_handle *h, int32_t enable) {
+  if (!h) return PF_BAD_ARG;
+  cudaSetDevice(h->dev);
+  PF_CUDA(cudaStreamSynchronize(h->stream));
+  pf_prof_flush(h);
+  for (int c = 0; c < PROF_N; ++c) {
+    h->prof_ms[c] = 0.0;
+    h->prof_n[c] = 0;
+  }
+  h->prof = enable != 0;
+  return PF_OK;
+}
+
+int pf_profile_read(pf_handle *h, int32_t cls, double *ms_total, int64_t *launches) {
+  if (!h || cls < 0 || cls >= PROF_N) return PF_BAD_ARG;
+  cudaSetDevice(h->dev);
+  PF_CUDA(cudaStreamSynchronize(h->stream));
+  pf_prof_flush(h);
+  if (ms_total) *ms_total = h->prof_ms[cls];
+  if (launches) *launches = h->prof_n[cls];
+  return PF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,183 @@
+// Internal declarations shared by the puffgpu translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/puffgpu.h"
+
+// Puffin's global pi is a default-kind (single precision) literal
+// (puffin/lib/common/puffin_constants.f90:22).  GetKValues uses its own
+// full-precision pi (transforms.f90:492).
+#define PF_PUFFIN_PI ((double)3.14159265358979323846f)
+#define PF_FULL_PI 3.14159265358979323846
+
+// Device status word bits (one word per handle, OR-ed by the kernels).
+enum : unsigned int {
+  ST_OUT_OF_WINDOW = 1u,
+  ST_OUT_OF_Z2 = 2u,
+  ST_OVERFLOW = 4u,
+};
+
+// Undulator b-field coefficients for one RK4 stage.  Every stage-uniform
+// sub-expression of bfields.f90 is evaluated once on the host, left to right
+// as the Fortran writes it, so the per-particle remainder keeps the
+// reference's operation order.
+struct BFieldCoef {
+  int type;      // pf_und_type
+  int place;     // 0 start, 1 main, 2 end
+  int one_d;
+  int focusing;
+  int tcase;     // helical/puffin start/end: 0 none, 1 use ux, 2 use c1x (7*pi*rho side)
+  double bx0, by0;        // x/y-independent parts of bx, by
+  double focx, focy;      // strong-focusing coefficients
+  double S, C;            // sin/cos of the section's phase argument
+  double c1;              // sqrt(eta)/2/rho
+  double ux, uy;          // start/end section coefficients of x and y
+  double u3;              // planepole/curved section factor
+  double fx, fy;
+  double kx, ky, kxky, czs, cze;  // curved-pole constants
+  double szt;             // phase argument (curved start, per-particle division)
+};
+
+// Everything a stage kernel needs, passed by value.
+struct StageArgs {
+  // particle arrays
+  const double *x, *y, *z2, *px, *py, *gam, *chi;
+  const double *kin[6];   // derivative used to form the stage state (stage > 1)
+  double *kout[6];        // derivative written by this stage
+  double *kacc[6];        // k2 (stage 2 out) / k2+k3 (stage 3 in/out) / read (stage 4)
+  const double *k1[6];    // stage 4: k1
+  double *ynext[6];       // stage 4: committed state
+  int64_t np;
+  double cstate;          // state = y + cstate * kin
+  double h6;
+  // field (inner window)
+  const double *ar, *ai;  // stage field A_s
+  unsigned long long *acc_lo_r, *acc_hi_r, *acc_lo_i, *acc_hi_i;
+  int64_t nix, niy, npl;  // window dims and planes held
+  int64_t nz2;
+  int periodic;
+  int one_d;
+  double dx, dy, dz2, halfx, halfy, dV3;
+  // physics
+  double eta, kappa, rho, gamma_r, aw, n2col, sInv2rho, dxc, k2;
+  int field_evolve, electrons_evolve, coupling;
+  int fix_e;              // fixed-point scale exponent of the deposit
+  int fix_maxexp;         // overflow guard: |contribution * 2^E| < 2^fix_maxexp
+  BFieldCoef bf;
+  unsigned int *status;
+};
+
+struct NodeArgs {
+  int64_t n;                  // window nodes
+  unsigned long long *acc_lo_r, *acc_hi_r, *acc_lo_i, *acc_hi_i;
+  double *wr, *wi;            // window field state (ac_rfield_in)
+  double *asr, *asi;          // stage field
+  double *d0r, *d0i;          // k1 of the field
+  double *d12r, *d12i;        // k2 (then k2+k3) of the field
+  double coef;                // hh or h
+  double h6;
+  int fix_e;
+  const unsigned int *status;
+};
+
+struct DiffPlan;  // FFT plan (fft.cu)
+
+enum { PROF_STAGE = 0, PROF_NODES = 1, PROF_FFT = 2, PROF_DIFF = 3, PROF_OTHER = 4, PROF_N = 5 };
+
+struct ProfEvent {
+  cudaEvent_t a, b;
+  int cls;
+};
+
+struct pf_handle {
+  pf_params p;
+  int dev = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::string err;
+  int64_t launches = 0;
+
+  // particles
+  int64_t np = 0;
+  int64_t cap = 0;
+  double *y[2][6] = {};       // double-buffered x, y, z2, px, py, gamma
+  int cur = 0;
+  double *chi = nullptr;
+  double *k1[6] = {}, *ka[6] = {}, *kb[6] = {};
+  int fix_e = 0, fix_maxexp = 126;
+  double chi_max = 0.0;
+
+  // field
+  int64_t nouter = 0;         // nx*ny*nz2
+  double *or_ = nullptr, *oi_ = nullptr;   // outer mesh
+  int nix = 0, niy = 0;       // window
+  int64_t npl = 0;            // planes held in the window (nz2 or nz2-1)
+  int64_t nwin = 0, wcap = 0;
+  double *wr = nullptr, *wi = nullptr;     // window field state
+  double *asr = nullptr, *asi = nullptr;   // stage field
+  double *d0r = nullptr, *d0i = nullptr, *d12r = nullptr, *d12i = nullptr;
+  unsigned long long *acc = nullptr;       // 4 * wcap words
+  bool window_valid = false;  // window holds the outer mesh's current values
+
+  // taper state
+  double n2col = 1.0, n2col0 = 1.0, undgrad = 0.0;
+
+  // device scalars
+  unsigned int *d_status = nullptr;
+  double *d_red = nullptr;    // reduction scratch (window search)
+  unsigned int *h_status = nullptr;  // pinned
+
+  DiffPlan *diff = nullptr;
+
+  // optional per-kernel-class timing
+  bool prof = false;
+  std::vector<ProfEvent> prof_pending;
+  std::vector<ProfEvent> prof_pool;
+  double prof_ms[PROF_N] = {};
+  int64_t prof_n[PROF_N] = {};
+  int prof_open = -1;
+};
+
+// Record the start/end of a timed launch of class cls (no-op when disabled).
+void pf_prof_begin(pf_handle *h, int cls);
+void pf_prof_end(pf_handle *h);
+// Accumulate the elapsed times of completed launches (after a stream sync).
+void pf_prof_flush(pf_handle *h);
+
+// fp64 RK4 step on the device; returns the device status word.
+int pf_rk4_fp64(pf_handle *h, double szl, double hstep, unsigned int *status_out);
+// window management
+int pf_window_from_particles(pf_handle *h, int *nix, int *niy);
+int pf_outer_to_inner(pf_handle *h);
+int pf_inner_to_outer(pf_handle *h);
+// diffraction
+int pf_diffract_outer(pf_handle *h, double dz);
+void pf_diff_destroy(DiffPlan *d);
+
+void pf_stage_coefficients(const pf_params &p, double sz, double n2col, int place,
+                           BFieldCoef *bf);
+void pf_taper_stage(pf_handle *h, double sz, double *n2col, int *place);
+
+#define PF_CUDA(call)                                                     \
+  do {                                                                    \
+    cudaError_t e_ = (call);                                              \
+    if (e_ != cudaSuccess) {                                              \
+      h->err = std::string(#call) + ": " + cudaGetErrorString(e_);        \
+      return PF_CUDA_ERR;                                                 \
+    }                                                                     \
+  } while (0)
+
+#define PF_LAUNCHED(h)                                                    \
+  do {                                                                    \
+    (h)->launches++;                                                      \
+    cudaError_t e_ = cudaGetLastError();                                  \
+    if (e_ != cudaSuccess) {                                              \
+      (h)->err = std::string("kernel launch: ") + cudaGetErrorString(e_); \
+      return PF_CUDA_ERR;                                                 \
+    }                                                                     \
+  } while (0)

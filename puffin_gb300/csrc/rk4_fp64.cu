@@ -1,0 +1,607 @@
+// FP64 RK4 macroparticle push: one fused kernel per RK4 stage (state
+// update + p2 + trilinear weights + gather + deposit + b-fields + equations)
+// and one node kernel per stage over the inner-window field.
+//
+// Reference: rk4par (puffin/lib/interaction/puffin_mpi_RK4.f90:142-328),
+// getrhs (rhs.f90:60-330), getInterps_3D / getFFelecs_3D / getSource_3D
+// (system_interpolation.f90:25-248) and their 1D forms
+// (system_interpolation_1D.f90:24-179), getP2 (gamma_to_p2.f90:84-85),
+// the six equations (puffin_equations.f90:17-176), bfields.f90.
+//
+// Deposit: every contribution w_c * s is converted exactly (truncation at
+// 2^-E) to a 128-bit fixed-point integer and added with two 64-bit integer
+// atomics (low word, then high word plus the low word's carry).  Integer
+// addition is associative, so dA/dz is bit-identical run to run whatever the
+// order in which the atomics land; the reference's OpenMP atomics
+// (system_interpolation.f90:174-241) are not.
+#include <math.h>
+#include <string.h>
+
+#include "pf_internal.h"
+
+namespace {
+
+typedef unsigned long long u64;
+
+__device__ __forceinline__ void bfield(const BFieldCoef &b, double x, double y,
+                                       double &bx, double &by, double &bz) {
+  const double pi = PF_PUFFIN_PI;
+  bx = b.bx0;
+  by = b.by0;
+  bz = 0.0;
+  if (b.type == PF_UND_CURVED) {
+    double shx = sinh(b.kx * x), shy = sinh(b.ky * y);
+    double chx = cosh(b.kx * x), chy = cosh(b.ky * y);
+    if (b.place == 0) {
+      bx = b.kxky * shx * shy * b.szt / 4.0 / pi * b.S;
+      by = chx * chy * b.szt / 4.0 / pi * b.S;
+      bz = b.czs * chx * shy * b.u3 * b.C;
+    } else if (b.place == 2) {
+      bx = b.kxky * shx * shy * b.u3 * b.S;
+      by = chx * chy * b.u3 * b.S;
+      bz = b.cze * chx * shy * b.u3 * b.C;
+    } else {
+      bx = b.kxky * shx * shy * b.S;
+      by = chx * chy * b.S;
+      bz = b.cze * chx * shy * b.C;
+    }
+    if (b.one_d) bz = 0.0;
+  } else if (b.type == PF_UND_PLANEPOLE) {
+    if (!b.one_d) {
+      double sh = sinh(b.c1 * y);
+      bz = (b.place == 1) ? sh * b.C : sh * b.u3 * b.C;
+    }
+  } else if (!b.one_d) {
+    const bool hel = (b.type == PF_UND_HELICAL);
+    if (b.place == 1) {
+      bz = hel ? b.c1 * (-(x * b.S) + y * b.C)
+               : b.c1 * (-(b.fx * x * b.S) + b.fy * y * b.C);
+    } else {
+      double t = (b.tcase == 0) ? 0.0 : -(b.ux * x * b.S);
+      bz = t + b.uy * y * b.C;
+    }
+  }
+  if (b.focusing) {
+    bx = b.focx * y + bx;
+    by = -(b.focy * x) + by;
+  }
+}
+
+// Exact conversion of c * 2^E (truncated toward zero) to a two's-complement
+// 128-bit integer (hi:lo).  Returns false when |c * 2^E| >= 2^maxexp.
+__device__ __forceinline__ bool to_fix(double c, int E, int maxexp, u64 &lo, u64 &hi) {
+  u64 b = (u64)__double_as_longlong(c);
+  int ex = (int)((b >> 52) & 0x7ffull);
+  lo = 0;
+  hi = 0;
+  if (ex == 0) return true;             // zero or subnormal: below resolution
+  if (ex == 0x7ff) return false;        // inf / nan
+  u64 m = (b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+  int s = ex - 1075 + E;                // |c| * 2^E = m * 2^s
+  if (s + 53 > maxexp) return false;
+  if (s >= 64) {
+    hi = m << (s - 64);
+  } else if (s > 0) {
+    lo = m << s;
+    hi = m >> (64 - s);
+  } else if (s == 0) {
+    lo = m;
+  } else if (s > -53) {
+    lo = m >> (-s);
+  } else {
+    return true;
+  }
+  if (b >> 63) {                         // negate
+    u64 nlo = ~lo + 1ull;
+    hi = ~hi + (lo == 0 ? 1ull : 0ull);
+    lo = nlo;
+  }
+  return true;
+}
+
+__device__ __forceinline__ void fix_add(u64 *lo_arr, u64 *hi_arr, int64_t n, u64 lo, u64 hi) {
+  if (lo == 0 && hi == 0) return;
+  u64 old = atomicAdd(lo_arr + n, lo);
+  u64 carry = (old + lo < old) ? 1ull : 0ull;
+  u64 add = hi + carry;
+  if (add != 0) atomicAdd(hi_arr + n, add);
+}
+
+__device__ __forceinline__ double fix_to_double(u64 lo, u64 hi, double inv_scale) {
+  bool neg = (long long)hi < 0;
+  if (neg) {
+    u64 nlo = ~lo + 1ull;
+    hi = ~hi + (lo == 0 ? 1ull : 0ull);
+    lo = nlo;
+  }
+  double v = __ull2double_rn(hi) * 18446744073709551616.0 + __ull2double_rn(lo);
+  v = v * inv_scale;
+  return neg ? -v : v;
+}
+
+template <int STAGE, bool ONED>
+__global__ void __launch_bounds__(256) k_stage(const StageArgs a) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.np) return;
+  if (*((volatile unsigned int *)a.status) != 0u) return;
+
+  const double y0[6] = {a.x[i], a.y[i], a.z2[i], a.px[i], a.py[i], a.gam[i]};
+  double s[6];
+  double kin[6];
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    if (STAGE > 1) {
+      kin[j] = a.kin[j][i];
+      s[j] = y0[j] + a.cstate * kin[j];
+    } else {
+      kin[j] = 0.0;
+      s[j] = y0[j];
+    }
+  }
+  const double X = s[0], Y = s[1], Z2 = s[2], PX = s[3], PY = s[4], G = s[5];
+  const double chi = a.chi[i];
+
+  // getP2 (gamma_to_p2.f90:84-85)
+  const double aa = 1.0 / (a.gamma_r * (G * G));   // a.gamma_r holds gamma0**2
+  const double bb = 1.0 + a.aw * ((PX * PX) + (PY * PY));  // a.aw holds aw**2
+  const double p2 = ((1.0 / sqrt(1.0 - aa * bb)) - 1.0) / a.eta;
+  const double q = 1.0 + a.eta * p2;
+
+  // interpolation (getInterps_3D / getInterps_1D)
+  double w[8];
+  int64_t node[8];
+  bool ok = true;
+  {
+    const double z2n = floor(Z2 / a.dz2) + 1.0;
+    const double locz2 = Z2 - (z2n - 1.0) * a.dz2;
+    int64_t pz0 = 0, pz1 = 0;
+    if (a.periodic) {
+      if (!(fabs(z2n) < 9.0e15)) {
+        ok = false;
+        atomicOr(a.status, ST_OUT_OF_Z2);
+      } else {
+        int64_t m = ((int64_t)z2n - 1) % a.npl;
+        if (m < 0) m += a.npl;
+        pz0 = m;
+        pz1 = (m + 1 == a.npl) ? 0 : m + 1;
+      }
+    } else {
+      if (!(z2n >= 1.0 && z2n < (double)a.nz2)) {
+        ok = false;
+        atomicOr(a.status, ST_OUT_OF_Z2);
+      } else {
+        pz0 = (int64_t)z2n - 1;
+        pz1 = pz0 + 1;
+      }
+    }
+    if (ONED) {
+      const double w1 = (1.0 - locz2 / a.dz2);
+      w[0] = w1;
+      w[1] = 1.0 - w1;
+      node[0] = pz0;
+      node[1] = pz1;
+    } else {
+      const double xn = floor((X + a.halfx) / a.dx) + 1.0;
+      const double locx = X + a.halfx - (xn - 1.0) * a.dx;
+      const double x2 = locx / a.dx, x1 = 1.0 - x2;
+      const double yn = floor((Y + a.halfy) / a.dy) + 1.0;
+      const double locy = Y + a.halfy - (yn - 1.0) * a.dy;
+      const double y2 = locy / a.dy, y1 = 1.0 - y2;
+      const double zw2 = locz2 / a.dz2, zw1 = 1.0 - zw2;
+      if (!(xn >= 1.0 && xn < (double)a.nix && yn >= 1.0 && yn < (double)a.niy)) {
+        ok = false;
+        atomicOr(a.status, ST_OUT_OF_WINDOW);
+      }
+      const int64_t ntr = a.nix * a.niy;
+      const int64_t ix = ok ? (int64_t)xn - 1 : 0, iy = ok ? (int64_t)yn - 1 : 0;
+      const int64_t b0 = ix + iy * a.nix + pz0 * ntr, b1 = ix + iy * a.nix + pz1 * ntr;
+      w[0] = x1 * y1 * zw1;
+      w[1] = x2 * y1 * zw1;
+      w[2] = x1 * y2 * zw1;
+      w[3] = x2 * y2 * zw1;
+      w[4] = x1 * y1 * zw2;
+      w[5] = x2 * y1 * zw2;
+      w[6] = x1 * y2 * zw2;
+      w[7] = x2 * y2 * zw2;
+      node[0] = b0;
+      node[1] = b0 + 1;
+      node[2] = b0 + a.nix;
+      node[3] = b0 + a.nix + 1;
+      node[4] = b1;
+      node[5] = b1 + 1;
+      node[6] = b1 + a.nix;
+      node[7] = b1 + a.nix + 1;
+    }
+  }
+  constexpr int NC = ONED ? 2 : 8;
+
+  // gather (getFFelecs)
+  double fr = 0.0, fi = 0.0;
+  if (ok) {
+    fr = w[0] * __ldg(a.ar + node[0]);
+    fi = w[0] * __ldg(a.ai + node[0]);
+#pragma unroll
+    for (int c = 1; c < NC; ++c) {
+      fr = w[c] * __ldg(a.ar + node[c]) + fr;
+      fi = w[c] * __ldg(a.ai + node[c]) + fi;
+    }
+    // deposit (getSource)
+    if (a.field_evolve) {
+      double sr, si;
+      if (ONED) {
+        const double dw = (chi / a.dV3) * q / G;
+        sr = dw * PX;
+        si = dw * PY;
+      } else {
+        const double cq = (chi / a.dV3) * q;
+        sr = cq * PX / G;
+        si = cq * PY / G;
+      }
+      bool fits = true;
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        u64 lo, hi;
+        fits &= to_fix(w[c] * sr, a.fix_e, a.fix_maxexp, lo, hi);
+        fix_add(a.acc_lo_r, a.acc_hi_r, node[c], lo, hi);
+        fits &= to_fix(w[c] * si, a.fix_e, a.fix_maxexp, lo, hi);
+        fix_add(a.acc_lo_i, a.acc_hi_i, node[c], lo, hi);
+      }
+      if (!fits) atomicOr(a.status, ST_OVERFLOW);
+    }
+  }
+  if (!a.coupling) {
+    fr = 0.0;
+    fi = 0.0;
+  }
+
+  double k[6];
+  if (a.electrons_evolve) {
+    double bx, by, bz;
+    bfield(a.bf, X, Y, bx, by, bz);
+    const double ep = a.eta * p2 / a.k2;
+    k[2] = p2;
+    k[0] = a.dxc * q / G * PX;
+    k[1] = -(a.dxc * q / G * PY);
+    k[3] = a.sInv2rho * (a.n2col * by - ep * fr) + a.kappa * PY / G * q * a.n2col * bz;
+    k[4] = a.sInv2rho * (a.n2col * bx - ep * fi) - a.kappa * PX / G * q * a.n2col * bz;
+    k[5] = -(a.rho * q / G * 2.0 * (PX * fr + PY * fi));
+  } else {
+#pragma unroll
+    for (int j = 0; j < 6; ++j) k[j] = 0.0;
+  }
+
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    if (STAGE == 1) {
+      a.kout[j][i] = k[j];
+    } else if (STAGE == 2) {
+      a.kacc[j][i] = k[j];
+    } else if (STAGE == 3) {
+      a.kout[j][i] = k[j];
+      a.kacc[j][i] = kin[j] + k[j];
+    } else {
+      const double k1 = a.k1[j][i];
+      const double k23 = a.kacc[j][i];
+      a.ynext[j][i] = y0[j] + a.h6 * (k1 + k[j] + 2.0 * k23);
+    }
+  }
+}
+
+template <int STAGE>
+__global__ void __launch_bounds__(256) k_nodes(const NodeArgs a, const double inv_scale) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= a.n) return;
+  const double dr = fix_to_double(a.acc_lo_r[n], a.acc_hi_r[n], inv_scale);
+  const double di = fix_to_double(a.acc_lo_i[n], a.acc_hi_i[n], inv_scale);
+  a.acc_lo_r[n] = 0ull;
+  a.acc_hi_r[n] = 0ull;
+  a.acc_lo_i[n] = 0ull;
+  a.acc_hi_i[n] = 0ull;
+  const double wr = a.wr[n], wi = a.wi[n];
+  if (STAGE == 1) {
+    a.d0r[n] = dr;
+    a.d0i[n] = di;
+    a.asr[n] = wr + a.coef * dr;
+    a.asi[n] = wi + a.coef * di;
+  } else if (STAGE == 2) {
+    a.d12r[n] = dr;
+    a.d12i[n] = di;
+    a.asr[n] = wr + a.coef * dr;
+    a.asi[n] = wi + a.coef * di;
+  } else if (STAGE == 3) {
+    a.asr[n] = wr + a.coef * dr;
+    a.asi[n] = wi + a.coef * di;
+    a.d12r[n] = a.d12r[n] + dr;
+    a.d12i[n] = a.d12i[n] + di;
+  } else {
+    if (*a.status == 0u) {
+      a.wr[n] = wr + a.h6 * (a.d0r[n] + dr + 2.0 * a.d12r[n]);
+      a.wi[n] = wi + a.h6 * (a.d0i[n] + di + 2.0 * a.d12i[n]);
+    }
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+
+// getAlpha (wiggler_taper.f90:39-47) + adjUndPlace (puffin_equations.f90:218-254)
+void pf_taper_stage(pf_handle *h, double sz, double *n2col, int *place) {
+  const pf_params &p = h->p;
+  if ((sz >= p.szfs) && (sz <= p.szfe)) {
+    h->n2col = h->n2col0 + h->undgrad * (sz - p.szfs);
+  } else if (sz > p.szfe) {
+    h->n2col0 = h->n2col;
+  }
+  *n2col = h->n2col;
+  if (p.und_ends) {
+    if (sz <= p.szfs) *place = 0;
+    else if (sz >= p.szfe) *place = 2;
+    else *place = 1;
+  } else {
+    *place = 1;
+  }
+}
+
+// Stage-uniform parts of bfields.f90, evaluated left to right.
+void pf_stage_coefficients(const pf_params &p, double sz, double n2col, int place,
+                           BFieldCoef *b) {
+  (void)n2col;
+  const double pi = PF_PUFFIN_PI, rho = p.rho;
+  const double seta = sqrt(p.eta);
+  *b = BFieldCoef();
+  b->type = p.und_type;
+  b->place = place;
+  b->one_d = p.one_d;
+  b->focusing = p.focusing;
+  b->focx = seta * (p.kbysf * p.kbysf) / p.kappa;
+  b->focy = seta * (p.kbxsf * p.kbxsf) / p.kappa;
+  b->c1 = seta / 2.0 / rho;
+  b->fx = p.fx;
+  b->fy = p.fy;
+  double szt = sz / 2.0 / rho;
+  if (p.und_type == PF_UND_CURVED) {
+    b->kx = p.kx_und;
+    b->ky = p.ky_und;
+    b->kxky = p.kx_und / p.ky_und;
+    b->czs = seta / 2.0 / rho / p.ky_und;
+    b->cze = seta / 2.0 / rho / p.kx_und;
+    if (place == 0) {
+      b->szt = szt;
+      b->S = sin(szt);
+      b->C = cos(szt);
+      b->u3 = (szt / 4.0 / pi);
+    } else if (place == 2) {
+      double s = (sz - p.szfe) / 2.0 / rho;
+      b->S = sin(s);
+      b->C = cos(s);
+      b->u3 = (-s / 4.0 / pi + 1.0);
+    } else {
+      b->S = sin(szt);
+      b->C = cos(szt);
+    }
+  } else if (p.und_type == PF_UND_PLANEPOLE) {
+    b->bx0 = 0.0;
+    if (place == 0) {
+      b->by0 = szt / 4.0 / pi * sin(szt);
+      b->u3 = (szt / 4.0 / pi);
+      b->C = cos(szt);
+    } else if (place == 2) {
+      double s = (sz - p.szfe) / 2.0 / rho;
+      b->by0 = (-s / 4.0 / pi + 1.0) * sin(s);
+      b->u3 = (-s / 4.0 / pi + 1.0);
+      b->C = cos(s);
+    } else {
+      b->by0 = sin(szt);
+      b->C = cos(szt);
+    }
+  } else {
+    const bool hel = (p.und_type == PF_UND_HELICAL);
+    const double f = hel ? 1.0 : p.fx;
+    // bx
+    if (place == 0) {
+      b->bx0 = hel ? (sz - pi * rho) / (6.0 * pi * rho) * cos(szt)
+                   : f * (sz - pi * rho) / (6.0 * pi * rho) * cos(szt);
+      if (sz < pi * rho) b->bx0 = 0.0;
+      else if (sz > 7.0 * pi * rho) b->bx0 = hel ? cos(szt) : f * cos(szt);
+    } else if (place == 2) {
+      double s2 = sz - p.szfe;
+      b->bx0 = hel ? -((s2 - 7.0 * pi * rho) / (6.0 * pi * rho) * cos(s2 / 2.0 / rho))
+                   : -(f * (s2 - 7.0 * pi * rho) / (6.0 * pi * rho) * cos(s2 / 2.0 / rho));
+      if (s2 < pi * rho) b->bx0 = hel ? cos(s2 / 2.0 / rho) : f * cos(s2 / 2.0 / rho);
+      else if (s2 > 7.0 * pi * rho) b->bx0 = 0.0;
+    } else {
+      b->bx0 = hel ? cos(szt) : f * cos(szt);
+    }
+    // by
+    if (place == 0) {
+      b->by0 = hel ? szt / 4.0 / pi * sin(szt) : p.fy * szt / 4.0 / pi * sin(szt);
+    } else if (place == 2) {
+      double s = (sz - p.szfe) / 2.0 / rho;
+      b->by0 = hel ? (-s / 4.0 / pi + 1.0) * sin(s) : p.fy * (-s / 4.0 / pi + 1.0) * sin(s);
+    } else {
+      b->by0 = hel ? sin(szt) : p.fy * sin(szt);
+    }
+    // bz
+    const double c1 = b->c1;
+    if (place == 1) {
+      b->S = sin(szt);
+      b->C = cos(szt);
+    } else if (place == 0) {
+      b->S = sin(szt);
+      b->C = cos(szt);
+      if (sz < pi * rho) {
+        b->tcase = 0;
+      } else if (sz > 7.0 * pi * rho) {
+        b->tcase = 2;
+        b->ux = hel ? c1 : c1 * p.fx;
+      } else {
+        b->tcase = 1;
+        double u = c1 * (sz - pi * rho) / (6.0 * pi * rho);
+        b->ux = hel ? u : u * p.fx;
+      }
+      double uy = szt / 4.0 / pi * seta / 2.0 / rho;
+      b->uy = hel ? uy : uy * p.fy;
+    } else {
+      double s2 = sz - p.szfe;
+      b->S = sin(s2 / 2.0 / rho);
+      b->C = cos(s2 / 2.0 / rho);
+      if (s2 < pi * rho) {
+        b->tcase = 2;
+        b->ux = hel ? c1 : c1 * p.fx;
+      } else if (s2 > 7.0 * pi * rho) {
+        b->tcase = 0;
+      } else {
+        b->tcase = 1;
+        double u = c1 * (s2 - 7.0 * pi * rho) / (6.0 * pi * rho);
+        b->ux = hel ? u : u * p.fx;
+      }
+      double uy = (-(s2 / 8.0 / pi / rho) + 1.0) * seta / 2.0 / rho;
+      b->uy = hel ? uy : uy * p.fy;
+    }
+  }
+}
+
+static int launch_stage(pf_handle *h, int stage, StageArgs &a) {
+  const int threads = 256;
+  const int64_t blocks = (h->np + threads - 1) / threads;
+  if (blocks == 0) return PF_OK;
+  const bool oned = h->p.one_d != 0;
+  pf_prof_begin(h, PROF_STAGE);
+#define PF_STAGE_CASE(S)                                                             \
+  case S:                                                                            \
+    if (oned) k_stage<S, true><<<(unsigned)blocks, threads, 0, h->stream>>>(a);      \
+    else k_stage<S, false><<<(unsigned)blocks, threads, 0, h->stream>>>(a);          \
+    break;
+  switch (stage) {
+    PF_STAGE_CASE(1)
+    PF_STAGE_CASE(2)
+    PF_STAGE_CASE(3)
+    PF_STAGE_CASE(4)
+  }
+#undef PF_STAGE_CASE
+  pf_prof_end(h);
+  PF_LAUNCHED(h);
+  return PF_OK;
+}
+
+static int launch_nodes(pf_handle *h, int stage, NodeArgs &n) {
+  const int threads = 256;
+  const int64_t blocks = (n.n + threads - 1) / threads;
+  if (blocks == 0) return PF_OK;
+  const double inv_scale = ldexp(1.0, -h->fix_e);
+  pf_prof_begin(h, PROF_NODES);
+  switch (stage) {
+    case 1: k_nodes<1><<<(unsigned)blocks, threads, 0, h->stream>>>(n, inv_scale); break;
+    case 2: k_nodes<2><<<(unsigned)blocks, threads, 0, h->stream>>>(n, inv_scale); break;
+    case 3: k_nodes<3><<<(unsigned)blocks, threads, 0, h->stream>>>(n, inv_scale); break;
+    case 4: k_nodes<4><<<(unsigned)blocks, threads, 0, h->stream>>>(n, inv_scale); break;
+  }
+  pf_prof_end(h);
+  PF_LAUNCHED(h);
+  return PF_OK;
+}
+
+int pf_rk4_fp64(pf_handle *h, double szl, double hstep, unsigned int *status_out) {
+  const pf_params &p = h->p;
+  const double hh = hstep * 0.5, h6 = hstep / 6.0, szh = szl + hh;
+  const double stage_sz[4] = {szl, szh, szh, szl + hstep};
+  const double stage_c[4] = {0.0, hh, hh, hstep};
+  const int nxt = h->cur ^ 1;
+
+  PF_CUDA(cudaMemsetAsync(h->d_status, 0, sizeof(unsigned int), h->stream));
+
+  StageArgs a;
+  memset(&a, 0, sizeof(a));
+  a.x = h->y[h->cur][0];
+  a.y = h->y[h->cur][1];
+  a.z2 = h->y[h->cur][2];
+  a.px = h->y[h->cur][3];
+  a.py = h->y[h->cur][4];
+  a.gam = h->y[h->cur][5];
+  a.chi = h->chi;
+  a.np = h->np;
+  a.h6 = h6;
+  a.acc_lo_r = h->acc;
+  a.acc_hi_r = h->acc + h->wcap;
+  a.acc_lo_i = h->acc + 2 * h->wcap;
+  a.acc_hi_i = h->acc + 3 * h->wcap;
+  a.nix = h->nix;
+  a.niy = h->niy;
+  a.npl = h->npl;
+  a.nz2 = p.nz2;
+  a.periodic = (p.mesh_type == PF_MESH_PERIODIC);
+  a.one_d = p.one_d;
+  a.dx = p.dx;
+  a.dy = p.dy;
+  a.dz2 = p.dz2;
+  a.dV3 = p.dx * p.dy * p.dz2;
+  a.halfx = ((double)(h->nix - 1) / 2.0) * p.dx;
+  a.halfy = ((double)(h->niy - 1) / 2.0) * p.dy;
+  a.eta = p.eta;
+  a.kappa = p.kappa;
+  a.rho = p.rho;
+  a.gamma_r = p.gamma_r * p.gamma_r;  // gamma0**2, as used by getP2
+  a.aw = p.aw * p.aw;                 // aw**2
+  a.sInv2rho = 1.0 / (2.0 * p.rho);
+  a.dxc = 2.0 * p.rho * p.kappa / sqrt(p.eta);
+  a.k2 = p.kappa * p.kappa;
+  a.field_evolve = p.field_evolve;
+  a.electrons_evolve = p.electrons_evolve;
+  a.coupling = p.coupling;
+  a.fix_e = h->fix_e;
+  a.fix_maxexp = h->fix_maxexp;
+  a.status = h->d_status;
+
+  NodeArgs n;
+  memset(&n, 0, sizeof(n));
+  n.n = h->nwin;
+  n.acc_lo_r = a.acc_lo_r;
+  n.acc_hi_r = a.acc_hi_r;
+  n.acc_lo_i = a.acc_lo_i;
+  n.acc_hi_i = a.acc_hi_i;
+  n.wr = h->wr;
+  n.wi = h->wi;
+  n.asr = h->asr;
+  n.asi = h->asi;
+  n.d0r = h->d0r;
+  n.d0i = h->d0i;
+  n.d12r = h->d12r;
+  n.d12i = h->d12i;
+  n.h6 = h6;
+  n.fix_e = h->fix_e;
+  n.status = h->d_status;
+
+  for (int s = 1; s <= 4; ++s) {
+    double n2col;
+    int place;
+    pf_taper_stage(h, stage_sz[s - 1], &n2col, &place);
+    a.n2col = n2col;
+    pf_stage_coefficients(p, stage_sz[s - 1], n2col, place, &a.bf);
+    a.cstate = stage_c[s - 1];
+    a.ar = (s == 1) ? h->wr : h->asr;
+    a.ai = (s == 1) ? h->wi : h->asi;
+    for (int j = 0; j < 6; ++j) {
+      a.kin[j] = (s == 2) ? h->k1[j] : (s == 3) ? h->ka[j] : (s == 4) ? h->kb[j] : nullptr;
+      a.kout[j] = (s == 1) ? h->k1[j] : (s == 3) ? h->kb[j] : nullptr;
+      a.kacc[j] = (s >= 2) ? h->ka[j] : nullptr;
+      a.k1[j] = h->k1[j];
+      a.ynext[j] = h->y[nxt][j];
+    }
+    int rc = launch_stage(h, s, a);
+    if (rc) return rc;
+    // the next stage's field is A0 + hh*d0, A0 + hh*d1, A0 + h*d2
+    n.coef = (s == 3) ? hstep : hh;
+    rc = launch_nodes(h, s, n);
+    if (rc) return rc;
+  }
+  PF_CUDA(cudaMemcpyAsync(h->h_status, h->d_status, sizeof(unsigned int),
+                          cudaMemcpyDeviceToHost, h->stream));
+  PF_CUDA(cudaStreamSynchronize(h->stream));
+  pf_prof_flush(h);
+  *status_out = *h->h_status;
+  if (*status_out == 0u) h->cur = nxt;
+  return PF_OK;
+}

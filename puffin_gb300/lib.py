@@ -1,0 +1,120 @@
+"""ctypes binding of libpuffgpu.so (the C ABI declared in include/puffgpu.h).
+
+The library is the only compute path: there is no CPU fallback.  Loading
+fails loudly when the shared library has not been built.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import _build
+
+PF_OK, PF_OUT_OF_WINDOW, PF_OUT_OF_Z2, PF_BAD_ARG, PF_CUDA_ERR, PF_TIMEOUT, \
+    PF_NO_DEVICE, PF_OVERFLOW, PF_STATE = range(9)
+STATUS_NAMES = {
+    PF_OK: "PF_OK", PF_OUT_OF_WINDOW: "PF_OUT_OF_WINDOW", PF_OUT_OF_Z2: "PF_OUT_OF_Z2",
+    PF_BAD_ARG: "PF_BAD_ARG", PF_CUDA_ERR: "PF_CUDA_ERR", PF_TIMEOUT: "PF_TIMEOUT",
+    PF_NO_DEVICE: "PF_NO_DEVICE", PF_OVERFLOW: "PF_OVERFLOW", PF_STATE: "PF_STATE",
+}
+UND_PUFFIN, UND_HELICAL, UND_PLANEPOLE, UND_CURVED = 0, 1, 2, 3
+MESH_TEMPORAL, MESH_PERIODIC = 0, 1
+FP64, MIXED = 0, 1
+
+_DOUBLES = ("rho", "eta", "kappa", "aw", "gamma_r", "fx", "fy", "kx_und", "ky_und",
+            "kbxsf", "kbysf", "szfs", "szfe", "n2col0", "undgrad", "dx", "dy", "dz2",
+            "sbeta", "sfilt_frac", "sperwaves")
+_INTS = ("und_type", "mesh_type", "nx", "ny", "nz2", "nix", "niy", "nbx", "nby", "nbz2",
+         "one_d", "focusing", "und_ends", "field_evolve", "electrons_evolve", "coupling",
+         "qfilter", "redist_every", "precision", "device")
+
+
+class Params(ctypes.Structure):
+    """Mirror of struct pf_params (include/puffgpu.h)."""
+    _fields_ = [(k, ctypes.c_double) for k in _DOUBLES] + [(k, ctypes.c_int32) for k in _INTS]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+SYMBOLS = (
+    "pf_default_params", "pf_create", "pf_destroy", "pf_set_particles", "pf_get_particles",
+    "pf_set_particles_dev", "pf_get_particles_dev", "pf_num_particles", "pf_set_field",
+    "pf_get_field", "pf_set_field_dev", "pf_get_field_dev", "pf_set_taper", "pf_get_taper",
+    "pf_get_window", "pf_rk4_step", "pf_redistribute", "pf_wrap_z2", "pf_diffract", "pf_run",
+    "pf_sync", "pf_kernel_launches", "pf_last_error", "pf_abi_version", "pf_get_stream",
+    "pf_profile", "pf_profile_read",
+)
+PROF_STAGE, PROF_NODES, PROF_FFT, PROF_DIFF, PROF_OTHER = range(5)
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = False):
+    """Load libpuffgpu.so and declare every entry point's prototype."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not os.path.exists(path):
+        if build_if_missing:
+            _build.build_library()
+        else:
+            raise RuntimeError(
+                f"libpuffgpu.so not found at {path}: build it with "
+                "`python -c 'import __graft_entry__ as g; g.build()'`")
+    L = ctypes.CDLL(path)
+    H = ctypes.c_void_p
+    dp = ctypes.POINTER(ctypes.c_double)
+    P = ctypes.POINTER(Params)
+    i32, i64, f64 = ctypes.c_int32, ctypes.c_int64, ctypes.c_double
+    proto = {
+        "pf_default_params": (None, [P]),
+        "pf_create": (ctypes.c_int, [P, ctypes.POINTER(H)]),
+        "pf_destroy": (ctypes.c_int, [H]),
+        "pf_set_particles": (ctypes.c_int, [H, i64] + [ctypes.c_void_p] * 7),
+        "pf_get_particles": (ctypes.c_int, [H] + [ctypes.c_void_p] * 7),
+        "pf_set_particles_dev": (ctypes.c_int, [H, i64] + [ctypes.c_void_p] * 7),
+        "pf_get_particles_dev": (ctypes.c_int, [H] + [ctypes.c_void_p] * 7),
+        "pf_num_particles": (i64, [H]),
+        "pf_set_field": (ctypes.c_int, [H, ctypes.c_void_p, ctypes.c_void_p]),
+        "pf_get_field": (ctypes.c_int, [H, ctypes.c_void_p, ctypes.c_void_p]),
+        "pf_set_field_dev": (ctypes.c_int, [H, ctypes.c_void_p, ctypes.c_void_p]),
+        "pf_get_field_dev": (ctypes.c_int, [H, ctypes.c_void_p, ctypes.c_void_p]),
+        "pf_set_taper": (ctypes.c_int, [H, f64, f64, f64]),
+        "pf_get_taper": (ctypes.c_int, [H, dp, dp, dp]),
+        "pf_get_window": (ctypes.c_int, [H, ctypes.POINTER(i32), ctypes.POINTER(i32)]),
+        "pf_rk4_step": (ctypes.c_int, [H, f64, f64]),
+        "pf_redistribute": (ctypes.c_int, [H]),
+        "pf_wrap_z2": (ctypes.c_int, [H]),
+        "pf_diffract": (ctypes.c_int, [H, f64]),
+        "pf_run": (ctypes.c_int, [H, i32, i32, i32, f64, dp, ctypes.POINTER(i32)]),
+        "pf_sync": (ctypes.c_int, [H]),
+        "pf_kernel_launches": (i64, [H]),
+        "pf_last_error": (ctypes.c_char_p, [H]),
+        "pf_abi_version": (ctypes.c_int, []),
+        "pf_get_stream": (ctypes.c_void_p, [H]),
+        "pf_profile": (ctypes.c_int, [H, i32]),
+        "pf_profile_read": (ctypes.c_int, [H, i32, dp, ctypes.POINTER(i64)]),
+    }
+    for name, (res, args) in proto.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def default_params(**overrides) -> Params:
+    p = Params()
+    load().pf_default_params(ctypes.byref(p))
+    for k, v in overrides.items():
+        if not hasattr(p, k):
+            raise KeyError(k)
+        setattr(p, k, v)
+    return p

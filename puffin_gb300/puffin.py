@@ -1,0 +1,206 @@
+"""Host-side mirror of Puffin's hot-path interface over the puffgpu C ABI.
+
+``Puffin`` holds one undulator module's particles and field on the GPU and
+exposes the reference's operations under their own names:
+
+* ``rk4par(szl, h)``        rk4par (puffin/lib/interaction/puffin_mpi_RK4.f90:38)
+* ``diffractIM(dz)``         inner2Outer + diffractIM + outer2Inner
+                             (puffin/lib/diffraction/diffraction.f90:46)
+* ``redistribute()``         getInNode + getLocalFieldIndices
+                             (puffin/lib/parallel/para_field.f90:1432, 83)
+* ``und_section(...)``       the RK4/diffraction loop of UndSection
+                             (puffin/lib/undulator.f90:182-333)
+
+Error behaviour follows the reference: a particle leaving the inner window
+makes ``rk4par`` return False with the state unchanged (qPArrOK_G = .false.),
+and the conditions where the reference STOPs raise ``PuffinError``.
+Arrays are numpy float64 on the host, or CUDA torch tensors (float64,
+contiguous) which are used in place on the device.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import lib as L
+
+PARTICLE_KEYS = ("x", "y", "z2", "px", "py", "gam", "chi")
+
+
+class PuffinError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{L.STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+def _is_torch_cuda(a):
+    return hasattr(a, "is_cuda") and a.is_cuda
+
+
+def _host(a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a, a.ctypes.data
+
+
+def _dev(t):
+    import torch
+    if t.dtype != torch.float64 or not t.is_contiguous():
+        raise ValueError("device arrays must be contiguous float64 CUDA tensors")
+    return t, t.data_ptr()
+
+
+class Puffin:
+    def __init__(self, params: L.Params | None = None, **overrides):
+        self._lib = L.load()
+        p = L.default_params() if params is None else params
+        for k, v in overrides.items():
+            setattr(p, k, v)
+        self.params = p
+        h = ctypes.c_void_p()
+        rc = self._lib.pf_create(ctypes.byref(p), ctypes.byref(h))
+        if rc != L.PF_OK:
+            raise PuffinError(rc, self._lib.pf_last_error(None).decode())
+        self._h = h
+        self.n_outer = p.nx * p.ny * p.nz2
+
+    # -- life cycle -----------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.pf_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc, allow=()):
+        if rc == L.PF_OK or rc in allow:
+            return rc
+        raise PuffinError(rc, self._lib.pf_last_error(self._h).decode())
+
+    # -- particles --------------------------------------------------------------
+    def set_particles(self, x, y, z2, px, py, gam, chi):
+        arrs = [x, y, z2, px, py, gam, chi]
+        if all(_is_torch_cuda(a) for a in arrs):
+            keep = [_dev(a) for a in arrs]
+            fn = self._lib.pf_set_particles_dev
+        else:
+            keep = [_host(a) for a in arrs]
+            fn = self._lib.pf_set_particles
+        n = len(keep[0][0])
+        if any(len(k[0]) != n for k in keep):
+            raise ValueError("particle arrays differ in length")
+        self._check(fn(self._h, n, *(k[1] for k in keep)))
+
+    @property
+    def n_particles(self):
+        return int(self._lib.pf_num_particles(self._h))
+
+    def get_particles(self, out=None):
+        n = self.n_particles
+        if out is not None and all(_is_torch_cuda(out[k]) for k in PARTICLE_KEYS):
+            self._check(self._lib.pf_get_particles_dev(
+                self._h, *(_dev(out[k])[1] for k in PARTICLE_KEYS)))
+            return out
+        res = {k: np.empty(n) for k in PARTICLE_KEYS}
+        self._check(self._lib.pf_get_particles(
+            self._h, *(res[k].ctypes.data for k in PARTICLE_KEYS)))
+        return res
+
+    # -- field ----------------------------------------------------------------
+    def set_field(self, re, im):
+        if _is_torch_cuda(re) and _is_torch_cuda(im):
+            (re, pr), (im, pi) = _dev(re), _dev(im)
+            fn = self._lib.pf_set_field_dev
+        else:
+            (re, pr), (im, pi) = _host(re), _host(im)
+            fn = self._lib.pf_set_field
+        if re.size != self.n_outer or im.size != self.n_outer:
+            raise ValueError(f"field arrays must hold nx*ny*nz2 = {self.n_outer} values")
+        self._check(fn(self._h, pr, pi))
+
+    def get_field(self, out=None):
+        if out is not None and _is_torch_cuda(out[0]):
+            self._check(self._lib.pf_get_field_dev(self._h, _dev(out[0])[1], _dev(out[1])[1]))
+            return out
+        re = np.empty(self.n_outer)
+        im = np.empty(self.n_outer)
+        self._check(self._lib.pf_get_field(self._h, re.ctypes.data, im.ctypes.data))
+        return re, im
+
+    # -- taper / window ---------------------------------------------------------
+    def set_taper(self, n2col, n2col0, undgrad):
+        self._check(self._lib.pf_set_taper(self._h, n2col, n2col0, undgrad))
+
+    def get_taper(self):
+        a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        self._check(self._lib.pf_get_taper(self._h, ctypes.byref(a), ctypes.byref(b),
+                                           ctypes.byref(c)))
+        return a.value, b.value, c.value
+
+    @property
+    def window(self):
+        a, b = ctypes.c_int32(), ctypes.c_int32()
+        self._check(self._lib.pf_get_window(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    # -- the hot path -------------------------------------------------------------
+    def rk4par(self, szl: float, h: float) -> bool:
+        """One RK4 step; False (state unchanged) if a particle left the window."""
+        rc = self._check(self._lib.pf_rk4_step(self._h, float(szl), float(h)),
+                         allow=(L.PF_OUT_OF_WINDOW,))
+        return rc == L.PF_OK
+
+    rk4_step = rk4par
+
+    def redistribute(self):
+        self._check(self._lib.pf_redistribute(self._h))
+
+    def wrap_z2(self):
+        self._check(self._lib.pf_wrap_z2(self._h))
+
+    def diffractIM(self, dz: float):
+        self._check(self._lib.pf_diffract(self._h, float(dz)))
+
+    diffract = diffractIM
+
+    def und_section(self, nsteps: int, isteps4diff: int, qdiffraction: bool, h: float,
+                    szl: float = 0.0):
+        """UndSection's loop; returns the new local zbar."""
+        z = ctypes.c_double(szl)
+        done = ctypes.c_int32(0)
+        self._check(self._lib.pf_run(self._h, int(nsteps), int(isteps4diff),
+                                     int(bool(qdiffraction)), float(h), ctypes.byref(z),
+                                     ctypes.byref(done)))
+        return z.value
+
+    def sync(self):
+        self._check(self._lib.pf_sync(self._h))
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(self._lib.pf_kernel_launches(self._h))
+
+    @property
+    def stream_handle(self) -> int:
+        """cudaStream_t of the handle (wrap with torch.cuda.ExternalStream)."""
+        return int(self._lib.pf_get_stream(self._h) or 0)
+
+    def profile(self, enable: bool = True):
+        self._check(self._lib.pf_profile(self._h, int(enable)))
+
+    def profile_read(self, kernel_class: int):
+        ms = ctypes.c_double()
+        n = ctypes.c_int64()
+        self._check(self._lib.pf_profile_read(self._h, int(kernel_class), ctypes.byref(ms),
+                                              ctypes.byref(n)))
+        return ms.value, n.value

@@ -1,0 +1,294 @@
+"""GPU parity: the puffgpu C ABI against the CPU oracle on the same seeded
+inputs, and against the reference's own golden dump for the 1D path.
+
+Tolerances (floating point; the GPU uses FMA contraction and an exact
+fixed-point deposit sum, the oracle sequential FP64 sums):
+* one RK4 step: rtol 1e-12 on particles, 1e-12 of the field scale;
+* 32 steps with diffraction: rtol 1e-9 (the FEL instability amplifies
+  rounding differences step by step);
+* the reference's own 1D end-to-end test: 1e-10 absolute, as in
+  test/testMPIIntegration.pf:94-128.
+"""
+import math
+import os
+
+import numpy as np
+import pytest
+
+import puffin_gb300 as P
+from puffin_gb300 import configs
+from oracle import oracle as O
+from tests import golden_beam as GB
+from tests.oracle_bridge import assert_beam_close, oracle_beam, oracle_config
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "f1main_expected.npz")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _threads():
+    O.set_threads(1)
+
+
+def run_gpu_steps(params, beam, field, h, nsteps, szl=0.0, taper=None):
+    with P.Puffin(params) as sim:
+        sim.set_particles(*(beam[k] for k in P.PARTICLE_KEYS))
+        sim.set_field(*field)
+        if taper is not None:
+            sim.set_taper(*taper)
+        for _ in range(nsteps):
+            assert sim.rk4par(szl, h)
+            szl += h
+        return sim.get_particles(), sim.get_field(), sim.window, sim.get_taper()
+
+
+def run_oracle_steps(params, beam, field, h, nsteps, nix, niy, szl=0.0, taper=None):
+    cfg = oracle_config(params)
+    b = oracle_beam(beam)
+    re, im = (np.array(a, dtype=np.float64) for a in field)
+    if cfg.mesh_type == O.MESH_PERIODIC:
+        n = cfg.nx * cfg.ny
+        re[-n:] = re[:n]
+        im[-n:] = im[:n]
+    wr, wi = O.outer_to_inner(cfg, re, im, nix, niy)
+    t = O.Taper(*(taper or (params.n2col0, params.n2col0, params.undgrad)))
+    for _ in range(nsteps):
+        assert O.rk4_step(cfg, t, szl, h, b, wr, wi, nix, niy) == 0
+        szl += h
+    O.inner_to_outer(cfg, re, im, wr, wi, nix, niy)
+    return b, (re, im), t
+
+
+def random_field(params, seed, amp=1e-3):
+    rng = np.random.default_rng(seed)
+    n = params.nx * params.ny * params.nz2
+    return amp * rng.standard_normal(n), amp * rng.standard_normal(n)
+
+
+def field_close(got, want, rel):
+    scale = max(np.max(np.abs(want[0])), np.max(np.abs(want[1])), 1e-300)
+    np.testing.assert_allclose(got[0], want[0], rtol=0, atol=rel * scale)
+    np.testing.assert_allclose(got[1], want[1], rtol=0, atol=rel * scale)
+
+
+# ---------------------------------------------------------------------------
+def test_golden_1d_reference_run():
+    """The reference's 2-rank end-to-end test, run through the GPU library."""
+    g = np.load(GOLD)
+    cfg, h = GB.config()
+    ob = GB.initial_beam(cfg, g["electrons"][:, 6])
+    beam = {k: getattr(ob, k).copy() for k in P.PARTICLE_KEYS}
+    p = P.default_params(rho=cfg.rho, aw=cfg.aw, gamma_r=cfg.gamma_r, eta=cfg.eta,
+                         kappa=cfg.kappa, fx=cfg.fx, fy=cfg.fy, und_type=P.UND_PUFFIN,
+                         nx=1, ny=1, nz2=cfg.nz2, dx=1.0, dy=1.0, dz2=cfg.dz2, one_d=1,
+                         szfs=0.0, szfe=cfg.szfe)
+    got, (fr, fi), win, taper = run_gpu_steps(p, beam, (np.zeros(cfg.nz2), np.zeros(cfg.nz2)),
+                                              h, GB.NSTEPS)
+    assert win == (1, 1)
+    szl = 0.0
+    for _ in range(GB.NSTEPS):
+        szl = szl + h
+    b = O.Beam(*(got[k] for k in P.PARTICLE_KEYS))
+    O.match_out(cfg, b, szl, taper[0])
+    O.correct_trans(b)
+    e = g["electrons"]
+    assert b.n == 319
+    for j, k in enumerate(("x", "y", "z2", "px", "py", "gam")):
+        np.testing.assert_allclose(getattr(b, k), e[:, j], rtol=0, atol=1e-10, err_msg=k)
+    np.testing.assert_allclose(fr, g["aperp"][0], rtol=0, atol=1e-10)
+    np.testing.assert_allclose(fi, g["aperp"][1], rtol=0, atol=1e-10)
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_one_step_periodic_helical(seed):
+    w = configs.config1(np_=3000, seed=seed)
+    field = random_field(w.params, seed)
+    got, gf, (nix, niy), _ = run_gpu_steps(w.params, w.beam, field, w.h, 1)
+    b, of, _ = run_oracle_steps(w.params, w.beam, field, w.h, 1, nix, niy)
+    assert_beam_close(got, b, rtol=1e-12, atol=1e-15)
+    field_close(gf, of, 1e-12)
+
+
+def _planepole_params(**kw):
+    rho, aw, gr = 0.004, 1.2, 800.0
+    eta, kappa, fx, fy = configs.calc_scaling(rho, aw, gr, P.UND_PLANEPOLE)
+    lamr = 4.0 * configs.PUFFIN_PI * rho
+    p = P.default_params(rho=rho, aw=aw, gamma_r=gr, eta=eta, kappa=kappa, fx=fx, fy=fy,
+                         und_type=P.UND_PLANEPOLE, nx=33, ny=33, nz2=96, dx=0.3, dy=0.3,
+                         dz2=lamr / 16.0, mesh_type=P.MESH_TEMPORAL)
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def _beam3d(p, n, seed, zlo, zhi, sig=1.0):
+    rng = np.random.default_rng(seed)
+    beam = {"x": sig * np.clip(rng.standard_normal(n), -3, 3),
+            "y": sig * np.clip(rng.standard_normal(n), -3, 3),
+            "z2": rng.uniform(zlo, zhi, n),
+            "px": 0.02 * rng.standard_normal(n), "py": 0.02 * rng.standard_normal(n),
+            "gam": 1.0 + 1e-3 * rng.standard_normal(n),
+            "chi": rng.uniform(0.5, 1.5, n) * 1e-3}
+    configs.match_in(p, beam)
+    return beam
+
+
+@pytest.mark.parametrize("place_sz", [0.0, 0.05, 0.9])
+def test_one_step_planepole_taper_ends_focusing(place_sz):
+    """Temporal mesh, planepole with undulator ends (start/main/end sections),
+    a linear taper and strong focusing."""
+    lamr = 4.0 * configs.PUFFIN_PI * 0.004
+    p = _planepole_params(und_ends=1, szfs=2 * lamr, szfe=0.8, undgrad=-0.05, focusing=1,
+                          kbxsf=0.3, kbysf=0.4)
+    beam = _beam3d(p, 2500, 7, 0.2, 0.8)
+    field = random_field(p, 3)
+    h = lamr / 24.0
+    taper = (1.0, 1.0, p.undgrad)
+    got, gf, (nix, niy), gt = run_gpu_steps(p, beam, field, h, 2, szl=place_sz, taper=taper)
+    b, of, ot = run_oracle_steps(p, beam, field, h, 2, nix, niy, szl=place_sz, taper=taper)
+    assert_beam_close(got, b, rtol=1e-12, atol=1e-15)
+    field_close(gf, of, 1e-12)
+    assert gt[0] == ot.n2col and gt[1] == ot.n2col0
+
+
+@pytest.mark.parametrize("und", [P.UND_HELICAL, P.UND_PUFFIN, P.UND_CURVED])
+@pytest.mark.parametrize("place_sz", [0.0, 0.03, 0.5])
+def test_one_step_undulator_types(und, place_sz):
+    rho, aw, gr = 0.005, 1.0, 400.0
+    eta, kappa, fx, fy = configs.calc_scaling(rho, aw, gr, und, 0.8, 0.6)
+    lamr = 4.0 * configs.PUFFIN_PI * rho
+    kw = {}
+    if und == P.UND_CURVED:
+        kx = math.sqrt(eta / (8.0 * rho ** 2))
+        kw = dict(kx_und=kx, ky_und=kx)
+    p = P.default_params(rho=rho, aw=aw, gamma_r=gr, eta=eta, kappa=kappa, fx=fx, fy=fy,
+                         und_type=und, nx=25, ny=25, nz2=65, dx=0.25, dy=0.25, dz2=lamr / 16,
+                         mesh_type=P.MESH_PERIODIC, sperwaves=4.0, und_ends=1,
+                         szfs=2 * lamr, szfe=0.4, **kw)
+    beam = _beam3d(p, 2000, 11, 0.0, 4 * lamr, sig=0.7)
+    field = random_field(p, 5)
+    h = lamr / 30.0
+    got, gf, (nix, niy), _ = run_gpu_steps(p, beam, field, h, 2, szl=place_sz)
+    b, of, _ = run_oracle_steps(p, beam, field, h, 2, nix, niy, szl=place_sz)
+    assert_beam_close(got, b, rtol=1e-12, atol=1e-15)
+    field_close(gf, of, 1e-12)
+
+
+@pytest.mark.parametrize("mesh", [P.MESH_PERIODIC, P.MESH_TEMPORAL])
+def test_diffraction_matches_oracle(mesh):
+    rho = 0.005
+    lamr = 4.0 * configs.PUFFIN_PI * rho
+    if mesh == P.MESH_PERIODIC:
+        p = P.default_params(rho=rho, eta=1e-5, kappa=0.2, nx=21, ny=21, nz2=65, dx=0.2, dy=0.2,
+                             dz2=lamr / 16, mesh_type=mesh, sperwaves=4.0)
+    else:
+        p = P.default_params(rho=rho, eta=1e-5, kappa=0.2, nx=33, ny=35, nz2=128, dx=0.3,
+                             dy=0.25, dz2=lamr / 16, mesh_type=mesh)
+    field = random_field(p, 9, amp=1.0)
+    with P.Puffin(p) as sim:
+        sim.set_field(*field)
+        sim.diffractIM(0.37)
+        gf = sim.get_field()
+    cfg = oracle_config(p)
+    re, im = (a.copy() for a in field)
+    if mesh == P.MESH_PERIODIC:
+        n = p.nx * p.ny
+        re[-n:] = re[:n]
+        im[-n:] = im[:n]
+    O.diffract(cfg, re, im, 0.37)
+    field_close(gf, (re, im), 1e-12)
+
+
+def test_run_with_diffraction_matches_oracle():
+    """pf_run (UndSection's loop) against oracle.undulator_run: 32 steps with
+    diffraction every 16 steps and merged half steps."""
+    w = configs.config1(np_=4096, seed=21, nsteps=32)
+    field = random_field(w.params, 4, amp=1e-2)
+    with P.Puffin(w.params) as sim:
+        sim.set_particles(*(w.beam[k] for k in P.PARTICLE_KEYS))
+        sim.set_field(*field)
+        szl = sim.und_section(w.nsteps, w.isteps4diff, True, w.h)
+        got = sim.get_particles()
+        gf = sim.get_field()
+    cfg = oracle_config(w.params)
+    b = oracle_beam(w.beam)
+    re, im = (a.copy() for a in field)
+    n = cfg.nx * cfg.ny
+    re[-n:] = re[:n]
+    im[-n:] = im[:n]
+    r = O.undulator_run(cfg, b, re, im, w.h, w.nsteps, w.isteps4diff, True)
+    assert r.status == 0
+    assert abs(szl - w.nsteps * w.h) < 1e-12
+    assert_beam_close(got, b, rtol=1e-9, atol=1e-12)
+    field_close(gf, (re, im), 1e-9)
+
+
+def test_deposit_is_bit_reproducible():
+    w = configs.config1(np_=20000, seed=3, nsteps=4)
+    field = random_field(w.params, 2)
+    outs = []
+    for _ in range(2):
+        got, gf, _, _ = run_gpu_steps(w.params, w.beam, field, w.h, 4)
+        outs.append((got, gf))
+    for k in ("x", "y", "z2", "px", "py", "gam"):
+        np.testing.assert_array_equal(outs[0][0][k], outs[1][0][k])
+    np.testing.assert_array_equal(outs[0][1][0], outs[1][1][0])
+    np.testing.assert_array_equal(outs[0][1][1], outs[1][1][1])
+
+
+def test_out_of_window_leaves_state_and_recovers():
+    w = configs.config1(np_=1000, seed=5)
+    beam = {k: v.copy() for k, v in w.beam.items()}
+    field = random_field(w.params, 6)
+    with P.Puffin(w.params, nix=11, niy=11) as sim:
+        sim.set_particles(*(beam[k] for k in P.PARTICLE_KEYS))
+        sim.set_field(*field)
+        assert sim.window == (11, 11)
+        before = sim.get_particles()
+        f0 = sim.get_field()
+        assert sim.rk4par(0.0, w.h) is False          # qPArrOK_G = .false.
+        after = sim.get_particles()
+        for k in P.PARTICLE_KEYS:
+            np.testing.assert_array_equal(before[k], after[k])
+        f1 = sim.get_field()
+        np.testing.assert_array_equal(f0[0], f1[0])
+        sim.redistribute()                             # getInNode + wrap
+        assert sim.window == (21, 21)
+        assert sim.rk4par(0.0, w.h) is True
+
+
+def test_out_of_temporal_mesh_raises():
+    p = _planepole_params()
+    beam = _beam3d(p, 100, 1, 0.1, 0.5)
+    beam["z2"][7] = (p.nz2 - 1) * p.dz2 + 0.5 * p.dz2   # beyond the last node
+    with P.Puffin(p) as sim:
+        sim.set_particles(*(beam[k] for k in P.PARTICLE_KEYS))
+        with pytest.raises(P.PuffinError) as e:
+            sim.rk4par(0.0, 1e-3)
+        assert e.value.code == P.lib.PF_OUT_OF_Z2
+
+
+def test_empty_beam_is_a_no_op_on_the_field():
+    p = _planepole_params(nix=9, niy=9)
+    field = random_field(p, 8)
+    with P.Puffin(p) as sim:
+        e = np.zeros(0)
+        sim.set_particles(e, e, e, e, e, e, e)
+        sim.set_field(*field)
+        assert sim.rk4par(0.0, 1e-3)
+        gf = sim.get_field()
+    np.testing.assert_array_equal(gf[0], field[0])
+    np.testing.assert_array_equal(gf[1], field[1])
+
+
+def test_device_arrays_round_trip():
+    torch = pytest.importorskip("torch")
+    w = configs.config1(np_=777, seed=9)
+    t = {k: torch.tensor(w.beam[k], dtype=torch.float64, device="cuda") for k in P.PARTICLE_KEYS}
+    with P.Puffin(w.params) as sim:
+        sim.set_particles(*(t[k] for k in P.PARTICLE_KEYS))
+        out = {k: torch.empty_like(t[k]) for k in P.PARTICLE_KEYS}
+        sim.get_particles(out)
+    torch.cuda.synchronize()
+    for k in P.PARTICLE_KEYS:
+        assert torch.equal(out[k], t[k])
