@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--np", type=int, default=2 ** 23, help="macroparticles")
     ap.add_argument("--e2e-steps", type=int, default=8)
+    ap.add_argument("--nz2", type=int, default=4096,
+                    help="z2 nodes of the mesh (smaller only for profiling captures)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     return ap.parse_args()
@@ -200,7 +202,7 @@ def run_gpu(args, rank, world):
 
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
-    w = configs.config2(np_=args.np)
+    w = configs.config2(np_=args.np, nz2=args.nz2)
     p = w.params
     p.device = dev
     sim = P.Puffin(p)
@@ -265,7 +267,7 @@ def run_gpu(args, rank, world):
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
     t0.record(stream)
-    for _ in range(args.e2e_steps):
+    for _ in range(max(0, args.e2e_steps)):
         assert lib.pf_set_particles(sim._h, n, *ptrs) == 0
         assert lib.pf_set_field(sim._h, fre.ctypes.data, fim.ctypes.data) == 0
         step()
@@ -273,7 +275,7 @@ def run_gpu(args, rank, world):
         assert lib.pf_get_field(sim._h, fre.ctypes.data, fim.ctypes.data) == 0
     t1.record(stream)
     torch.cuda.synchronize()
-    e2e_ms = t0.elapsed_time(t1)
+    e2e_ms = max(t0.elapsed_time(t1), 1e-9)
     h2d = 7 * 8 * n + 2 * 8 * sim.n_outer
     d2h = h2d
     sim.close()
@@ -286,7 +288,7 @@ def run_gpu(args, rank, world):
         return None
 
     value = world * n * args.steps / (ms * 1e-3)
-    e2e_value = world * n * args.e2e_steps / (e2e_ms * 1e-3)
+    e2e_value = world * n * args.e2e_steps / (e2e_ms * 1e-3) if args.e2e_steps > 0 else None
     peak, peak_kind = measured_peaks()
     stage_avg = stage_ms / max(1, stage_n)
     achieved = n * BYTES_PER_PARTICLE_STAGE / (stage_avg * 1e-3) / 1e9

@@ -146,7 +146,7 @@ def config1(np_=2 ** 16, seed=SEED, nsteps=2000):
                     lamr / 32.0, nsteps, 16, True, beam, (np.zeros(n), np.zeros(n)))
 
 
-def config2(np_=2 ** 23, seed=SEED, nperiods=20):
+def config2(np_=2 ** 23, seed=SEED, nperiods=20, nz2=4096):
     """3D temporal planepole, aw_rms = 0.8 (peak 0.8*sqrt 2), rho=0.002,
     gamma_r=2000, linear taper -1% over the module, 129x129 (dx=dy=0.5) x 4096
     z2 nodes, flat-top beam over 80% of z2 with sigma_perp = 1.5 and 0.01%
@@ -154,7 +154,6 @@ def config2(np_=2 ** 23, seed=SEED, nperiods=20):
     rho, aw, gr = 0.002, 0.8 * math.sqrt(2.0), 2000.0
     lamr = 4.0 * PUFFIN_PI * rho
     dz2 = lamr / 16.0
-    nz2 = 4096
     nsteps = nperiods * 24
     h = lamr / 24.0
     zlen = nsteps * h
@@ -174,7 +173,7 @@ def config2(np_=2 ** 23, seed=SEED, nperiods=20):
     }
     match_in(p, beam)
     n = p.nx * p.ny * p.nz2
-    return Workload("config2: temporal planepole 129x129x4096, rho=0.002, gamma_r=2000, taper -1%",
+    return Workload(f"config2: temporal planepole 129x129x{nz2}, rho=0.002, gamma_r=2000, taper -1%",
                     p, h, nsteps, 8, True, beam, (np.zeros(n), np.zeros(n)))
 
 

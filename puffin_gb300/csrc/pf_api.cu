@@ -412,6 +412,7 @@ static int set_particles_impl(pf_handle *h, int64_t n, const double *const src[7
   int rc = alloc_particles(h, n);
   if (rc) return rc;
   h->np = n;
+  h->particles_set = true;
   const size_t b = sizeof(double) * (size_t)n;
   if (n > 0) {
     for (int j = 0; j < 6; ++j)
@@ -551,7 +552,7 @@ int pf_get_window(const pf_handle *h, int32_t *nix, int32_t *niy) {
 
 int pf_rk4_step(pf_handle *h, double szl, double hstep) {
   if (!h) return PF_BAD_ARG;
-  if (h->nwin == 0 || h->cap == 0) {
+  if (!h->particles_set || h->nwin == 0) {
     h->err = "pf_rk4_step: particles not set";
     return PF_STATE;
   }

@@ -65,6 +65,7 @@ struct StageArgs {
   double dx, dy, dz2, halfx, halfy, dV3;
   // physics
   double eta, kappa, rho, gamma_r, aw, n2col, sInv2rho, dxc, k2;
+  double inv_eta, eta_k2, rho2, kn2col, inv_dx, inv_dy, inv_dz2, inv_dV3;
   int field_evolve, electrons_evolve, coupling;
   int fix_e;              // fixed-point scale exponent of the deposit
   int fix_maxexp;         // overflow guard: |contribution * 2^E| < 2^fix_maxexp
@@ -105,6 +106,7 @@ struct pf_handle {
   // particles
   int64_t np = 0;
   int64_t cap = 0;
+  bool particles_set = false;
   double *y[2][6] = {};       // double-buffered x, y, z2, px, py, gamma
   int cur = 0;
   double *chi = nullptr;

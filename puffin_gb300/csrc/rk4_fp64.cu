@@ -141,19 +141,27 @@ __global__ void __launch_bounds__(256) k_stage(const StageArgs a) {
   const double X = s[0], Y = s[1], Z2 = s[2], PX = s[3], PY = s[4], G = s[5];
   const double chi = a.chi[i];
 
-  // getP2 (gamma_to_p2.f90:84-85)
+  // getP2 (gamma_to_p2.f90:84-85).  1 - u loses ~7 digits, so u and the
+  // square root and reciprocal that follow keep IEEE division/sqrt and the
+  // reference's operation order; after the cancellation (r - 1) a reciprocal
+  // multiply is exact to an ulp.
   const double aa = 1.0 / (a.gamma_r * (G * G));   // a.gamma_r holds gamma0**2
   const double bb = 1.0 + a.aw * ((PX * PX) + (PY * PY));  // a.aw holds aw**2
-  const double p2 = ((1.0 / sqrt(1.0 - aa * bb)) - 1.0) / a.eta;
+  const double p2 = ((1.0 / sqrt(1.0 - aa * bb)) - 1.0) * a.inv_eta;
   const double q = 1.0 + a.eta * p2;
+  const double rG = 1.0 / G;
+  const double qrG = q * rG;
 
-  // interpolation (getInterps_3D / getInterps_1D)
+  // interpolation (getInterps_3D / getInterps_1D): cell index and fraction
+  // from one scaled coordinate t = position / cell size
   double w[8];
   int64_t node[8];
   bool ok = true;
   {
-    const double z2n = floor(Z2 / a.dz2) + 1.0;
-    const double locz2 = Z2 - (z2n - 1.0) * a.dz2;
+    const double tz = Z2 * a.inv_dz2;
+    const double fz = floor(tz);
+    const double z2n = fz + 1.0;
+    const double zw2 = tz - fz;
     int64_t pz0 = 0, pz1 = 0;
     if (a.periodic) {
       if (!(fabs(z2n) < 9.0e15)) {
@@ -175,19 +183,21 @@ __global__ void __launch_bounds__(256) k_stage(const StageArgs a) {
       }
     }
     if (ONED) {
-      const double w1 = (1.0 - locz2 / a.dz2);
+      const double w1 = 1.0 - zw2;
       w[0] = w1;
       w[1] = 1.0 - w1;
       node[0] = pz0;
       node[1] = pz1;
     } else {
-      const double xn = floor((X + a.halfx) / a.dx) + 1.0;
-      const double locx = X + a.halfx - (xn - 1.0) * a.dx;
-      const double x2 = locx / a.dx, x1 = 1.0 - x2;
-      const double yn = floor((Y + a.halfy) / a.dy) + 1.0;
-      const double locy = Y + a.halfy - (yn - 1.0) * a.dy;
-      const double y2 = locy / a.dy, y1 = 1.0 - y2;
-      const double zw2 = locz2 / a.dz2, zw1 = 1.0 - zw2;
+      const double tx = (X + a.halfx) * a.inv_dx;
+      const double fx = floor(tx);
+      const double xn = fx + 1.0;
+      const double x2 = tx - fx, x1 = 1.0 - x2;
+      const double ty = (Y + a.halfy) * a.inv_dy;
+      const double fy = floor(ty);
+      const double yn = fy + 1.0;
+      const double y2 = ty - fy, y1 = 1.0 - y2;
+      const double zw1 = 1.0 - zw2;
       if (!(xn >= 1.0 && xn < (double)a.nix && yn >= 1.0 && yn < (double)a.niy)) {
         ok = false;
         atomicOr(a.status, ST_OUT_OF_WINDOW);
@@ -195,14 +205,15 @@ __global__ void __launch_bounds__(256) k_stage(const StageArgs a) {
       const int64_t ntr = a.nix * a.niy;
       const int64_t ix = ok ? (int64_t)xn - 1 : 0, iy = ok ? (int64_t)yn - 1 : 0;
       const int64_t b0 = ix + iy * a.nix + pz0 * ntr, b1 = ix + iy * a.nix + pz1 * ntr;
-      w[0] = x1 * y1 * zw1;
-      w[1] = x2 * y1 * zw1;
-      w[2] = x1 * y2 * zw1;
-      w[3] = x2 * y2 * zw1;
-      w[4] = x1 * y1 * zw2;
-      w[5] = x2 * y1 * zw2;
-      w[6] = x1 * y2 * zw2;
-      w[7] = x2 * y2 * zw2;
+      const double x1y1 = x1 * y1, x2y1 = x2 * y1, x1y2 = x1 * y2, x2y2 = x2 * y2;
+      w[0] = x1y1 * zw1;
+      w[1] = x2y1 * zw1;
+      w[2] = x1y2 * zw1;
+      w[3] = x2y2 * zw1;
+      w[4] = x1y1 * zw2;
+      w[5] = x2y1 * zw2;
+      w[6] = x1y2 * zw2;
+      w[7] = x2y2 * zw2;
       node[0] = b0;
       node[1] = b0 + 1;
       node[2] = b0 + a.nix;
@@ -227,16 +238,10 @@ __global__ void __launch_bounds__(256) k_stage(const StageArgs a) {
     }
     // deposit (getSource)
     if (a.field_evolve) {
-      double sr, si;
-      if (ONED) {
-        const double dw = (chi / a.dV3) * q / G;
-        sr = dw * PX;
-        si = dw * PY;
-      } else {
-        const double cq = (chi / a.dV3) * q;
-        sr = cq * PX / G;
-        si = cq * PY / G;
-      }
+      // (chi/dV3) (1 + eta p2) p / Gamma
+      const double dw = chi * a.inv_dV3 * qrG;
+      const double sr = dw * PX;
+      const double si = dw * PY;
       bool fits = true;
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
@@ -258,13 +263,14 @@ __global__ void __launch_bounds__(256) k_stage(const StageArgs a) {
   if (a.electrons_evolve) {
     double bx, by, bz;
     bfield(a.bf, X, Y, bx, by, bz);
-    const double ep = a.eta * p2 / a.k2;
+    const double ep = p2 * a.eta_k2;           // eta p2 / kappa^2
+    const double cz = a.kn2col * qrG * bz;     // kappa (1 + eta p2) / Gamma alpha bz
     k[2] = p2;
-    k[0] = a.dxc * q / G * PX;
-    k[1] = -(a.dxc * q / G * PY);
-    k[3] = a.sInv2rho * (a.n2col * by - ep * fr) + a.kappa * PY / G * q * a.n2col * bz;
-    k[4] = a.sInv2rho * (a.n2col * bx - ep * fi) - a.kappa * PX / G * q * a.n2col * bz;
-    k[5] = -(a.rho * q / G * 2.0 * (PX * fr + PY * fi));
+    k[0] = a.dxc * qrG * PX;
+    k[1] = -(a.dxc * qrG * PY);
+    k[3] = a.sInv2rho * (a.n2col * by - ep * fr) + cz * PY;
+    k[4] = a.sInv2rho * (a.n2col * bx - ep * fi) - cz * PX;
+    k[5] = -(a.rho2 * qrG * (PX * fr + PY * fi));
   } else {
 #pragma unroll
     for (int j = 0; j < 6; ++j) k[j] = 0.0;
@@ -548,6 +554,13 @@ int pf_rk4_fp64(pf_handle *h, double szl, double hstep, unsigned int *status_out
   a.sInv2rho = 1.0 / (2.0 * p.rho);
   a.dxc = 2.0 * p.rho * p.kappa / sqrt(p.eta);
   a.k2 = p.kappa * p.kappa;
+  a.inv_eta = 1.0 / p.eta;
+  a.eta_k2 = p.eta / a.k2;
+  a.rho2 = 2.0 * p.rho;
+  a.inv_dx = 1.0 / p.dx;
+  a.inv_dy = 1.0 / p.dy;
+  a.inv_dz2 = 1.0 / p.dz2;
+  a.inv_dV3 = 1.0 / a.dV3;
   a.field_evolve = p.field_evolve;
   a.electrons_evolve = p.electrons_evolve;
   a.coupling = p.coupling;
@@ -579,6 +592,7 @@ int pf_rk4_fp64(pf_handle *h, double szl, double hstep, unsigned int *status_out
     int place;
     pf_taper_stage(h, stage_sz[s - 1], &n2col, &place);
     a.n2col = n2col;
+    a.kn2col = p.kappa * n2col;
     pf_stage_coefficients(p, stage_sz[s - 1], n2col, place, &a.bf);
     a.cstate = stage_c[s - 1];
     a.ar = (s == 1) ? h->wr : h->asr;

@@ -140,7 +140,8 @@ def test_one_step_planepole_taper_ends_focusing(place_sz):
     lamr = 4.0 * configs.PUFFIN_PI * 0.004
     p = _planepole_params(und_ends=1, szfs=2 * lamr, szfe=0.8, undgrad=-0.05, focusing=1,
                           kbxsf=0.3, kbysf=0.4)
-    beam = _beam3d(p, 2500, 7, 0.2, 0.8)
+    lz2 = (p.nz2 - 1) * p.dz2
+    beam = _beam3d(p, 2500, 7, 0.2 * lz2, 0.8 * lz2)
     field = random_field(p, 3)
     h = lamr / 24.0
     taper = (1.0, 1.0, p.undgrad)
@@ -259,7 +260,8 @@ def test_out_of_window_leaves_state_and_recovers():
 
 def test_out_of_temporal_mesh_raises():
     p = _planepole_params()
-    beam = _beam3d(p, 100, 1, 0.1, 0.5)
+    lz2 = (p.nz2 - 1) * p.dz2
+    beam = _beam3d(p, 100, 1, 0.1 * lz2, 0.5 * lz2)
     beam["z2"][7] = (p.nz2 - 1) * p.dz2 + 0.5 * p.dz2   # beyond the last node
     with P.Puffin(p) as sim:
         sim.set_particles(*(beam[k] for k in P.PARTICLE_KEYS))
