@@ -187,6 +187,31 @@ const char *pf_last_error(const pf_handle *h);
 
 int pf_abi_version(void);
 
+/* Allocation-free RK4 step (no counterpart in the reference).  For callers
+ * that cannot allocate device memory -- a host program whose device memory
+ * belongs to its own pool allocator, a plugin host that hands in buffers it
+ * allocated up front, or a loop that cannot afford cudaMalloc's implicit
+ * device-wide synchronisation.  It does what pf_rk4_step does, without a
+ * handle: the caller passes the particle arrays and the inner-window field
+ * (nix * niy * planes values each, planes = nz2 or nz2 - 1 on the periodic
+ * mesh, layout of outer2Inner) as device pointers, updated in place, and the
+ * taper state (n2col, n2col0) in host memory, updated like getAlpha does.
+ * The RK4 temporaries live in one fixed-size file-scope device array of the
+ * library, held by every GPU that loads it until the process exits.
+ * Limits: np <= PF_NOALLOC_MAX_PARTICLES and nix*niy*planes <=
+ * PF_NOALLOC_MAX_NODES, else PF_BAD_ARG.  Calls share that array: calls that
+ * overlap on the GPU (different streams, several host threads) race.  The
+ * first call on a device looks up the array's device address with that device
+ * current; make it before any stream capture.  stream may be NULL (the
+ * default stream).  Returns as pf_rk4_step; on PF_OUT_OF_WINDOW the state is
+ * left unchanged. */
+#define PF_NOALLOC_MAX_PARTICLES 32768
+#define PF_NOALLOC_MAX_NODES 32768
+int pf_rk4_step_noalloc(const pf_params *p, double *n2col, double *n2col0, double szl,
+                        double hstep, int64_t np, double *x, double *y, double *z2, double *px,
+                        double *py, double *gam, const double *chi, double *wr, double *wi,
+                        int32_t nix, int32_t niy, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -17,6 +17,9 @@
 #include <math.h>
 #include <string.h>
 
+#include <algorithm>
+#include <mutex>
+
 #include "pf_internal.h"
 
 namespace {
@@ -617,5 +620,247 @@ int pf_rk4_fp64(pf_handle *h, double szl, double hstep, unsigned int *status_out
   pf_prof_flush(h);
   *status_out = *h->h_status;
   if (*status_out == 0u) h->cur = nxt;
+  return PF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free RK4 step.
+//
+// Some callers of this library cannot allocate device memory: a host program
+// whose device memory belongs to its own pool allocator and forbids allocations
+// from outside it, a plugin host that hands in buffers it allocated up front,
+// or a time-critical loop that cannot afford cudaMalloc's implicit device-wide
+// synchronisation.  pf_rk4_step_noalloc serves them: the caller owns the
+// particle arrays and the inner-window field (device memory, updated in place)
+// and the RK4 temporaries live in the fixed-size file-scope device array below,
+// which every GPU that loads this library holds until the process exits.
+//
+// Limits: at most PF_NOALLOC_MAX_PARTICLES macroparticles and
+// PF_NOALLOC_MAX_NODES inner-window nodes (nix * niy * planes held); larger
+// problems are rejected with PF_BAD_ARG.  Every call uses the same array and
+// leaves its contents behind, so each call clears what must start at zero (the
+// deposit accumulators and the status word); two calls that overlap on the GPU
+// (e.g. on different streams) race on it.  The first call on a device looks up
+// the array's device address (cudaGetSymbolAddress) with that device current;
+// make that first call before any stream capture.
+namespace {
+
+constexpr int64_t NA_NP = PF_NOALLOC_MAX_PARTICLES;
+constexpr int64_t NA_NW = PF_NOALLOC_MAX_NODES;
+// doubles: k1, ka, kb, next state (6 arrays each of NA_NP); stage field,
+// field slopes d0, d12 (re, im each of NA_NW); then 4 * NA_NW 64-bit deposit
+// words, the status word and a reduction word.
+constexpr size_t NA_DOUBLES = (size_t)24 * NA_NP + (size_t)6 * NA_NW;
+constexpr size_t NA_BYTES = NA_DOUBLES * 8 + (size_t)4 * NA_NW * 8 + 2 * 256;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
+
+std::mutex g_noalloc_mutex;
+void *g_noalloc_ptr[64] = {};
+
+__global__ void k_noalloc_absmax(const double *v, int64_t n, unsigned long long *out) {
+  unsigned long long m = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    m = max(m, (unsigned long long)__double_as_longlong(fabs(v[i])));
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+}  // namespace
+
+extern "C" int pf_rk4_step_noalloc(const pf_params *p, double *n2col, double *n2col0,
+                                   double szl, double hstep, int64_t np, double *x, double *y,
+                                   double *z2, double *px, double *py, double *gam,
+                                   const double *chi, double *wr, double *wi, int32_t nix,
+                                   int32_t niy, void *stream) {
+  if (!p || !n2col || !n2col0 || np < 0 || nix < 1 || niy < 1) return PF_BAD_ARG;
+  if (np > 0 && (!x || !y || !z2 || !px || !py || !gam || !chi)) return PF_BAD_ARG;
+  if (!wr || !wi) return PF_BAD_ARG;
+  if (p->precision != PF_FP64 || p->nz2 < 2 || p->dz2 <= 0.0 || p->dx <= 0.0 || p->dy <= 0.0)
+    return PF_BAD_ARG;
+  if (p->one_d && (nix != 1 || niy != 1)) return PF_BAD_ARG;
+  const int64_t npl = (p->mesh_type == PF_MESH_PERIODIC) ? p->nz2 - 1 : p->nz2;
+  const int64_t nwin = (int64_t)nix * niy * npl;
+  if (np > NA_NP || nwin > NA_NW) return PF_BAD_ARG;  // beyond the fixed scratch
+  cudaStream_t st = (cudaStream_t)stream;
+
+  // one-time lookup of the scratch array's device address on this device
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return PF_CUDA_ERR;
+  unsigned char *base;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+      void *ptr = nullptr;
+      if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || !ptr) return PF_CUDA_ERR;
+      g_noalloc_ptr[dev] = ptr;
+    }
+    base = (unsigned char *)g_noalloc_ptr[dev];
+  }
+  double *dbl = (double *)base;
+  double *k1[6], *ka[6], *kb[6], *ynext[6];
+  for (int j = 0; j < 6; ++j) {
+    k1[j] = dbl + (size_t)j * NA_NP;
+    ka[j] = dbl + (size_t)(6 + j) * NA_NP;
+    kb[j] = dbl + (size_t)(12 + j) * NA_NP;
+    ynext[j] = dbl + (size_t)(18 + j) * NA_NP;
+  }
+  double *fld = dbl + (size_t)24 * NA_NP;
+  double *asr = fld, *asi = fld + NA_NW, *d0r = fld + 2 * NA_NW, *d0i = fld + 3 * NA_NW;
+  double *d12r = fld + 4 * NA_NW, *d12i = fld + 5 * NA_NW;
+  unsigned long long *acc = (unsigned long long *)(base + NA_DOUBLES * 8);
+  unsigned int *status = (unsigned int *)(base + NA_DOUBLES * 8 + (size_t)4 * NA_NW * 8);
+  unsigned long long *red = (unsigned long long *)((unsigned char *)status + 256);
+
+  // the array keeps the previous call's contents: clear what must start at zero
+  if (cudaMemsetAsync(acc, 0, (size_t)4 * NA_NW * 8, st) != cudaSuccess) return PF_CUDA_ERR;
+  if (cudaMemsetAsync(status, 0, sizeof(unsigned int), st) != cudaSuccess) return PF_CUDA_ERR;
+  if (cudaMemsetAsync(red, 0, sizeof(unsigned long long), st) != cudaSuccess) return PF_CUDA_ERR;
+
+  // fixed-point scale of the deposit from max |chi| / dV3
+  double chimax = 0.0;
+  if (np > 0) {
+    k_noalloc_absmax<<<(unsigned)std::min<int64_t>((np + 255) / 256, 1024), 256, 0, st>>>(chi, np, red);
+    if (cudaGetLastError() != cudaSuccess) return PF_CUDA_ERR;
+    unsigned long long r = 0;
+    if (cudaMemcpyAsync(&r, red, sizeof(r), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+      return PF_CUDA_ERR;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return PF_CUDA_ERR;
+    memcpy(&chimax, &r, sizeof(r));
+  }
+  int lg = 0;
+  while ((int64_t(1) << lg) < 2 * np + 2) ++lg;
+  const int fix_maxexp = 126 - lg;
+  const double smax = chimax / (p->dx * p->dy * p->dz2);
+  const int fix_e = fix_maxexp - 16 - ((smax > 0.0 && isfinite(smax)) ? ilogb(smax) + 1 : 0);
+
+  StageArgs a;
+  memset(&a, 0, sizeof(a));
+  a.x = x;
+  a.y = y;
+  a.z2 = z2;
+  a.px = px;
+  a.py = py;
+  a.gam = gam;
+  a.chi = chi;
+  a.np = np;
+  a.h6 = hstep / 6.0;
+  a.acc_lo_r = acc;
+  a.acc_hi_r = acc + NA_NW;
+  a.acc_lo_i = acc + 2 * NA_NW;
+  a.acc_hi_i = acc + 3 * NA_NW;
+  a.nix = nix;
+  a.niy = niy;
+  a.npl = npl;
+  a.nz2 = p->nz2;
+  a.periodic = (p->mesh_type == PF_MESH_PERIODIC);
+  a.one_d = p->one_d;
+  a.dx = p->dx;
+  a.dy = p->dy;
+  a.dz2 = p->dz2;
+  a.dV3 = p->dx * p->dy * p->dz2;
+  a.halfx = ((double)(nix - 1) / 2.0) * p->dx;
+  a.halfy = ((double)(niy - 1) / 2.0) * p->dy;
+  a.eta = p->eta;
+  a.kappa = p->kappa;
+  a.rho = p->rho;
+  a.gamma_r = p->gamma_r * p->gamma_r;
+  a.aw = p->aw * p->aw;
+  a.sInv2rho = 1.0 / (2.0 * p->rho);
+  a.dxc = 2.0 * p->rho * p->kappa / sqrt(p->eta);
+  a.k2 = p->kappa * p->kappa;
+  a.inv_eta = 1.0 / p->eta;
+  a.eta_k2 = p->eta / a.k2;
+  a.rho2 = 2.0 * p->rho;
+  a.inv_dx = 1.0 / p->dx;
+  a.inv_dy = 1.0 / p->dy;
+  a.inv_dz2 = 1.0 / p->dz2;
+  a.inv_dV3 = 1.0 / a.dV3;
+  a.field_evolve = p->field_evolve;
+  a.electrons_evolve = p->electrons_evolve;
+  a.coupling = p->coupling;
+  a.fix_e = fix_e;
+  a.fix_maxexp = fix_maxexp;
+  a.status = status;
+
+  NodeArgs nd;
+  memset(&nd, 0, sizeof(nd));
+  nd.n = nwin;
+  nd.acc_lo_r = a.acc_lo_r;
+  nd.acc_hi_r = a.acc_hi_r;
+  nd.acc_lo_i = a.acc_lo_i;
+  nd.acc_hi_i = a.acc_hi_i;
+  nd.wr = wr;
+  nd.wi = wi;
+  nd.asr = asr;
+  nd.asi = asi;
+  nd.d0r = d0r;
+  nd.d0i = d0i;
+  nd.d12r = d12r;
+  nd.d12i = d12i;
+  nd.h6 = a.h6;
+  nd.fix_e = fix_e;
+  nd.status = status;
+  const double inv_scale = ldexp(1.0, -fix_e);
+
+  const double hh = hstep * 0.5, szh = szl + hh;
+  const double stage_sz[4] = {szl, szh, szh, szl + hstep};
+  const double stage_c[4] = {0.0, hh, hh, hstep};
+  const unsigned pg = (unsigned)std::max<int64_t>(1, (np + 255) / 256);
+  const unsigned ng = (unsigned)std::max<int64_t>(1, (nwin + 255) / 256);
+  for (int s = 1; s <= 4; ++s) {
+    // getAlpha (wiggler_taper.f90:39-47) and adjUndPlace on the caller's state
+    const double sz = stage_sz[s - 1];
+    if ((sz >= p->szfs) && (sz <= p->szfe)) *n2col = *n2col0 + p->undgrad * (sz - p->szfs);
+    else if (sz > p->szfe) *n2col0 = *n2col;
+    int place = 1;
+    if (p->und_ends) place = (sz <= p->szfs) ? 0 : (sz >= p->szfe) ? 2 : 1;
+    a.n2col = *n2col;
+    a.kn2col = p->kappa * *n2col;
+    pf_stage_coefficients(*p, sz, *n2col, place, &a.bf);
+    a.cstate = stage_c[s - 1];
+    a.ar = (s == 1) ? wr : asr;
+    a.ai = (s == 1) ? wi : asi;
+    for (int j = 0; j < 6; ++j) {
+      a.kin[j] = (s == 2) ? k1[j] : (s == 3) ? ka[j] : (s == 4) ? kb[j] : nullptr;
+      a.kout[j] = (s == 1) ? k1[j] : (s == 3) ? kb[j] : nullptr;
+      a.kacc[j] = (s >= 2) ? ka[j] : nullptr;
+      a.k1[j] = k1[j];
+      a.ynext[j] = ynext[j];
+    }
+    if (np > 0) {
+      const bool oned = p->one_d != 0;
+      switch (s) {
+        case 1: oned ? k_stage<1, true><<<pg, 256, 0, st>>>(a) : k_stage<1, false><<<pg, 256, 0, st>>>(a); break;
+        case 2: oned ? k_stage<2, true><<<pg, 256, 0, st>>>(a) : k_stage<2, false><<<pg, 256, 0, st>>>(a); break;
+        case 3: oned ? k_stage<3, true><<<pg, 256, 0, st>>>(a) : k_stage<3, false><<<pg, 256, 0, st>>>(a); break;
+        default: oned ? k_stage<4, true><<<pg, 256, 0, st>>>(a) : k_stage<4, false><<<pg, 256, 0, st>>>(a); break;
+      }
+      if (cudaGetLastError() != cudaSuccess) return PF_CUDA_ERR;
+    }
+    nd.coef = (s == 3) ? hstep : hh;
+    switch (s) {
+      case 1: k_nodes<1><<<ng, 256, 0, st>>>(nd, inv_scale); break;
+      case 2: k_nodes<2><<<ng, 256, 0, st>>>(nd, inv_scale); break;
+      case 3: k_nodes<3><<<ng, 256, 0, st>>>(nd, inv_scale); break;
+      default: k_nodes<4><<<ng, 256, 0, st>>>(nd, inv_scale); break;
+    }
+    if (cudaGetLastError() != cudaSuccess) return PF_CUDA_ERR;
+  }
+  unsigned int hst = 0;
+  if (cudaMemcpyAsync(&hst, status, sizeof(hst), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+    return PF_CUDA_ERR;
+  if (cudaStreamSynchronize(st) != cudaSuccess) return PF_CUDA_ERR;
+  if (hst != 0u) {
+    if (hst & ST_OVERFLOW) return PF_OVERFLOW;
+    if (hst & ST_OUT_OF_Z2) return PF_OUT_OF_Z2;
+    return PF_OUT_OF_WINDOW;  // state left unchanged, as the reference
+  }
+  double *dst[6] = {x, y, z2, px, py, gam};
+  for (int j = 0; j < 6 && np > 0; ++j)
+    if (cudaMemcpyAsync(dst[j], ynext[j], sizeof(double) * (size_t)np, cudaMemcpyDeviceToDevice,
+                        st) != cudaSuccess)
+      return PF_CUDA_ERR;
+  if (cudaStreamSynchronize(st) != cudaSuccess) return PF_CUDA_ERR;
   return PF_OK;
 }

@@ -204,3 +204,28 @@ class Puffin:
         self._check(self._lib.pf_profile_read(self._h, int(kernel_class), ctypes.byref(ms),
                                               ctypes.byref(n)))
         return ms.value, n.value
+
+
+def rk4_step_noalloc(params, taper, szl, h, particles, wr, wi, nix, niy, stream=None):
+    """One RK4 step through pf_rk4_step_noalloc, for callers that cannot
+    allocate device memory (their device memory belongs to another allocator,
+    or they must avoid cudaMalloc's implicit synchronisation): the caller's
+    CUDA float64 tensors are updated in place and the library's temporaries
+    come from its fixed-size static device array (at most
+    NOALLOC_MAX_PARTICLES macroparticles and NOALLOC_MAX_NODES window nodes).
+    ``taper`` is a two-element list [n2col, n2col0], updated in place.
+    Returns True, or False (state unchanged) if a particle left the window."""
+    lib = L.load()
+    n2c = ctypes.c_double(taper[0])
+    n2c0 = ctypes.c_double(taper[1])
+    ptrs = [_dev(particles[k])[1] for k in PARTICLE_KEYS]
+    np_ = len(particles["x"])
+    rc = lib.pf_rk4_step_noalloc(ctypes.byref(params), ctypes.byref(n2c), ctypes.byref(n2c0),
+                                 float(szl), float(h), np_, *ptrs, _dev(wr)[1], _dev(wi)[1],
+                                 int(nix), int(niy), stream)
+    taper[0], taper[1] = n2c.value, n2c0.value
+    if rc == L.PF_OUT_OF_WINDOW:
+        return False
+    if rc != L.PF_OK:
+        raise PuffinError(rc, "pf_rk4_step_noalloc failed")
+    return True
