@@ -59,6 +59,7 @@ def parse():
     ap.add_argument("--nz2", type=int, default=4096,
                     help="z2 nodes of the mesh (smaller only for profiling captures)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision leg")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     return ap.parse_args()
 
@@ -193,18 +194,20 @@ def cpu_baseline(w, seconds):
 
 
 # ---------------------------------------------------------------------------
-def run_gpu(args, rank, world):
+def _time_path(args, dev, precision, world, stream_events=True):
+    """Run the workload on one precision path: W warm-up steps, then K timed
+    steps (CUDA events on the library's stream).  Returns timings, the
+    per-kernel-class device times and the final radiated power sum |A|^2."""
     import torch
 
     import puffin_gb300 as P
     from puffin_gb300 import configs
     from puffin_gb300 import lib as L
 
-    dev = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(dev)
     w = configs.config2(np_=args.np, nz2=args.nz2)
     p = w.params
     p.device = dev
+    p.precision = precision
     sim = P.Puffin(p)
     sim.set_particles(*(w.beam[k] for k in P.PARTICLE_KEYS))
     sim.set_field(*w.field)
@@ -241,12 +244,32 @@ def run_gpu(args, rank, world):
         e1.record(stream)
         torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
-    launches = sim.kernel_launches - launches0
-    stage_ms, stage_n = sim.profile_read(L.PROF_STAGE)
-    nodes_ms, nodes_n = sim.profile_read(L.PROF_NODES)
-    fft_ms, fft_n = sim.profile_read(L.PROF_FFT)
-    diff_ms, diff_n = sim.profile_read(L.PROF_DIFF)
+    out = {
+        "w": w, "sim": sim, "step": step, "stream": stream, "win": win, "ms": ms,
+        "launches": sim.kernel_launches - launches0, "clocks": clk.summary(),
+        "kernel": {name: sim.profile_read(cls) for name, cls in
+                   (("stage", L.PROF_STAGE), ("nodes", L.PROF_NODES), ("fft", L.PROF_FFT),
+                    ("diff_elementwise", L.PROF_DIFF))},
+    }
     sim.profile(False)
+    fr, fi = sim.get_field()
+    out["power"] = float(np.sum(fr * fr + fi * fi))
+    return out
+
+
+def run_gpu(args, rank, world):
+    import torch
+
+    import puffin_gb300 as P
+    from puffin_gb300 import lib as L
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    r64 = _time_path(args, dev, P.FP64, world)
+    w, sim, step, stream, win = r64["w"], r64["sim"], r64["step"], r64["stream"], r64["win"]
+    p = w.params
+    ms = r64["ms"]
+    every = w.isteps4diff
 
     # end to end through the C ABI with host buffers
     n = w.np
@@ -280,16 +303,23 @@ def run_gpu(args, rank, world):
     d2h = h2d
     sim.close()
 
-    times = torch.tensor([ms, e2e_ms], dtype=torch.float64, device=f"cuda:{dev}")
+    rmx = None
+    if not args.no_mixed:
+        rmx = _time_path(args, dev, P.MIXED, world)
+        rmx["sim"].close()
+
+    times = torch.tensor([ms, e2e_ms, rmx["ms"] if rmx else 0.0], dtype=torch.float64,
+                         device=f"cuda:{dev}")
     if world > 1:
         torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
-    ms, e2e_ms = float(times[0]), float(times[1])
+    ms, e2e_ms, mx_ms = (float(v) for v in times)
     if rank != 0:
         return None
 
     value = world * n * args.steps / (ms * 1e-3)
     e2e_value = world * n * args.e2e_steps / (e2e_ms * 1e-3) if args.e2e_steps > 0 else None
     peak, peak_kind = measured_peaks()
+    stage_ms, stage_n = r64["kernel"]["stage"]
     stage_avg = stage_ms / max(1, stage_n)
     achieved = n * BYTES_PER_PARTICLE_STAGE / (stage_avg * 1e-3) / 1e9
     # FP64 peak of this GPU, measured with a cuBLAS DGEMM
@@ -305,6 +335,8 @@ def run_gpu(args, rank, world):
     torch.cuda.synchronize()
     dgemm_tflops = 3 * 2 * 4096 ** 3 / (g0.elapsed_time(g1) * 1e-3) / 1e12
     fp64_achieved = n * FLOPS_PER_PARTICLE_STAGE / (stage_avg * 1e-3) / 1e12
+    kern = {k: v[0] for k, v in r64["kernel"].items()}
+    kern.update({k + "_launches": v[1] for k, v in r64["kernel"].items()})
     rec = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup,
@@ -313,25 +345,40 @@ def run_gpu(args, rank, world):
         "data": "synthetic (seeded beam and zero seed field; no dataset)",
         "config": {
             "workload": w.name, "macroparticles": n, "mesh": [p.nx, p.ny, p.nz2],
-            "inner_window": list(win),
-            "steps_per_period": 24, "diffraction_every": every, "precision": "fp64",
+            "inner_window": list(win), "steps_per_period": 24, "diffraction_every": every,
+            "precision": "fp64 (value); mixed in 'mixed'",
             "parallelism": f"replicas x{world}",
             "l2": "inputs larger than L2 (particle state 470 MB, field 1.09 GB per array pair)",
         },
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "steps": args.e2e_steps},
-        "gpu_launches": launches,
-        "kernel_ms": {"stage": stage_ms, "nodes": nodes_ms, "fft": fft_ms, "diff_elementwise": diff_ms,
-                      "stage_launches": stage_n, "node_launches": nodes_n, "fft_launches": fft_n,
-                      "diff_launches": diff_n},
-        "roofline": {"kernel": "k_stage (fused RK4 stage)", "bound": "hbm", "achieved": achieved,
-                     "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+        "gpu_launches": r64["launches"] + (rmx["launches"] if rmx else 0),
+        "kernel_ms": kern,
+        "roofline": {"kernel": "k_stage (fused FP64 RK4 stage)", "bound": "hbm",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": f"{peak_kind} copy bandwidth (burst)", "traffic": None,
                      "fp64": {"achieved_tflops": fp64_achieved, "peak_tflops": dgemm_tflops,
                               "peak_kind": "measured cuBLAS DGEMM 4096^3",
                               "frac": fp64_achieved / dgemm_tflops}},
-        "clocks": clk.summary(),
+        "clocks": r64["clocks"],
     }
+    if rmx:
+        mst, msn = rmx["kernel"]["stage"]
+        mavg = mst / max(1, msn)
+        m_ach = n * BYTES_PER_PARTICLE_STAGE / (mavg * 1e-3) / 1e9
+        mk = {k: v[0] for k, v in rmx["kernel"].items()}
+        rec["mixed"] = {
+            "value": world * n * args.steps / (mx_ms * 1e-3), "unit": UNIT,
+            "ms_per_step": mx_ms / args.steps, "speedup_vs_fp64": ms / mx_ms,
+            "dtype": "f32 field/weights/deposit/FFT, f64 state/p2/RK4 combination",
+            "power_rel_error_vs_fp64": abs(rmx["power"] - r64["power"]) / max(r64["power"], 1e-300),
+            "power_after_steps": {"fp64": r64["power"], "mixed": rmx["power"],
+                                  "steps": args.warmup + args.steps},
+            "kernel_ms": mk,
+            "roofline": {"kernel": "k_stage_mixed", "bound": "hbm", "achieved": m_ach,
+                         "peak": peak, "unit": "GB/s", "frac": m_ach / peak},
+            "clocks": rmx["clocks"],
+        }
     return rec
 
 

@@ -1,0 +1,850 @@
+// FFT diffraction kernels and host plan, instantiated once per real type
+// (included by fft.cu with FFT_T = double / float and FFT_NS = fft64 / fft32).
+
+namespace FFT_NS {
+
+typedef FFT_T real;
+
+
+struct cplx {
+  real r, i;
+};
+
+__device__ __forceinline__ cplx cmul(cplx a, cplx b) {
+  return cplx{a.r * b.r - a.i * b.i, a.r * b.i + a.i * b.r};
+}
+__device__ __forceinline__ cplx cadd(cplx a, cplx b) { return cplx{a.r + b.r, a.i + b.i}; }
+__device__ __forceinline__ cplx csub(cplx a, cplx b) { return cplx{a.r - b.r, a.i - b.i}; }
+
+constexpr int MAX_PASSES = 16;
+constexpr int NTHREADS = 256;
+
+// odd prime radices with unrolled butterflies; offsets into c_roots
+constexpr int ODD_R[] = {3, 5, 7, 11, 13, 17, 43};
+constexpr int N_ODD = 7;
+__host__ __device__ constexpr int root_off(int R) {
+  int off = 0;
+  for (int q = 0; q < N_ODD; ++q) {
+    if (ODD_R[q] == R) return off;
+    off += ODD_R[q];
+  }
+  return -1;
+}
+constexpr int ROOTS_TOTAL = 3 + 5 + 7 + 11 + 13 + 17 + 43;
+__constant__ cplx c_roots[ROOTS_TOTAL];  // (cos, sin)(2 pi m / R)
+
+
+struct AxisPlan {
+  int n;
+  int npass;
+  int radix[MAX_PASSES];
+  int ns[MAX_PASSES];
+  int twoff[MAX_PASSES];
+  int64_t stride;   // element stride along the axis
+  int64_t inner;    // base(L) = L % inner + (L / inner) * ostride
+  int64_t ostride;
+  int64_t nlines;
+  int lpb;
+  int axis;         // 0 x, 1 y, 2 z
+};
+
+struct MulTables {
+  const cplx *px, *py;         // propagator factors (x,z) and (y,z)
+  const real *dxt, *dyt;       // damping factors (x,z) and (y,z)
+  const unsigned char *zflag;  // bit0: pass band, bit1: kz != 0
+  const real *mask;            // transverse mask (y,x)
+  const real *mz;              // z2 mask
+  int nx, ny, nz;
+  int qfilter;
+  real ffact;
+};
+
+enum { MID_NONE = 0, MID_PROP = 1, MID_DAMP = 2, MID_SPLIT = 3, MID_RECOMB = 4 };
+
+struct FftArgs {
+  cplx *A;
+  cplx *anb;
+  const real *re_in, *im_in;    // split input (first pass)
+  real *re_out, *im_out;        // split output (last pass)
+  const cplx *tw_f, *tw_b;      // per-pass twiddles, forward and backward
+  AxisPlan ax;
+  MulTables T;
+  int dir;       // direction of the first transform: 0 forward, 1 backward
+  int mid;       // MID_*: operation after the first transform
+  int second;    // run the opposite transform after the mid operation
+  int load_split, store_split;
+  int mirror;    // periodic: also write plane nz (mirror of plane 0) of the output
+};
+
+__device__ __forceinline__ int64_t line_base(const AxisPlan &p, int64_t L) {
+  return (L % p.inner) + (L / p.inner) * p.ostride;
+}
+
+// ---- butterflies -------------------------------------------------------------
+template <bool INV>
+__device__ __forceinline__ cplx mul_mi(cplx b) {  // b * (-i) forward, b * (+i) backward
+  return INV ? cplx{-b.i, b.r} : cplx{b.i, -b.r};
+}
+
+template <bool INV>
+__device__ __forceinline__ void dft4(cplx &x0, cplx &x1, cplx &x2, cplx &x3) {
+  const cplx a0 = cadd(x0, x2), a1 = csub(x0, x2);
+  const cplx b0 = cadd(x1, x3), b1 = mul_mi<INV>(csub(x1, x3));
+  x0 = cadd(a0, b0);
+  x2 = csub(a0, b0);
+  x1 = cadd(a1, b1);
+  x3 = csub(a1, b1);
+}
+
+// DFT of v[0..R) written to dst[0], dst[ds], ..., dst[(R-1) ds].
+template <int R, bool INV>
+__device__ __forceinline__ void dft_store(cplx *v, cplx *dst, int ds) {
+  if constexpr (R == 2) {
+    dst[0] = cadd(v[0], v[1]);
+    dst[ds] = csub(v[0], v[1]);
+  } else if constexpr (R == 4) {
+    dft4<INV>(v[0], v[1], v[2], v[3]);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) dst[r * ds] = v[r];
+  } else if constexpr (R == 8) {
+    cplx e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
+    cplx o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
+    dft4<INV>(e0, e1, e2, e3);
+    dft4<INV>(o0, o1, o2, o3);
+    const real s = (real)0.70710678118654752440;
+    // W8^1 = (s, -s) forward, (s, s) backward; W8^2 = -i / +i; W8^3 = (-s, -s) / (-s, s)
+    const cplx t1 = INV ? cplx{s * (o1.r - o1.i), s * (o1.r + o1.i)}
+                        : cplx{s * (o1.r + o1.i), s * (o1.i - o1.r)};
+    const cplx t2 = mul_mi<INV>(o2);
+    const cplx t3 = INV ? cplx{-s * (o3.r + o3.i), s * (o3.r - o3.i)}
+                        : cplx{s * (o3.i - o3.r), -s * (o3.r + o3.i)};
+    dst[0] = cadd(e0, o0);
+    dst[4 * ds] = csub(e0, o0);
+    dst[ds] = cadd(e1, t1);
+    dst[5 * ds] = csub(e1, t1);
+    dst[2 * ds] = cadd(e2, t2);
+    dst[6 * ds] = csub(e2, t2);
+    dst[3 * ds] = cadd(e3, t3);
+    dst[7 * ds] = csub(e3, t3);
+  }
+}
+
+// Threads that share one odd-prime butterfly (each computes a subset of the
+// output pairs), so a pass over few long butterflies still fills the block.
+__host__ __device__ constexpr int odd_groups(int R) {
+  return R >= 43 ? 7 : (R >= 17 ? 4 : (R >= 13 ? 3 : (R >= 11 ? 5 : 1)));
+}
+
+// Odd prime radix: X[q] = x0 + sum_j a_j cos(2 pi jq/R) -/+ i sum_j b_j sin(2 pi jq/R)
+// with a_j = v_j + v_{R-j}, b_j = v_j - v_{R-j} formed as the inputs arrive,
+// so only (R-1) complex values are live.  Thread g of the G sharing the
+// butterfly writes X[0] (g = 0) and the pairs q = g+1, g+1+G, ...
+template <int R, bool INV>
+__device__ __forceinline__ void odd_butterfly(const cplx *src, int nb, const cplx *twk, bool twiddle,
+                                              cplx *dst, int ds, int g) {
+  constexpr int H = (R - 1) / 2;
+  constexpr int G = odd_groups(R);
+  constexpr int OFF = root_off(R);
+  static_assert(OFF >= 0, "radix without an unrolled butterfly");
+  cplx a[H], b[H];
+  const cplx x0 = src[0];
+  cplx s0 = x0;
+#pragma unroll
+  for (int j = 1; j <= H; ++j) {
+    cplx u = src[j * nb], w = src[(R - j) * nb];
+    if (twiddle) {
+      u = cmul(u, twk[j]);
+      w = cmul(w, twk[R - j]);
+    }
+    a[j - 1] = cadd(u, w);
+    b[j - 1] = csub(u, w);
+    s0 = cadd(s0, a[j - 1]);
+  }
+  if (g == 0) dst[0] = s0;
+  // the root index m = j*q mod R is uniform across the threads of a group
+#pragma unroll 1
+  for (int q = g + 1; q <= H; q += G) {
+    cplx C = x0, S{(real)0, (real)0};
+    int m = 0;
+#pragma unroll
+    for (int j = 1; j <= H; ++j) {
+      m += q;
+      if (m >= R) m -= R;
+      const real c = c_roots[OFF + m].r;
+      const real sn = c_roots[OFF + m].i;
+      C.r = fma(a[j - 1].r, c, C.r);
+      C.i = fma(a[j - 1].i, c, C.i);
+      S.r = fma(b[j - 1].r, sn, S.r);
+      S.i = fma(b[j - 1].i, sn, S.i);
+    }
+    if (!INV) {
+      dst[q * ds] = cplx{C.r + S.i, C.i - S.r};
+      dst[(R - q) * ds] = cplx{C.r - S.i, C.i + S.r};
+    } else {
+      dst[q * ds] = cplx{C.r - S.i, C.i + S.r};
+      dst[(R - q) * ds] = cplx{C.r + S.i, C.i - S.r};
+    }
+  }
+}
+
+// Odd prime radix shared by G > 1 threads per butterfly: the G threads first
+// form a_j, b_j together into shared scratch (stride R complex per butterfly,
+// which keeps the groups of a warp on distinct banks), then each computes its
+// output pairs reading them back.  Only a handful of registers stay live.
+template <int R, bool INV>
+__device__ __forceinline__ void odd_pass_shared(const cplx *in, cplx *out, int n, int nl, int Ns,
+                                                const cplx *tw, cplx *scratch) {
+  constexpr int H = (R - 1) / 2;
+  constexpr int G = odd_groups(R);
+  constexpr int OFF = root_off(R);
+  constexpr int BPR = NTHREADS / G;  // butterflies per round
+  const int nb = n / R;
+  const int nbt = nl * nb;
+  const int btl = threadIdx.x / G, g = threadIdx.x - (threadIdx.x / G) * G;
+  for (int base = 0; base < nbt; base += BPR) {
+    const int bt = base + btl;
+    const bool act = (btl < BPR) && (bt < nbt);
+    int l = 0, j = 0, k = 0;
+    cplx *ab = scratch + btl * R;
+    if (act) {
+      l = bt / nb;
+      j = bt - l * nb;
+      k = j % Ns;
+      const cplx *src = in + l * n + j;
+      const cplx *twk = tw + k * R;
+      for (int jj = g + 1; jj <= H; jj += G) {
+        cplx u = src[jj * nb], w = src[(R - jj) * nb];
+        if (Ns > 1) {
+          u = cmul(u, twk[jj]);
+          w = cmul(w, twk[R - jj]);
+        }
+        ab[jj - 1] = cadd(u, w);
+        ab[H + jj - 1] = csub(u, w);
+      }
+    }
+    __syncthreads();
+    if (act) {
+      const cplx x0 = in[l * n + j];
+      cplx *dst = out + l * n + (j / Ns) * Ns * R + k;
+      if (g == 0) {
+        cplx s0 = x0;
+#pragma unroll
+        for (int jj = 0; jj < H; ++jj) s0 = cadd(s0, ab[jj]);
+        dst[0] = s0;
+      }
+#pragma unroll 1
+      for (int q = g + 1; q <= H; q += G) {
+        cplx C = x0, S{(real)0, (real)0};
+        int m = 0;
+#pragma unroll
+        for (int jj = 1; jj <= H; ++jj) {
+          m += q;
+          if (m >= R) m -= R;
+          const real c = c_roots[OFF + m].r;
+          const real sn = c_roots[OFF + m].i;
+          const cplx av = ab[jj - 1], bv = ab[H + jj - 1];
+          C.r = fma(av.r, c, C.r);
+          C.i = fma(av.i, c, C.i);
+          S.r = fma(bv.r, sn, S.r);
+          S.i = fma(bv.i, sn, S.i);
+        }
+        if (!INV) {
+          dst[q * Ns] = cplx{C.r + S.i, C.i - S.r};
+          dst[(R - q) * Ns] = cplx{C.r - S.i, C.i + S.r};
+        } else {
+          dst[q * Ns] = cplx{C.r - S.i, C.i + S.r};
+          dst[(R - q) * Ns] = cplx{C.r + S.i, C.i - S.r};
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// scratch (complex values) an odd radix needs in odd_pass_shared
+__host__ __device__ constexpr int odd_scratch(int R) {
+  return odd_groups(R) > 1 ? (NTHREADS / odd_groups(R)) * R : 0;
+}
+
+// One Stockham pass of radix R from `in` to `out` over nl lines of length n.
+template <int R, bool INV>
+__device__ __forceinline__ void stockham_pass(const cplx *in, cplx *out, int n, int nl, int Ns,
+                                              const cplx *tw, cplx *scratch) {
+  const int nb = n / R;
+  if constexpr (R == 2 || R == 4 || R == 8) {
+    const int total = nl * nb;
+    for (int t = threadIdx.x; t < total; t += NTHREADS) {
+      const int l = t / nb, j = t - l * nb;
+      const int k = j % Ns;
+      const cplx *src = in + l * n + j;
+      cplx *dst = out + l * n + (j / Ns) * Ns * R + k;
+      cplx v[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[r] = src[r * nb];
+      if (Ns > 1) {
+#pragma unroll
+        for (int r = 1; r < R; ++r) v[r] = cmul(v[r], tw[k * R + r]);
+      }
+      dft_store<R, INV>(v, dst, Ns);
+    }
+  } else if constexpr (odd_groups(R) > 1) {
+    odd_pass_shared<R, INV>(in, out, n, nl, Ns, tw, scratch);
+  } else {
+    const int total = nl * nb;
+    for (int t = threadIdx.x; t < total; t += NTHREADS) {
+      const int l = t / nb, j = t - l * nb;
+      const int k = j % Ns;
+      odd_butterfly<R, INV>(in + l * n + j, nb, tw + k * R, Ns > 1,
+                            out + l * n + (j / Ns) * Ns * R + k, Ns, 0);
+    }
+  }
+}
+
+// All passes of one transform; returns the buffer that holds the result.
+template <bool INV>
+__device__ __noinline__ cplx *transform(cplx *buf0, cplx *buf1, cplx *scratch, const AxisPlan &p,
+                                        int nl, const cplx *tw) {
+  cplx *in = buf0, *out = buf1;
+  for (int ps = 0; ps < p.npass; ++ps) {
+    const int R = p.radix[ps], Ns = p.ns[ps];
+    const cplx *twp = tw + p.twoff[ps];
+    switch (R) {
+      case 2: stockham_pass<2, INV>(in, out, p.n, nl, Ns, twp, scratch); break;
+      case 4: stockham_pass<4, INV>(in, out, p.n, nl, Ns, twp, scratch); break;
+      case 8: stockham_pass<8, INV>(in, out, p.n, nl, Ns, twp, scratch); break;
+      case 3: stockham_pass<3, INV>(in, out, p.n, nl, Ns, twp, scratch); break;
+      case 5: stockham_pass<5, INV>(in, out, p.n, nl, Ns, twp, scratch); break;
+      case 7: stockham_pass<7, INV>(in, out, p.n, nl, Ns, twp, scratch); break;
+      case 11: stockham_pass<11, INV>(in, out, p.n, nl, Ns, twp, scratch); break;
+      case 13: stockham_pass<13, INV>(in, out, p.n, nl, Ns, twp, scratch); break;
+      case 17: stockham_pass<17, INV>(in, out, p.n, nl, Ns, twp, scratch); break;
+      case 43: stockham_pass<43, INV>(in, out, p.n, nl, Ns, twp, scratch); break;
+      default: break;  // excluded when the plan is built
+    }
+    __syncthreads();
+    cplx *tmp = in;
+    in = out;
+    out = tmp;
+  }
+  return in;
+}
+
+__device__ __forceinline__ cplx *run_transform(cplx *b0, cplx *b1, cplx *scratch, const FftArgs &a,
+                                               int nl, int inv) {
+  return inv ? transform<true>(b0, b1, scratch, a.ax, nl, a.tw_b)
+             : transform<false>(b0, b1, scratch, a.ax, nl, a.tw_f);
+}
+
+// element coordinates (x, y, z) of element j of line L along the plan's axis
+__device__ __forceinline__ void coords(const AxisPlan &p, const MulTables &T, int64_t L, int j,
+                                       int &x, int &y, int &z) {
+  if (p.axis == 0) {
+    x = j;
+    y = (int)(L % T.ny);
+    z = (int)(L / T.ny);
+  } else if (p.axis == 1) {
+    x = (int)(L % T.nx);
+    y = j;
+    z = (int)(L / T.nx);
+  } else {
+    x = (int)(L % T.nx);
+    y = (int)(L / T.nx);
+    z = j;
+  }
+}
+
+__device__ __forceinline__ cplx mid_op(const FftArgs &a, int64_t pos, int x, int y, int z, cplx v) {
+  const MulTables &T = a.T;
+  if (a.mid == MID_PROP) {  // MultiplyExp (diffraction.f90:155-176)
+    const unsigned char f = T.zflag[z];
+    if (f & 1) {
+      if (f & 2) v = cmul(cmul(T.px[(int64_t)z * T.nx + x], T.py[(int64_t)z * T.ny + y]), v);
+    } else if (T.qfilter) {
+      v = cplx{(real)0, (real)0};
+    }
+  } else if (a.mid == MID_DAMP) {  // AbsorptionStep damping (diffraction.f90:480-501)
+    if (T.zflag[z] & 2) {
+      const real f = T.dxt[(int64_t)z * T.nx + x] * T.dyt[(int64_t)z * T.ny + y];
+      v = cplx{f * v.r, f * v.i};
+    }
+  } else if (a.mid == MID_SPLIT) {  // /ffact then mask split (diffraction.f90:310, 454-470)
+    v = cplx{v.r / T.ffact, v.i / T.ffact};
+    const real mk = T.mask[(int64_t)y * T.nx + x];
+    const real m = mk + T.mz[z] * ((real)1 - mk);
+    const real nbm = (real)1 - m;
+    a.anb[pos] = cplx{nbm * v.r, nbm * v.i};
+    v = cplx{m * v.r, m * v.i};
+  } else if (a.mid == MID_RECOMB) {  // /ffact then + A_nb (diffraction.f90:513-517)
+    const cplx b = a.anb[pos];
+    v = cplx{v.r / T.ffact + b.r, v.i / T.ffact + b.i};
+  }
+  return v;
+}
+
+__device__ __forceinline__ void store(const FftArgs &a, int64_t pos, cplx v) {
+  if (a.store_split) {
+    a.re_out[pos] = v.r;
+    a.im_out[pos] = v.i;
+    if (a.mirror) {
+      const int64_t plane = (int64_t)a.T.nx * a.T.ny;
+      if (pos < plane) {
+        a.re_out[pos + plane * a.T.nz] = v.r;
+        a.im_out[pos + plane * a.T.nz] = v.i;
+      }
+    }
+  } else {
+    a.A[pos] = v;
+    if (a.mirror) {  // the complex output is the outer mesh itself
+      const int64_t plane = (int64_t)a.T.nx * a.T.ny;
+      if (pos < plane) a.A[pos + plane * a.T.nz] = v;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(NTHREADS) k_fft(const FftArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cplx *smem_all = reinterpret_cast<cplx *>(smem_raw);
+  const AxisPlan &p = a.ax;
+  const int n = p.n;
+  const int64_t L0 = (int64_t)blockIdx.x * p.lpb;
+  const int nl = (int)min((int64_t)p.lpb, p.nlines - L0);
+  const int tid = threadIdx.x;
+  cplx *smem = smem_all;
+  cplx *other = smem_all + (size_t)p.lpb * n;
+  cplx *scratch = smem_all + (size_t)2 * p.lpb * n;
+
+  // load: consecutive threads take consecutive lines (adjacent in memory)
+  for (int t = tid; t < nl * n; t += NTHREADS) {
+    int l, j;
+    if (p.stride == 1) {
+      l = t / n;
+      j = t - l * n;
+    } else {
+      l = t % nl;
+      j = t / nl;
+    }
+    const int64_t pos = line_base(p, L0 + l) + (int64_t)j * p.stride;
+    smem[l * n + j] = a.load_split ? cplx{a.re_in[pos], a.im_in[pos]} : a.A[pos];
+  }
+  __syncthreads();
+  {
+    cplx *res = run_transform(smem, other, scratch, a, nl, a.dir);
+    if (res != smem) {
+      other = smem;
+      smem = res;
+    }
+  }
+
+  if (a.mid != MID_NONE) {
+    for (int t = tid; t < nl * n; t += NTHREADS) {
+      const int l = t / n, j = t - l * n;
+      int x, y, z;
+      coords(p, a.T, L0 + l, j, x, y, z);
+      const int64_t pos = line_base(p, L0 + l) + (int64_t)j * p.stride;
+      smem[t] = mid_op(a, pos, x, y, z, smem[t]);
+    }
+    __syncthreads();
+    if (a.second) {
+      cplx *res = run_transform(smem, other, scratch, a, nl, !a.dir);
+      if (res != smem) {
+        other = smem;
+        smem = res;
+      }
+    }
+  }
+
+  for (int t = tid; t < nl * n; t += NTHREADS) {
+    int l, j;
+    if (p.stride == 1) {
+      l = t / n;
+      j = t - l * n;
+    } else {
+      l = t % nl;
+      j = t / nl;
+    }
+    const int64_t pos = line_base(p, L0 + l) + (int64_t)j * p.stride;
+    store(a, pos, smem[l * n + j]);
+  }
+}
+
+// Element-wise form of a pass whose axis has length 1 (no transform): the
+// load/store conversion and the split / recombine operations still apply.
+__global__ void k_elementwise(const FftArgs a) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const MulTables &T = a.T;
+  const int64_t n = (int64_t)T.nx * T.ny * T.nz;
+  if (t >= n) return;
+  const int x = (int)(t % T.nx), y = (int)((t / T.nx) % T.ny);
+  const int z = (int)(t / ((int64_t)T.nx * T.ny));
+  cplx v = a.load_split ? cplx{a.re_in[t], a.im_in[t]} : a.A[t];
+  v = mid_op(a, t, x, y, z, v);
+  store(a, t, v);
+}
+
+// per-call tables: propagator and damping factors for step h
+__global__ void k_tables(cplx *px, cplx *py, real *dxt, real *dyt, const double *kx,
+                         const double *ky, const double *kz, int nx, int ny, int nz, double h,
+                         double sbeta) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nxz = (int64_t)nx * nz, nyz = (int64_t)ny * nz;
+  if (t < nxz) {
+    const int z = (int)(t / nx), x = (int)(t % nx);
+    const double kzz = kz[z];
+    const double th = h * (kx[x] * kx[x]) / (2.0 * kzz);
+    double s, c;
+    sincos(th, &s, &c);
+    px[t] = (kzz != 0.0) ? cplx{(real)c, (real)s} : cplx{(real)1, (real)0};
+    dxt[t] = (real)((kzz != 0.0) ? exp(-h * sbeta * fabs(kx[x]) / sqrt(fabs(2.0 * kzz))) : 1.0);
+  } else if (t < nxz + nyz) {
+    t -= nxz;
+    const int z = (int)(t / ny), y = (int)(t % ny);
+    const double kzz = kz[z];
+    const double th = h * (ky[y] * ky[y]) / (2.0 * kzz);
+    double s, c;
+    sincos(th, &s, &c);
+    py[t] = (kzz != 0.0) ? cplx{(real)c, (real)s} : cplx{(real)1, (real)0};
+    dyt[t] = (real)((kzz != 0.0) ? exp(-h * sbeta * fabs(ky[y]) / sqrt(fabs(2.0 * kzz))) : 1.0);
+  }
+}
+
+
+
+struct Plan {
+  int nx = 0, ny = 0, nz = 0;
+  int64_t n = 0;
+  AxisPlan ax[3];
+  size_t smem[3] = {0, 0, 0};
+  cplx *A = nullptr, *anb = nullptr;
+  cplx *tw = nullptr;  // forward block then backward block
+  size_t ntw = 0;
+  cplx *px = nullptr, *py = nullptr;
+  real *dxt = nullptr, *dyt = nullptr;
+  double *kx = nullptr, *ky = nullptr, *kz = nullptr;
+  real *mask = nullptr, *mz = nullptr;
+  unsigned char *zflag = nullptr;
+  double ffact = 1.0;
+};
+
+static void destroy(Plan *d) {
+  if (!d) return;
+  void *ptrs[] = {d->A, d->anb, d->tw, d->px, d->py, d->dxt, d->dyt,
+                  d->kx, d->ky, d->kz, d->mask, d->mz, d->zflag};
+  for (void *q : ptrs) cudaFree(q);
+  delete d;
+}
+
+static bool radix_supported(int r) {
+  if (r == 2 || r == 4 || r == 8) return true;
+  for (int q = 0; q < N_ODD; ++q)
+    if (ODD_R[q] == r) return true;
+  return false;
+}
+
+static std::vector<int> factorize(int n) {
+  std::vector<int> f;
+  while (n % 8 == 0) { f.push_back(8); n /= 8; }
+  while (n % 4 == 0) { f.push_back(4); n /= 4; }
+  while (n % 2 == 0) { f.push_back(2); n /= 2; }
+  for (int p = 3; n > 1; p += 2)
+    while (n % p == 0) { f.push_back(p); n /= p; }
+  return f;
+}
+
+// linspace (base_functions.f90:67-98)
+static std::vector<double> linspace(double a, double b, int n) {
+  std::vector<double> v(n);
+  if (n == 1) { v[0] = a; return v; }
+  const double d = (b - a) / (double)(n - 1);
+  for (int i = 0; i < n; ++i) v[i] = a + i * d;
+  return v;
+}
+
+static double sq(double v) { return v * v; }
+
+// Mask1D2 (masks.f90:266-302): the lower-end assignment is made second and
+// wins where the two ends overlap.
+static std::vector<double> mask1d2(const std::vector<double> &x, double dx, int nx, int nb) {
+  const double pi = PF_PUFFIN_PI;
+  std::vector<double> m(nx, 0.0);
+  const double lb = (nb - 1) * dx, x01 = x[nx - 1], x02 = x[0];
+  for (int j = std::max(0, nx - nb); j < nx; ++j) m[j] = sq(cos(pi * (x[j] - x01) / (2.0 * lb)));
+  for (int j = 0; j < std::min(nb, nx); ++j) m[j] = sq(cos(pi * (x[j] - x02) / (2.0 * lb)));
+  for (int j = nb; j < nx - nb; ++j) m[j] = 0.0;
+  return m;
+}
+
+// Maskf4 (masks.f90:329-361)
+static std::vector<double> maskf4(const std::vector<double> &x, double dx, int nx, int nb) {
+  const double pi = PF_PUFFIN_PI;
+  std::vector<double> m(nx, 0.0);
+  const double lb = (nb - 1) * dx, x01 = x[std::max(0, nx - nb)], x02 = x[std::min(nb, nx) - 1];
+  for (int j = std::max(0, nx - nb); j < nx; ++j) m[j] = sq(cos(pi * (x[j] - x01) / (2.0 * lb)));
+  for (int j = 0; j < std::min(nb, nx); ++j) m[j] = sq(cos(pi * (x[j] - x02) / (2.0 * lb)));
+  for (int j = nb; j < nx - nb; ++j) m[j] = 1.0;
+  return m;
+}
+
+static int build_plan(pf_handle *h, Plan *&out) {
+  const pf_params &p = h->p;
+  Plan *d = new Plan();
+  out = d;
+  d->nx = p.nx;
+  d->ny = p.ny;
+  d->nz = (int)h->npl;
+  d->n = (int64_t)d->nx * d->ny * d->nz;
+  d->ffact = (double)p.nx * (double)p.ny * (double)d->nz;
+  const int dims[3] = {d->nx, d->ny, d->nz};
+  const int64_t strides[3] = {1, d->nx, (int64_t)d->nx * d->ny};
+  if (d->nz < 2) {
+    h->err = "diffraction needs at least 2 z2 planes in the transform";
+    return PF_BAD_ARG;
+  }
+
+  // roots of unity of the unrolled odd radices
+  {
+    std::vector<cplx> roots;
+    for (int q = 0; q < N_ODD; ++q)
+      for (int m = 0; m < ODD_R[q]; ++m) {
+        const double ang = 2.0 * PF_FULL_PI * (double)m / (double)ODD_R[q];
+        roots.push_back(cplx{(real)cos(ang), (real)sin(ang)});
+      }
+    PF_CUDA(cudaMemcpyToSymbol(c_roots, roots.data(), roots.size() * sizeof(cplx)));
+  }
+
+  std::vector<cplx> tab, tabb;
+  int max_smem = 0;
+  PF_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->dev));
+  for (int a = 0; a < 3; ++a) {
+    AxisPlan &ap = d->ax[a];
+    memset(&ap, 0, sizeof(ap));
+    ap.axis = a;
+    ap.n = dims[a];
+    ap.stride = strides[a];
+    if (a == 0) {
+      ap.inner = 1;
+      ap.ostride = d->nx;
+      ap.nlines = (int64_t)d->ny * d->nz;
+    } else if (a == 1) {
+      ap.inner = d->nx;
+      ap.ostride = (int64_t)d->nx * d->ny;
+      ap.nlines = (int64_t)d->nx * d->nz;
+    } else {
+      ap.inner = (int64_t)d->nx * d->ny;
+      ap.ostride = 0;
+      ap.nlines = (int64_t)d->nx * d->ny;
+    }
+    if (ap.n == 1) continue;
+    const std::vector<int> f = factorize(ap.n);
+    for (int r : f)
+      if (!radix_supported(r)) {
+        h->err = "FFT length " + std::to_string(ap.n) + " has a prime factor " +
+                 std::to_string(r) + " without a butterfly (supported: 2, 3, 5, 7, 11, 13, 17, 43)";
+        return PF_BAD_ARG;
+      }
+    if ((int)f.size() > MAX_PASSES) {
+      h->err = "FFT length has too many factors";
+      return PF_BAD_ARG;
+    }
+    ap.npass = (int)f.size();
+    int scratch = 0;
+    for (int r : f) scratch = std::max(scratch, odd_scratch(r));
+    int ns = 1;
+    int64_t lpb = (int64_t)1 << 20;
+    for (int ps = 0; ps < ap.npass; ++ps) {
+      const int R = f[ps];
+      ap.radix[ps] = R;
+      ap.ns[ps] = ns;
+      ap.twoff[ps] = (int)tab.size();
+      for (int k = 0; k < ns; ++k)
+        for (int r = 0; r < R; ++r) {
+          const double ang = -2.0 * PF_FULL_PI * (double)(k * r) / (double)(ns * R);
+          tab.push_back(cplx{(real)cos(ang), (real)sin(ang)});
+          tabb.push_back(cplx{(real)cos(ang), (real)-sin(ang)});
+        }
+      ns *= R;
+    }
+    // lines per block: about 2048 points per block, adjacent lines for the
+    // strided axes, two buffers within the shared-memory limit
+    lpb = std::max<int64_t>(1, 2048 / ap.n);
+    lpb = std::min<int64_t>(lpb, ap.nlines);
+    auto bytes = [&](int64_t lp) { return (size_t)(2 * lp * ap.n + scratch) * sizeof(cplx); };
+    while (lpb > 1 && bytes(lpb) > (size_t)max_smem) --lpb;
+    if (bytes(lpb) > (size_t)max_smem) {
+      h->err = "FFT line too long for shared memory";
+      return PF_BAD_ARG;
+    }
+    ap.lpb = (int)lpb;
+    d->smem[a] = bytes(lpb);
+  }
+  d->ntw = tab.size();
+  if (d->ntw) {
+    PF_CUDA(cudaMalloc(&d->tw, 2 * d->ntw * sizeof(cplx)));
+    PF_CUDA(cudaMemcpy(d->tw, tab.data(), d->ntw * sizeof(cplx), cudaMemcpyHostToDevice));
+    PF_CUDA(cudaMemcpy(d->tw + d->ntw, tabb.data(), d->ntw * sizeof(cplx),
+                       cudaMemcpyHostToDevice));
+  }
+  PF_CUDA(cudaFuncSetAttribute(k_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+
+  PF_CUDA(cudaMalloc(&d->A, d->n * sizeof(cplx)));
+  PF_CUDA(cudaMalloc(&d->anb, d->n * sizeof(cplx)));
+  PF_CUDA(cudaMalloc(&d->px, (size_t)d->nx * d->nz * sizeof(cplx)));
+  PF_CUDA(cudaMalloc(&d->py, (size_t)d->ny * d->nz * sizeof(cplx)));
+  PF_CUDA(cudaMalloc(&d->dxt, (size_t)d->nx * d->nz * sizeof(real)));
+  PF_CUDA(cudaMalloc(&d->dyt, (size_t)d->ny * d->nz * sizeof(real)));
+
+  // k-values (transforms.f90:472-590), full-precision pi
+  auto kvals = [](int m, double len) {
+    std::vector<double> k(m);
+    const int mx = (int)ceil((double)m / 2.0);
+    for (int i = 0; i < m; ++i) k[i] = 2.0 * PF_FULL_PI * (double)(i >= mx ? i - m : i) / len;
+    return k;
+  };
+  const std::vector<double> kx = kvals(d->nx, (double)d->nx * p.dx);
+  const std::vector<double> ky = kvals(d->ny, (double)d->ny * p.dy);
+  const std::vector<double> kz = kvals(d->nz, (double)d->nz * p.dz2);
+  PF_CUDA(cudaMalloc(&d->kx, kx.size() * sizeof(double)));
+  PF_CUDA(cudaMalloc(&d->ky, ky.size() * sizeof(double)));
+  PF_CUDA(cudaMalloc(&d->kz, kz.size() * sizeof(double)));
+  PF_CUDA(cudaMemcpy(d->kx, kx.data(), kx.size() * sizeof(double), cudaMemcpyHostToDevice));
+  PF_CUDA(cudaMemcpy(d->ky, ky.data(), ky.size() * sizeof(double), cudaMemcpyHostToDevice));
+  PF_CUDA(cudaMemcpy(d->kz, kz.data(), kz.size() * sizeof(double), cudaMemcpyHostToDevice));
+
+  // filter cutoff (diffraction.f90:138-139; sFilt from setup_calcs.f90:208-210)
+  const double ppi = PF_PUFFIN_PI;
+  const double lenz2 = p.dz2 * p.nz2;
+  const double sfilt = lenz2 / (4 * ppi * p.rho) * p.sfilt_frac;
+  double cutoff = 2.0 * ppi * sfilt / ((double)p.nz2 * p.dz2);
+  if (p.mesh_type == PF_MESH_PERIODIC && p.sperwaves <= 1.1) cutoff = 0.0;
+  std::vector<unsigned char> zf(d->nz);
+  for (int z = 0; z < d->nz; ++z)
+    zf[z] = (unsigned char)(((kz[z] > cutoff) || (kz[z] < -cutoff)) ? 1 : 0) |
+            (unsigned char)((kz[z] != 0.0) ? 2 : 0);
+  PF_CUDA(cudaMalloc(&d->zflag, zf.size()));
+  PF_CUDA(cudaMemcpy(d->zflag, zf.data(), zf.size(), cudaMemcpyHostToDevice));
+
+  // masks (masks.f90:50-189, 366-430)
+  const double lenx = (d->nx - 1) * p.dx, leny = (d->ny - 1) * p.dy;
+  const std::vector<double> xs = linspace(-lenx / 2, lenx / 2, d->nx);
+  const std::vector<double> ys = linspace(-leny / 2, leny / 2, d->ny);
+  const std::vector<double> maskx = mask1d2(xs, p.dx, d->nx, p.nbx);
+  const std::vector<double> masky = mask1d2(ys, p.dy, d->ny, p.nby);
+  const std::vector<double> maskx2 = maskf4(xs, p.dx, d->nx, p.nbx);
+  std::vector<double> m2((size_t)d->nx * d->ny);
+  for (int y = 0; y < d->ny; ++y)
+    for (int x = 0; x < d->nx; ++x)
+      m2[(size_t)y * d->nx + x] = 1.0 * maskx[x] + maskx2[x] * masky[y];
+  std::vector<double> mzv(d->nz, 0.0);
+  if (p.mesh_type != PF_MESH_PERIODIC) {
+    const double dx = p.dz2;
+    const std::vector<double> xz = linspace(0.0 * dx, (double)(d->nz - 1) * dx, d->nz);
+    const double lb = (p.nbz2 - 1) * dx;
+    const double lf = (p.nz2 - 1 * dx);  // getZ2Mask's own form (masks.f90:366-430)
+    const double x0 = lf - lb / 2.0;
+    const int fbn = p.nz2 - p.nbz2 + 1;
+    for (int i = 0; i < d->nz; ++i)
+      if (i + 1 >= fbn) mzv[i] = sq(cos(ppi * (xz[i] - x0) / lb));
+  }
+  {
+    const std::vector<real> m2r(m2.begin(), m2.end()), mzr(mzv.begin(), mzv.end());
+    PF_CUDA(cudaMalloc(&d->mask, m2r.size() * sizeof(real)));
+    PF_CUDA(cudaMalloc(&d->mz, mzr.size() * sizeof(real)));
+    PF_CUDA(cudaMemcpy(d->mask, m2r.data(), m2r.size() * sizeof(real), cudaMemcpyHostToDevice));
+    PF_CUDA(cudaMemcpy(d->mz, mzr.data(), mzr.size() * sizeof(real), cudaMemcpyHostToDevice));
+  }
+  return PF_OK;
+}
+
+// One fused pass along `axis`; an axis of length 1 degrades to the
+// element-wise form (load/store conversion, split, recombine).
+static int fft_pass(pf_handle *h, Plan *d, FftArgs a, int axis) {
+  a.ax = d->ax[axis];
+  if (a.ax.n == 1) {
+    if (a.mid == MID_SPLIT || a.mid == MID_RECOMB || a.load_split || a.store_split) {
+      const unsigned g = (unsigned)((d->n + 255) / 256);
+      pf_prof_begin(h, PROF_DIFF);
+      k_elementwise<<<g, 256, 0, h->stream>>>(a);
+      pf_prof_end(h);
+      PF_LAUNCHED(h);
+    }
+    return PF_OK;
+  }
+  const int64_t blocks = (a.ax.nlines + a.ax.lpb - 1) / a.ax.lpb;
+  pf_prof_begin(h, PROF_FFT);
+  k_fft<<<(unsigned)blocks, NTHREADS, d->smem[axis], h->stream>>>(a);
+  pf_prof_end(h);
+  PF_LAUNCHED(h);
+  return PF_OK;
+}
+
+// Diffract the outer mesh: split real/imaginary arrays (re, im) or, when
+// those are null, the interleaved complex mesh oc (nz2 planes either way).
+static int diffract(pf_handle *h, Plan *&plan, real *re, real *im, cplx *oc, double dz) {
+  const pf_params &p = h->p;
+  if (!plan) {
+    int rc = build_plan(h, plan);
+    if (rc) return rc;
+  }
+  Plan *d = plan;
+  FftArgs a;
+  memset(&a, 0, sizeof(a));
+  a.A = d->A;
+  a.anb = d->anb;
+  a.tw_f = d->tw;
+  a.tw_b = d->tw + d->ntw;
+  a.T.px = d->px;
+  a.T.py = d->py;
+  a.T.dxt = d->dxt;
+  a.T.dyt = d->dyt;
+  a.T.zflag = d->zflag;
+  a.T.mask = d->mask;
+  a.T.mz = d->mz;
+  a.T.nx = d->nx;
+  a.T.ny = d->ny;
+  a.T.nz = d->nz;
+  a.T.qfilter = p.qfilter;
+  a.T.ffact = (real)d->ffact;
+  const bool split = (re != nullptr);
+  if (!split) a.A = oc;  // transform the complex outer mesh in place
+  a.re_in = re;
+  a.im_in = im;
+  a.re_out = re;
+  a.im_out = im;
+  a.mirror = (p.mesh_type == PF_MESH_PERIODIC);
+
+  const int64_t ntab = (int64_t)(d->nx + d->ny) * d->nz;
+  pf_prof_begin(h, PROF_DIFF);
+  k_tables<<<(unsigned)((ntab + 255) / 256), 256, 0, h->stream>>>(
+      d->px, d->py, d->dxt, d->dyt, d->kx, d->ky, d->kz, d->nx, d->ny, d->nz, dz, p.sbeta);
+  pf_prof_end(h);
+  PF_LAUNCHED(h);
+
+  struct Step {
+    int axis, dir, mid, second, load_split, store_split;
+  };
+  const Step steps[9] = {
+      {0, 0, MID_NONE, 0, 1, 0},    // x fwd (from re/im)
+      {1, 0, MID_NONE, 0, 0, 0},    // y fwd
+      {2, 0, MID_PROP, 1, 0, 0},    // z fwd, propagate + filter, z inv
+      {1, 1, MID_NONE, 0, 0, 0},    // y inv
+      {0, 1, MID_SPLIT, 1, 0, 0},   // x inv, /ffact, mask split, x fwd
+      {1, 0, MID_NONE, 0, 0, 0},    // y fwd
+      {2, 0, MID_DAMP, 1, 0, 0},    // z fwd, damp, z inv
+      {1, 1, MID_NONE, 0, 0, 0},    // y inv
+      {0, 1, MID_RECOMB, 0, 0, 1},  // x inv, /ffact, + A_nb (to re/im)
+  };
+  for (const Step &s : steps) {
+    FftArgs b = a;
+    b.dir = s.dir;
+    b.mid = s.mid;
+    b.second = s.second;
+    b.load_split = split && s.load_split;
+    b.store_split = split && s.store_split;
+    // the mirror plane is written by the last pass only
+    b.mirror = a.mirror && s.store_split;
+    const int rc = fft_pass(h, d, b, s.axis);
+    if (rc) return rc;
+  }
+  return PF_OK;
+}
+
+}  // namespace FFT_NS

@@ -82,6 +82,45 @@ __global__ void k_window_copy(double *wr, double *wi, double *or_, double *oi, i
   }
 }
 
+__global__ void k_window_copy_c32(float2 *w, float2 *o, int nix, int niy, int64_t npl, int nx,
+                                  int ny, int64_t nz2, int to_outer, int mirror) {
+  const int64_t nw = (int64_t)nix * niy * npl;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nw) return;
+  const int ix = (int)(t % nix);
+  const int iy = (int)((t / nix) % niy);
+  const int64_t iz = t / ((int64_t)nix * niy);
+  const int ox = (nx - nix) / 2, oy = (ny - niy) / 2;
+  const int64_t plane = (int64_t)nx * ny;
+  const int64_t oo = (ix + ox) + (int64_t)nx * (iy + oy) + plane * iz;
+  if (to_outer) {
+    o[oo] = w[t];
+    if (mirror && iz == 0) o[oo + plane * (nz2 - 1)] = w[t];
+  } else {
+    w[t] = o[oo];
+  }
+}
+
+// FP64 split field <-> interleaved complex float (mixed precision transfers)
+__global__ void k_to_c32(float2 *o, const double *re, const double *im, int64_t n) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) o[t] = make_float2((float)re[t], (float)im[t]);
+}
+
+__global__ void k_from_c32(const float2 *o, double *re, double *im, int64_t n) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) {
+    const float2 v = o[t];
+    re[t] = (double)v.x;
+    im[t] = (double)v.y;
+  }
+}
+
+__global__ void k_mirror_plane_c32(float2 *o, int64_t plane, int64_t nz2) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < plane) o[plane * (nz2 - 1) + t] = o[t];
+}
+
 // Periodic wrap of z2 (para_field.f90:212-215)
 __global__ void k_wrap_z2(double *z2, int64_t n, double lenz2) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -161,6 +200,11 @@ static void free_window(pf_handle *h) {
   }
   cudaFree(h->acc);
   h->acc = nullptr;
+  void **c32[] = {&h->w32, &h->as32, &h->d0_32, &h->d12_32, &h->acc32};
+  for (auto p : c32) {
+    cudaFree(*p);
+    *p = nullptr;
+  }
   h->wcap = 0;
   h->nwin = 0;
   h->window_valid = false;
@@ -187,10 +231,16 @@ static int alloc_window(pf_handle *h, int nix, int niy) {
   if (nw > h->wcap) {
     free_window(h);
     const size_t b = sizeof(double) * (size_t)nw;
-    double **ptrs[] = {&h->wr, &h->wi, &h->asr, &h->asi, &h->d0r, &h->d0i, &h->d12r, &h->d12i};
-    for (auto p : ptrs) PF_CUDA(cudaMalloc(p, b));
-    PF_CUDA(cudaMalloc(&h->acc, 4 * b));
-    PF_CUDA(cudaMemsetAsync(h->acc, 0, 4 * b, h->stream));
+    if (h->p.precision == PF_MIXED) {
+      void **c32[] = {&h->w32, &h->as32, &h->d0_32, &h->d12_32, &h->acc32};
+      for (auto p : c32) PF_CUDA(cudaMalloc(p, b));  // float2 per node
+      PF_CUDA(cudaMemsetAsync(h->acc32, 0, b, h->stream));
+    } else {
+      double **ptrs[] = {&h->wr, &h->wi, &h->asr, &h->asi, &h->d0r, &h->d0i, &h->d12r, &h->d12i};
+      for (auto p : ptrs) PF_CUDA(cudaMalloc(p, b));
+      PF_CUDA(cudaMalloc(&h->acc, 4 * b));
+      PF_CUDA(cudaMemsetAsync(h->acc, 0, 4 * b, h->stream));
+    }
     h->wcap = nw;
   }
   h->nix = nix;
@@ -201,6 +251,14 @@ static int alloc_window(pf_handle *h, int nix, int niy) {
 
 int pf_outer_to_inner(pf_handle *h) {
   if (h->nwin == 0) return PF_OK;
+  if (h->p.precision == PF_MIXED) {
+    k_window_copy_c32<<<grid_for(h->nwin, 256), 256, 0, h->stream>>>(
+        (float2 *)h->w32, (float2 *)h->oc32, h->nix, h->niy, h->npl, h->p.nx, h->p.ny, h->p.nz2,
+        0, 0);
+    PF_LAUNCHED(h);
+    h->window_valid = true;
+    return PF_OK;
+  }
   k_window_copy<<<grid_for(h->nwin, 256), 256, 0, h->stream>>>(
       h->wr, h->wi, h->or_, h->oi_, h->nix, h->niy, h->npl, h->p.nx, h->p.ny, h->p.nz2, 0, 0);
   PF_LAUNCHED(h);
@@ -211,6 +269,13 @@ int pf_outer_to_inner(pf_handle *h) {
 int pf_inner_to_outer(pf_handle *h) {
   if (h->nwin == 0 || !h->window_valid) return PF_OK;
   const int mirror = (h->p.mesh_type == PF_MESH_PERIODIC);
+  if (h->p.precision == PF_MIXED) {
+    k_window_copy_c32<<<grid_for(h->nwin, 256), 256, 0, h->stream>>>(
+        (float2 *)h->w32, (float2 *)h->oc32, h->nix, h->niy, h->npl, h->p.nx, h->p.ny, h->p.nz2,
+        1, mirror);
+    PF_LAUNCHED(h);
+    return PF_OK;
+  }
   k_window_copy<<<grid_for(h->nwin, 256), 256, 0, h->stream>>>(
       h->wr, h->wi, h->or_, h->oi_, h->nix, h->niy, h->npl, h->p.nx, h->p.ny, h->p.nz2, 1,
       mirror);
@@ -337,8 +402,8 @@ int pf_create(const pf_params *p, pf_handle **out) {
     g_err = "pf_create: one_d requires nx = ny = 1";
     return PF_BAD_ARG;
   }
-  if (p->precision != PF_FP64) {
-    g_err = "pf_create: only the FP64 path is built in this library";
+  if (p->precision != PF_FP64 && p->precision != PF_MIXED) {
+    g_err = "pf_create: precision must be PF_FP64 or PF_MIXED";
     return PF_BAD_ARG;
   }
   int ndev = 0;
@@ -371,10 +436,15 @@ int pf_create(const pf_params *p, pf_handle **out) {
   if ((e = cudaMalloc(&h->d_status, 64)) != cudaSuccess) return fail(e, "status");
   if ((e = cudaMalloc(&h->d_red, 64)) != cudaSuccess) return fail(e, "reduction scratch");
   if ((e = cudaMallocHost(&h->h_status, 64)) != cudaSuccess) return fail(e, "pinned status");
-  if ((e = cudaMalloc(&h->or_, sizeof(double) * h->nouter)) != cudaSuccess) return fail(e, "field");
-  if ((e = cudaMalloc(&h->oi_, sizeof(double) * h->nouter)) != cudaSuccess) return fail(e, "field");
-  cudaMemsetAsync(h->or_, 0, sizeof(double) * h->nouter, h->stream);
-  cudaMemsetAsync(h->oi_, 0, sizeof(double) * h->nouter, h->stream);
+  if (p->precision == PF_MIXED) {
+    if ((e = cudaMalloc(&h->oc32, sizeof(float2) * h->nouter)) != cudaSuccess) return fail(e, "field");
+    cudaMemsetAsync(h->oc32, 0, sizeof(float2) * h->nouter, h->stream);
+  } else {
+    if ((e = cudaMalloc(&h->or_, sizeof(double) * h->nouter)) != cudaSuccess) return fail(e, "field");
+    if ((e = cudaMalloc(&h->oi_, sizeof(double) * h->nouter)) != cudaSuccess) return fail(e, "field");
+    cudaMemsetAsync(h->or_, 0, sizeof(double) * h->nouter, h->stream);
+    cudaMemsetAsync(h->oi_, 0, sizeof(double) * h->nouter, h->stream);
+  }
   cudaMemsetAsync(h->d_status, 0, 64, h->stream);
   if ((e = cudaStreamSynchronize(h->stream)) != cudaSuccess) return fail(e, "sync");
   *out = h;
@@ -395,6 +465,8 @@ int pf_destroy(pf_handle *h) {
   pf_diff_destroy(h->diff);
   cudaFree(h->or_);
   cudaFree(h->oi_);
+  cudaFree(h->oc32);
+  cudaFree(h->staging);
   cudaFree(h->d_status);
   cudaFree(h->d_red);
   if (h->h_status) cudaFreeHost(h->h_status);
@@ -486,12 +558,26 @@ static int set_field_impl(pf_handle *h, const double *re, const double *im, cuda
   if (!h || !re || !im) return PF_BAD_ARG;
   cudaSetDevice(h->dev);
   const size_t b = sizeof(double) * (size_t)h->nouter;
-  PF_CUDA(cudaMemcpyAsync(h->or_, re, b, kind, h->stream));
-  PF_CUDA(cudaMemcpyAsync(h->oi_, im, b, kind, h->stream));
-  if (h->p.mesh_type == PF_MESH_PERIODIC) {  // pupd8: the head plane wins
-    const int64_t plane = (int64_t)h->p.nx * h->p.ny;
-    k_mirror_plane<<<grid_for(plane, 256), 256, 0, h->stream>>>(h->or_, h->oi_, plane, h->p.nz2);
+  const int64_t plane = (int64_t)h->p.nx * h->p.ny;
+  if (h->p.precision == PF_MIXED) {
+    if (!h->staging) PF_CUDA(cudaMalloc(&h->staging, 2 * b));
+    PF_CUDA(cudaMemcpyAsync(h->staging, re, b, kind, h->stream));
+    PF_CUDA(cudaMemcpyAsync(h->staging + h->nouter, im, b, kind, h->stream));
+    k_to_c32<<<grid_for(h->nouter, 256), 256, 0, h->stream>>>((float2 *)h->oc32, h->staging,
+                                                             h->staging + h->nouter, h->nouter);
     PF_LAUNCHED(h);
+    if (h->p.mesh_type == PF_MESH_PERIODIC) {
+      k_mirror_plane_c32<<<grid_for(plane, 256), 256, 0, h->stream>>>((float2 *)h->oc32, plane,
+                                                                     h->p.nz2);
+      PF_LAUNCHED(h);
+    }
+  } else {
+    PF_CUDA(cudaMemcpyAsync(h->or_, re, b, kind, h->stream));
+    PF_CUDA(cudaMemcpyAsync(h->oi_, im, b, kind, h->stream));
+    if (h->p.mesh_type == PF_MESH_PERIODIC) {  // pupd8: the head plane wins
+      k_mirror_plane<<<grid_for(plane, 256), 256, 0, h->stream>>>(h->or_, h->oi_, plane, h->p.nz2);
+      PF_LAUNCHED(h);
+    }
   }
   if (h->nwin > 0) {
     int rc = pf_outer_to_inner(h);
@@ -514,8 +600,17 @@ static int get_field_impl(pf_handle *h, double *re, double *im, cudaMemcpyKind k
   int rc = pf_inner_to_outer(h);
   if (rc) return rc;
   const size_t b = sizeof(double) * (size_t)h->nouter;
-  PF_CUDA(cudaMemcpyAsync(re, h->or_, b, kind, h->stream));
-  PF_CUDA(cudaMemcpyAsync(im, h->oi_, b, kind, h->stream));
+  if (h->p.precision == PF_MIXED) {
+    if (!h->staging) PF_CUDA(cudaMalloc(&h->staging, 2 * b));
+    k_from_c32<<<grid_for(h->nouter, 256), 256, 0, h->stream>>>(
+        (const float2 *)h->oc32, h->staging, h->staging + h->nouter, h->nouter);
+    PF_LAUNCHED(h);
+    PF_CUDA(cudaMemcpyAsync(re, h->staging, b, kind, h->stream));
+    PF_CUDA(cudaMemcpyAsync(im, h->staging + h->nouter, b, kind, h->stream));
+  } else {
+    PF_CUDA(cudaMemcpyAsync(re, h->or_, b, kind, h->stream));
+    PF_CUDA(cudaMemcpyAsync(im, h->oi_, b, kind, h->stream));
+  }
   PF_CUDA(cudaStreamSynchronize(h->stream));
   return PF_OK;
 }
@@ -558,7 +653,8 @@ int pf_rk4_step(pf_handle *h, double szl, double hstep) {
   }
   cudaSetDevice(h->dev);
   unsigned int st = 0;
-  int rc = pf_rk4_fp64(h, szl, hstep, &st);
+  int rc = (h->p.precision == PF_MIXED) ? pf_rk4_mixed(h, szl, hstep, &st)
+                                         : pf_rk4_fp64(h, szl, hstep, &st);
   if (rc) return rc;
   rc = status_to_rc(st);
   if (rc == PF_OUT_OF_Z2) h->err = "a macroparticle's z2 node lies outside the temporal mesh";
@@ -601,7 +697,8 @@ int pf_diffract(pf_handle *h, double dz) {
   cudaSetDevice(h->dev);
   int rc = pf_inner_to_outer(h);
   if (rc) return rc;
-  rc = pf_diffract_outer(h, dz);
+  rc = (h->p.precision == PF_MIXED) ? pf_diffract_outer_c32(h, h->oc32, dz)
+                                     : pf_diffract_outer(h, dz);
   if (rc) return rc;
   if (h->nwin > 0) {
     rc = pf_outer_to_inner(h);

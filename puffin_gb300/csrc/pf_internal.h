@@ -126,6 +126,11 @@ struct pf_handle {
   unsigned long long *acc = nullptr;       // 4 * wcap words
   bool window_valid = false;  // window holds the outer mesh's current values
 
+  // mixed precision: interleaved complex-float outer mesh and window arrays
+  void *oc32 = nullptr;
+  void *w32 = nullptr, *as32 = nullptr, *d0_32 = nullptr, *d12_32 = nullptr, *acc32 = nullptr;
+  double *staging = nullptr;  // FP64 staging for field transfers (2 * nouter)
+
   // taper state
   double n2col = 1.0, n2col0 = 1.0, undgrad = 0.0;
 
@@ -153,12 +158,16 @@ void pf_prof_flush(pf_handle *h);
 
 // fp64 RK4 step on the device; returns the device status word.
 int pf_rk4_fp64(pf_handle *h, double szl, double hstep, unsigned int *status_out);
+// mixed-precision RK4 step
+int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_out);
 // window management
 int pf_window_from_particles(pf_handle *h, int *nix, int *niy);
 int pf_outer_to_inner(pf_handle *h);
 int pf_inner_to_outer(pf_handle *h);
 // diffraction
 int pf_diffract_outer(pf_handle *h, double dz);
+// diffraction of an interleaved complex-float outer mesh (mixed precision)
+int pf_diffract_outer_c32(pf_handle *h, void *outer, double dz);
 void pf_diff_destroy(DiffPlan *d);
 
 void pf_stage_coefficients(const pf_params &p, double sz, double n2col, int place,

@@ -1,0 +1,529 @@
+// Mixed-precision RK4 macroparticle push.
+//
+// FP64: the particle state (x, y, z2, px, py, Gamma), the RK4 stage state and
+// stage combination, p2 (the z2 velocity, which sets the ponderomotive phase)
+// and the cell index and fractional position in each direction.
+// FP32: the field window, the interpolation weights, the gather, the source
+// term and its deposit, the b-fields and the momentum/energy equations.
+//
+// p2 (gamma_to_p2.f90:84-85) is (1/sqrt(1-u) - 1)/eta with
+// u = (1 + aw^2 p_perp^2)/(gamma0^2 Gamma^2) of order 1e-7: the reference form
+// cancels 7 digits.  Here r - 1 = 1/sqrt(1-u) - 1 is summed as its binomial
+// series u/2 + 3u^2/8 + 5u^3/16 + ... (seven terms, truncation below 1e-18 of
+// the result for u < 1e-3; the reference form is used above that), which is
+// accurate to an ulp in FP64 and needs no square root or division.
+//
+// Deposit: each block of 1024 macroparticles (4 per thread) accumulates its
+// contributions to the two z2 planes its particles start from in a
+// shared-memory tile, with compensated (TwoSum) float atomics: the rounding
+// error of every add is recovered from the value the atomic returns and added
+// to a second tile, so the tile sums carry about twice FP32's precision.  The
+// tile is then flushed to HBM with one float2 atomic per non-zero node.
+// Contributions outside the tile go straight to HBM.  Macroparticles ordered
+// along z2 (as Puffin's beams are generated) make the tile catch nearly all.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <climits>
+
+#include "pf_internal.h"
+
+namespace {
+
+constexpr int MX_THREADS = 256;
+constexpr int MX_PPT = 4;  // macroparticles per thread
+constexpr int MX_TILE_PLANES = 2;
+
+struct BFieldF {
+  int type, place, one_d, focusing, tcase;
+  float bx0, by0, focx, focy, S, C, c1, ux, uy, u3, fx, fy, kx, ky, kxky, czs, cze, szt;
+};
+
+struct MixArgs {
+  const double *x, *y, *z2, *px, *py, *gam, *chi;
+  const double *kin[6];
+  double *kout[6];
+  double *kacc[6];
+  const double *k1[6];
+  double *ynext[6];
+  int64_t np;
+  double cstate, h6;
+  const float2 *as;  // stage field (window, interleaved complex)
+  float2 *acc;       // deposit accumulator (window)
+  int nix, niy;
+  int64_t npl, nz2;
+  int periodic, one_d, tile;
+  double halfx, halfy, inv_dx, inv_dy, inv_dz2;
+  double inv_g02, aw2, inv_eta, eta;
+  float inv_dV3, sInv2rho, dxc, eta_k2, kn2col, n2col, rho2;
+  BFieldF bf;
+  int field_evolve, electrons_evolve, coupling;
+  unsigned int *status;
+};
+
+struct MixNodeArgs {
+  int64_t n;
+  float2 *acc, *w, *as, *d0, *d12;
+  float coef, h6;
+  const unsigned int *status;
+};
+
+__device__ __forceinline__ void bfield_f(const BFieldF &b, float x, float y, float &bx, float &by,
+                                         float &bz) {
+  const float pi = (float)PF_PUFFIN_PI;
+  bx = b.bx0;
+  by = b.by0;
+  bz = 0.f;
+  if (b.type == PF_UND_CURVED) {
+    const float shx = sinhf(b.kx * x), shy = sinhf(b.ky * y);
+    const float chx = coshf(b.kx * x), chy = coshf(b.ky * y);
+    if (b.place == 0) {
+      bx = b.kxky * shx * shy * b.szt / 4.f / pi * b.S;
+      by = chx * chy * b.szt / 4.f / pi * b.S;
+      bz = b.czs * chx * shy * b.u3 * b.C;
+    } else if (b.place == 2) {
+      bx = b.kxky * shx * shy * b.u3 * b.S;
+      by = chx * chy * b.u3 * b.S;
+      bz = b.cze * chx * shy * b.u3 * b.C;
+    } else {
+      bx = b.kxky * shx * shy * b.S;
+      by = chx * chy * b.S;
+      bz = b.cze * chx * shy * b.C;
+    }
+    if (b.one_d) bz = 0.f;
+  } else if (b.type == PF_UND_PLANEPOLE) {
+    if (!b.one_d) {
+      const float sh = sinhf(b.c1 * y);
+      bz = (b.place == 1) ? sh * b.C : sh * b.u3 * b.C;
+    }
+  } else if (!b.one_d) {
+    const bool hel = (b.type == PF_UND_HELICAL);
+    if (b.place == 1) {
+      bz = hel ? b.c1 * (-(x * b.S) + y * b.C) : b.c1 * (-(b.fx * x * b.S) + b.fy * y * b.C);
+    } else {
+      const float t = (b.tcase == 0) ? 0.f : -(b.ux * x * b.S);
+      bz = t + b.uy * y * b.C;
+    }
+  }
+  if (b.focusing) {
+    bx = b.focx * y + bx;
+    by = -(b.focy * x) + by;
+  }
+}
+
+// compensated shared-memory add: the atomic returns the old value, so the
+// rounding error of old + v is known exactly (TwoSum) and kept in c
+__device__ __forceinline__ void tile_add(float *s, float *c, float v) {
+  const float old = atomicAdd(s, v);
+  const float t = __fadd_rn(old, v);
+  const float bp = __fsub_rn(t, old);
+  const float e = __fadd_rn(__fsub_rn(old, __fsub_rn(t, bp)), __fsub_rn(v, bp));
+  if (e != 0.f) atomicAdd(c, e);
+}
+
+__device__ __forceinline__ void global_add(float2 *a, float2 v) {
+  atomicAdd(&a->x, v.x);
+  atomicAdd(&a->y, v.y);
+}
+
+// r - 1 = 1/sqrt(1 - u) - 1
+__device__ __forceinline__ double rsqrt1m_minus1(double u) {
+  if (u < 1.0e-3) {
+    // binomial coefficients C(2k,k)/4^k: 1/2, 3/8, 5/16, 35/128, 63/256, 231/1024, 429/2048
+    double s = 429.0 / 2048.0;
+    s = fma(s, u, 231.0 / 1024.0);
+    s = fma(s, u, 63.0 / 256.0);
+    s = fma(s, u, 35.0 / 128.0);
+    s = fma(s, u, 5.0 / 16.0);
+    s = fma(s, u, 3.0 / 8.0);
+    s = fma(s, u, 0.5);
+    return u * s;
+  }
+  return 1.0 / sqrt(1.0 - u) - 1.0;
+}
+
+template <int STAGE, bool ONED>
+__global__ void __launch_bounds__(MX_THREADS) k_stage_mixed(const MixArgs a) {
+  extern __shared__ __align__(16) float tile[];  // [2][planes*ntr] (sum, comp) float2 each
+  const int ntr = a.nix * a.niy;
+  const int tile_n = MX_TILE_PLANES * ntr;
+  float2 *tsum = reinterpret_cast<float2 *>(tile);
+  float2 *tcomp = tsum + tile_n;
+  __shared__ int s_pzlo;
+
+  if (a.tile) {
+    for (int t = threadIdx.x; t < 2 * tile_n; t += MX_THREADS) tsum[t] = make_float2(0.f, 0.f);
+    if (threadIdx.x == 0) s_pzlo = INT_MAX;
+    __syncthreads();
+  }
+  const bool halted = (*((volatile unsigned int *)a.status) != 0u);
+
+  // per particle kept until the deposit: source terms, weights, base nodes
+  float sr[MX_PPT], si[MX_PPT], wx[MX_PPT], wy[MX_PPT], wz[MX_PPT];
+  int64_t base0[MX_PPT];
+  int pz0v[MX_PPT], pz1v[MX_PPT];
+  bool dep[MX_PPT];
+  int my_pzlo = INT_MAX;
+
+#pragma unroll
+  for (int q = 0; q < MX_PPT; ++q) {
+    dep[q] = false;
+    const int64_t i = (int64_t)blockIdx.x * (MX_THREADS * MX_PPT) + q * MX_THREADS + threadIdx.x;
+    if (halted || i >= a.np) continue;
+    const double y0[6] = {a.x[i], a.y[i], a.z2[i], a.px[i], a.py[i], a.gam[i]};
+    double s[6], kin[6];
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      kin[j] = (STAGE > 1) ? a.kin[j][i] : 0.0;
+      s[j] = (STAGE > 1) ? y0[j] + a.cstate * kin[j] : y0[j];
+    }
+    const double G = s[5];
+    // 1/Gamma: FP32 seed and two Newton steps in FP64
+    double rG = (double)__frcp_rn((float)G);
+    rG = fma(rG, fma(-G, rG, 1.0), rG);
+    rG = fma(rG, fma(-G, rG, 1.0), rG);
+    const double bb = fma(a.aw2, fma(s[3], s[3], s[4] * s[4]), 1.0);
+    const double u = bb * a.inv_g02 * (rG * rG);
+    const double p2 = rsqrt1m_minus1(u) * a.inv_eta;
+    const double q64 = fma(a.eta, p2, 1.0);
+    const float qrG = (float)(q64 * rG);
+    const float X = (float)s[0], Y = (float)s[1], PX = (float)s[3], PY = (float)s[4];
+
+    // cell and fraction in FP64, weights in FP32
+    const double tz = s[2] * a.inv_dz2;
+    const double fz = floor(tz);
+    const float zw2 = (float)(tz - fz);
+    bool ok = true;
+    int pz0 = 0, pz1 = 0;
+    if (a.periodic) {
+      if (!(fabs(fz) < 9.0e15)) {
+        ok = false;
+        atomicOr(a.status, ST_OUT_OF_Z2);
+      } else {
+        int64_t m = (int64_t)fz % a.npl;
+        if (m < 0) m += a.npl;
+        pz0 = (int)m;
+        pz1 = (m + 1 == a.npl) ? 0 : (int)m + 1;
+      }
+    } else {
+      if (!(fz >= 0.0 && fz + 1.0 < (double)a.nz2)) {
+        ok = false;
+        atomicOr(a.status, ST_OUT_OF_Z2);
+      } else {
+        pz0 = (int)fz;
+        pz1 = pz0 + 1;
+      }
+    }
+    float x2 = 0.f, y2 = 0.f;
+    int64_t b0 = 0;
+    if (!ONED) {
+      const double tx = (s[0] + a.halfx) * a.inv_dx;
+      const double fx = floor(tx);
+      const double ty = (s[1] + a.halfy) * a.inv_dy;
+      const double fy = floor(ty);
+      if (!(fx >= 0.0 && fx + 1.0 < (double)a.nix && fy >= 0.0 && fy + 1.0 < (double)a.niy)) {
+        ok = false;
+        atomicOr(a.status, ST_OUT_OF_WINDOW);
+      } else {
+        x2 = (float)(tx - fx);
+        y2 = (float)(ty - fy);
+        b0 = (int64_t)fx + (int64_t)fy * a.nix;
+      }
+    }
+    const float x1 = 1.f - x2, y1 = 1.f - y2, zw1 = 1.f - zw2;
+
+    float fr = 0.f, fi = 0.f;
+    if (ok) {
+      if (ONED) {
+        const float2 c0 = a.as[pz0], c1 = a.as[pz1];
+        fr = zw1 * c0.x + zw2 * c1.x;
+        fi = zw1 * c0.y + zw2 * c1.y;
+      } else {
+        const float2 *p0 = a.as + (int64_t)pz0 * ntr + b0;
+        const float2 *p1 = a.as + (int64_t)pz1 * ntr + b0;
+        const float2 c0 = p0[0], c1 = p0[1], c2 = p0[a.nix], c3 = p0[a.nix + 1];
+        const float2 c4 = p1[0], c5 = p1[1], c6 = p1[a.nix], c7 = p1[a.nix + 1];
+        const float w0 = x1 * y1, w1 = x2 * y1, w2 = x1 * y2, w3 = x2 * y2;
+        fr = zw1 * (w0 * c0.x + w1 * c1.x + w2 * c2.x + w3 * c3.x) +
+             zw2 * (w0 * c4.x + w1 * c5.x + w2 * c6.x + w3 * c7.x);
+        fi = zw1 * (w0 * c0.y + w1 * c1.y + w2 * c2.y + w3 * c3.y) +
+             zw2 * (w0 * c4.y + w1 * c5.y + w2 * c6.y + w3 * c7.y);
+      }
+      if (a.field_evolve) {
+        const float dw = (float)a.chi[i] * a.inv_dV3 * qrG;
+        sr[q] = dw * PX;
+        si[q] = dw * PY;
+        wx[q] = x2;
+        wy[q] = y2;
+        wz[q] = zw2;
+        base0[q] = b0;
+        pz0v[q] = pz0;
+        pz1v[q] = pz1;
+        dep[q] = true;
+        my_pzlo = min(my_pzlo, pz0);
+      }
+    }
+    if (!a.coupling) {
+      fr = 0.f;
+      fi = 0.f;
+    }
+
+    double k[6];
+    if (a.electrons_evolve) {
+      float bx, by, bz;
+      bfield_f(a.bf, X, Y, bx, by, bz);
+      const float ep = (float)p2 * a.eta_k2;
+      const float cz = a.kn2col * qrG * bz;
+      k[2] = p2;
+      k[0] = (double)(a.dxc * qrG * PX);
+      k[1] = (double)(-(a.dxc * qrG * PY));
+      k[3] = (double)(a.sInv2rho * (a.n2col * by - ep * fr) + cz * PY);
+      k[4] = (double)(a.sInv2rho * (a.n2col * bx - ep * fi) - cz * PX);
+      k[5] = (double)(-(a.rho2 * qrG * (PX * fr + PY * fi)));
+    } else {
+#pragma unroll
+      for (int j = 0; j < 6; ++j) k[j] = 0.0;
+    }
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      if (STAGE == 1) {
+        a.kout[j][i] = k[j];
+      } else if (STAGE == 2) {
+        a.kacc[j][i] = k[j];
+      } else if (STAGE == 3) {
+        a.kout[j][i] = k[j];
+        a.kacc[j][i] = kin[j] + k[j];
+      } else {
+        a.ynext[j][i] = y0[j] + a.h6 * (a.k1[j][i] + k[j] + 2.0 * a.kacc[j][i]);
+      }
+    }
+  }
+
+  // deposit
+  if (a.tile) {
+    for (int o = 16; o > 0; o >>= 1) my_pzlo = min(my_pzlo, __shfl_xor_sync(0xffffffffu, my_pzlo, o));
+    if ((threadIdx.x & 31) == 0 && my_pzlo != INT_MAX) atomicMin(&s_pzlo, my_pzlo);
+    __syncthreads();
+  }
+  const int pzlo = a.tile ? s_pzlo : 0;
+#pragma unroll
+  for (int q = 0; q < MX_PPT; ++q) {
+    if (!dep[q]) continue;
+    const float z2w = wz[q], z1w = 1.f - z2w;
+    const float x2 = wx[q], x1 = 1.f - x2, y2 = wy[q], y1 = 1.f - y2;
+    const int nc = ONED ? 2 : 8;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      if (c >= nc) break;
+      float w;
+      int64_t node;
+      int plane;
+      if (ONED) {
+        plane = (c == 0) ? pz0v[q] : pz1v[q];
+        w = (c == 0) ? z1w : z2w;
+        node = 0;
+      } else {
+        const int cx = c & 1, cy = (c >> 1) & 1, cz = c >> 2;
+        w = (cx ? x2 : x1) * (cy ? y2 : y1) * (cz ? z2w : z1w);
+        plane = cz ? pz1v[q] : pz0v[q];
+        node = base0[q] + cx + (int64_t)cy * a.nix;
+      }
+      const float vr = w * sr[q], vi = w * si[q];
+      const int tp = plane - pzlo;
+      if (a.tile && tp >= 0 && tp < MX_TILE_PLANES) {
+        const int ti = tp * ntr + (int)node;
+        tile_add(&tsum[ti].x, &tcomp[ti].x, vr);
+        tile_add(&tsum[ti].y, &tcomp[ti].y, vi);
+      } else {
+        global_add(a.acc + (int64_t)plane * ntr + node, make_float2(vr, vi));
+      }
+    }
+  }
+  if (a.tile) {
+    __syncthreads();
+    if (pzlo != INT_MAX) {
+      for (int t = threadIdx.x; t < tile_n; t += MX_THREADS) {
+        const int plane = pzlo + t / ntr;
+        if (plane >= a.npl) break;
+        const float2 s = tsum[t], c = tcomp[t];
+        const float2 v = make_float2(s.x + c.x, s.y + c.y);
+        if (v.x != 0.f || v.y != 0.f) global_add(a.acc + (int64_t)plane * ntr + (t - (plane - pzlo) * ntr), v);
+      }
+    }
+  }
+}
+
+template <int STAGE>
+__global__ void __launch_bounds__(256) k_nodes_mixed(const MixNodeArgs a) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= a.n) return;
+  const float2 d = a.acc[n];
+  a.acc[n] = make_float2(0.f, 0.f);
+  const float2 w = a.w[n];
+  if (STAGE == 1) {
+    a.d0[n] = d;
+    a.as[n] = make_float2(w.x + a.coef * d.x, w.y + a.coef * d.y);
+  } else if (STAGE == 2) {
+    a.d12[n] = d;
+    a.as[n] = make_float2(w.x + a.coef * d.x, w.y + a.coef * d.y);
+  } else if (STAGE == 3) {
+    a.as[n] = make_float2(w.x + a.coef * d.x, w.y + a.coef * d.y);
+    const float2 e = a.d12[n];
+    a.d12[n] = make_float2(e.x + d.x, e.y + d.y);
+  } else {
+    if (*a.status == 0u) {
+      const float2 d0 = a.d0[n], e = a.d12[n];
+      a.w[n] = make_float2(w.x + a.h6 * (d0.x + d.x + 2.f * e.x), w.y + a.h6 * (d0.y + d.y + 2.f * e.y));
+    }
+  }
+}
+
+BFieldF to_float(const BFieldCoef &b) {
+  BFieldF f;
+  f.type = b.type;
+  f.place = b.place;
+  f.one_d = b.one_d;
+  f.focusing = b.focusing;
+  f.tcase = b.tcase;
+  f.bx0 = (float)b.bx0;
+  f.by0 = (float)b.by0;
+  f.focx = (float)b.focx;
+  f.focy = (float)b.focy;
+  f.S = (float)b.S;
+  f.C = (float)b.C;
+  f.c1 = (float)b.c1;
+  f.ux = (float)b.ux;
+  f.uy = (float)b.uy;
+  f.u3 = (float)b.u3;
+  f.fx = (float)b.fx;
+  f.fy = (float)b.fy;
+  f.kx = (float)b.kx;
+  f.ky = (float)b.ky;
+  f.kxky = (float)b.kxky;
+  f.czs = (float)b.czs;
+  f.cze = (float)b.cze;
+  f.szt = (float)b.szt;
+  return f;
+}
+
+}  // namespace
+
+int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_out) {
+  const pf_params &p = h->p;
+  const double hh = hstep * 0.5, szh = szl + hh;
+  const double stage_sz[4] = {szl, szh, szh, szl + hstep};
+  const double stage_c[4] = {0.0, hh, hh, hstep};
+  const int nxt = h->cur ^ 1;
+  PF_CUDA(cudaMemsetAsync(h->d_status, 0, sizeof(unsigned int), h->stream));
+
+  MixArgs a;
+  memset(&a, 0, sizeof(a));
+  a.x = h->y[h->cur][0];
+  a.y = h->y[h->cur][1];
+  a.z2 = h->y[h->cur][2];
+  a.px = h->y[h->cur][3];
+  a.py = h->y[h->cur][4];
+  a.gam = h->y[h->cur][5];
+  a.chi = h->chi;
+  a.np = h->np;
+  a.h6 = hstep / 6.0;
+  a.acc = (float2 *)h->acc32;
+  a.nix = h->nix;
+  a.niy = h->niy;
+  a.npl = h->npl;
+  a.nz2 = p.nz2;
+  a.periodic = (p.mesh_type == PF_MESH_PERIODIC);
+  a.one_d = p.one_d;
+  a.halfx = ((double)(h->nix - 1) / 2.0) * p.dx;
+  a.halfy = ((double)(h->niy - 1) / 2.0) * p.dy;
+  a.inv_dx = 1.0 / p.dx;
+  a.inv_dy = 1.0 / p.dy;
+  a.inv_dz2 = 1.0 / p.dz2;
+  a.inv_g02 = 1.0 / (p.gamma_r * p.gamma_r);
+  a.aw2 = p.aw * p.aw;
+  a.inv_eta = 1.0 / p.eta;
+  a.eta = p.eta;
+  a.inv_dV3 = (float)(1.0 / (p.dx * p.dy * p.dz2));
+  a.sInv2rho = (float)(1.0 / (2.0 * p.rho));
+  a.dxc = (float)(2.0 * p.rho * p.kappa / sqrt(p.eta));
+  a.eta_k2 = (float)(p.eta / (p.kappa * p.kappa));
+  a.rho2 = (float)(2.0 * p.rho);
+  a.field_evolve = p.field_evolve;
+  a.electrons_evolve = p.electrons_evolve;
+  a.coupling = p.coupling;
+  a.status = h->d_status;
+  const int ntr = h->nix * h->niy;
+  const size_t tile_bytes = (size_t)2 * MX_TILE_PLANES * ntr * sizeof(float2);
+  a.tile = tile_bytes <= 48 * 1024 ? 1 : 0;
+  const size_t smem = a.tile ? tile_bytes : 0;
+
+  MixNodeArgs n;
+  memset(&n, 0, sizeof(n));
+  n.n = h->nwin;
+  n.acc = (float2 *)h->acc32;
+  n.w = (float2 *)h->w32;
+  n.as = (float2 *)h->as32;
+  n.d0 = (float2 *)h->d0_32;
+  n.d12 = (float2 *)h->d12_32;
+  n.h6 = (float)(hstep / 6.0);
+  n.status = h->d_status;
+
+  const int64_t per_block = (int64_t)MX_THREADS * MX_PPT;
+  const unsigned pg = (unsigned)std::max<int64_t>(1, (h->np + per_block - 1) / per_block);
+  const unsigned ng = (unsigned)std::max<int64_t>(1, (h->nwin + 255) / 256);
+  const bool oned = p.one_d != 0;
+  for (int s = 1; s <= 4; ++s) {
+    double n2col;
+    int place;
+    pf_taper_stage(h, stage_sz[s - 1], &n2col, &place);
+    BFieldCoef bf;
+    pf_stage_coefficients(p, stage_sz[s - 1], n2col, place, &bf);
+    a.bf = to_float(bf);
+    a.n2col = (float)n2col;
+    a.kn2col = (float)(p.kappa * n2col);
+    a.cstate = stage_c[s - 1];
+    a.as = (const float2 *)((s == 1) ? h->w32 : h->as32);
+    for (int j = 0; j < 6; ++j) {
+      a.kin[j] = (s == 2) ? h->k1[j] : (s == 3) ? h->ka[j] : (s == 4) ? h->kb[j] : nullptr;
+      a.kout[j] = (s == 1) ? h->k1[j] : (s == 3) ? h->kb[j] : nullptr;
+      a.kacc[j] = (s >= 2) ? h->ka[j] : nullptr;
+      a.k1[j] = h->k1[j];
+      a.ynext[j] = h->y[nxt][j];
+    }
+    if (h->np > 0) {
+      pf_prof_begin(h, PROF_STAGE);
+#define PF_MIX_CASE(S)                                                                 \
+  case S:                                                                              \
+    if (oned) k_stage_mixed<S, true><<<pg, MX_THREADS, smem, h->stream>>>(a);          \
+    else k_stage_mixed<S, false><<<pg, MX_THREADS, smem, h->stream>>>(a);              \
+    break;
+      switch (s) {
+        PF_MIX_CASE(1)
+        PF_MIX_CASE(2)
+        PF_MIX_CASE(3)
+        PF_MIX_CASE(4)
+      }
+#undef PF_MIX_CASE
+      pf_prof_end(h);
+      PF_LAUNCHED(h);
+    }
+    n.coef = (float)((s == 3) ? hstep : hh);
+    pf_prof_begin(h, PROF_NODES);
+    switch (s) {
+      case 1: k_nodes_mixed<1><<<ng, 256, 0, h->stream>>>(n); break;
+      case 2: k_nodes_mixed<2><<<ng, 256, 0, h->stream>>>(n); break;
+      case 3: k_nodes_mixed<3><<<ng, 256, 0, h->stream>>>(n); break;
+      default: k_nodes_mixed<4><<<ng, 256, 0, h->stream>>>(n); break;
+    }
+    pf_prof_end(h);
+    PF_LAUNCHED(h);
+  }
+  PF_CUDA(cudaMemcpyAsync(h->h_status, h->d_status, sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                          h->stream));
+  PF_CUDA(cudaStreamSynchronize(h->stream));
+  pf_prof_flush(h);
+  *status_out = *h->h_status;
+  if (*status_out == 0u) h->cur = nxt;
+  return PF_OK;
+}
