@@ -14,7 +14,7 @@
 // accurate to an ulp in FP64 and needs no square root or division.
 //
 // Deposit: each block of 1024 macroparticles (4 per thread) accumulates its
-// contributions to the two z2 planes its particles start from in a
+// contributions to the three z2 planes its particles start from in a
 // shared-memory tile, with compensated (TwoSum) float atomics: the rounding
 // error of every add is recovered from the value the atomic returns and added
 // to a second tile, so the tile sums carry about twice FP32's precision.  The
@@ -33,7 +33,7 @@ namespace {
 
 constexpr int MX_THREADS = 256;
 constexpr int MX_PPT = 4;  // macroparticles per thread
-constexpr int MX_TILE_PLANES = 2;
+constexpr int MX_TILE_PLANES = 3;
 
 struct BFieldF {
   int type, place, one_d, focusing, tcase;
@@ -455,7 +455,7 @@ int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_ou
   a.status = h->d_status;
   const int ntr = h->nix * h->niy;
   const size_t tile_bytes = (size_t)2 * MX_TILE_PLANES * ntr * sizeof(float2);
-  a.tile = tile_bytes <= 48 * 1024 ? 1 : 0;
+  a.tile = tile_bytes <= 96 * 1024 ? 1 : 0;
   const size_t smem = a.tile ? tile_bytes : 0;
 
   MixNodeArgs n;
@@ -469,6 +469,17 @@ int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_ou
   n.h6 = (float)(hstep / 6.0);
   n.status = h->d_status;
 
+  static bool attr_set = false;
+  if (!attr_set) {
+    // the tile may exceed the 48 KB default of dynamic shared memory
+    const void *fns[] = {(const void *)k_stage_mixed<1, false>, (const void *)k_stage_mixed<2, false>,
+                         (const void *)k_stage_mixed<3, false>, (const void *)k_stage_mixed<4, false>,
+                         (const void *)k_stage_mixed<1, true>,  (const void *)k_stage_mixed<2, true>,
+                         (const void *)k_stage_mixed<3, true>,  (const void *)k_stage_mixed<4, true>};
+    for (const void *f : fns)
+      PF_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+    attr_set = true;
+  }
   const int64_t per_block = (int64_t)MX_THREADS * MX_PPT;
   const unsigned pg = (unsigned)std::max<int64_t>(1, (h->np + per_block - 1) / per_block);
   const unsigned ng = (unsigned)std::max<int64_t>(1, (h->nwin + 255) / 256);
