@@ -163,6 +163,24 @@ int pf_diffract(pf_handle *h, double dz);
 int pf_run(pf_handle *h, int32_t nsteps, int32_t isteps4diff, int32_t qdiffraction,
            double hstep, double *szl, int32_t *steps_done);
 
+/* Diagnostics of the current state, as the reference's integrated-data
+ * writer computes them:
+ *   pf_power      power per z2 plane, n = nz2 values: |A|^2 on a 1D mesh
+ *                 (fPower_1D), else the 2D trapezoid over x and y with the
+ *                 reference's single-precision accumulation (fPower_3D,
+ *                 m_trapz2D; puffin/lib/io/av_write.f90:141-276);
+ *   pf_bunching   |b_m| per slice of one resonant wavelength, harmonic m >= 1,
+ *                 linear slice weights, zero where a slice holds no charge
+ *                 (getSliceTwiss, av_write.f90:405-770; slice count
+ *                 pf_num_slices as write_adapter.f90:110-112);
+ *   pf_spectrum   one-sided |DFT|^2 along z2 of the on-axis field (central
+ *                 transverse node), x (re) and y (im) parts, nunique =
+ *                 ceil((nz2+1)/2) bins (utilities/pyPlotting/plotSpecPow.py:58-110). */
+int pf_power(pf_handle *h, double *power, int64_t n);
+int64_t pf_num_slices(const pf_handle *h);
+int pf_bunching(pf_handle *h, int32_t harmonic, double *b, int64_t nslices);
+int pf_spectrum(pf_handle *h, double *sx, double *sy, int64_t nunique);
+
 /* Block until all work queued by the handle is done. */
 int pf_sync(pf_handle *h);
 

@@ -622,3 +622,86 @@ def correct_trans(beam: Beam):
     beam.py[:] -= mpy
     beam.x[:] -= mx
     beam.y[:] -= my
+
+
+# ---------------------------------------------------------------------------
+# Diagnostics (puffin/lib/io/av_write.f90, write_adapter.f90:110-112,
+# utilities/pyPlotting/plotSpecPow.py:58-110)
+# ---------------------------------------------------------------------------
+def _trapz_f32(x, y):
+    """m_trapz: a default-real (single precision) accumulator updated with a
+    double-precision term each step."""
+    acc = np.float32(0.0)
+    for i in range(len(x) - 1):
+        acc = np.float32(float(acc) + (x[i + 1] - x[i]) * (y[i + 1] + y[i]) / 2.0)
+    return float(acc)
+
+
+def power(cfg: Config, re, im):
+    """gPower: fPower_1D (|A|^2) or fPower_3D (2D trapezoid) per z2 plane."""
+    R = re.reshape(cfg.nz2, cfg.ny, cfg.nx)
+    I = im.reshape(cfg.nz2, cfg.ny, cfg.nx)
+    inten = R * R + I * I
+    if cfg.nx == 1 and cfg.ny == 1:
+        return inten.reshape(cfg.nz2).copy()
+    lx, ly = cfg.dx * (cfg.nx - 1), cfg.dy * (cfg.ny - 1)
+    xa = _linspace(-lx / 2.0, lx / 2.0, cfg.nx)
+    ya = _linspace(-ly / 2.0, ly / 2.0, cfg.ny)
+    out = np.empty(cfg.nz2)
+    for z in range(cfg.nz2):
+        cul = np.array([_trapz_f32(xa, inten[z, iy]) for iy in range(cfg.ny)])
+        out[z] = _trapz_f32(ya, cul)
+    return out
+
+
+def num_slices(cfg: Config):
+    pi = PUFFIN_PI
+    if cfg.mesh_type == MESH_TEMPORAL:
+        return math.ceil((cfg.dz2 * cfg.nz2) / (4 * pi * cfg.rho))
+    return math.ceil((cfg.dz2 * float(cfg.nz2 - 1)) / (4 * pi * cfg.rho))
+
+
+def bunching(cfg: Config, z2, chi, harmonic=1):
+    """|b_m| per slice as getSliceTwiss (av_write.f90:500-650, 700-770)."""
+    ns = num_slices(cfg)
+    S = 4 * PUFFIN_PI * cfg.rho
+    br = np.zeros(ns + 1)
+    bi = np.zeros(ns + 1)
+    sd = np.zeros(ns + 1)
+    periodic = cfg.mesh_type == MESH_PERIODIC
+    for z, c in zip(z2, chi):
+        s = math.ceil(z / S)
+        if periodic:
+            if s >= ns:
+                s = s - math.floor(float(s) / float(ns)) * ns + 1
+            if s < 1:
+                raise ValueError("slice index out of bounds")
+        elif s > ns or s < 1:
+            raise ValueError("slice index out of bounds")
+        ph = float(harmonic) * z / (2.0 * cfg.rho)
+        w0 = (s * S - z) / S
+        sd[s - 1] += c
+        br[s - 1] += c * math.cos(ph) * w0
+        bi[s - 1] += c * math.sin(ph) * w0
+        if not periodic:
+            w1 = -((s - 1) * S - z) / S
+            br[s] += c * math.cos(ph) * w1
+            bi[s] += c * math.sin(ph) * w1
+    return np.where(sd[:ns] > 0, np.sqrt(br[:ns] ** 2 + bi[:ns] ** 2) / S, 0.0)
+
+
+def spectrum(cfg: Config, re, im):
+    """One-sided |FFT|^2 of the on-axis x (re) and y (im) field along z2."""
+    R = re.reshape(cfg.nz2, cfg.ny, cfg.nx)[:, (cfg.ny - 1) // 2, (cfg.nx - 1) // 2]
+    I = im.reshape(cfg.nz2, cfg.ny, cfg.nx)[:, (cfg.ny - 1) // 2, (cfg.nx - 1) // 2]
+    n = cfg.nz2
+    nu = int(np.ceil((n + 1) / 2))
+    out = []
+    for f in (R, I):
+        p = np.abs(np.fft.fft(f, n=n)[:nu]) ** 2
+        if n % 2 == 1:
+            p[1:] *= 2
+        else:
+            p[1:-1] *= 2
+        out.append(p)
+    return out[0], out[1]

@@ -467,6 +467,7 @@ int pf_destroy(pf_handle *h) {
   cudaFree(h->oi_);
   cudaFree(h->oc32);
   cudaFree(h->staging);
+  cudaFree(h->diag);
   cudaFree(h->d_status);
   cudaFree(h->d_red);
   if (h->h_status) cudaFreeHost(h->h_status);

@@ -131,6 +131,10 @@ struct pf_handle {
   void *w32 = nullptr, *as32 = nullptr, *d0_32 = nullptr, *d12_32 = nullptr, *acc32 = nullptr;
   double *staging = nullptr;  // FP64 staging for field transfers (2 * nouter)
 
+  // diagnostics scratch
+  double *diag = nullptr;
+  size_t diag_cap = 0;
+
   // taper state
   double n2col = 1.0, n2col0 = 1.0, undgrad = 0.0;
 

@@ -46,7 +46,8 @@ SYMBOLS = (
     "pf_get_field", "pf_set_field_dev", "pf_get_field_dev", "pf_set_taper", "pf_get_taper",
     "pf_get_window", "pf_rk4_step", "pf_redistribute", "pf_wrap_z2", "pf_diffract", "pf_run",
     "pf_sync", "pf_kernel_launches", "pf_last_error", "pf_abi_version", "pf_get_stream",
-    "pf_profile", "pf_profile_read", "pf_rk4_step_noalloc",
+    "pf_profile", "pf_profile_read", "pf_rk4_step_noalloc", "pf_power", "pf_num_slices",
+    "pf_bunching", "pf_spectrum",
 )
 NOALLOC_MAX_PARTICLES = 32768
 NOALLOC_MAX_NODES = 32768
@@ -103,6 +104,10 @@ def load(build_if_missing: bool = False):
         "pf_get_stream": (ctypes.c_void_p, [H]),
         "pf_profile": (ctypes.c_int, [H, i32]),
         "pf_profile_read": (ctypes.c_int, [H, i32, dp, ctypes.POINTER(i64)]),
+        "pf_power": (ctypes.c_int, [H, ctypes.c_void_p, i64]),
+        "pf_num_slices": (i64, [H]),
+        "pf_bunching": (ctypes.c_int, [H, i32, ctypes.c_void_p, i64]),
+        "pf_spectrum": (ctypes.c_int, [H, ctypes.c_void_p, ctypes.c_void_p, i64]),
         "pf_rk4_step_noalloc": (ctypes.c_int, [P, dp, dp, f64, f64, i64] + [ctypes.c_void_p] * 9
                                 + [i32, i32, ctypes.c_void_p]),
     }

@@ -183,6 +183,27 @@ class Puffin:
                                      ctypes.byref(done)))
         return z.value
 
+    # -- diagnostics ------------------------------------------------------------
+    def power(self):
+        """Power per z2 plane (fPower_1D / fPower_3D)."""
+        out = np.empty(self.params.nz2)
+        self._check(self._lib.pf_power(self._h, out.ctypes.data, len(out)))
+        return out
+
+    def bunching(self, harmonic: int = 1):
+        """|b_m| per resonant-wavelength slice (getSliceTwiss)."""
+        n = int(self._lib.pf_num_slices(self._h))
+        out = np.empty(n)
+        self._check(self._lib.pf_bunching(self._h, int(harmonic), out.ctypes.data, n))
+        return out
+
+    def spectrum(self):
+        """One-sided on-axis spectrum of the x (re) and y (im) field parts."""
+        nu = (self.params.nz2 + 2) // 2
+        sx, sy = np.empty(nu), np.empty(nu)
+        self._check(self._lib.pf_spectrum(self._h, sx.ctypes.data, sy.ctypes.data, nu))
+        return sx, sy
+
     def sync(self):
         self._check(self._lib.pf_sync(self._h))
 
