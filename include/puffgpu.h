@@ -181,6 +181,45 @@ int64_t pf_num_slices(const pf_handle *h);
 int pf_bunching(pf_handle *h, int32_t harmonic, double *b, int64_t nslices);
 int pf_spectrum(pf_handle *h, double *sx, double *sy, int64_t nunique);
 
+/* Completed RK4 steps counted over the handle's life (the reference's
+ * iCsteps, kept across undulator modules): pf_run wraps z2 on the periodic
+ * mesh whenever this count reaches a multiple of redist_every
+ * (undulator.f90:320-326).  pf_set_step_count restores it on resume. */
+int64_t pf_step_count(const pf_handle *h);
+int pf_set_step_count(pf_handle *h, int64_t csteps);
+
+/* Beam-line elements between undulator modules, applied to the macroparticles
+ * on the device (puffin/lib/acc_lattice.f90; the element loop is
+ * puffin/lib/puffin_module.f90:57-89):
+ *   pf_drift          driftSection (:478-518): z2 += dz p2, and x, y move
+ *                     with the transverse velocity unless one_d; then
+ *                     diffracts the field over dz if qdiffraction;
+ *   pf_chicane        disperse (:420-463): z2 -= 2 disp (Gamma - 1) and
+ *                     += slip, diffraction over zbar (> 0) if qdiffraction,
+ *                     then the periodic z2 wrap;
+ *   pf_quad           Quad (:531-561): thin-lens kick of px, py (not on 1D);
+ *   pf_modulation     bModulation (:575-585): Gamma += mag cos(k z2);
+ *   pf_match_in/out   matchIn / matchOut (:743-828 / :638-725): the undulator
+ *                     entry/exit offsets of x, y, px, py at zbar sz for the
+ *                     handle's undulator type and current taper factor;
+ *   pf_correct_trans  correctTrans (:601-623): subtract the chi-weighted
+ *                     means of px, py, x, y (a fixed-order reduction, so the
+ *                     result is the same every run);
+ *   pf_init_undulator initUndulator (:848-895): the module's undulator type,
+ *                     ux, uy, focusing factors, taper start value mf and
+ *                     gradient, and the ends sZFS / sZFE from nsteps, hstep
+ *                     and und_ends. */
+int pf_drift(pf_handle *h, double dz, int32_t qdiffraction);
+int pf_chicane(pf_handle *h, double disp, double slip, double zbar, int32_t qdiffraction);
+int pf_quad(pf_handle *h, double qfx, double qfy);
+int pf_modulation(pf_handle *h, double mag, double wavenum);
+int pf_match_in(pf_handle *h, double sz);
+int pf_match_out(pf_handle *h, double sz);
+int pf_correct_trans(pf_handle *h);
+int pf_init_undulator(pf_handle *h, int32_t und_type, double fx, double fy, double kbxsf,
+                      double kbysf, double mf, double taper, int32_t nsteps, double hstep,
+                      int32_t und_ends);
+
 /* Block until all work queued by the handle is done. */
 int pf_sync(pf_handle *h);
 

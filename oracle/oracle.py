@@ -494,17 +494,20 @@ class RunResult:
     status: int
     retries: int = 0
     power: list = field(default_factory=list)
+    csteps: int = 0
+    window: tuple = (0, 0)
 
 
 def undulator_run(cfg: Config, beam: Beam, re: np.ndarray, im: np.ndarray,
                   h: float, nsteps: int, isteps4diff: int, qdiffraction: bool,
                   redist_every: int = 60, taper: Taper | None = None,
                   nix: int | None = None, niy: int | None = None,
-                  on_step=None) -> RunResult:
+                  on_step=None, csteps0: int = 0) -> RunResult:
     """Drive rk4_step + diffract like UndSection: a first half diffraction
-    step, merged half steps between RK4 blocks, periodic z2 wraps every
-    ``redist_every`` steps, and up to 3 retries with a recomputed inner window
-    when a particle leaves it."""
+    step, merged half steps between RK4 blocks, periodic z2 wraps whenever the
+    cumulative step count (iCsteps, starting from ``csteps0``) is a multiple of
+    ``redist_every`` (undulator.f90:325), and up to 3 retries with a
+    recomputed inner window when a particle leaves it."""
     taper = taper or Taper(cfg.n2col0, cfg.n2col0, cfg.undgrad)
     if nix is None:
         nix, niy = get_in_node(cfg, beam.x, beam.y)
@@ -529,7 +532,8 @@ def undulator_run(cfg: Config, beam: Beam, re: np.ndarray, im: np.ndarray,
             wrap_z2(cfg, beam.z2)
             wr, wi = outer_to_inner(cfg, re, im, nix, niy)
         else:
-            return RunResult(istep - 1, st, retries)
+            return RunResult(istep - 1, st, retries, csteps=csteps0 + istep - 1,
+                             window=(nix, niy))
         szl = szl + h
         if qdiffraction and (istep % isteps4diff == 0 or istep == nsteps):
             inner_to_outer(cfg, re, im, wr, wi, nix, niy)
@@ -544,10 +548,10 @@ def undulator_run(cfg: Config, beam: Beam, re: np.ndarray, im: np.ndarray,
             wr, wi = outer_to_inner(cfg, re, im, nix, niy)
         if on_step is not None:
             on_step(istep, beam, wr, wi, nix, niy)
-        if istep % redist_every == 0:
+        if (csteps0 + istep) % redist_every == 0:
             wrap_z2(cfg, beam.z2)
     inner_to_outer(cfg, re, im, wr, wi, nix, niy)
-    return RunResult(nsteps, 0, retries)
+    return RunResult(nsteps, 0, retries, csteps=csteps0 + nsteps, window=(nix, niy))
 
 
 # ---------------------------------------------------------------------------
@@ -705,3 +709,109 @@ def spectrum(cfg: Config, re, im):
             p[1:-1] *= 2
         out.append(p)
     return out[0], out[1]
+
+
+# ---------------------------------------------------------------------------
+# Beam-line elements (puffin/lib/acc_lattice.f90) and the element loop
+# (puffin/lib/puffin_module.f90:57-89)
+# ---------------------------------------------------------------------------
+def drift(cfg: Config, beam: Beam, dz: float):
+    """driftSection (acc_lattice.f90:478-518), particle part."""
+    sp2 = p2(beam.gam, beam.px, beam.py, cfg)
+    beam.z2[:] = beam.z2 + dz * sp2
+    if not cfg.one_d:
+        c = 2 * cfg.rho * cfg.kappa / math.sqrt(cfg.eta)
+        beam.x[:] = beam.x + (c * (1 + cfg.eta * sp2) / beam.gam * beam.px) * dz
+        beam.y[:] = beam.y - (c * (1 + cfg.eta * sp2) / beam.gam * beam.py) * dz
+
+
+def chicane(cfg: Config, beam: Beam, disp: float, slip: float):
+    """disperse (acc_lattice.f90:420-463), particle part before the wrap."""
+    beam.z2[:] = beam.z2 - 2.0 * disp * (beam.gam - 1.0) + slip
+
+
+def quad(cfg: Config, beam: Beam, qfx: float, qfy: float):
+    """Quad (acc_lattice.f90:531-561)."""
+    if cfg.one_d:
+        return
+    c = math.sqrt(cfg.eta) / (2 * cfg.rho * cfg.kappa)
+    beam.px[:] = beam.px + c * beam.x / qfx
+    beam.py[:] = beam.py - c * beam.y / qfy
+
+
+def modulation(beam: Beam, mag: float, k: float):
+    """bModulation (acc_lattice.f90:575-585)."""
+    beam.gam[:] = beam.gam + (mag * np.cos(k * beam.z2))
+
+
+def init_undulator(cfg: Config, taper: Taper, und_type, fx, fy, kbxsf, kbysf, mf, grad,
+                   nsteps, hstep, und_ends):
+    """initUndulator (acc_lattice.f90:848-895)."""
+    taper.n2col0 = mf
+    taper.n2col = mf
+    taper.undgrad = grad
+    cfg.n2col0, cfg.undgrad = mf, grad
+    cfg.und_type, cfg.fx, cfg.fy, cfg.kbxsf, cfg.kbysf = und_type, fx, fy, kbxsf, kbysf
+    cfg.und_ends = bool(und_ends)
+    if und_ends:
+        cfg.szfs = 4.0 * PUFFIN_PI * cfg.rho * 2.0
+        cfg.szfe = nsteps * hstep - 4.0 * PUFFIN_PI * cfg.rho * 2.0
+    else:
+        cfg.szfs = 0.0
+        cfg.szfe = nsteps * hstep
+
+
+def run_lattice(cfg: Config, beam: Beam, re, im, elements, qdiffraction=True,
+                redist_every=60, sz=0.0):
+    """The element loop of puffin_module.f90:57-89 over undulator, quad,
+    chicane, drift and modulation elements (tuples as in
+    puffin_gb300.lattice).  Returns (sz, csteps)."""
+    taper = Taper(cfg.n2col0, cfg.n2col0, cfg.undgrad)
+    csteps = 0
+    # the inner window is set once (setup_calcs.f90:1292) and recomputed only
+    # when a particle leaves it
+    nix, niy = get_in_node(cfg, beam.x, beam.y)
+    for el in elements:
+        kind = el[0]
+        if kind == "undulator":
+            (_, und_type, fx, fy, kbxsf, kbysf, mf, grad, nsteps, h, isteps4diff) = el
+            init_undulator(cfg, taper, und_type, fx, fy, kbxsf, kbysf, mf, grad, nsteps, h,
+                           cfg.und_ends)
+            sz0 = sz
+            if not cfg.und_ends:
+                match_in(cfg, beam, 0.0, taper.n2col)
+            wrap_z2(cfg, beam.z2)     # getLocalFieldIndices (undulator.f90:102)
+            r = undulator_run(cfg, beam, re, im, h, nsteps, isteps4diff, qdiffraction,
+                              redist_every, taper, nix=nix, niy=niy, csteps0=csteps)
+            if r.status:
+                raise RuntimeError(f"undulator run failed with status {r.status}")
+            csteps = r.csteps
+            nix, niy = r.window
+            szl = 0.0
+            for _ in range(nsteps):
+                szl = szl + h
+            sz = sz0 + szl
+            if not cfg.und_ends:
+                match_out(cfg, beam, sz, taper.n2col)
+            correct_trans(beam)
+        elif kind == "quad":
+            quad(cfg, beam, el[1], el[2])
+        elif kind == "chicane":
+            _, zbar, disp, slip = el
+            chicane(cfg, beam, disp, slip)
+            if qdiffraction and zbar > 0.0:
+                diffract(cfg, re, im, zbar)
+            sz = sz + zbar
+            if cfg.mesh_type == MESH_PERIODIC:
+                wrap_z2(cfg, beam.z2)
+        elif kind == "drift":
+            dz = el[1]
+            drift(cfg, beam, dz)
+            if qdiffraction:
+                diffract(cfg, re, im, dz)
+            sz = sz + dz
+        elif kind == "modulation":
+            modulation(beam, el[1], el[2])
+        else:
+            raise ValueError(kind)
+    return sz, csteps

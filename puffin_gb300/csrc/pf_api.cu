@@ -468,6 +468,7 @@ int pf_destroy(pf_handle *h) {
   cudaFree(h->oc32);
   cudaFree(h->staging);
   cudaFree(h->diag);
+  cudaFree(h->lat_scratch);
   cudaFree(h->d_status);
   cudaFree(h->d_red);
   if (h->h_status) cudaFreeHost(h->h_status);
@@ -741,13 +742,22 @@ int pf_run(pf_handle *h, int32_t nsteps, int32_t isteps4diff, int32_t qdiffracti
       rc = pf_diffract(h, dzdf + dzds);
       if (rc) return rc;
     }
-    if (istep % redist == 0) {
+    h->csteps++;
+    if (h->csteps % redist == 0) {
       rc = pf_wrap_z2(h);
       if (rc) return rc;
     }
     if (steps_done) *steps_done = istep;
   }
   PF_CUDA(cudaStreamSynchronize(h->stream));
+  return PF_OK;
+}
+
+int64_t pf_step_count(const pf_handle *h) { return h ? h->csteps : -1; }
+
+int pf_set_step_count(pf_handle *h, int64_t csteps) {
+  if (!h || csteps < 0) return PF_BAD_ARG;
+  h->csteps = csteps;
   return PF_OK;
 }
 

@@ -134,6 +134,11 @@ struct pf_handle {
   // diagnostics scratch
   double *diag = nullptr;
   size_t diag_cap = 0;
+  double *lat_scratch = nullptr;  // partial sums of the chi-weighted means
+
+  // completed RK4 steps over the handle's life (the reference's iCsteps); the
+  // z2 wrap cadence counts these
+  int64_t csteps = 0;
 
   // taper state
   double n2col = 1.0, n2col0 = 1.0, undgrad = 0.0;

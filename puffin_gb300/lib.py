@@ -47,7 +47,9 @@ SYMBOLS = (
     "pf_get_window", "pf_rk4_step", "pf_redistribute", "pf_wrap_z2", "pf_diffract", "pf_run",
     "pf_sync", "pf_kernel_launches", "pf_last_error", "pf_abi_version", "pf_get_stream",
     "pf_profile", "pf_profile_read", "pf_rk4_step_noalloc", "pf_power", "pf_num_slices",
-    "pf_bunching", "pf_spectrum",
+    "pf_bunching", "pf_spectrum", "pf_step_count", "pf_set_step_count", "pf_drift",
+    "pf_chicane", "pf_quad", "pf_modulation", "pf_match_in", "pf_match_out",
+    "pf_correct_trans", "pf_init_undulator",
 )
 NOALLOC_MAX_PARTICLES = 32768
 NOALLOC_MAX_NODES = 32768
@@ -108,6 +110,16 @@ def load(build_if_missing: bool = False):
         "pf_num_slices": (i64, [H]),
         "pf_bunching": (ctypes.c_int, [H, i32, ctypes.c_void_p, i64]),
         "pf_spectrum": (ctypes.c_int, [H, ctypes.c_void_p, ctypes.c_void_p, i64]),
+        "pf_step_count": (i64, [H]),
+        "pf_set_step_count": (ctypes.c_int, [H, i64]),
+        "pf_drift": (ctypes.c_int, [H, f64, i32]),
+        "pf_chicane": (ctypes.c_int, [H, f64, f64, f64, i32]),
+        "pf_quad": (ctypes.c_int, [H, f64, f64]),
+        "pf_modulation": (ctypes.c_int, [H, f64, f64]),
+        "pf_match_in": (ctypes.c_int, [H, f64]),
+        "pf_match_out": (ctypes.c_int, [H, f64]),
+        "pf_correct_trans": (ctypes.c_int, [H]),
+        "pf_init_undulator": (ctypes.c_int, [H, i32, f64, f64, f64, f64, f64, f64, i32, f64, i32]),
         "pf_rk4_step_noalloc": (ctypes.c_int, [P, dp, dp, f64, f64, i64] + [ctypes.c_void_p] * 9
                                 + [i32, i32, ctypes.c_void_p]),
     }

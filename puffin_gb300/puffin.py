@@ -183,6 +183,54 @@ class Puffin:
                                      ctypes.byref(done)))
         return z.value
 
+    # -- cumulative step count (iCsteps) -----------------------------------------
+    @property
+    def step_count(self) -> int:
+        return int(self._lib.pf_step_count(self._h))
+
+    @step_count.setter
+    def step_count(self, n: int):
+        self._check(self._lib.pf_set_step_count(self._h, int(n)))
+
+    # -- beam-line elements (acc_lattice.f90) --------------------------------------
+    def drift(self, dz: float, qdiffraction: bool = True):
+        """driftSection (acc_lattice.f90:478-518)."""
+        self._check(self._lib.pf_drift(self._h, float(dz), int(bool(qdiffraction))))
+
+    def disperse(self, disp: float, slip: float, zbar: float, qdiffraction: bool = True):
+        """disperse: a chicane (acc_lattice.f90:420-463)."""
+        self._check(self._lib.pf_chicane(self._h, float(disp), float(slip), float(zbar),
+                                         int(bool(qdiffraction))))
+
+    def quad(self, qfx: float, qfy: float):
+        """Quad point transform (acc_lattice.f90:531-561)."""
+        self._check(self._lib.pf_quad(self._h, float(qfx), float(qfy)))
+
+    def modulation(self, mag: float, wavenum: float):
+        """bModulation (acc_lattice.f90:575-585)."""
+        self._check(self._lib.pf_modulation(self._h, float(mag), float(wavenum)))
+
+    def matchIn(self, sz: float):
+        self._check(self._lib.pf_match_in(self._h, float(sz)))
+
+    def matchOut(self, sz: float):
+        self._check(self._lib.pf_match_out(self._h, float(sz)))
+
+    def correctTrans(self):
+        self._check(self._lib.pf_correct_trans(self._h))
+
+    def init_undulator(self, und_type: int, fx: float, fy: float, kbxsf: float, kbysf: float,
+                       mf: float, taper: float, nsteps: int, hstep: float, und_ends: bool):
+        """initUndulator (acc_lattice.f90:848-895)."""
+        self._check(self._lib.pf_init_undulator(self._h, int(und_type), float(fx), float(fy),
+                                                float(kbxsf), float(kbysf), float(mf),
+                                                float(taper), int(nsteps), float(hstep),
+                                                int(bool(und_ends))))
+        for k, v in (("und_type", und_type), ("fx", fx), ("fy", fy), ("kbxsf", kbxsf),
+                     ("kbysf", kbysf), ("n2col0", mf), ("undgrad", taper),
+                     ("und_ends", int(bool(und_ends)))):
+            setattr(self.params, k, v)
+
     # -- diagnostics ------------------------------------------------------------
     def power(self):
         """Power per z2 plane (fPower_1D / fPower_3D)."""
