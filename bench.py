@@ -61,6 +61,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision leg")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--np3", type=int, default=2 ** 24,
+                    help="macroparticles of the mixed-vs-FP64 leg on the config-1 mesh (0: skip)")
+    ap.add_argument("--steps3", type=int, default=32)
     return ap.parse_args()
 
 
@@ -194,17 +197,23 @@ def cpu_baseline(w, seconds):
 
 
 # ---------------------------------------------------------------------------
-def _time_path(args, dev, precision, world, stream_events=True):
-    """Run the workload on one precision path: W warm-up steps, then K timed
+def _time_path(args, dev, precision, world, workload="config2", steps=None, warmup=None):
+    """Run a workload on one precision path: W warm-up steps, then K timed
     steps (CUDA events on the library's stream).  Returns timings, the
-    per-kernel-class device times and the final radiated power sum |A|^2."""
+    per-kernel-class device times, the final radiated power sum |A|^2 and the
+    diagnostics (power per z2 plane, |b1| per slice, on-axis spectrum)."""
     import torch
 
     import puffin_gb300 as P
     from puffin_gb300 import configs
     from puffin_gb300 import lib as L
 
-    w = configs.config2(np_=args.np, nz2=args.nz2)
+    steps = args.steps if steps is None else steps
+    warmup = args.warmup if warmup is None else warmup
+    if workload == "config2":
+        w = configs.config2(np_=args.np, nz2=args.nz2)
+    else:
+        w = configs.config3(np_=args.np3)
     p = w.params
     p.device = dev
     p.precision = precision
@@ -227,7 +236,7 @@ def _time_path(args, dev, precision, world, stream_events=True):
         if state["i"] % every == 0:
             sim.diffractIM(every * w.h)   # merged end + start half steps
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         step()
     sim.sync()
     if world > 1:
@@ -239,7 +248,7 @@ def _time_path(args, dev, precision, world, stream_events=True):
     with ClockSampler(dev) as clk:
         torch.cuda.synchronize()
         e0.record(stream)
-        for _ in range(args.steps):
+        for _ in range(steps):
             step()
         e1.record(stream)
         torch.cuda.synchronize()
@@ -254,7 +263,26 @@ def _time_path(args, dev, precision, world, stream_events=True):
     sim.profile(False)
     fr, fi = sim.get_field()
     out["power"] = float(np.sum(fr * fr + fi * fi))
+    out["diag"] = {"power_z": sim.power(), "b1": sim.bunching(1), "spectrum": sim.spectrum()[0]}
+    out["steps"], out["warmup"] = steps, warmup
     return out
+
+
+def output_errors(r64, rmx):
+    """Error of the mixed path against the FP64 path per output: power vs z
+    (max |dP| over max P), |b1| per slice (max absolute difference) and the
+    on-axis spectrum (relative L2 error)."""
+    d64, dmx = r64["diag"], rmx["diag"]
+    pz64, pzmx = d64["power_z"], dmx["power_z"]
+    s64, smx = d64["spectrum"], dmx["spectrum"]
+    return {
+        "total_power_rel": abs(rmx["power"] - r64["power"]) / max(r64["power"], 1e-300),
+        "power_vs_z_max_rel": float(np.max(np.abs(pzmx - pz64)) / max(np.max(pz64), 1e-300)),
+        "b1_max_abs": float(np.max(np.abs(dmx["b1"] - d64["b1"]))),
+        "b1_max_fp64": float(np.max(d64["b1"])),
+        "spectrum_rel_l2": float(np.linalg.norm(smx - s64) / max(np.linalg.norm(s64), 1e-300)),
+        "after_steps": r64["warmup"] + r64["steps"],
+    }
 
 
 def run_gpu(args, rank, world):
@@ -304,15 +332,22 @@ def run_gpu(args, rank, world):
     sim.close()
 
     rmx = None
+    c3 = None
     if not args.no_mixed:
         rmx = _time_path(args, dev, P.MIXED, world)
         rmx["sim"].close()
+        if args.np3 > 0:
+            c3 = {}
+            for name, prec in (("fp64", P.FP64), ("mixed", P.MIXED)):
+                c3[name] = _time_path(args, dev, prec, world, "config3", args.steps3, args.warmup)
+                c3[name]["sim"].close()
 
-    times = torch.tensor([ms, e2e_ms, rmx["ms"] if rmx else 0.0], dtype=torch.float64,
-                         device=f"cuda:{dev}")
+    times = torch.tensor([ms, e2e_ms, rmx["ms"] if rmx else 0.0,
+                          c3["fp64"]["ms"] if c3 else 0.0, c3["mixed"]["ms"] if c3 else 0.0],
+                         dtype=torch.float64, device=f"cuda:{dev}")
     if world > 1:
         torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
-    ms, e2e_ms, mx_ms = (float(v) for v in times)
+    ms, e2e_ms, mx_ms, c3_64_ms, c3_mx_ms = (float(v) for v in times)
     if rank != 0:
         return None
 
@@ -352,7 +387,8 @@ def run_gpu(args, rank, world):
         },
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "steps": args.e2e_steps},
-        "gpu_launches": r64["launches"] + (rmx["launches"] if rmx else 0),
+        "gpu_launches": r64["launches"] + (rmx["launches"] if rmx else 0)
+        + (c3["fp64"]["launches"] + c3["mixed"]["launches"] if c3 else 0),
         "kernel_ms": kern,
         "roofline": {"kernel": "k_stage (fused FP64 RK4 stage)", "bound": "hbm",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -374,10 +410,28 @@ def run_gpu(args, rank, world):
             "power_rel_error_vs_fp64": abs(rmx["power"] - r64["power"]) / max(r64["power"], 1e-300),
             "power_after_steps": {"fp64": r64["power"], "mixed": rmx["power"],
                                   "steps": args.warmup + args.steps},
+            "errors_vs_fp64": output_errors(r64, rmx),
             "kernel_ms": mk,
             "roofline": {"kernel": "k_stage_mixed", "bound": "hbm", "achieved": m_ach,
                          "peak": peak, "unit": "GB/s", "frac": m_ach / peak},
             "clocks": rmx["clocks"],
+        }
+    if c3:
+        w3 = c3["fp64"]["w"]
+        n3 = w3.np
+        rec["mixed_config3"] = {
+            "workload": w3.name, "macroparticles": n3,
+            "mesh": [w3.params.nx, w3.params.ny, w3.params.nz2],
+            "steps": args.steps3, "warmup": args.warmup,
+            "fp64": {"value": world * n3 * args.steps3 / (c3_64_ms * 1e-3),
+                     "ms_per_step": c3_64_ms / args.steps3,
+                     "kernel_ms": {k: v[0] for k, v in c3["fp64"]["kernel"].items()}},
+            "mixed": {"value": world * n3 * args.steps3 / (c3_mx_ms * 1e-3),
+                      "ms_per_step": c3_mx_ms / args.steps3,
+                      "kernel_ms": {k: v[0] for k, v in c3["mixed"]["kernel"].items()}},
+            "speedup_vs_fp64": c3_64_ms / c3_mx_ms,
+            "errors_vs_fp64": output_errors(c3["fp64"], c3["mixed"]),
+            "unit": UNIT,
         }
     return rec
 

@@ -68,6 +68,7 @@ struct FftArgs {
   real *re_out, *im_out;        // split output (last pass)
   const cplx *tw_f, *tw_b;      // per-pass twiddles, forward and backward
   AxisPlan ax;
+  AxisPlan ay;   // the y axis, for the transverse-plane kernel (ax is then x)
   MulTables T;
   int dir;       // direction of the first transform: 0 forward, 1 backward
   int mid;       // MID_*: operation after the first transform
@@ -78,6 +79,32 @@ struct FftArgs {
 
 __device__ __forceinline__ int64_t line_base(const AxisPlan &p, int64_t L) {
   return (L % p.inner) + (L / p.inner) * p.ostride;
+}
+
+// Asynchronous global -> shared copies (cp.async): a thread issues all of its
+// loads of a line group or plane before waiting once, so the whole block's
+// reads are in flight together.
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void *smem, const void *gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  if constexpr (BYTES == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(sa), "l"(gmem), "n"(BYTES)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
+// element pos of the pass input into shared slot dst
+__device__ __forceinline__ void load_async(cplx *dst, const FftArgs &a, int64_t pos) {
+  if (a.load_split) {
+    cp_async<sizeof(real)>(&dst->r, a.re_in + pos);
+    cp_async<sizeof(real)>(&dst->i, a.im_in + pos);
+  } else {
+    cp_async<sizeof(cplx)>(dst, a.A + pos);
+  }
 }
 
 // ---- butterflies -------------------------------------------------------------
@@ -424,8 +451,9 @@ __global__ void __launch_bounds__(NTHREADS) k_fft(const FftArgs a) {
       j = t / nl;
     }
     const int64_t pos = line_base(p, L0 + l) + (int64_t)j * p.stride;
-    smem[l * n + j] = a.load_split ? cplx{a.re_in[pos], a.im_in[pos]} : a.A[pos];
+    load_async(smem + l * n + j, a, pos);
   }
+  cp_async_wait_all();
   __syncthreads();
   {
     cplx *res = run_transform(smem, other, scratch, a, nl, a.dir);
@@ -481,6 +509,225 @@ __global__ void k_elementwise(const FftArgs a) {
   store(a, t, v);
 }
 
+// ---- in-place passes on one shared-memory buffer ----------------------------
+// The transverse-plane kernel (a whole nx*ny plane per block: the x and y
+// transforms of one pass over HBM) and the long-line kernel (a few adjacent
+// z2 lines per block, so that every 32-byte sector of the strided z2 axis is
+// used in full) hold their data in a single shared buffer.  A pass stages
+// the inputs of each thread's butterflies in registers, the block syncs, and
+// the outputs overwrite the inputs.  Element j of line l sits at
+// buf[l * ls + j * es].
+constexpr int PT = 512;  // threads of the in-place kernels
+__host__ __device__ constexpr int ip_cap() { return sizeof(real) == 4 ? 16896 : 8448; }
+__host__ __device__ constexpr int ip_maxb(int R) { return (ip_cap() + R * PT - 1) / (R * PT); }
+
+template <int R, bool INV>
+__device__ __noinline__ void ip_pass(cplx *buf, int n, int nl, int ls, int es, int Ns,
+                                     const cplx *tw) {
+  constexpr int MAXB = ip_maxb(R);
+  const int nb = n / R;
+  const int total = nl * nb;
+  int obase[MAXB];
+  if constexpr (R == 2 || R == 4 || R == 8) {
+    cplx v[MAXB][R];
+#pragma unroll
+    for (int b = 0; b < MAXB; ++b) {
+      const int t = threadIdx.x + b * PT;
+      obase[b] = -1;
+      if (t < total) {
+        const int l = t / nb, j = t - l * nb;
+        const int k = j % Ns;
+        const cplx *src = buf + l * ls + j * es;
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[b][r] = src[r * nb * es];
+        if (Ns > 1) {
+#pragma unroll
+          for (int r = 1; r < R; ++r) v[b][r] = cmul(v[b][r], tw[k * R + r]);
+        }
+        obase[b] = l * ls + ((j / Ns) * Ns * R + k) * es;
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int b = 0; b < MAXB; ++b)
+      if (obase[b] >= 0) dft_store<R, INV>(v[b], buf + obase[b], Ns * es);
+    __syncthreads();
+  } else {
+    constexpr int H = (R - 1) / 2;
+    constexpr int OFF = root_off(R);
+    static_assert(OFF >= 0, "radix without an unrolled butterfly");
+    cplx x0[MAXB], av[MAXB][H], bv[MAXB][H];
+#pragma unroll
+    for (int b = 0; b < MAXB; ++b) {
+      const int t = threadIdx.x + b * PT;
+      obase[b] = -1;
+      if (t < total) {
+        const int l = t / nb, j = t - l * nb;
+        const int k = j % Ns;
+        const cplx *src = buf + l * ls + j * es;
+        const cplx *twk = tw + k * R;
+        x0[b] = src[0];
+#pragma unroll
+        for (int q = 1; q <= H; ++q) {
+          cplx u = src[q * nb * es], w = src[(R - q) * nb * es];
+          if (Ns > 1) {
+            u = cmul(u, twk[q]);
+            w = cmul(w, twk[R - q]);
+          }
+          av[b][q - 1] = cadd(u, w);
+          bv[b][q - 1] = csub(u, w);
+        }
+        obase[b] = l * ls + ((j / Ns) * Ns * R + k) * es;
+      }
+    }
+    __syncthreads();
+    const int ds = Ns * es;
+#pragma unroll
+    for (int b = 0; b < MAXB; ++b) {
+      if (obase[b] < 0) continue;
+      cplx *dst = buf + obase[b];
+      cplx s0 = x0[b];
+#pragma unroll
+      for (int q = 0; q < H; ++q) s0 = cadd(s0, av[b][q]);
+      dst[0] = s0;
+      // every thread runs the same (q, j) sequence, so the root index is
+      // uniform across the warp and the constant bank broadcasts it
+#pragma unroll 1
+      for (int q = 1; q <= H; ++q) {
+        cplx C = x0[b], S{(real)0, (real)0};
+        int m = 0;
+#pragma unroll
+        for (int j = 1; j <= H; ++j) {
+          m += q;
+          if (m >= R) m -= R;
+          const real c = c_roots[OFF + m].r;
+          const real sn = c_roots[OFF + m].i;
+          C.r = fma(av[b][j - 1].r, c, C.r);
+          C.i = fma(av[b][j - 1].i, c, C.i);
+          S.r = fma(bv[b][j - 1].r, sn, S.r);
+          S.i = fma(bv[b][j - 1].i, sn, S.i);
+        }
+        if (!INV) {
+          dst[q * ds] = cplx{C.r + S.i, C.i - S.r};
+          dst[(R - q) * ds] = cplx{C.r - S.i, C.i + S.r};
+        } else {
+          dst[q * ds] = cplx{C.r - S.i, C.i + S.r};
+          dst[(R - q) * ds] = cplx{C.r + S.i, C.i - S.r};
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// whether an axis of nl lines can run in place in one block
+__host__ __device__ inline bool ip_fits(const AxisPlan &p, int nl) {
+  for (int ps = 0; ps < p.npass; ++ps) {
+    const int R = p.radix[ps];
+    if ((int64_t)nl * (p.n / R) > (int64_t)PT * ip_maxb(R)) return false;
+    if (sizeof(real) == 8 && R > 17) return false;  // register budget of an FP64 butterfly
+  }
+  return true;
+}
+
+template <bool INV>
+__device__ __forceinline__ void ip_transform(cplx *buf, const AxisPlan &p, int nl, int ls, int es,
+                                             const cplx *tw) {
+  for (int ps = 0; ps < p.npass; ++ps) {
+    const int R = p.radix[ps], Ns = p.ns[ps];
+    const cplx *twp = tw + p.twoff[ps];
+    switch (R) {
+      case 2: ip_pass<2, INV>(buf, p.n, nl, ls, es, Ns, twp); break;
+      case 4: ip_pass<4, INV>(buf, p.n, nl, ls, es, Ns, twp); break;
+      case 8: ip_pass<8, INV>(buf, p.n, nl, ls, es, Ns, twp); break;
+      case 3: ip_pass<3, INV>(buf, p.n, nl, ls, es, Ns, twp); break;
+      case 5: ip_pass<5, INV>(buf, p.n, nl, ls, es, Ns, twp); break;
+      case 7: ip_pass<7, INV>(buf, p.n, nl, ls, es, Ns, twp); break;
+      case 11: ip_pass<11, INV>(buf, p.n, nl, ls, es, Ns, twp); break;
+      case 13: ip_pass<13, INV>(buf, p.n, nl, ls, es, Ns, twp); break;
+      case 17: ip_pass<17, INV>(buf, p.n, nl, ls, es, Ns, twp); break;
+      case 43:
+        if constexpr (sizeof(real) == 4) ip_pass<43, INV>(buf, p.n, nl, ls, es, Ns, twp);
+        break;
+      default: break;  // excluded when the plan is built
+    }
+  }
+}
+
+// the 2D transverse transform of the plane in buf (x fastest, pitch nx)
+__device__ __forceinline__ void xy_transform(cplx *buf, const FftArgs &a, int inv) {
+  const int nx = a.T.nx, ny = a.T.ny;
+  if (!inv) {
+    if (nx > 1) ip_transform<false>(buf, a.ax, ny, nx, 1, a.tw_f);
+    if (ny > 1) ip_transform<false>(buf, a.ay, nx, 1, nx, a.tw_f);
+  } else {
+    if (ny > 1) ip_transform<true>(buf, a.ay, nx, 1, nx, a.tw_b);
+    if (nx > 1) ip_transform<true>(buf, a.ax, ny, nx, 1, a.tw_b);
+  }
+}
+
+// One block per z2 plane: x and y transforms (and the mid operation and the
+// opposite transforms) with a single read and write of the plane.
+__global__ void __launch_bounds__(PT, 1) k_fft_plane(const FftArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cplx *buf = reinterpret_cast<cplx *>(smem_raw);
+  const int nx = a.T.nx;
+  const int64_t plane = (int64_t)nx * a.T.ny;
+  const int z = blockIdx.x;
+  const int64_t off = (int64_t)z * plane;
+  for (int64_t t = threadIdx.x; t < plane; t += PT) load_async(buf + t, a, off + t);
+  cp_async_wait_all();
+  __syncthreads();
+  xy_transform(buf, a, a.dir);
+  if (a.mid != MID_NONE) {
+    for (int64_t t = threadIdx.x; t < plane; t += PT)
+      buf[t] = mid_op(a, off + t, (int)(t % nx), (int)(t / nx), z, buf[t]);
+    __syncthreads();
+    if (a.second) xy_transform(buf, a, !a.dir);
+  }
+  for (int64_t t = threadIdx.x; t < plane; t += PT) store(a, off + t, buf[t]);
+}
+
+// Long lines (the z2 axis): lpb adjacent lines per block, lines padded by one
+// element in shared memory; consecutive threads load consecutive lines, which
+// are adjacent in HBM.
+__global__ void __launch_bounds__(PT, 1) k_fft_long(const FftArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cplx *buf = reinterpret_cast<cplx *>(smem_raw);
+  const AxisPlan &p = a.ax;
+  const int n = p.n, ls = n + 1;
+  const int64_t L0 = (int64_t)blockIdx.x * p.lpb;
+  const int nl = (int)min((int64_t)p.lpb, p.nlines - L0);
+  for (int t = threadIdx.x; t < nl * n; t += PT) {
+    const int l = t % nl, j = t / nl;
+    const int64_t pos = line_base(p, L0 + l) + (int64_t)j * p.stride;
+    load_async(buf + l * ls + j, a, pos);
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  if (a.dir) ip_transform<true>(buf, p, nl, ls, 1, a.tw_b);
+  else ip_transform<false>(buf, p, nl, ls, 1, a.tw_f);
+  if (a.mid != MID_NONE) {
+    for (int t = threadIdx.x; t < nl * n; t += PT) {
+      const int l = t / n, j = t - l * n;
+      int x, y, z;
+      coords(p, a.T, L0 + l, j, x, y, z);
+      const int64_t pos = line_base(p, L0 + l) + (int64_t)j * p.stride;
+      buf[l * ls + j] = mid_op(a, pos, x, y, z, buf[l * ls + j]);
+    }
+    __syncthreads();
+    if (a.second) {
+      if (!a.dir) ip_transform<true>(buf, p, nl, ls, 1, a.tw_b);
+      else ip_transform<false>(buf, p, nl, ls, 1, a.tw_f);
+    }
+  }
+  for (int t = threadIdx.x; t < nl * n; t += PT) {
+    const int l = t % nl, j = t / nl;
+    const int64_t pos = line_base(p, L0 + l) + (int64_t)j * p.stride;
+    store(a, pos, buf[l * ls + j]);
+  }
+}
+
 // per-call tables: propagator and damping factors for step h
 __global__ void k_tables(cplx *px, cplx *py, real *dxt, real *dyt, const double *kx,
                          const double *ky, const double *kz, int nx, int ny, int nz, double h,
@@ -514,6 +761,11 @@ struct Plan {
   int64_t n = 0;
   AxisPlan ax[3];
   size_t smem[3] = {0, 0, 0};
+  bool plane = false;        // x and y in one k_fft_plane pass
+  size_t plane_smem = 0;
+  bool zlong = false;        // z2 with k_fft_long
+  AxisPlan axl;              // the z2 plan of k_fft_long (its own lpb)
+  size_t zlong_smem = 0;
   cplx *A = nullptr, *anb = nullptr;
   cplx *tw = nullptr;  // forward block then backward block
   size_t ntw = 0;
@@ -676,6 +928,34 @@ static int build_plan(pf_handle *h, Plan *&out) {
     ap.lpb = (int)lpb;
     d->smem[a] = bytes(lpb);
   }
+  // transverse-plane kernel: the whole nx*ny plane in one shared buffer
+  {
+    const int64_t pts = (int64_t)d->nx * d->ny;
+    const size_t b = (size_t)pts * sizeof(cplx);
+    d->plane = (d->nx > 1 || d->ny > 1) && pts <= ip_cap() && b <= (size_t)max_smem &&
+               (d->nx == 1 || ip_fits(d->ax[0], d->ny)) && (d->ny == 1 || ip_fits(d->ax[1], d->nx));
+    d->plane_smem = b;
+  }
+  // long z2 lines: the line kernel reads fewer than 32 bytes of adjacent
+  // lines per row; give each block enough adjacent lines to fill a sector
+  {
+    const AxisPlan &az = d->ax[2];
+    const int want = (int)((32 + sizeof(cplx) - 1) / sizeof(cplx));
+    if (az.n > 1 && (int64_t)az.lpb * (int64_t)sizeof(cplx) < 32) {
+      int g = (int)std::min<int64_t>(want, az.nlines);
+      auto fits = [&](int gg) {
+        return (size_t)gg * (az.n + 1) * sizeof(cplx) <= (size_t)max_smem &&
+               (int64_t)gg * az.n <= ip_cap() && ip_fits(az, gg);
+      };
+      while (g > 1 && !fits(g)) --g;
+      if (g > az.lpb && fits(g)) {
+        d->zlong = true;
+        d->axl = az;
+        d->axl.lpb = g;
+        d->zlong_smem = (size_t)g * (az.n + 1) * sizeof(cplx);
+      }
+    }
+  }
   d->ntw = tab.size();
   if (d->ntw) {
     PF_CUDA(cudaMalloc(&d->tw, 2 * d->ntw * sizeof(cplx)));
@@ -684,6 +964,8 @@ static int build_plan(pf_handle *h, Plan *&out) {
                        cudaMemcpyHostToDevice));
   }
   PF_CUDA(cudaFuncSetAttribute(k_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+  PF_CUDA(cudaFuncSetAttribute(k_fft_plane, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+  PF_CUDA(cudaFuncSetAttribute(k_fft_long, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
 
   PF_CUDA(cudaMalloc(&d->A, d->n * sizeof(cplx)));
   PF_CUDA(cudaMalloc(&d->anb, d->n * sizeof(cplx)));
@@ -768,9 +1050,29 @@ static int fft_pass(pf_handle *h, Plan *d, FftArgs a, int axis) {
     }
     return PF_OK;
   }
+  if (axis == 2 && d->zlong) {
+    a.ax = d->axl;
+    const int64_t blocks = (a.ax.nlines + a.ax.lpb - 1) / a.ax.lpb;
+    pf_prof_begin(h, PROF_FFT);
+    k_fft_long<<<(unsigned)blocks, PT, d->zlong_smem, h->stream>>>(a);
+    pf_prof_end(h);
+    PF_LAUNCHED(h);
+    return PF_OK;
+  }
   const int64_t blocks = (a.ax.nlines + a.ax.lpb - 1) / a.ax.lpb;
   pf_prof_begin(h, PROF_FFT);
   k_fft<<<(unsigned)blocks, NTHREADS, d->smem[axis], h->stream>>>(a);
+  pf_prof_end(h);
+  PF_LAUNCHED(h);
+  return PF_OK;
+}
+
+// One transverse-plane pass (x and y together).
+static int plane_pass(pf_handle *h, Plan *d, FftArgs a) {
+  a.ax = d->ax[0];
+  a.ay = d->ax[1];
+  pf_prof_begin(h, PROF_FFT);
+  k_fft_plane<<<(unsigned)d->nz, PT, d->plane_smem, h->stream>>>(a);
   pf_prof_end(h);
   PF_LAUNCHED(h);
   return PF_OK;
@@ -818,6 +1120,32 @@ static int diffract(pf_handle *h, Plan *&plan, real *re, real *im, cplx *oc, dou
   pf_prof_end(h);
   PF_LAUNCHED(h);
 
+  if (d->plane) {
+    // five passes: xy fwd | z fwd * prop * z inv | xy inv, split, xy fwd |
+    // z fwd * damp * z inv | xy inv, + A_nb
+    struct PStep {
+      int plane, dir, mid, second, load_split, store_split;
+    };
+    const PStep ps[5] = {
+        {1, 0, MID_NONE, 0, 1, 0},
+        {0, 0, MID_PROP, 1, 0, 0},
+        {1, 1, MID_SPLIT, 1, 0, 0},
+        {0, 0, MID_DAMP, 1, 0, 0},
+        {1, 1, MID_RECOMB, 0, 0, 1},
+    };
+    for (const PStep &s : ps) {
+      FftArgs b = a;
+      b.dir = s.dir;
+      b.mid = s.mid;
+      b.second = s.second;
+      b.load_split = split && s.load_split;
+      b.store_split = split && s.store_split;
+      b.mirror = a.mirror && s.store_split;
+      const int rc = s.plane ? plane_pass(h, d, b) : fft_pass(h, d, b, 2);
+      if (rc) return rc;
+    }
+    return PF_OK;
+  }
   struct Step {
     int axis, dir, mid, second, load_split, store_split;
   };

@@ -20,6 +20,8 @@
 #include <algorithm>
 #include <mutex>
 
+#include <climits>
+
 #include "pf_internal.h"
 
 namespace {
@@ -122,12 +124,22 @@ __device__ __forceinline__ double fix_to_double(u64 lo, u64 hi, double inv_scale
   return neg ? -v : v;
 }
 
-template <int STAGE, bool ONED>
-__global__ void __launch_bounds__(256) k_stage(const StageArgs a) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.np) return;
-  if (*((volatile unsigned int *)a.status) != 0u) return;
+// Shared-memory deposit tile of the dense mode: the 128-bit fixed-point sums
+// (lo and hi words, re and im) of FT_PLANES window planes starting at pzlo.
+// Integer addition is associative, so the tile and its flush to HBM give the
+// same bits as the direct atomics, whatever the order.
+constexpr int FT_PLANES = 3;
+constexpr int FT_PPB = 8192;  // macroparticles per block in the dense mode
+constexpr int FT_THREADS = 256;
 
+struct FixTile {
+  u64 *lo_r, *hi_r, *lo_i, *hi_i;
+  int pzlo, ntr;
+};
+
+template <int STAGE, bool ONED, bool TILE>
+__device__ __forceinline__ void stage_particle(const StageArgs &a, const int64_t i,
+                                               const FixTile &t) {
   const double y0[6] = {a.x[i], a.y[i], a.z2[i], a.px[i], a.py[i], a.gam[i]};
   double s[6];
   double kin[6];
@@ -160,12 +172,12 @@ __global__ void __launch_bounds__(256) k_stage(const StageArgs a) {
   double w[8];
   int64_t node[8];
   bool ok = true;
+  int64_t pz0 = 0, pz1 = 0;
   {
     const double tz = Z2 * a.inv_dz2;
     const double fz = floor(tz);
     const double z2n = fz + 1.0;
     const double zw2 = tz - fz;
-    int64_t pz0 = 0, pz1 = 0;
     if (a.periodic) {
       if (!(fabs(z2n) < 9.0e15)) {
         ok = false;
@@ -248,11 +260,22 @@ __global__ void __launch_bounds__(256) k_stage(const StageArgs a) {
       bool fits = true;
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
-        u64 lo, hi;
-        fits &= to_fix(w[c] * sr, a.fix_e, a.fix_maxexp, lo, hi);
-        fix_add(a.acc_lo_r, a.acc_hi_r, node[c], lo, hi);
-        fits &= to_fix(w[c] * si, a.fix_e, a.fix_maxexp, lo, hi);
-        fix_add(a.acc_lo_i, a.acc_hi_i, node[c], lo, hi);
+        u64 lor, hir, loi, hii;
+        fits &= to_fix(w[c] * sr, a.fix_e, a.fix_maxexp, lor, hir);
+        fits &= to_fix(w[c] * si, a.fix_e, a.fix_maxexp, loi, hii);
+        int tp = -1, ti = 0;
+        if constexpr (TILE) {
+          const int64_t plane = (ONED ? c == 0 : c < 4) ? pz0 : pz1;
+          tp = (int)plane - t.pzlo;
+          ti = tp * t.ntr + (int)(node[c] - plane * t.ntr);
+        }
+        if (TILE && tp >= 0 && tp < FT_PLANES) {
+          fix_add(t.lo_r, t.hi_r, ti, lor, hir);
+          fix_add(t.lo_i, t.hi_i, ti, loi, hii);
+        } else {
+          fix_add(a.acc_lo_r, a.acc_hi_r, node[c], lor, hir);
+          fix_add(a.acc_lo_i, a.acc_hi_i, node[c], loi, hii);
+        }
       }
       if (!fits) atomicOr(a.status, ST_OVERFLOW);
     }
@@ -292,6 +315,60 @@ __global__ void __launch_bounds__(256) k_stage(const StageArgs a) {
       const double k1 = a.k1[j][i];
       const double k23 = a.kacc[j][i];
       a.ynext[j][i] = y0[j] + a.h6 * (k1 + k[j] + 2.0 * k23);
+    }
+  }
+}
+
+template <int STAGE, bool ONED, bool TILE = false>
+__global__ void __launch_bounds__(256) k_stage(const StageArgs a) {
+  if constexpr (!TILE) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.np) return;
+    if (*((volatile unsigned int *)a.status) != 0u) return;
+    stage_particle<STAGE, ONED, false>(a, i, FixTile{});
+  } else {
+    // dense mode: FT_PPB consecutive macroparticles per block deposit into
+    // a shared tile of FT_PLANES planes from the lowest plane they start
+    // from (z2 only moves forward within a step, p2 > 0); the tile is then
+    // added to the window accumulators, one pair of atomics per node
+    extern __shared__ u64 ftile[];
+    __shared__ int s_pzlo;
+    const int ntr = (int)(a.nix * a.niy);
+    const int tn = FT_PLANES * ntr;
+    for (int k = threadIdx.x; k < 4 * tn; k += FT_THREADS) ftile[k] = 0ull;
+    if (threadIdx.x == 0) s_pzlo = INT_MAX;
+    __syncthreads();
+    const int64_t i0 = (int64_t)blockIdx.x * FT_PPB;
+    const int64_t i1 = min(a.np, i0 + FT_PPB);
+    const bool halted = (*((volatile unsigned int *)a.status) != 0u);
+    int my = INT_MAX;
+    if (!halted) {
+      for (int64_t i = i0 + threadIdx.x; i < i1; i += FT_THREADS) {
+        const double fz = floor(a.z2[i] * a.inv_dz2);
+        if (!(fabs(fz) < 2.0e9)) continue;
+        int m = (int)fz;
+        if (a.periodic) {
+          m %= (int)a.npl;
+          if (m < 0) m += (int)a.npl;
+        }
+        my = min(my, m);
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) my = min(my, __shfl_xor_sync(0xffffffffu, my, o));
+    if ((threadIdx.x & 31) == 0 && my != INT_MAX) atomicMin(&s_pzlo, my);
+    __syncthreads();
+    const FixTile t{ftile, ftile + tn, ftile + 2 * tn, ftile + 3 * tn, s_pzlo, ntr};
+    if (!halted)
+      for (int64_t i = i0 + threadIdx.x; i < i1; i += FT_THREADS)
+        stage_particle<STAGE, ONED, true>(a, i, t);
+    __syncthreads();
+    if (t.pzlo == INT_MAX) return;
+    for (int k = threadIdx.x; k < tn; k += FT_THREADS) {
+      const int64_t plane = (int64_t)t.pzlo + k / ntr;
+      if (plane >= a.npl) break;
+      const int64_t node = plane * ntr + (k % ntr);
+      fix_add(a.acc_lo_r, a.acc_hi_r, node, t.lo_r[k], t.hi_r[k]);
+      fix_add(a.acc_lo_i, a.acc_hi_i, node, t.lo_i[k], t.hi_i[k]);
     }
   }
 }
@@ -473,16 +550,43 @@ void pf_stage_coefficients(const pf_params &p, double sz, double n2col, int plac
   }
 }
 
+// Dense beams (many macroparticles per window cell) deposit through the
+// shared tile: direct atomics would pile onto few addresses.
+static bool dense_mode(const pf_handle *h, size_t *smem) {
+  const int64_t ntr = (int64_t)h->nix * h->niy;
+  const size_t bytes = (size_t)4 * FT_PLANES * ntr * sizeof(u64);
+  *smem = bytes;
+  return h->np >= (int64_t)8 * h->npl * ntr && bytes <= 96 * 1024;
+}
+
 static int launch_stage(pf_handle *h, int stage, StageArgs &a) {
   const int threads = 256;
   const int64_t blocks = (h->np + threads - 1) / threads;
   if (blocks == 0) return PF_OK;
   const bool oned = h->p.one_d != 0;
+  size_t smem = 0;
+  const bool dense = dense_mode(h, &smem);
+  const int64_t dblocks = (h->np + FT_PPB - 1) / FT_PPB;
+  static bool attr_set = false;
+  if (dense && !attr_set) {
+    const void *fns[] = {(const void *)k_stage<1, false, true>, (const void *)k_stage<2, false, true>,
+                         (const void *)k_stage<3, false, true>, (const void *)k_stage<4, false, true>,
+                         (const void *)k_stage<1, true, true>,  (const void *)k_stage<2, true, true>,
+                         (const void *)k_stage<3, true, true>,  (const void *)k_stage<4, true, true>};
+    for (const void *f : fns)
+      PF_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+    attr_set = true;
+  }
   pf_prof_begin(h, PROF_STAGE);
-#define PF_STAGE_CASE(S)                                                             \
-  case S:                                                                            \
-    if (oned) k_stage<S, true><<<(unsigned)blocks, threads, 0, h->stream>>>(a);      \
-    else k_stage<S, false><<<(unsigned)blocks, threads, 0, h->stream>>>(a);          \
+#define PF_STAGE_CASE(S)                                                                   \
+  case S:                                                                                  \
+    if (dense) {                                                                           \
+      if (oned) k_stage<S, true, true><<<(unsigned)dblocks, FT_THREADS, smem, h->stream>>>(a); \
+      else k_stage<S, false, true><<<(unsigned)dblocks, FT_THREADS, smem, h->stream>>>(a);     \
+    } else {                                                                               \
+      if (oned) k_stage<S, true><<<(unsigned)blocks, threads, 0, h->stream>>>(a);          \
+      else k_stage<S, false><<<(unsigned)blocks, threads, 0, h->stream>>>(a);              \
+    }                                                                                      \
     break;
   switch (stage) {
     PF_STAGE_CASE(1)

@@ -1,21 +1,33 @@
 // Mixed-precision RK4 macroparticle push.
 //
-// FP64: the particle state (x, y, z2, px, py, Gamma), the RK4 stage state and
-// stage combination, p2 (the z2 velocity, which sets the ponderomotive phase)
-// and the cell index and fractional position in each direction.
-// FP32: the field window, the interpolation weights, the gather, the source
-// term and its deposit, the b-fields and the momentum/energy equations.
+// FP64: the particle state (x, y, z2, px, py, Gamma) in HBM and every RK4
+// stage combination y + h/6 (k1 + k4 + 2 (k2 + k3)); the stage values of z2,
+// Gamma, px and py; p2 (the z2 velocity, which sets the ponderomotive phase)
+// and the z2 cell index and fraction.
+// FP32: the field window, the transverse stage coordinates and interpolation
+// weights, the gather, the source term and its deposit, the b-fields, the
+// momentum/energy equations, and the slopes of x, y, px, py and Gamma (the
+// z2 slope p2 stays FP64).
+//
+// GB300 issues FP64 at 1/64 of the FP32 rate, so this kernel is bound by its
+// FP64 instruction count: conversions between FP32 and FP64 are done with
+// integer operations (f2d, d2f_rn below), which keeps them off the FP64 pipe,
+// and 1/Gamma is a FP32 reciprocal refined by one FP64 Newton step.
 //
 // p2 (gamma_to_p2.f90:84-85) is (1/sqrt(1-u) - 1)/eta with
 // u = (1 + aw^2 p_perp^2)/(gamma0^2 Gamma^2) of order 1e-7: the reference form
 // cancels 7 digits.  Here r - 1 = 1/sqrt(1-u) - 1 is summed as its binomial
-// series u/2 + 3u^2/8 + 5u^3/16 + ... (seven terms, truncation below 1e-18 of
-// the result for u < 1e-3; the reference form is used above that), which is
-// accurate to an ulp in FP64 and needs no square root or division.
+// series u/2 + 3u^2/8 + 5u^3/16 + ... (five terms for u < 1e-4, seven for
+// u < 1e-3, truncation below 1e-16 of the result; the reference form above
+// that), which is accurate to a few ulps in FP64 and needs no square root or
+// division.
 //
-// Deposit: each block of 1024 macroparticles (4 per thread) accumulates its
-// contributions to the three z2 planes its particles start from in a
-// shared-memory tile, with compensated (TwoSum) float atomics: the rounding
+// Deposit: each block of 2048 macroparticles (4 per thread) accumulates its
+// contributions to the three z2 planes from the lowest plane its particles
+// start from in a shared-memory tile, deposited as each macroparticle's
+// slopes are computed (nothing per particle is kept, which keeps the kernel
+// near 64 registers and two 512-thread blocks per SM), with compensated
+// (TwoSum) float atomics: the rounding
 // error of every add is recovered from the value the atomic returns and added
 // to a second tile, so the tile sums carry about twice FP32's precision.  The
 // tile is then flushed to HBM with one float2 atomic per non-zero node.
@@ -31,7 +43,7 @@
 
 namespace {
 
-constexpr int MX_THREADS = 256;
+constexpr int MX_THREADS = 512;
 constexpr int MX_PPT = 4;  // macroparticles per thread
 constexpr int MX_TILE_PLANES = 3;
 
@@ -42,13 +54,19 @@ struct BFieldF {
 
 struct MixArgs {
   const double *x, *y, *z2, *px, *py, *gam, *chi;
-  const double *kin[6];
-  double *kout[6];
-  double *kacc[6];
-  const double *k1[6];
+  // slopes: FP32 arrays for x, y, px, py, Gamma (index 2 unused), FP64 for z2
+  const float *kin_f[6];
+  const double *kin_z;
+  float *kout_f[6];
+  double *kout_z;
+  float *kacc_f[6];
+  double *kacc_z;
+  const float *k1_f[6];
+  const double *k1_z;
   double *ynext[6];
   int64_t np;
   double cstate, h6;
+  float cstate_f, eta_f, inv_dx_f, inv_dy_f, hx_dx, hy_dy;
   const float2 *as;  // stage field (window, interleaved complex)
   float2 *acc;       // deposit accumulator (window)
   int nix, niy;
@@ -127,8 +145,43 @@ __device__ __forceinline__ void global_add(float2 *a, float2 v) {
   atomicAdd(&a->y, v.y);
 }
 
+// FP32 -> FP64, exact, with integer operations.  Zero and FP32 subnormals
+// give a signed zero (slopes that small are below every tolerance here);
+// infinities and NaNs map to infinities and NaNs.
+__device__ __forceinline__ double f2d(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned sign = u & 0x80000000u;
+  const unsigned e = (u >> 23) & 0xffu;
+  if (e == 0u) return __hiloint2double((int)sign, 0);
+  const unsigned ed = (e == 255u) ? 2047u : e + 896u;  // rebias 127 -> 1023
+  const unsigned m = u & 0x7fffffu;
+  return __hiloint2double((int)(sign | (ed << 20) | (m >> 3)), (int)(m << 29));
+}
+
+// FP64 -> FP32 rounded to nearest (ties away from zero) with integer
+// operations; magnitudes below FP32's normal range give a signed zero and
+// above it an infinity.
+__device__ __forceinline__ float d2f_rn(double d) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  const unsigned sign = hi & 0x80000000u;
+  const int e = (int)((hi >> 20) & 0x7ffu) - 896;
+  if (e <= 0) return __uint_as_float(sign);
+  if (e >= 255) return __uint_as_float(sign | 0x7f800000u);
+  const unsigned mag = ((unsigned)e << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+  return __uint_as_float(sign | (mag + ((lo >> 28) & 1u)));  // a carry rounds into the exponent
+}
+
 // r - 1 = 1/sqrt(1 - u) - 1
 __device__ __forceinline__ double rsqrt1m_minus1(double u) {
+  if (u < 1.0e-4) {
+    double s = 63.0 / 256.0;
+    s = fma(s, u, 35.0 / 128.0);
+    s = fma(s, u, 5.0 / 16.0);
+    s = fma(s, u, 3.0 / 8.0);
+    s = fma(s, u, 0.5);
+    return u * s;
+  }
   if (u < 1.0e-3) {
     // binomial coefficients C(2k,k)/4^k: 1/2, 3/8, 5/16, 35/128, 63/256, 231/1024, 429/2048
     double s = 429.0 / 2048.0;
@@ -152,59 +205,84 @@ __global__ void __launch_bounds__(MX_THREADS) k_stage_mixed(const MixArgs a) {
   float2 *tcomp = tsum + tile_n;
   __shared__ int s_pzlo;
 
+  const bool halted = (*((volatile unsigned int *)a.status) != 0u);
   if (a.tile) {
+    // tile origin: the lowest z2 plane the block's macroparticles start from
+    // (stage positions only move forward from there, p2 > 0)
     for (int t = threadIdx.x; t < 2 * tile_n; t += MX_THREADS) tsum[t] = make_float2(0.f, 0.f);
     if (threadIdx.x == 0) s_pzlo = INT_MAX;
     __syncthreads();
-  }
-  const bool halted = (*((volatile unsigned int *)a.status) != 0u);
-
-  // per particle kept until the deposit: source terms, weights, base nodes
-  float sr[MX_PPT], si[MX_PPT], wx[MX_PPT], wy[MX_PPT], wz[MX_PPT];
-  int64_t base0[MX_PPT];
-  int pz0v[MX_PPT], pz1v[MX_PPT];
-  bool dep[MX_PPT];
-  int my_pzlo = INT_MAX;
-
+    int my_pzlo = INT_MAX;
 #pragma unroll
+    for (int q = 0; q < MX_PPT; ++q) {
+      const int64_t i = (int64_t)blockIdx.x * (MX_THREADS * MX_PPT) + q * MX_THREADS + threadIdx.x;
+      if (halted || i >= a.np) continue;
+      const double fz = floor(a.z2[i] * a.inv_dz2);
+      if (!(fabs(fz) < 2.0e9)) continue;
+      int m = (int)fz;
+      if (a.periodic) {
+        m %= (int)a.npl;
+        if (m < 0) m += (int)a.npl;
+      }
+      my_pzlo = min(my_pzlo, m);
+    }
+    for (int o = 16; o > 0; o >>= 1) my_pzlo = min(my_pzlo, __shfl_xor_sync(0xffffffffu, my_pzlo, o));
+    if ((threadIdx.x & 31) == 0 && my_pzlo != INT_MAX) atomicMin(&s_pzlo, my_pzlo);
+    __syncthreads();
+  }
+  const int pzlo = a.tile ? s_pzlo : 0;
+
+#pragma unroll 1
   for (int q = 0; q < MX_PPT; ++q) {
-    dep[q] = false;
     const int64_t i = (int64_t)blockIdx.x * (MX_THREADS * MX_PPT) + q * MX_THREADS + threadIdx.x;
     if (halted || i >= a.np) continue;
-    const double y0[6] = {a.x[i], a.y[i], a.z2[i], a.px[i], a.py[i], a.gam[i]};
-    double s[6], kin[6];
-#pragma unroll
-    for (int j = 0; j < 6; ++j) {
-      kin[j] = (STAGE > 1) ? a.kin[j][i] : 0.0;
-      s[j] = (STAGE > 1) ? y0[j] + a.cstate * kin[j] : y0[j];
+    // FP64 state; stage values of z2, Gamma, px, py in FP64, of x, y in FP32
+    const double x0 = a.x[i], yv0 = a.y[i], z0 = a.z2[i], px0 = a.px[i], py0 = a.py[i],
+                 g0 = a.gam[i];
+    float kin[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    double kz_in = 0.0;
+    double zs = z0, gs = g0, pxs = px0, pys = py0;
+    float X = d2f_rn(x0), Y = d2f_rn(yv0);
+    if (STAGE > 1) {
+      kin[0] = a.kin_f[0][i];
+      kin[1] = a.kin_f[1][i];
+      kin[3] = a.kin_f[3][i];
+      kin[4] = a.kin_f[4][i];
+      kin[5] = a.kin_f[5][i];
+      kz_in = a.kin_z[i];
+      zs = fma(a.cstate, kz_in, z0);
+      gs = fma(a.cstate, f2d(kin[5]), g0);
+      pxs = fma(a.cstate, f2d(kin[3]), px0);
+      pys = fma(a.cstate, f2d(kin[4]), py0);
+      X = fmaf(a.cstate_f, kin[0], X);
+      Y = fmaf(a.cstate_f, kin[1], Y);
     }
-    const double G = s[5];
-    // 1/Gamma: FP32 seed and two Newton steps in FP64
-    double rG = (double)__frcp_rn((float)G);
-    rG = fma(rG, fma(-G, rG, 1.0), rG);
-    rG = fma(rG, fma(-G, rG, 1.0), rG);
-    const double bb = fma(a.aw2, fma(s[3], s[3], s[4] * s[4]), 1.0);
+    const float Gf = d2f_rn(gs), PX = d2f_rn(pxs), PY = d2f_rn(pys);
+    // 1/Gamma: FP32 reciprocal and one FP64 Newton step (relative error ~1e-14)
+    const float rGf = __frcp_rn(Gf);
+    double rG = f2d(rGf);
+    rG = fma(rG, fma(-gs, rG, 1.0), rG);
+    const double bb = fma(a.aw2, fma(pxs, pxs, pys * pys), 1.0);
     const double u = bb * a.inv_g02 * (rG * rG);
     const double p2 = rsqrt1m_minus1(u) * a.inv_eta;
-    const double q64 = fma(a.eta, p2, 1.0);
-    const float qrG = (float)(q64 * rG);
-    const float X = (float)s[0], Y = (float)s[1], PX = (float)s[3], PY = (float)s[4];
+    const float p2f = d2f_rn(p2);
+    const float qrG = fmaf(a.eta_f, p2f, 1.f) * rGf;
 
-    // cell and fraction in FP64, weights in FP32
-    const double tz = s[2] * a.inv_dz2;
+    // z2 cell and fraction in FP64, fraction and weights in FP32
+    const double tz = zs * a.inv_dz2;
     const double fz = floor(tz);
-    const float zw2 = (float)(tz - fz);
+    const float zw2 = d2f_rn(tz - fz);
     bool ok = true;
     int pz0 = 0, pz1 = 0;
     if (a.periodic) {
-      if (!(fabs(fz) < 9.0e15)) {
+      if (!(fabs(fz) < 2.0e9)) {
         ok = false;
         atomicOr(a.status, ST_OUT_OF_Z2);
       } else {
-        int64_t m = (int64_t)fz % a.npl;
-        if (m < 0) m += a.npl;
-        pz0 = (int)m;
-        pz1 = (m + 1 == a.npl) ? 0 : (int)m + 1;
+        int m = (int)((long long)fz % a.npl);
+        if (m < 0) m += (int)a.npl;
+        pz0 = m;
+        pz1 = (m + 1 == a.npl) ? 0 : m + 1;
       }
     } else {
       if (!(fz >= 0.0 && fz + 1.0 < (double)a.nz2)) {
@@ -218,16 +296,17 @@ __global__ void __launch_bounds__(MX_THREADS) k_stage_mixed(const MixArgs a) {
     float x2 = 0.f, y2 = 0.f;
     int64_t b0 = 0;
     if (!ONED) {
-      const double tx = (s[0] + a.halfx) * a.inv_dx;
-      const double fx = floor(tx);
-      const double ty = (s[1] + a.halfy) * a.inv_dy;
-      const double fy = floor(ty);
-      if (!(fx >= 0.0 && fx + 1.0 < (double)a.nix && fy >= 0.0 && fy + 1.0 < (double)a.niy)) {
+      // (x + halfx) / dx in one rounding
+      const float tx = fmaf(X, a.inv_dx_f, a.hx_dx);
+      const float fx = floorf(tx);
+      const float ty = fmaf(Y, a.inv_dy_f, a.hy_dy);
+      const float fy = floorf(ty);
+      if (!(fx >= 0.f && fx + 1.f < (float)a.nix && fy >= 0.f && fy + 1.f < (float)a.niy)) {
         ok = false;
         atomicOr(a.status, ST_OUT_OF_WINDOW);
       } else {
-        x2 = (float)(tx - fx);
-        y2 = (float)(ty - fy);
+        x2 = tx - fx;
+        y2 = ty - fy;
         b0 = (int64_t)fx + (int64_t)fy * a.nix;
       }
     }
@@ -251,17 +330,36 @@ __global__ void __launch_bounds__(MX_THREADS) k_stage_mixed(const MixArgs a) {
              zw2 * (w0 * c4.y + w1 * c5.y + w2 * c6.y + w3 * c7.y);
       }
       if (a.field_evolve) {
-        const float dw = (float)a.chi[i] * a.inv_dV3 * qrG;
-        sr[q] = dw * PX;
-        si[q] = dw * PY;
-        wx[q] = x2;
-        wy[q] = y2;
-        wz[q] = zw2;
-        base0[q] = b0;
-        pz0v[q] = pz0;
-        pz1v[q] = pz1;
-        dep[q] = true;
-        my_pzlo = min(my_pzlo, pz0);
+        // deposit (chi/dV3) (1 + eta p2)/Gamma p w_c to the 8 (2 on 1D) nodes
+        const float dw = d2f_rn(a.chi[i]) * a.inv_dV3 * qrG;
+        const float sr = dw * PX, si = dw * PY;
+        const int nc = ONED ? 2 : 8;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          if (c >= nc) break;
+          float w;
+          int64_t node;
+          int plane;
+          if (ONED) {
+            plane = (c == 0) ? pz0 : pz1;
+            w = (c == 0) ? zw1 : zw2;
+            node = 0;
+          } else {
+            const int cx = c & 1, cy = (c >> 1) & 1, cz = c >> 2;
+            w = (cx ? x2 : x1) * (cy ? y2 : y1) * (cz ? zw2 : zw1);
+            plane = cz ? pz1 : pz0;
+            node = b0 + cx + (int64_t)cy * a.nix;
+          }
+          const float vr = w * sr, vi = w * si;
+          const int tp = plane - pzlo;
+          if (a.tile && tp >= 0 && tp < MX_TILE_PLANES) {
+            const int ti = tp * ntr + (int)node;
+            tile_add(&tsum[ti].x, &tcomp[ti].x, vr);
+            tile_add(&tsum[ti].y, &tcomp[ti].y, vi);
+          } else {
+            global_add(a.acc + (int64_t)plane * ntr + node, make_float2(vr, vi));
+          }
+        }
       }
     }
     if (!a.coupling) {
@@ -269,77 +367,50 @@ __global__ void __launch_bounds__(MX_THREADS) k_stage_mixed(const MixArgs a) {
       fi = 0.f;
     }
 
-    double k[6];
+    float k[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    double kz = 0.0;
     if (a.electrons_evolve) {
       float bx, by, bz;
       bfield_f(a.bf, X, Y, bx, by, bz);
-      const float ep = (float)p2 * a.eta_k2;
+      const float ep = p2f * a.eta_k2;
       const float cz = a.kn2col * qrG * bz;
-      k[2] = p2;
-      k[0] = (double)(a.dxc * qrG * PX);
-      k[1] = (double)(-(a.dxc * qrG * PY));
-      k[3] = (double)(a.sInv2rho * (a.n2col * by - ep * fr) + cz * PY);
-      k[4] = (double)(a.sInv2rho * (a.n2col * bx - ep * fi) - cz * PX);
-      k[5] = (double)(-(a.rho2 * qrG * (PX * fr + PY * fi)));
-    } else {
-#pragma unroll
-      for (int j = 0; j < 6; ++j) k[j] = 0.0;
+      kz = p2;
+      k[0] = a.dxc * qrG * PX;
+      k[1] = -(a.dxc * qrG * PY);
+      k[3] = a.sInv2rho * (a.n2col * by - ep * fr) + cz * PY;
+      k[4] = a.sInv2rho * (a.n2col * bx - ep * fi) - cz * PX;
+      k[5] = -(a.rho2 * qrG * (PX * fr + PY * fi));
     }
+    constexpr int kF[5] = {0, 1, 3, 4, 5};
+    if (STAGE == 1) {
 #pragma unroll
-    for (int j = 0; j < 6; ++j) {
-      if (STAGE == 1) {
-        a.kout[j][i] = k[j];
-      } else if (STAGE == 2) {
-        a.kacc[j][i] = k[j];
-      } else if (STAGE == 3) {
-        a.kout[j][i] = k[j];
-        a.kacc[j][i] = kin[j] + k[j];
-      } else {
-        a.ynext[j][i] = y0[j] + a.h6 * (a.k1[j][i] + k[j] + 2.0 * a.kacc[j][i]);
+      for (int t = 0; t < 5; ++t) a.kout_f[kF[t]][i] = k[kF[t]];
+      a.kout_z[i] = kz;
+    } else if (STAGE == 2) {
+#pragma unroll
+      for (int t = 0; t < 5; ++t) a.kacc_f[kF[t]][i] = k[kF[t]];
+      a.kacc_z[i] = kz;
+    } else if (STAGE == 3) {
+#pragma unroll
+      for (int t = 0; t < 5; ++t) {
+        a.kout_f[kF[t]][i] = k[kF[t]];
+        a.kacc_f[kF[t]][i] = kin[kF[t]] + k[kF[t]];
       }
+      a.kout_z[i] = kz;
+      a.kacc_z[i] = kz_in + kz;
+    } else {
+      // y + h/6 (k1 + k4 + 2 (k2 + k3)): the slope sum in FP32, the update in FP64
+      const double y0[6] = {x0, yv0, z0, px0, py0, g0};
+#pragma unroll
+      for (int t = 0; t < 5; ++t) {
+        const int j = kF[t];
+        const float sum = a.k1_f[j][i] + k[j] + 2.f * a.kacc_f[j][i];
+        a.ynext[j][i] = fma(a.h6, f2d(sum), y0[j]);
+      }
+      a.ynext[2][i] = fma(a.h6, a.k1_z[i] + kz + 2.0 * a.kacc_z[i], z0);
     }
   }
 
-  // deposit
-  if (a.tile) {
-    for (int o = 16; o > 0; o >>= 1) my_pzlo = min(my_pzlo, __shfl_xor_sync(0xffffffffu, my_pzlo, o));
-    if ((threadIdx.x & 31) == 0 && my_pzlo != INT_MAX) atomicMin(&s_pzlo, my_pzlo);
-    __syncthreads();
-  }
-  const int pzlo = a.tile ? s_pzlo : 0;
-#pragma unroll
-  for (int q = 0; q < MX_PPT; ++q) {
-    if (!dep[q]) continue;
-    const float z2w = wz[q], z1w = 1.f - z2w;
-    const float x2 = wx[q], x1 = 1.f - x2, y2 = wy[q], y1 = 1.f - y2;
-    const int nc = ONED ? 2 : 8;
-#pragma unroll
-    for (int c = 0; c < 8; ++c) {
-      if (c >= nc) break;
-      float w;
-      int64_t node;
-      int plane;
-      if (ONED) {
-        plane = (c == 0) ? pz0v[q] : pz1v[q];
-        w = (c == 0) ? z1w : z2w;
-        node = 0;
-      } else {
-        const int cx = c & 1, cy = (c >> 1) & 1, cz = c >> 2;
-        w = (cx ? x2 : x1) * (cy ? y2 : y1) * (cz ? z2w : z1w);
-        plane = cz ? pz1v[q] : pz0v[q];
-        node = base0[q] + cx + (int64_t)cy * a.nix;
-      }
-      const float vr = w * sr[q], vi = w * si[q];
-      const int tp = plane - pzlo;
-      if (a.tile && tp >= 0 && tp < MX_TILE_PLANES) {
-        const int ti = tp * ntr + (int)node;
-        tile_add(&tsum[ti].x, &tcomp[ti].x, vr);
-        tile_add(&tsum[ti].y, &tcomp[ti].y, vi);
-      } else {
-        global_add(a.acc + (int64_t)plane * ntr + node, make_float2(vr, vi));
-      }
-    }
-  }
   if (a.tile) {
     __syncthreads();
     if (pzlo != INT_MAX) {
@@ -440,6 +511,11 @@ int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_ou
   a.inv_dx = 1.0 / p.dx;
   a.inv_dy = 1.0 / p.dy;
   a.inv_dz2 = 1.0 / p.dz2;
+  a.inv_dx_f = (float)(1.0 / p.dx);
+  a.inv_dy_f = (float)(1.0 / p.dy);
+  a.hx_dx = (float)(a.halfx / p.dx);
+  a.hy_dy = (float)(a.halfy / p.dy);
+  a.eta_f = (float)p.eta;
   a.inv_g02 = 1.0 / (p.gamma_r * p.gamma_r);
   a.aw2 = p.aw * p.aw;
   a.inv_eta = 1.0 / p.eta;
@@ -494,14 +570,24 @@ int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_ou
     a.n2col = (float)n2col;
     a.kn2col = (float)(p.kappa * n2col);
     a.cstate = stage_c[s - 1];
+    a.cstate_f = (float)stage_c[s - 1];
     a.as = (const float2 *)((s == 1) ? h->w32 : h->as32);
+    // the slope arrays are FP64-sized; in this mode they hold FP32 values,
+    // except the z2 slope
+    double *const *kin = (s == 2) ? h->k1 : (s == 3) ? h->ka : (s == 4) ? h->kb : nullptr;
+    double *const *kout = (s == 1) ? h->k1 : (s == 3) ? h->kb : nullptr;
+    double *const *kacc = (s >= 2) ? h->ka : nullptr;
     for (int j = 0; j < 6; ++j) {
-      a.kin[j] = (s == 2) ? h->k1[j] : (s == 3) ? h->ka[j] : (s == 4) ? h->kb[j] : nullptr;
-      a.kout[j] = (s == 1) ? h->k1[j] : (s == 3) ? h->kb[j] : nullptr;
-      a.kacc[j] = (s >= 2) ? h->ka[j] : nullptr;
-      a.k1[j] = h->k1[j];
+      a.kin_f[j] = kin ? (const float *)kin[j] : nullptr;
+      a.kout_f[j] = kout ? (float *)kout[j] : nullptr;
+      a.kacc_f[j] = kacc ? (float *)kacc[j] : nullptr;
+      a.k1_f[j] = (const float *)h->k1[j];
       a.ynext[j] = h->y[nxt][j];
     }
+    a.kin_z = kin ? kin[2] : nullptr;
+    a.kout_z = kout ? kout[2] : nullptr;
+    a.kacc_z = kacc ? kacc[2] : nullptr;
+    a.k1_z = h->k1[2];
     if (h->np > 0) {
       pf_prof_begin(h, PROF_STAGE);
 #define PF_MIX_CASE(S)                                                                 \

@@ -200,6 +200,28 @@ def test_diffraction_matches_oracle(mesh):
     field_close(gf, (re, im), 1e-12)
 
 
+@pytest.mark.parametrize("precision", [P.FP64, P.MIXED])
+@pytest.mark.parametrize("shape", [(17, 21, 2048), (129, 129, 8), (129, 17, 1536), (17, 33, 600)])
+def test_diffraction_kernel_shapes(shape, precision):
+    """Meshes that select each diffraction kernel form: the transverse-plane
+    pass (plane in shared memory), the nine line passes with the radix-43
+    butterfly, and the long z2 lines with several adjacent lines per block.
+    FP64 to 1e-12 of the field scale, the mixed (FP32) transform to 2e-5."""
+    nx, ny, nz2 = shape
+    rho = 0.005
+    lamr = 4.0 * configs.PUFFIN_PI * rho
+    p = P.default_params(rho=rho, eta=1e-5, kappa=0.2, nx=nx, ny=ny, nz2=nz2, dx=0.3, dy=0.25,
+                         dz2=lamr / 16, mesh_type=P.MESH_TEMPORAL, precision=precision)
+    field = random_field(p, 11, amp=1.0)
+    with P.Puffin(p) as sim:
+        sim.set_field(*field)
+        sim.diffractIM(0.29)
+        gf = sim.get_field()
+    re, im = (a.copy() for a in field)
+    O.diffract(oracle_config(p), re, im, 0.29)
+    field_close(gf, (re, im), 1e-12 if precision == P.FP64 else 2e-5)
+
+
 def test_run_with_diffraction_matches_oracle():
     """pf_run (UndSection's loop) against oracle.undulator_run: 32 steps with
     diffraction every 16 steps and merged half steps."""
@@ -235,6 +257,25 @@ def test_deposit_is_bit_reproducible():
         np.testing.assert_array_equal(outs[0][0][k], outs[1][0][k])
     np.testing.assert_array_equal(outs[0][1][0], outs[1][1][0])
     np.testing.assert_array_equal(outs[0][1][1], outs[1][1][1])
+
+
+def test_dense_beam_tiled_deposit():
+    """2^18 macroparticles on the config-1 mesh (about ten per window cell)
+    select the shared-memory deposit tile: one RK4 step against the oracle
+    (rtol 1e-12) and bit-identical repeats."""
+    w = configs.config1(np_=2 ** 18, seed=9, nsteps=2)
+    field = random_field(w.params, 5)
+    outs = []
+    for _ in range(2):
+        got, gf, (nix, niy), _ = run_gpu_steps(w.params, w.beam, field, w.h, 1)
+        outs.append((got, gf))
+    assert w.np >= 8 * (w.params.nz2 - 1) * nix * niy      # the dense mode is selected
+    for k in ("x", "y", "z2", "px", "py", "gam"):
+        np.testing.assert_array_equal(outs[0][0][k], outs[1][0][k])
+    np.testing.assert_array_equal(outs[0][1][0], outs[1][1][0])
+    b, of, _ = run_oracle_steps(w.params, w.beam, field, w.h, 1, nix, niy)
+    assert_beam_close(outs[0][0], b, rtol=1e-12, atol=1e-15)
+    field_close(outs[0][1], of, 1e-12)
 
 
 def test_out_of_window_leaves_state_and_recovers():
