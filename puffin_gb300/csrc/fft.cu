@@ -35,14 +35,18 @@
 
 #define FFT_T double
 #define FFT_NS fft64
+#define FFT_REAL_IS_FLOAT 0
 #include "fft_kernels.cuh"
 #undef FFT_T
 #undef FFT_NS
+#undef FFT_REAL_IS_FLOAT
 #define FFT_T float
 #define FFT_NS fft32
+#define FFT_REAL_IS_FLOAT 1
 #include "fft_kernels.cuh"
 #undef FFT_T
 #undef FFT_NS
+#undef FFT_REAL_IS_FLOAT
 
 struct DiffPlan {
   fft64::Plan *p64 = nullptr;

@@ -156,6 +156,37 @@ __device__ __forceinline__ void dft_store(cplx *v, cplx *dst, int ds) {
   }
 }
 
+// DFT of v[0..R) in place, outputs in natural order (R = 2, 4, 8).
+template <int R, bool INV>
+__device__ __forceinline__ void dft_regs(cplx *v) {
+  if constexpr (R == 2) {
+    const cplx a = v[0], b = v[1];
+    v[0] = cadd(a, b);
+    v[1] = csub(a, b);
+  } else if constexpr (R == 4) {
+    dft4<INV>(v[0], v[1], v[2], v[3]);
+  } else if constexpr (R == 8) {
+    cplx e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
+    cplx o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
+    dft4<INV>(e0, e1, e2, e3);
+    dft4<INV>(o0, o1, o2, o3);
+    const real s = (real)0.70710678118654752440;
+    const cplx t1 = INV ? cplx{s * (o1.r - o1.i), s * (o1.r + o1.i)}
+                        : cplx{s * (o1.r + o1.i), s * (o1.i - o1.r)};
+    const cplx t2 = mul_mi<INV>(o2);
+    const cplx t3 = INV ? cplx{-s * (o3.r + o3.i), s * (o3.r - o3.i)}
+                        : cplx{s * (o3.i - o3.r), -s * (o3.r + o3.i)};
+    v[0] = cadd(e0, o0);
+    v[4] = csub(e0, o0);
+    v[1] = cadd(e1, t1);
+    v[5] = csub(e1, t1);
+    v[2] = cadd(e2, t2);
+    v[6] = csub(e2, t2);
+    v[3] = cadd(e3, t3);
+    v[7] = csub(e3, t3);
+  }
+}
+
 // Threads that share one odd-prime butterfly (each computes a subset of the
 // output pairs), so a pass over few long butterflies still fills the block.
 __host__ __device__ constexpr int odd_groups(int R) {
@@ -509,24 +540,56 @@ __global__ void k_elementwise(const FftArgs a) {
   store(a, t, v);
 }
 
-// ---- in-place passes on one shared-memory buffer ----------------------------
+// ---- in-place kernels specialised per transform length ------------------------
 // The transverse-plane kernel (a whole nx*ny plane per block: the x and y
-// transforms of one pass over HBM) and the long-line kernel (a few adjacent
-// z2 lines per block, so that every 32-byte sector of the strided z2 axis is
-// used in full) hold their data in a single shared buffer.  A pass stages
-// the inputs of each thread's butterflies in registers, the block syncs, and
-// the outputs overwrite the inputs.  Element j of line l sits at
-// buf[l * ls + j * es].
+// transforms of one pass over HBM) and the long-line kernel (G adjacent z2
+// lines per block, so that every 32-byte sector of the strided z2 axis is
+// used in full) hold their data in a single shared buffer.  A pass stages the
+// inputs of each thread's butterflies in registers, the block syncs, and the
+// outputs overwrite the inputs.  Lengths, radices and line counts are
+// template constants, so each pass is straight-line code with constant index
+// arithmetic; the host picks an instantiation for the mesh, and meshes
+// without one use the two-buffer line kernel above.  Element j of line l sits
+// at buf[l * ls + j * es].
 constexpr int PT = 512;  // threads of the in-place kernels
-__host__ __device__ constexpr int ip_cap() { return sizeof(real) == 4 ? 16896 : 8448; }
-__host__ __device__ constexpr int ip_maxb(int R) { return (ip_cap() + R * PT - 1) / (R * PT); }
 
-template <int R, bool INV>
-__device__ __noinline__ void ip_pass(cplx *buf, int n, int nl, int ls, int es, int Ns,
-                                     const cplx *tw) {
-  constexpr int MAXB = ip_maxb(R);
-  const int nb = n / R;
-  const int total = nl * nb;
+// the host's factorisation (factorize below): eights, fours, twos, odd primes
+__host__ __device__ constexpr int fac_count(int n) {
+  int c = 0;
+  while (n % 8 == 0) { n /= 8; ++c; }
+  while (n % 4 == 0) { n /= 4; ++c; }
+  while (n % 2 == 0) { n /= 2; ++c; }
+  for (int p = 3; n > 1; p += 2)
+    while (n % p == 0) { n /= p; ++c; }
+  return c;
+}
+__host__ __device__ constexpr int fac_radix(int n, int k) {
+  int c = 0;
+  while (n % 8 == 0) { if (c++ == k) return 8; n /= 8; }
+  while (n % 4 == 0) { if (c++ == k) return 4; n /= 4; }
+  while (n % 2 == 0) { if (c++ == k) return 2; n /= 2; }
+  for (int p = 3; n > 1; p += 2)
+    while (n % p == 0) { if (c++ == k) return p; n /= p; }
+  return 1;
+}
+__host__ __device__ constexpr int fac_ns(int n, int k) {
+  int ns = 1;
+  for (int q = 0; q < k; ++q) ns *= fac_radix(n, q);
+  return ns;
+}
+
+// Shared-memory slot of logical element i: the XOR swizzle spreads the
+// strided accesses of the Stockham passes (stride R*NS elements) over all
+// banks; every access to the in-place buffer goes through it.
+__device__ __forceinline__ int sw(int i) {
+  return (sizeof(real) == 4) ? (i ^ ((i >> 4) & 15)) : (i ^ ((i >> 3) & 7));
+}
+
+template <int N, int NL, int R, int NS, bool INV>
+__device__ __forceinline__ void ip_pass(cplx *buf, int nl, int ls, int es, const cplx *tw) {
+  constexpr int NB = N / R;
+  constexpr int MAXB = (NL * NB + PT - 1) / PT;
+  const int total = nl * NB;
   int obase[MAXB];
   if constexpr (R == 2 || R == 4 || R == 8) {
     cplx v[MAXB][R];
@@ -535,22 +598,26 @@ __device__ __noinline__ void ip_pass(cplx *buf, int n, int nl, int ls, int es, i
       const int t = threadIdx.x + b * PT;
       obase[b] = -1;
       if (t < total) {
-        const int l = t / nb, j = t - l * nb;
-        const int k = j % Ns;
-        const cplx *src = buf + l * ls + j * es;
+        const int l = t / NB, j = t - l * NB;
+        const int k = j % NS;
+        const int src = l * ls + j * es;
 #pragma unroll
-        for (int r = 0; r < R; ++r) v[b][r] = src[r * nb * es];
-        if (Ns > 1) {
+        for (int r = 0; r < R; ++r) v[b][r] = buf[sw(src + r * NB * es)];
+        if constexpr (NS > 1) {
 #pragma unroll
           for (int r = 1; r < R; ++r) v[b][r] = cmul(v[b][r], tw[k * R + r]);
         }
-        obase[b] = l * ls + ((j / Ns) * Ns * R + k) * es;
+        obase[b] = l * ls + ((j / NS) * NS * R + k) * es;
       }
     }
     __syncthreads();
 #pragma unroll
-    for (int b = 0; b < MAXB; ++b)
-      if (obase[b] >= 0) dft_store<R, INV>(v[b], buf + obase[b], Ns * es);
+    for (int b = 0; b < MAXB; ++b) {
+      if (obase[b] < 0) continue;
+      dft_regs<R, INV>(v[b]);
+#pragma unroll
+      for (int r = 0; r < R; ++r) buf[sw(obase[b] + r * NS * es)] = v[b][r];
+    }
     __syncthreads();
   } else {
     constexpr int H = (R - 1) / 2;
@@ -562,44 +629,41 @@ __device__ __noinline__ void ip_pass(cplx *buf, int n, int nl, int ls, int es, i
       const int t = threadIdx.x + b * PT;
       obase[b] = -1;
       if (t < total) {
-        const int l = t / nb, j = t - l * nb;
-        const int k = j % Ns;
-        const cplx *src = buf + l * ls + j * es;
-        const cplx *twk = tw + k * R;
-        x0[b] = src[0];
+        const int l = t / NB, j = t - l * NB;
+        const int k = j % NS;
+        const int src = l * ls + j * es;
+        x0[b] = buf[sw(src)];
 #pragma unroll
         for (int q = 1; q <= H; ++q) {
-          cplx u = src[q * nb * es], w = src[(R - q) * nb * es];
-          if (Ns > 1) {
-            u = cmul(u, twk[q]);
-            w = cmul(w, twk[R - q]);
+          cplx u = buf[sw(src + q * NB * es)], w = buf[sw(src + (R - q) * NB * es)];
+          if constexpr (NS > 1) {
+            u = cmul(u, tw[k * R + q]);
+            w = cmul(w, tw[k * R + R - q]);
           }
           av[b][q - 1] = cadd(u, w);
           bv[b][q - 1] = csub(u, w);
         }
-        obase[b] = l * ls + ((j / Ns) * Ns * R + k) * es;
+        obase[b] = l * ls + ((j / NS) * NS * R + k) * es;
       }
     }
     __syncthreads();
-    const int ds = Ns * es;
+    const int ds = NS * es;
 #pragma unroll
     for (int b = 0; b < MAXB; ++b) {
       if (obase[b] < 0) continue;
-      cplx *dst = buf + obase[b];
+      const int o = obase[b];
       cplx s0 = x0[b];
 #pragma unroll
       for (int q = 0; q < H; ++q) s0 = cadd(s0, av[b][q]);
-      dst[0] = s0;
-      // every thread runs the same (q, j) sequence, so the root index is
-      // uniform across the warp and the constant bank broadcasts it
-#pragma unroll 1
+      buf[sw(o)] = s0;
+      // every thread runs the same (q, j) sequence: the root is an immediate
+      // constant-bank operand
+#pragma unroll
       for (int q = 1; q <= H; ++q) {
         cplx C = x0[b], S{(real)0, (real)0};
-        int m = 0;
 #pragma unroll
         for (int j = 1; j <= H; ++j) {
-          m += q;
-          if (m >= R) m -= R;
+          const int m = (j * q) % R;
           const real c = c_roots[OFF + m].r;
           const real sn = c_roots[OFF + m].i;
           C.r = fma(av[b][j - 1].r, c, C.r);
@@ -608,11 +672,11 @@ __device__ __noinline__ void ip_pass(cplx *buf, int n, int nl, int ls, int es, i
           S.i = fma(bv[b][j - 1].i, sn, S.i);
         }
         if (!INV) {
-          dst[q * ds] = cplx{C.r + S.i, C.i - S.r};
-          dst[(R - q) * ds] = cplx{C.r - S.i, C.i + S.r};
+          buf[sw(o + q * ds)] = cplx{C.r + S.i, C.i - S.r};
+          buf[sw(o + (R - q) * ds)] = cplx{C.r - S.i, C.i + S.r};
         } else {
-          dst[q * ds] = cplx{C.r - S.i, C.i + S.r};
-          dst[(R - q) * ds] = cplx{C.r + S.i, C.i - S.r};
+          buf[sw(o + q * ds)] = cplx{C.r - S.i, C.i + S.r};
+          buf[sw(o + (R - q) * ds)] = cplx{C.r + S.i, C.i - S.r};
         }
       }
     }
@@ -620,113 +684,111 @@ __device__ __noinline__ void ip_pass(cplx *buf, int n, int nl, int ls, int es, i
   }
 }
 
-// whether an axis of nl lines can run in place in one block
-__host__ __device__ inline bool ip_fits(const AxisPlan &p, int nl) {
-  for (int ps = 0; ps < p.npass; ++ps) {
-    const int R = p.radix[ps];
-    if ((int64_t)nl * (p.n / R) > (int64_t)PT * ip_maxb(R)) return false;
-    if (sizeof(real) == 8 && R > 17) return false;  // register budget of an FP64 butterfly
-  }
-  return true;
-}
-
-template <bool INV>
-__device__ __forceinline__ void ip_transform(cplx *buf, const AxisPlan &p, int nl, int ls, int es,
-                                             const cplx *tw) {
-  for (int ps = 0; ps < p.npass; ++ps) {
-    const int R = p.radix[ps], Ns = p.ns[ps];
-    const cplx *twp = tw + p.twoff[ps];
-    switch (R) {
-      case 2: ip_pass<2, INV>(buf, p.n, nl, ls, es, Ns, twp); break;
-      case 4: ip_pass<4, INV>(buf, p.n, nl, ls, es, Ns, twp); break;
-      case 8: ip_pass<8, INV>(buf, p.n, nl, ls, es, Ns, twp); break;
-      case 3: ip_pass<3, INV>(buf, p.n, nl, ls, es, Ns, twp); break;
-      case 5: ip_pass<5, INV>(buf, p.n, nl, ls, es, Ns, twp); break;
-      case 7: ip_pass<7, INV>(buf, p.n, nl, ls, es, Ns, twp); break;
-      case 11: ip_pass<11, INV>(buf, p.n, nl, ls, es, Ns, twp); break;
-      case 13: ip_pass<13, INV>(buf, p.n, nl, ls, es, Ns, twp); break;
-      case 17: ip_pass<17, INV>(buf, p.n, nl, ls, es, Ns, twp); break;
-      case 43:
-        if constexpr (sizeof(real) == 4) ip_pass<43, INV>(buf, p.n, nl, ls, es, Ns, twp);
-        break;
-      default: break;  // excluded when the plan is built
-    }
+// all passes of a length-N transform over (at most) NL lines
+template <int N, int NL, bool INV, int K = 0>
+__device__ __forceinline__ void ip_transform(cplx *buf, int nl, int ls, int es, const cplx *tw,
+                                             const AxisPlan &p) {
+  if constexpr (K < fac_count(N)) {
+    ip_pass<N, NL, fac_radix(N, K), fac_ns(N, K), INV>(buf, nl, ls, es, tw + p.twoff[K]);
+    ip_transform<N, NL, INV, K + 1>(buf, nl, ls, es, tw, p);
   }
 }
 
-// the 2D transverse transform of the plane in buf (x fastest, pitch nx)
-__device__ __forceinline__ void xy_transform(cplx *buf, const FftArgs &a, int inv) {
-  const int nx = a.T.nx, ny = a.T.ny;
+template <int NX, int NY>
+__device__ __forceinline__ void xy_transform(cplx *buf, const FftArgs &a, bool inv) {
   if (!inv) {
-    if (nx > 1) ip_transform<false>(buf, a.ax, ny, nx, 1, a.tw_f);
-    if (ny > 1) ip_transform<false>(buf, a.ay, nx, 1, nx, a.tw_f);
+    ip_transform<NX, NY, false>(buf, NY, NX, 1, a.tw_f, a.ax);
+    ip_transform<NY, NX, false>(buf, NX, 1, NX, a.tw_f, a.ay);
   } else {
-    if (ny > 1) ip_transform<true>(buf, a.ay, nx, 1, nx, a.tw_b);
-    if (nx > 1) ip_transform<true>(buf, a.ax, ny, nx, 1, a.tw_b);
+    ip_transform<NY, NX, true>(buf, NX, 1, NX, a.tw_b, a.ay);
+    ip_transform<NX, NY, true>(buf, NY, NX, 1, a.tw_b, a.ax);
   }
 }
 
 // One block per z2 plane: x and y transforms (and the mid operation and the
 // opposite transforms) with a single read and write of the plane.
+template <int NX, int NY>
 __global__ void __launch_bounds__(PT, 1) k_fft_plane(const FftArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx *buf = reinterpret_cast<cplx *>(smem_raw);
-  const int nx = a.T.nx;
-  const int64_t plane = (int64_t)nx * a.T.ny;
+  constexpr int plane = NX * NY;
   const int z = blockIdx.x;
   const int64_t off = (int64_t)z * plane;
-  for (int64_t t = threadIdx.x; t < plane; t += PT) load_async(buf + t, a, off + t);
+  for (int t = threadIdx.x; t < plane; t += PT) load_async(buf + sw(t), a, off + t);
   cp_async_wait_all();
   __syncthreads();
-  xy_transform(buf, a, a.dir);
+  xy_transform<NX, NY>(buf, a, a.dir != 0);
   if (a.mid != MID_NONE) {
-    for (int64_t t = threadIdx.x; t < plane; t += PT)
-      buf[t] = mid_op(a, off + t, (int)(t % nx), (int)(t / nx), z, buf[t]);
+    for (int t = threadIdx.x; t < plane; t += PT)
+      buf[sw(t)] = mid_op(a, off + t, t % NX, t / NX, z, buf[sw(t)]);
     __syncthreads();
-    if (a.second) xy_transform(buf, a, !a.dir);
+    if (a.second) xy_transform<NX, NY>(buf, a, a.dir == 0);
   }
-  for (int64_t t = threadIdx.x; t < plane; t += PT) store(a, off + t, buf[t]);
+  for (int t = threadIdx.x; t < plane; t += PT) store(a, off + t, buf[sw(t)]);
 }
 
-// Long lines (the z2 axis): lpb adjacent lines per block, lines padded by one
-// element in shared memory; consecutive threads load consecutive lines, which
-// are adjacent in HBM.
+// Long lines (the z2 axis): G adjacent lines per block, lines padded by one
+// element in shared memory; consecutive threads load consecutive lines,
+// which are adjacent in HBM.
+template <int N, int G>
 __global__ void __launch_bounds__(PT, 1) k_fft_long(const FftArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx *buf = reinterpret_cast<cplx *>(smem_raw);
   const AxisPlan &p = a.ax;
-  const int n = p.n, ls = n + 1;
-  const int64_t L0 = (int64_t)blockIdx.x * p.lpb;
-  const int nl = (int)min((int64_t)p.lpb, p.nlines - L0);
-  for (int t = threadIdx.x; t < nl * n; t += PT) {
+  constexpr int ls = N + 1;
+  const int64_t L0 = (int64_t)blockIdx.x * G;
+  const int nl = (int)min((int64_t)G, p.nlines - L0);
+  for (int t = threadIdx.x; t < nl * N; t += PT) {
     const int l = t % nl, j = t / nl;
-    const int64_t pos = line_base(p, L0 + l) + (int64_t)j * p.stride;
-    load_async(buf + l * ls + j, a, pos);
+    load_async(buf + sw(l * ls + j), a, line_base(p, L0 + l) + (int64_t)j * p.stride);
   }
   cp_async_wait_all();
   __syncthreads();
-  if (a.dir) ip_transform<true>(buf, p, nl, ls, 1, a.tw_b);
-  else ip_transform<false>(buf, p, nl, ls, 1, a.tw_f);
+  if (a.dir) ip_transform<N, G, true>(buf, nl, ls, 1, a.tw_b, p);
+  else ip_transform<N, G, false>(buf, nl, ls, 1, a.tw_f, p);
   if (a.mid != MID_NONE) {
-    for (int t = threadIdx.x; t < nl * n; t += PT) {
-      const int l = t / n, j = t - l * n;
+    for (int t = threadIdx.x; t < nl * N; t += PT) {
+      const int l = t / N, j = t - l * N;
       int x, y, z;
       coords(p, a.T, L0 + l, j, x, y, z);
       const int64_t pos = line_base(p, L0 + l) + (int64_t)j * p.stride;
-      buf[l * ls + j] = mid_op(a, pos, x, y, z, buf[l * ls + j]);
+      buf[sw(l * ls + j)] = mid_op(a, pos, x, y, z, buf[sw(l * ls + j)]);
     }
     __syncthreads();
     if (a.second) {
-      if (!a.dir) ip_transform<true>(buf, p, nl, ls, 1, a.tw_b);
-      else ip_transform<false>(buf, p, nl, ls, 1, a.tw_f);
+      if (!a.dir) ip_transform<N, G, true>(buf, nl, ls, 1, a.tw_b, p);
+      else ip_transform<N, G, false>(buf, nl, ls, 1, a.tw_f, p);
     }
   }
-  for (int t = threadIdx.x; t < nl * n; t += PT) {
+  for (int t = threadIdx.x; t < nl * N; t += PT) {
     const int l = t % nl, j = t / nl;
-    const int64_t pos = line_base(p, L0 + l) + (int64_t)j * p.stride;
-    store(a, pos, buf[l * ls + j]);
+    store(a, line_base(p, L0 + l) + (int64_t)j * p.stride, buf[sw(l * ls + j)]);
   }
 }
+
+// Instantiated transverse planes (square meshes of the workloads) and long
+// z2 lines; a plane must fit the 227 KB of shared memory of one block.
+typedef void (*FftKernel)(const FftArgs);
+struct PlaneKernel {
+  int nx, ny;
+  FftKernel fn;
+};
+struct LongKernel {
+  int n, g;
+  FftKernel fn;
+};
+
+static const PlaneKernel kPlaneKernels[] = {
+    {17, 17, k_fft_plane<17, 17>}, {21, 21, k_fft_plane<21, 21>}, {33, 33, k_fft_plane<33, 33>},
+    {65, 65, k_fft_plane<65, 65>},
+#if FFT_REAL_IS_FLOAT
+    {129, 129, k_fft_plane<129, 129>},
+#endif
+};
+static const LongKernel kLongKernels[] = {
+    {2048, (sizeof(real) == 4) ? 4 : 2, k_fft_long<2048, (sizeof(real) == 4) ? 4 : 2>},
+    {4096, (sizeof(real) == 4) ? 4 : 2, k_fft_long<4096, (sizeof(real) == 4) ? 4 : 2>},
+};
 
 // per-call tables: propagator and damping factors for step h
 __global__ void k_tables(cplx *px, cplx *py, real *dxt, real *dyt, const double *kx,
@@ -761,10 +823,10 @@ struct Plan {
   int64_t n = 0;
   AxisPlan ax[3];
   size_t smem[3] = {0, 0, 0};
-  bool plane = false;        // x and y in one k_fft_plane pass
+  FftKernel plane = nullptr;  // x and y in one k_fft_plane pass
   size_t plane_smem = 0;
-  bool zlong = false;        // z2 with k_fft_long
-  AxisPlan axl;              // the z2 plan of k_fft_long (its own lpb)
+  FftKernel zlong = nullptr;  // z2 with k_fft_long
+  AxisPlan axl;               // the z2 plan of k_fft_long (its own lines per block)
   size_t zlong_smem = 0;
   cplx *A = nullptr, *anb = nullptr;
   cplx *tw = nullptr;  // forward block then backward block
@@ -929,33 +991,26 @@ static int build_plan(pf_handle *h, Plan *&out) {
     d->smem[a] = bytes(lpb);
   }
   // transverse-plane kernel: the whole nx*ny plane in one shared buffer
-  {
-    const int64_t pts = (int64_t)d->nx * d->ny;
-    const size_t b = (size_t)pts * sizeof(cplx);
-    d->plane = (d->nx > 1 || d->ny > 1) && pts <= ip_cap() && b <= (size_t)max_smem &&
-               (d->nx == 1 || ip_fits(d->ax[0], d->ny)) && (d->ny == 1 || ip_fits(d->ax[1], d->nx));
-    d->plane_smem = b;
-  }
-  // long z2 lines: the line kernel reads fewer than 32 bytes of adjacent
-  // lines per row; give each block enough adjacent lines to fill a sector
-  {
-    const AxisPlan &az = d->ax[2];
-    const int want = (int)((32 + sizeof(cplx) - 1) / sizeof(cplx));
-    if (az.n > 1 && (int64_t)az.lpb * (int64_t)sizeof(cplx) < 32) {
-      int g = (int)std::min<int64_t>(want, az.nlines);
-      auto fits = [&](int gg) {
-        return (size_t)gg * (az.n + 1) * sizeof(cplx) <= (size_t)max_smem &&
-               (int64_t)gg * az.n <= ip_cap() && ip_fits(az, gg);
-      };
-      while (g > 1 && !fits(g)) --g;
-      if (g > az.lpb && fits(g)) {
-        d->zlong = true;
-        d->axl = az;
-        d->axl.lpb = g;
-        d->zlong_smem = (size_t)g * (az.n + 1) * sizeof(cplx);
-      }
+  for (const PlaneKernel &k : kPlaneKernels)
+    if (k.nx == d->nx && k.ny == d->ny) {
+      d->plane = k.fn;
+      // whole swizzle groups of 16 elements (sw() permutes within a group)
+      d->plane_smem = (((size_t)d->nx * d->ny + 15) / 16) * 16 * sizeof(cplx);
+      PF_CUDA(cudaFuncSetAttribute((const void *)k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   max_smem));
     }
-  }
+  if (d->plane_smem > (size_t)max_smem) d->plane = nullptr;
+  // long z2 lines: G adjacent lines per block fill whole 32-byte sectors
+  for (const LongKernel &k : kLongKernels)
+    if (k.n == d->nz && d->ax[2].lpb < k.g && d->ax[2].nlines >= k.g) {
+      d->zlong = k.fn;
+      d->axl = d->ax[2];
+      d->axl.lpb = k.g;
+      d->zlong_smem = (((size_t)k.g * (k.n + 1) + 15) / 16) * 16 * sizeof(cplx);
+      PF_CUDA(cudaFuncSetAttribute((const void *)k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   max_smem));
+    }
+  if (d->zlong_smem > (size_t)max_smem) d->zlong = nullptr;
   d->ntw = tab.size();
   if (d->ntw) {
     PF_CUDA(cudaMalloc(&d->tw, 2 * d->ntw * sizeof(cplx)));
@@ -964,8 +1019,6 @@ static int build_plan(pf_handle *h, Plan *&out) {
                        cudaMemcpyHostToDevice));
   }
   PF_CUDA(cudaFuncSetAttribute(k_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
-  PF_CUDA(cudaFuncSetAttribute(k_fft_plane, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
-  PF_CUDA(cudaFuncSetAttribute(k_fft_long, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
 
   PF_CUDA(cudaMalloc(&d->A, d->n * sizeof(cplx)));
   PF_CUDA(cudaMalloc(&d->anb, d->n * sizeof(cplx)));
@@ -1054,7 +1107,7 @@ static int fft_pass(pf_handle *h, Plan *d, FftArgs a, int axis) {
     a.ax = d->axl;
     const int64_t blocks = (a.ax.nlines + a.ax.lpb - 1) / a.ax.lpb;
     pf_prof_begin(h, PROF_FFT);
-    k_fft_long<<<(unsigned)blocks, PT, d->zlong_smem, h->stream>>>(a);
+    d->zlong<<<(unsigned)blocks, PT, d->zlong_smem, h->stream>>>(a);
     pf_prof_end(h);
     PF_LAUNCHED(h);
     return PF_OK;
@@ -1072,7 +1125,7 @@ static int plane_pass(pf_handle *h, Plan *d, FftArgs a) {
   a.ax = d->ax[0];
   a.ay = d->ax[1];
   pf_prof_begin(h, PROF_FFT);
-  k_fft_plane<<<(unsigned)d->nz, PT, d->plane_smem, h->stream>>>(a);
+  d->plane<<<(unsigned)d->nz, PT, d->plane_smem, h->stream>>>(a);
   pf_prof_end(h);
   PF_LAUNCHED(h);
   return PF_OK;

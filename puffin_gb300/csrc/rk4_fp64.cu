@@ -260,22 +260,19 @@ __device__ __forceinline__ void stage_particle(const StageArgs &a, const int64_t
       bool fits = true;
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
-        u64 lor, hir, loi, hii;
-        fits &= to_fix(w[c] * sr, a.fix_e, a.fix_maxexp, lor, hir);
-        fits &= to_fix(w[c] * si, a.fix_e, a.fix_maxexp, loi, hii);
-        int tp = -1, ti = 0;
+        int ti = -1;  // tile slot of the node, -1: outside the tile
         if constexpr (TILE) {
           const int64_t plane = (ONED ? c == 0 : c < 4) ? pz0 : pz1;
-          tp = (int)plane - t.pzlo;
-          ti = tp * t.ntr + (int)(node[c] - plane * t.ntr);
+          const int tp = (int)plane - t.pzlo;
+          if (tp >= 0 && tp < FT_PLANES) ti = tp * t.ntr + (int)(node[c] - plane * t.ntr);
         }
-        if (TILE && tp >= 0 && tp < FT_PLANES) {
-          fix_add(t.lo_r, t.hi_r, ti, lor, hir);
-          fix_add(t.lo_i, t.hi_i, ti, loi, hii);
-        } else {
-          fix_add(a.acc_lo_r, a.acc_hi_r, node[c], lor, hir);
-          fix_add(a.acc_lo_i, a.acc_hi_i, node[c], loi, hii);
-        }
+        u64 lo, hi;
+        fits &= to_fix(w[c] * sr, a.fix_e, a.fix_maxexp, lo, hi);
+        if (TILE && ti >= 0) fix_add(t.lo_r, t.hi_r, ti, lo, hi);
+        else fix_add(a.acc_lo_r, a.acc_hi_r, node[c], lo, hi);
+        fits &= to_fix(w[c] * si, a.fix_e, a.fix_maxexp, lo, hi);
+        if (TILE && ti >= 0) fix_add(t.lo_i, t.hi_i, ti, lo, hi);
+        else fix_add(a.acc_lo_i, a.acc_hi_i, node[c], lo, hi);
       }
       if (!fits) atomicOr(a.status, ST_OVERFLOW);
     }

@@ -66,7 +66,9 @@ struct MixArgs {
   double *ynext[6];
   int64_t np;
   double cstate, h6;
-  float cstate_f, eta_f, inv_dx_f, inv_dy_f, hx_dx, hy_dy;
+  float cstate_f, eta_f, inv_dx_f, inv_dy_f, hx_dx, hy_dy, inv_dz2_f;
+  double aw2g, g02;    // aw^2 / gamma0^2, 1 / gamma0^2
+  double ser[7];       // binomial coefficients of 1/sqrt(1-u) - 1, times 1/eta
   const float2 *as;  // stage field (window, interleaved complex)
   float2 *acc;       // deposit accumulator (window)
   int nix, niy;
@@ -172,28 +174,54 @@ __device__ __forceinline__ float d2f_rn(double d) {
   return __uint_as_float(sign | (mag + ((lo >> 28) & 1u)));  // a carry rounds into the exponent
 }
 
-// r - 1 = 1/sqrt(1 - u) - 1
-__device__ __forceinline__ double rsqrt1m_minus1(double u) {
+// p2 = (1/sqrt(1 - u) - 1) / eta from the binomial series with the 1/eta
+// folded into the coefficients c[k] = C(2k+2, k+1) / 4^(k+1) / eta:
+// three terms for u < 2e-6, five for u < 1e-4, seven for u < 1e-3 (the
+// truncation stays below 1e-17 of the result), the closed form above
+__device__ __forceinline__ double p2_series(double u, const double *c, double inv_eta) {
+  if (u < 2.0e-6) return u * fma(fma(c[2], u, c[1]), u, c[0]);
   if (u < 1.0e-4) {
-    double s = 63.0 / 256.0;
-    s = fma(s, u, 35.0 / 128.0);
-    s = fma(s, u, 5.0 / 16.0);
-    s = fma(s, u, 3.0 / 8.0);
-    s = fma(s, u, 0.5);
+    double s = c[4];
+    s = fma(s, u, c[3]);
+    s = fma(s, u, c[2]);
+    s = fma(s, u, c[1]);
+    s = fma(s, u, c[0]);
     return u * s;
   }
   if (u < 1.0e-3) {
-    // binomial coefficients C(2k,k)/4^k: 1/2, 3/8, 5/16, 35/128, 63/256, 231/1024, 429/2048
-    double s = 429.0 / 2048.0;
-    s = fma(s, u, 231.0 / 1024.0);
-    s = fma(s, u, 63.0 / 256.0);
-    s = fma(s, u, 35.0 / 128.0);
-    s = fma(s, u, 5.0 / 16.0);
-    s = fma(s, u, 3.0 / 8.0);
-    s = fma(s, u, 0.5);
+    double s = c[6];
+#pragma unroll
+    for (int k = 5; k >= 0; --k) s = fma(s, u, c[k]);
     return u * s;
   }
-  return 1.0 / sqrt(1.0 - u) - 1.0;
+  return (1.0 / sqrt(1.0 - u) - 1.0) * inv_eta;
+}
+
+// Cell index and FP32 fraction of t >= 0 taken from the bits of t (integer
+// operations only); false for t < 0 or t >= 2^30, which the caller handles
+// in FP64.
+__device__ __forceinline__ bool cell_split(double t, int &ip, float &fr) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(t);
+  const int e = (int)((b >> 52) & 0x7ffull) - 1023;
+  if ((b >> 63) || e > 29) return false;
+  if (e < 0) {
+    ip = 0;
+    fr = d2f_rn(t);
+    return true;
+  }
+  const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+  const int sh = 52 - e;
+  ip = (int)(m >> sh);
+  const unsigned long long fb = m & ((1ull << sh) - 1ull);  // fraction * 2^sh
+  if (fb == 0ull) {
+    fr = 0.f;
+    return true;
+  }
+  const int lz = __clzll((long long)fb);
+  const int ex = (63 - lz) - sh;  // fraction = 1.xxx * 2^ex, ex < 0
+  const unsigned mant = (unsigned)((fb << (lz + 1)) >> 41);  // 23 bits below the leading one
+  fr = __uint_as_float((unsigned)(ex + 127) << 23 | mant);
+  return true;
 }
 
 template <int STAGE, bool ONED>
@@ -217,8 +245,9 @@ __global__ void __launch_bounds__(MX_THREADS) k_stage_mixed(const MixArgs a) {
     for (int q = 0; q < MX_PPT; ++q) {
       const int64_t i = (int64_t)blockIdx.x * (MX_THREADS * MX_PPT) + q * MX_THREADS + threadIdx.x;
       if (halted || i >= a.np) continue;
-      const double fz = floor(a.z2[i] * a.inv_dz2);
-      if (!(fabs(fz) < 2.0e9)) continue;
+      // an estimate is enough: a wrong origin only sends deposits to HBM
+      const float fz = floorf(d2f_rn(a.z2[i]) * a.inv_dz2_f);
+      if (!(fabsf(fz) < 1.0e9f)) continue;
       int m = (int)fz;
       if (a.periodic) {
         m %= (int)a.npl;
@@ -262,36 +291,39 @@ __global__ void __launch_bounds__(MX_THREADS) k_stage_mixed(const MixArgs a) {
     const float rGf = __frcp_rn(Gf);
     double rG = f2d(rGf);
     rG = fma(rG, fma(-gs, rG, 1.0), rG);
-    const double bb = fma(a.aw2, fma(pxs, pxs, pys * pys), 1.0);
-    const double u = bb * a.inv_g02 * (rG * rG);
-    const double p2 = rsqrt1m_minus1(u) * a.inv_eta;
+    const double u = fma(a.aw2g, fma(pxs, pxs, pys * pys), a.g02) * (rG * rG);
+    const double p2 = p2_series(u, a.ser, a.inv_eta);
     const float p2f = d2f_rn(p2);
     const float qrG = fmaf(a.eta_f, p2f, 1.f) * rGf;
 
-    // z2 cell and fraction in FP64, fraction and weights in FP32
+    // z2 cell and fraction from the FP64 position, fraction and weights in FP32
     const double tz = zs * a.inv_dz2;
-    const double fz = floor(tz);
-    const float zw2 = d2f_rn(tz - fz);
+    int iz = 0;
+    float zw2 = 0.f;
     bool ok = true;
-    int pz0 = 0, pz1 = 0;
-    if (a.periodic) {
+    if (!cell_split(tz, iz, zw2)) {
+      const double fz = floor(tz);
       if (!(fabs(fz) < 2.0e9)) {
         ok = false;
-        atomicOr(a.status, ST_OUT_OF_Z2);
       } else {
-        int m = (int)((long long)fz % a.npl);
-        if (m < 0) m += (int)a.npl;
-        pz0 = m;
-        pz1 = (m + 1 == a.npl) ? 0 : m + 1;
+        iz = (int)fz;
+        zw2 = d2f_rn(tz - fz);
       }
+    }
+    int pz0 = 0, pz1 = 0;
+    if (!ok) {
+      atomicOr(a.status, ST_OUT_OF_Z2);
+    } else if (a.periodic) {
+      int m = iz % (int)a.npl;
+      if (m < 0) m += (int)a.npl;
+      pz0 = m;
+      pz1 = (m + 1 == a.npl) ? 0 : m + 1;
+    } else if (!(iz >= 0 && iz + 1 < a.nz2)) {
+      ok = false;
+      atomicOr(a.status, ST_OUT_OF_Z2);
     } else {
-      if (!(fz >= 0.0 && fz + 1.0 < (double)a.nz2)) {
-        ok = false;
-        atomicOr(a.status, ST_OUT_OF_Z2);
-      } else {
-        pz0 = (int)fz;
-        pz1 = pz0 + 1;
-      }
+      pz0 = iz;
+      pz1 = iz + 1;
     }
     float x2 = 0.f, y2 = 0.f;
     int64_t b0 = 0;
@@ -516,6 +548,15 @@ int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_ou
   a.hx_dx = (float)(a.halfx / p.dx);
   a.hy_dy = (float)(a.halfy / p.dy);
   a.eta_f = (float)p.eta;
+  a.inv_dz2_f = (float)(1.0 / p.dz2);
+  a.aw2g = (p.aw * p.aw) / (p.gamma_r * p.gamma_r);
+  a.g02 = 1.0 / (p.gamma_r * p.gamma_r);
+  {
+    // 1/sqrt(1-u) - 1 = sum_k C(2k,k)/4^k u^k, k >= 1
+    const double cb[7] = {1.0 / 2.0, 3.0 / 8.0, 5.0 / 16.0, 35.0 / 128.0, 63.0 / 256.0,
+                          231.0 / 1024.0, 429.0 / 2048.0};
+    for (int k = 0; k < 7; ++k) a.ser[k] = cb[k] / p.eta;
+  }
   a.inv_g02 = 1.0 / (p.gamma_r * p.gamma_r);
   a.aw2 = p.aw * p.aw;
   a.inv_eta = 1.0 / p.eta;

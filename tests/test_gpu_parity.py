@@ -201,7 +201,8 @@ def test_diffraction_matches_oracle(mesh):
 
 
 @pytest.mark.parametrize("precision", [P.FP64, P.MIXED])
-@pytest.mark.parametrize("shape", [(17, 21, 2048), (129, 129, 8), (129, 17, 1536), (17, 33, 600)])
+@pytest.mark.parametrize("shape", [(17, 21, 4096), (129, 129, 8), (129, 17, 1536), (17, 33, 600),
+                                   (33, 33, 64), (65, 65, 32), (17, 17, 2048)])
 def test_diffraction_kernel_shapes(shape, precision):
     """Meshes that select each diffraction kernel form: the transverse-plane
     pass (plane in shared memory), the nine line passes with the radix-43
