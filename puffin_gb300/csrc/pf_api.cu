@@ -469,6 +469,7 @@ int pf_destroy(pf_handle *h) {
   cudaFree(h->staging);
   cudaFree(h->diag);
   cudaFree(h->lat_scratch);
+  cudaFree(h->snap);
   cudaFree(h->d_status);
   cudaFree(h->d_red);
   if (h->h_status) cudaFreeHost(h->h_status);
@@ -711,10 +712,55 @@ int pf_diffract(pf_handle *h, double dz) {
   return PF_OK;
 }
 
+// Bytes of the state an asynchronous block can change: the current particle
+// buffers and the window field.
+static size_t block_state_bytes(const pf_handle *h, size_t *wbytes) {
+  *wbytes = (h->p.precision == PF_MIXED) ? (size_t)h->nwin * 2 * sizeof(float)
+                                         : (size_t)h->nwin * 2 * sizeof(double);
+  return (size_t)6 * h->np * sizeof(double) + *wbytes;
+}
+
+// Copy the block state to (save) or from (restore) the snapshot buffer.
+static int block_snapshot(pf_handle *h, bool save) {
+  size_t wb;
+  const size_t need = block_state_bytes(h, &wb);
+  if (save && h->snap_cap < need) {
+    cudaFree(h->snap);
+    h->snap = nullptr;
+    h->snap_cap = 0;
+    PF_CUDA(cudaMalloc(&h->snap, need));
+    h->snap_cap = need;
+  }
+  char *s = (char *)h->snap;
+  const size_t pb = (size_t)h->np * sizeof(double);
+  for (int j = 0; j < 6; ++j) {
+    char *dst = save ? s + j * pb : (char *)h->y[h->cur][j];
+    const char *src = save ? (const char *)h->y[h->cur][j] : s + j * pb;
+    PF_CUDA(cudaMemcpyAsync(dst, src, pb, cudaMemcpyDeviceToDevice, h->stream));
+  }
+  char *ws = s + 6 * pb;
+  if (h->p.precision == PF_MIXED) {
+    PF_CUDA(cudaMemcpyAsync(save ? ws : (char *)h->w32, save ? (const char *)h->w32 : ws, wb,
+                            cudaMemcpyDeviceToDevice, h->stream));
+  } else {
+    const size_t half = wb / 2;
+    PF_CUDA(cudaMemcpyAsync(save ? ws : (char *)h->wr, save ? (const char *)h->wr : ws, half,
+                            cudaMemcpyDeviceToDevice, h->stream));
+    PF_CUDA(cudaMemcpyAsync(save ? ws + half : (char *)h->wi,
+                            save ? (const char *)h->wi : ws + half, half,
+                            cudaMemcpyDeviceToDevice, h->stream));
+  }
+  return PF_OK;
+}
+
 int pf_run(pf_handle *h, int32_t nsteps, int32_t isteps4diff, int32_t qdiffraction,
            double hstep, double *szl, int32_t *steps_done) {
   if (!h || !szl || nsteps < 0 || (qdiffraction && isteps4diff < 1)) return PF_BAD_ARG;
   if (steps_done) *steps_done = 0;
+  if (nsteps > 0 && (!h->particles_set || h->nwin == 0)) {
+    h->err = "pf_run: particles not set";
+    return PF_STATE;
+  }
   cudaSetDevice(h->dev);
   double dzds = 0.0;
   int rc;
@@ -724,30 +770,101 @@ int pf_run(pf_handle *h, int32_t nsteps, int32_t isteps4diff, int32_t qdiffracti
     if (rc) return rc;
   }
   const int redist = h->p.redist_every > 0 ? h->p.redist_every : 60;
-  for (int istep = 1; istep <= nsteps; ++istep) {
-    int tries = 0;
-    for (;;) {
-      rc = pf_rk4_step(h, *szl, hstep);
-      if (rc == PF_OK) break;
-      if (rc != PF_OUT_OF_WINDOW || ++tries > 3) return rc;
-      rc = pf_redistribute(h);  // getInNode + getLocalFieldIndices
-      if (rc) return rc;
-    }
+  // Steps between two diffraction calls run as one asynchronous block: the
+  // kernels of every step are queued without a host round trip and the status
+  // word is read once at the end (a failed step makes the rest of the block a
+  // no-op).  If it failed, the state saved before the block is restored and
+  // the block is replayed step by step with the reference's retries.  Used
+  // when the saved state is small (launch-bound problems); larger problems
+  // gain nothing from it and run step by step.
+  size_t wb;
+  const bool async_blocks = block_state_bytes(h, &wb) <= ((size_t)256 << 20);
+  auto after_step = [&](int istep) -> int {
     *szl = *szl + hstep;
     if (qdiffraction && (istep % isteps4diff == 0 || istep == nsteps)) {
       double dzdf = dzds;
       if (istep == nsteps) dzds = 0.0;
       else if (istep + isteps4diff <= nsteps) dzds = (double)isteps4diff * hstep / 2;
       else dzds = (double)(nsteps - istep) * hstep / 2;
-      rc = pf_diffract(h, dzdf + dzds);
-      if (rc) return rc;
+      int r = pf_diffract(h, dzdf + dzds);
+      if (r) return r;
     }
     h->csteps++;
     if (h->csteps % redist == 0) {
-      rc = pf_wrap_z2(h);
-      if (rc) return rc;
+      int r = pf_wrap_z2(h);
+      if (r) return r;
     }
     if (steps_done) *steps_done = istep;
+    return PF_OK;
+  };
+  auto eager_step = [&](int istep) -> int {
+    int tries = 0;
+    for (;;) {
+      int r = pf_rk4_step(h, *szl, hstep);
+      if (r == PF_OK) break;
+      if (r != PF_OUT_OF_WINDOW || ++tries > 3) return r;
+      r = pf_redistribute(h);  // getInNode + getLocalFieldIndices
+      if (r) return r;
+    }
+    return after_step(istep);
+  };
+  int istep = 1;
+  while (istep <= nsteps) {
+    // the block ends at the next diffraction step (or after 16 steps)
+    int last = qdiffraction ? std::min<int>(nsteps, ((istep - 1) / isteps4diff + 1) * isteps4diff)
+                            : std::min<int>(nsteps, istep + 15);
+    if (!async_blocks || last == istep) {
+      rc = eager_step(istep);
+      if (rc) return rc;
+      ++istep;
+      continue;
+    }
+    // asynchronous block istep..last; its last step's diffraction runs after
+    // the status check
+    const double szl0 = *szl, n2col = h->n2col, n2col0 = h->n2col0, undgrad = h->undgrad;
+    const int64_t csteps0 = h->csteps;
+    const int cur0 = h->cur;
+    rc = block_snapshot(h, true);
+    if (rc) return rc;
+    PF_CUDA(cudaMemsetAsync(h->d_status, 0, sizeof(unsigned int), h->stream));
+    for (int k = istep; k <= last; ++k) {
+      unsigned int *none = nullptr;
+      rc = (h->p.precision == PF_MIXED) ? pf_rk4_mixed(h, *szl, hstep, none)
+                                        : pf_rk4_fp64(h, *szl, hstep, none);
+      if (rc) return rc;
+      if (k < last) {
+        *szl = *szl + hstep;
+        h->csteps++;
+        if (h->csteps % redist == 0) {
+          rc = pf_wrap_z2(h);
+          if (rc) return rc;
+        }
+      }
+    }
+    PF_CUDA(cudaMemcpyAsync(h->h_status, h->d_status, sizeof(unsigned int),
+                            cudaMemcpyDeviceToHost, h->stream));
+    PF_CUDA(cudaStreamSynchronize(h->stream));
+    pf_prof_flush(h);
+    if (*h->h_status == 0u) {
+      rc = after_step(last);  // last step's position, diffraction and wrap
+      if (rc) return rc;
+      istep = last + 1;
+      continue;
+    }
+    // replay the block step by step from the saved state
+    h->cur = cur0;
+    rc = block_snapshot(h, false);
+    if (rc) return rc;
+    *szl = szl0;
+    h->n2col = n2col;
+    h->n2col0 = n2col0;
+    h->undgrad = undgrad;
+    h->csteps = csteps0;
+    for (int k = istep; k <= last; ++k) {
+      rc = eager_step(k);
+      if (rc) return rc;
+    }
+    istep = last + 1;
   }
   PF_CUDA(cudaStreamSynchronize(h->stream));
   return PF_OK;

@@ -136,6 +136,11 @@ struct pf_handle {
   size_t diag_cap = 0;
   double *lat_scratch = nullptr;  // partial sums of the chi-weighted means
 
+  // snapshot of the particles and the window before an asynchronous step
+  // block of pf_run (restored and replayed step by step if the block fails)
+  void *snap = nullptr;
+  size_t snap_cap = 0;
+
   // completed RK4 steps over the handle's life (the reference's iCsteps); the
   // z2 wrap cadence counts these
   int64_t csteps = 0;

@@ -621,7 +621,9 @@ int pf_rk4_fp64(pf_handle *h, double szl, double hstep, unsigned int *status_out
   const double stage_c[4] = {0.0, hh, hh, hstep};
   const int nxt = h->cur ^ 1;
 
-  PF_CUDA(cudaMemsetAsync(h->d_status, 0, sizeof(unsigned int), h->stream));
+  // status_out == nullptr: enqueue only (a step of an asynchronous block;
+  // the caller clears the status word once per block and reads it after)
+  if (status_out) PF_CUDA(cudaMemsetAsync(h->d_status, 0, sizeof(unsigned int), h->stream));
 
   StageArgs a;
   memset(&a, 0, sizeof(a));
@@ -715,8 +717,12 @@ int pf_rk4_fp64(pf_handle *h, double szl, double hstep, unsigned int *status_out
     rc = launch_nodes(h, s, n);
     if (rc) return rc;
   }
-  PF_CUDA(cudaMemcpyAsync(h->h_status, h->d_status, sizeof(unsigned int),
-                          cudaMemcpyDeviceToHost, h->stream));
+  if (!status_out) {
+    h->cur = nxt;  // committed optimistically; the block is replayed if it failed
+    return PF_OK;
+  }
+  PF_CUDA(cudaMemcpyAsync(h->h_status, h->d_status, sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                          h->stream));
   PF_CUDA(cudaStreamSynchronize(h->stream));
   pf_prof_flush(h);
   *status_out = *h->h_status;

@@ -26,13 +26,17 @@
 // contributions to the three z2 planes from the lowest plane its particles
 // start from in a shared-memory tile, deposited as each macroparticle's
 // slopes are computed (nothing per particle is kept, which keeps the kernel
-// near 64 registers and two 512-thread blocks per SM), with compensated
-// (TwoSum) float atomics: the rounding
-// error of every add is recovered from the value the atomic returns and added
-// to a second tile, so the tile sums carry about twice FP32's precision.  The
-// tile is then flushed to HBM with one float2 atomic per non-zero node.
-// Contributions outside the tile go straight to HBM.  Macroparticles ordered
-// along z2 (as Puffin's beams are generated) make the tile catch nearly all.
+// near 64 registers and two 512-thread blocks per SM).  The tile sums are
+// exact: each FP32 contribution is converted to a fixed-point integer
+// v * 2^E (|v * 2^E| < 2^39, E chosen per beam from max chi/dV3) split into
+// a signed high part (v >> 20) and a 20-bit low part, which are added with
+// two non-returning 32-bit shared-memory reductions into separate words; up
+// to 2048 low parts of < 2^20 cannot overflow 32 bits, so no carry is lost.
+// The flush forms (sum_hi 2^20 + sum_lo) 2^-E in FP32 once per node and adds
+// it to HBM with one float atomic per component.  Contributions
+// outside the tile, or larger than the tile's range, go straight to HBM.
+// Macroparticles ordered along z2 (as Puffin's beams are generated) make the
+// tile catch nearly all.
 #include <math.h>
 #include <string.h>
 
@@ -67,6 +71,8 @@ struct MixArgs {
   int64_t np;
   double cstate, h6;
   float cstate_f, eta_f, inv_dx_f, inv_dy_f, hx_dx, hy_dy, inv_dz2_f;
+  int fixE;            // tile fixed-point exponent
+  float tile_vmax;     // contributions at or above this go to HBM
   double aw2g, g02;    // aw^2 / gamma0^2, 1 / gamma0^2
   double ser[7];       // binomial coefficients of 1/sqrt(1-u) - 1, times 1/eta
   const float2 *as;  // stage field (window, interleaved complex)
@@ -132,14 +138,24 @@ __device__ __forceinline__ void bfield_f(const BFieldF &b, float x, float y, flo
   }
 }
 
-// compensated shared-memory add: the atomic returns the old value, so the
-// rounding error of old + v is known exactly (TwoSum) and kept in c
-__device__ __forceinline__ void tile_add(float *s, float *c, float v) {
-  const float old = atomicAdd(s, v);
-  const float t = __fadd_rn(old, v);
-  const float bp = __fsub_rn(t, old);
-  const float e = __fadd_rn(__fsub_rn(old, __fsub_rn(t, bp)), __fsub_rn(v, bp));
-  if (e != 0.f) atomicAdd(c, e);
+// v * 2^E truncated toward zero, from the bits of v (integer operations);
+// the caller guarantees |v * 2^E| < 2^39
+__device__ __forceinline__ long long f2fix(float v, int E) {
+  const unsigned u = __float_as_uint(v);
+  const int ex = (int)((u >> 23) & 0xffu);
+  if (ex == 0) return 0;
+  const long long m = (long long)((u & 0x7fffffu) | 0x800000u);
+  const int sh = ex - 150 + E;  // v * 2^E = m * 2^sh
+  const long long r = (sh >= 0) ? (m << sh) : (sh > -24 ? (m >> -sh) : 0);
+  return (u >> 31) ? -r : r;
+}
+
+// exact shared-tile add of a fixed-point value: high part (signed) and the
+// 20-bit low part into separate 32-bit words, non-returning reductions
+__device__ __forceinline__ void tile_add(int *hi, unsigned *lo, long long r) {
+  if (r == 0) return;
+  atomicAdd(hi, (int)(r >> 20));
+  atomicAdd(lo, (unsigned)(r & 0xFFFFFll));
 }
 
 __device__ __forceinline__ void global_add(float2 *a, float2 v) {
@@ -229,15 +245,18 @@ __global__ void __launch_bounds__(MX_THREADS) k_stage_mixed(const MixArgs a) {
   extern __shared__ __align__(16) float tile[];  // [2][planes*ntr] (sum, comp) float2 each
   const int ntr = a.nix * a.niy;
   const int tile_n = MX_TILE_PLANES * ntr;
-  float2 *tsum = reinterpret_cast<float2 *>(tile);
-  float2 *tcomp = tsum + tile_n;
+  // [re hi | im hi | re lo | im lo], tile_n words each
+  int *thi_r = reinterpret_cast<int *>(tile);
+  int *thi_i = thi_r + tile_n;
+  unsigned *tlo_r = reinterpret_cast<unsigned *>(thi_i + tile_n);
+  unsigned *tlo_i = tlo_r + tile_n;
   __shared__ int s_pzlo;
 
   const bool halted = (*((volatile unsigned int *)a.status) != 0u);
   if (a.tile) {
     // tile origin: the lowest z2 plane the block's macroparticles start from
     // (stage positions only move forward from there, p2 > 0)
-    for (int t = threadIdx.x; t < 2 * tile_n; t += MX_THREADS) tsum[t] = make_float2(0.f, 0.f);
+    for (int t = threadIdx.x; t < 4 * tile_n; t += MX_THREADS) thi_r[t] = 0;
     if (threadIdx.x == 0) s_pzlo = INT_MAX;
     __syncthreads();
     int my_pzlo = INT_MAX;
@@ -384,10 +403,11 @@ __global__ void __launch_bounds__(MX_THREADS) k_stage_mixed(const MixArgs a) {
           }
           const float vr = w * sr, vi = w * si;
           const int tp = plane - pzlo;
-          if (a.tile && tp >= 0 && tp < MX_TILE_PLANES) {
+          if (a.tile && tp >= 0 && tp < MX_TILE_PLANES && fabsf(vr) < a.tile_vmax &&
+              fabsf(vi) < a.tile_vmax) {
             const int ti = tp * ntr + (int)node;
-            tile_add(&tsum[ti].x, &tcomp[ti].x, vr);
-            tile_add(&tsum[ti].y, &tcomp[ti].y, vi);
+            tile_add(thi_r + ti, tlo_r + ti, f2fix(vr, a.fixE));
+            tile_add(thi_i + ti, tlo_i + ti, f2fix(vi, a.fixE));
           } else {
             global_add(a.acc + (int64_t)plane * ntr + node, make_float2(vr, vi));
           }
@@ -449,8 +469,10 @@ __global__ void __launch_bounds__(MX_THREADS) k_stage_mixed(const MixArgs a) {
       for (int t = threadIdx.x; t < tile_n; t += MX_THREADS) {
         const int plane = pzlo + t / ntr;
         if (plane >= a.npl) break;
-        const float2 s = tsum[t], c = tcomp[t];
-        const float2 v = make_float2(s.x + c.x, s.y + c.y);
+        // (hi 2^20 + lo) 2^-E in FP32 (the accumulators are FP32)
+        const float shi = ldexpf(1.f, 20 - a.fixE), slo = ldexpf(1.f, -a.fixE);
+        const float2 v = make_float2(fmaf((float)thi_r[t], shi, (float)tlo_r[t] * slo),
+                                     fmaf((float)thi_i[t], shi, (float)tlo_i[t] * slo));
         if (v.x != 0.f || v.y != 0.f) global_add(a.acc + (int64_t)plane * ntr + (t - (plane - pzlo) * ntr), v);
       }
     }
@@ -518,7 +540,9 @@ int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_ou
   const double stage_sz[4] = {szl, szh, szh, szl + hstep};
   const double stage_c[4] = {0.0, hh, hh, hstep};
   const int nxt = h->cur ^ 1;
-  PF_CUDA(cudaMemsetAsync(h->d_status, 0, sizeof(unsigned int), h->stream));
+  // status_out == nullptr: enqueue only (a step of an asynchronous block;
+  // the caller clears the status word once per block and reads it after)
+  if (status_out) PF_CUDA(cudaMemsetAsync(h->d_status, 0, sizeof(unsigned int), h->stream));
 
   MixArgs a;
   memset(&a, 0, sizeof(a));
@@ -571,7 +595,16 @@ int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_ou
   a.coupling = p.coupling;
   a.status = h->d_status;
   const int ntr = h->nix * h->niy;
-  const size_t tile_bytes = (size_t)2 * MX_TILE_PLANES * ntr * sizeof(float2);
+  const size_t tile_bytes = (size_t)4 * MX_TILE_PLANES * ntr * sizeof(int);
+  {
+    // |chi/dV3 (1 + eta p2)/Gamma p w| below 16 chi_max/dV3 for |p| (1+eta p2)/Gamma < 16;
+    // the rest goes to HBM
+    const double vmax = 16.0 * h->chi_max / (p.dx * p.dy * p.dz2);
+    int e = 0;
+    frexp(vmax > 0.0 ? vmax : 1.0, &e);  // vmax < 2^e
+    a.fixE = 39 - e;
+    a.tile_vmax = (float)ldexp(1.0, e);
+  }
   a.tile = tile_bytes <= 96 * 1024 ? 1 : 0;
   const size_t smem = a.tile ? tile_bytes : 0;
 
@@ -656,6 +689,10 @@ int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_ou
     }
     pf_prof_end(h);
     PF_LAUNCHED(h);
+  }
+  if (!status_out) {
+    h->cur = nxt;  // committed optimistically; the block is replayed if it failed
+    return PF_OK;
   }
   PF_CUDA(cudaMemcpyAsync(h->h_status, h->d_status, sizeof(unsigned int), cudaMemcpyDeviceToHost,
                           h->stream));

@@ -300,6 +300,35 @@ def test_out_of_window_leaves_state_and_recovers():
         assert sim.rk4par(0.0, w.h) is True
 
 
+def test_run_recovers_when_particles_leave_the_window_mid_block():
+    """A beam whose outer particles drift across the inner window edge during
+    pf_run: the asynchronous step block that fails is restored and replayed
+    step by step with the reference's window recomputation (two retries in
+    32 steps), and the result matches the oracle's UndSection restatement."""
+    w = configs.config1(np_=2000, seed=7, nsteps=32)
+    w.params.nx = w.params.ny = 41
+    beam = {k: a.copy() for k, a in w.beam.items()}
+    beam["px"] = beam["px"] + 20.0 * (beam["x"] > 0.8)
+    field = random_field(w.params, 1)
+    n = w.params.nx * w.params.ny
+    for f in field:
+        f[-n:] = f[:n]
+    with P.Puffin(w.params) as sim:
+        sim.set_particles(*(beam[k] for k in P.PARTICLE_KEYS))
+        sim.set_field(*field)
+        assert sim.window == (21, 21)
+        sim.und_section(32, 16, True, w.h)
+        got, gf, win = sim.get_particles(), sim.get_field(), sim.window
+    cfg = oracle_config(w.params)
+    b = oracle_beam(beam)
+    re, im = (a.copy() for a in field)
+    r = O.undulator_run(cfg, b, re, im, w.h, 32, 16, True)
+    assert r.status == 0 and r.retries == 2
+    assert win == r.window
+    assert_beam_close(got, b, rtol=1e-9, atol=1e-12)
+    field_close(gf, (re, im), 1e-9)
+
+
 def test_out_of_temporal_mesh_raises():
     p = _planepole_params()
     lz2 = (p.nz2 - 1) * p.dz2
