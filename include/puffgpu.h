@@ -137,6 +137,14 @@ int pf_get_field_dev(pf_handle *h, double *re, double *im);
 int pf_set_taper(pf_handle *h, double n2col, double n2col0, double undgrad);
 int pf_get_taper(const pf_handle *h, double *n2col, double *n2col0, double *undgrad);
 
+/* Piecewise-linear taper profile: alpha(z) through n >= 2 control points
+ * (z increasing, local zbar of the module), constant beyond the end points;
+ * n = 0 returns to the module's linear taper n2col0 + undgrad (z - sZFS)
+ * (wiggler_taper.f90:39-45).  The profile generalises the reference's
+ * per-module linear taper to the aw(z) profile that the adjoint
+ * differentiates. */
+int pf_set_taper_profile(pf_handle *h, int32_t n, const double *z, const double *alpha);
+
 /* Inner transverse window currently in use. */
 int pf_get_window(const pf_handle *h, int32_t *nix, int32_t *niy);
 
@@ -219,6 +227,30 @@ int pf_correct_trans(pf_handle *h);
 int pf_init_undulator(pf_handle *h, int32_t und_type, double fx, double fy, double kbxsf,
                       double kbysf, double mf, double taper, int32_t nsteps, double hstep,
                       int32_t und_ends);
+
+/* Adjoint of the RK4 / diffraction run (FP64 path), with checkpoint and
+ * recompute.  pf_adjoint_forward runs nsteps steps the way pf_run does
+ * (UndSection's loop, undulator.f90:182-333; no window retries: the window
+ * must hold the beam for the whole run) from the handle's particles with the
+ * energy chirp gamma += chirp (z2 - <z2>) applied and the initial field
+ * seed_amp * (seed_re, seed_im) (outer mesh), under the taper profile set by
+ * pf_set_taper_profile, keeping the state every checkpoint_every steps; it
+ * returns the final pulse energy E = dx dy dz2 sum |A|^2 over the outer mesh
+ * (unique z2 planes).  pf_adjoint_backward then returns denergy * dE/d(the
+ * ntaper profile values), dE/d(seed_amp) and dE/d(chirp), recomputing each
+ * segment of checkpoint_every steps once.  Both leave the handle's
+ * particles at the unchirped beam; the field must be set again before other
+ * calls. */
+/* Adjoint of one FP64 diffraction step over dz, applied in place to
+ * (re, im) on the outer mesh (host or device arrays; the unique z2 planes;
+ * the periodic mirror plane is left alone): the conjugate propagator and
+ * the self-adjoint filter, damping and masks in reversed order. */
+int pf_diffract_adjoint(pf_handle *h, double dz, double *re, double *im);
+int pf_adjoint_forward(pf_handle *h, int32_t nsteps, int32_t isteps4diff, int32_t qdiffraction,
+                       double hstep, int32_t checkpoint_every, const double *seed_re,
+                       const double *seed_im, double seed_amp, double chirp, double *energy);
+int pf_adjoint_backward(pf_handle *h, double denergy, double *g_taper, int32_t ntaper,
+                        double *g_seed, double *g_chirp);
 
 /* Block until all work queued by the handle is done. */
 int pf_sync(pf_handle *h);

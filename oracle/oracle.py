@@ -63,7 +63,8 @@ class _Params(ctypes.Structure):
 
 class _Taper(ctypes.Structure):
     _fields_ = [("n2col", ctypes.c_double), ("n2col0", ctypes.c_double),
-                ("undgrad", ctypes.c_double)]
+                ("undgrad", ctypes.c_double), ("nprof", ctypes.c_int),
+                ("pz", ctypes.c_void_p), ("pa", ctypes.c_void_p)]
 
 
 class _Stage(ctypes.Structure):
@@ -275,9 +276,16 @@ class Taper:
     n2col: float
     n2col0: float
     undgrad: float
+    profile_z: np.ndarray | None = None   # piecewise-linear alpha(z), if set
+    profile_a: np.ndarray | None = None
 
     def c(self):
-        return _Taper(self.n2col, self.n2col0, self.undgrad)
+        if self.profile_z is None:
+            return _Taper(self.n2col, self.n2col0, self.undgrad, 0, None, None)
+        self._pz = np.ascontiguousarray(self.profile_z, dtype=np.float64)
+        self._pa = np.ascontiguousarray(self.profile_a, dtype=np.float64)
+        return _Taper(self.n2col, self.n2col0, self.undgrad, len(self._pz),
+                      self._pz.ctypes.data, self._pa.ctypes.data)
 
     def update(self, t):
         self.n2col, self.n2col0, self.undgrad = t.n2col, t.n2col0, t.undgrad

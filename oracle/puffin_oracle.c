@@ -27,8 +27,20 @@ static const double PUFFIN_PI = (double)3.14159265358979323846f;
 
 /* ------------------------------------------------------------------------ */
 /* Taper and undulator section: wiggler_taper.f90:39-47, puffin_equations.f90:218-254 */
+static double profile_at(const or_taper *t, double sz) {
+  const int n = t->nprof;
+  if (sz <= t->pz[0]) return t->pa[0];
+  if (sz >= t->pz[n - 1]) return t->pa[n - 1];
+  int k = 0;
+  while (k + 1 < n && t->pz[k + 1] <= sz) ++k;
+  const double u = (sz - t->pz[k]) / (t->pz[k + 1] - t->pz[k]);
+  return t->pa[k] + u * (t->pa[k + 1] - t->pa[k]);
+}
+
 void or_stage_setup(const or_params *p, or_taper *t, double sz, or_stage *out) {
-  if ((sz >= p->szfs) && (sz <= p->szfe)) {
+  if (t->nprof > 1) {
+    t->n2col = profile_at(t, sz);
+  } else if ((sz >= p->szfs) && (sz <= p->szfe)) {
     t->n2col = t->n2col0 + t->undgrad * (sz - p->szfs);
   } else if (sz > p->szfe) {
     t->n2col0 = t->n2col;

@@ -70,6 +70,8 @@ typedef struct {
 /* Taper state (wiggler_taper.f90 keeps n2col and n2col0 as globals). */
 typedef struct {
   double n2col, n2col0, undgrad;
+  int nprof;                 /* > 1: piecewise-linear alpha(z) through (pz, pa) */
+  const double *pz, *pa;
 } or_taper;
 
 /* Evaluate getAlpha + adjUndPlace for one stage; mutates the taper state the

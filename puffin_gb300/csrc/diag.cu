@@ -10,6 +10,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <climits>
 #include <vector>
 
 #include "pf_internal.h"
@@ -60,54 +61,97 @@ __global__ void k_power(const double *re, const double *im, const float2 *oc, in
   }
 }
 
-// bunching at harmonic m with linear slice weights (av_write.f90:562-650)
+// bunching at harmonic m with linear slice weights (av_write.f90:562-650).
+// Macroparticles are ordered along z2, so a block's particles fall in a few
+// consecutive slices: each block sums into shared bins from its lowest slice
+// and adds the bins to HBM once; slices outside the bins go to HBM directly.
+constexpr int BUNCH_BINS = 64;
 __global__ void k_bunching(const double *z2, const double *chi, int64_t np, int harmonic,
                            double rho, double S, int nslices, int periodic, double *br,
                            double *bi, double *sd, unsigned int *status) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= np) return;
-  const double z = z2[i], c = chi[i];
-  int is = (int)ceil(z / S);
-  if (periodic) {
-    if (is >= nslices) is = is - (int)(floor((double)is / (double)nslices) * nslices) + 1;
-    if (is < 1) {
-      atomicOr(status, 1u);
-      return;
-    }
-  } else if (is > nslices || is < 1) {
-    atomicOr(status, 1u);
-    return;
+  __shared__ double s_r[BUNCH_BINS], s_i[BUNCH_BINS], s_d[BUNCH_BINS];
+  __shared__ int s_base;
+  for (int t = threadIdx.x; t < BUNCH_BINS; t += blockDim.x) {
+    s_r[t] = 0.0;
+    s_i[t] = 0.0;
+    s_d[t] = 0.0;
   }
-  const double ph = (double)harmonic * z / (2.0 * rho);
-  double sn, cs;
-  sincos(ph, &sn, &cs);
-  const double w0 = (is * S - z) / S;
-  atomicAdd(sd + (is - 1), c);
-  atomicAdd(br + (is - 1), c * cs * w0);
-  atomicAdd(bi + (is - 1), c * sn * w0);
-  if (!periodic) {
-    const double w1 = -((is - 1) * S - z) / S;
-    atomicAdd(br + is, c * cs * w1);  // slice is+1 (the arrays hold nslices+1)
-    atomicAdd(bi + is, c * sn * w1);
+  if (threadIdx.x == 0) s_base = INT_MAX;
+  __syncthreads();
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int is = 0;
+  bool ok = false;
+  double z = 0.0, c = 0.0;
+  if (i < np) {
+    z = z2[i];
+    c = chi[i];
+    is = (int)ceil(z / S);
+    ok = true;
+    if (periodic) {
+      if (is >= nslices) is = is - (int)(floor((double)is / (double)nslices) * nslices) + 1;
+      if (is < 1) ok = false;
+    } else if (is > nslices || is < 1) {
+      ok = false;
+    }
+    if (!ok) atomicOr(status, 1u);
+    else atomicMin(&s_base, is - 1);
+  }
+  __syncthreads();
+  const int base = s_base;
+  if (ok) {
+    const double ph = (double)harmonic * z / (2.0 * rho);
+    double sn, cs;
+    sincos(ph, &sn, &cs);
+    const double w0 = (is * S - z) / S;
+    auto add = [&](int slot, double vr, double vi, double vd) {
+      const int b = slot - base;
+      if (b >= 0 && b < BUNCH_BINS) {
+        atomicAdd(s_r + b, vr);
+        atomicAdd(s_i + b, vi);
+        if (vd != 0.0) atomicAdd(s_d + b, vd);
+      } else {
+        atomicAdd(br + slot, vr);
+        atomicAdd(bi + slot, vi);
+        if (vd != 0.0) atomicAdd(sd + slot, vd);
+      }
+    };
+    add(is - 1, c * cs * w0, c * sn * w0, c);
+    if (!periodic) {
+      const double w1 = -((is - 1) * S - z) / S;
+      add(is, c * cs * w1, c * sn * w1, 0.0);  // slice is+1 (the arrays hold nslices+1)
+    }
+  }
+  __syncthreads();
+  if (base == INT_MAX) return;
+  for (int t = threadIdx.x; t < BUNCH_BINS; t += blockDim.x) {
+    const int slot = base + t;
+    if (slot > nslices) break;
+    if (s_r[t] != 0.0) atomicAdd(br + slot, s_r[t]);
+    if (s_i[t] != 0.0) atomicAdd(bi + slot, s_i[t]);
+    if (s_d[t] != 0.0) atomicAdd(sd + slot, s_d[t]);
   }
 }
 
 // one-sided |DFT|^2 of the on-axis field (plotSpecPow.py:83-95), direct sum
+// with the roots of unity from a table (root index k z mod n)
 __global__ void k_spectrum(const double *re, const double *im, const float2 *oc, int64_t stride,
-                           int64_t off, int64_t n, int64_t nu, double *sx, double *sy) {
+                           int64_t off, int64_t n, int64_t nu, const double2 *roots, double *sx,
+                           double *sy) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= nu) return;
   double xr = 0.0, xi = 0.0, yr = 0.0, yi = 0.0;
+  int64_t m = 0;
   for (int64_t z = 0; z < n; ++z) {
     const int64_t pos = off + z * stride;
     const double a = oc ? (double)oc[pos].x : re[pos];
     const double b = oc ? (double)oc[pos].y : im[pos];
-    double s, c;
-    sincospi(-2.0 * (double)((k * z) % n) / (double)n, &s, &c);
-    xr += a * c;
-    xi += a * s;
-    yr += b * c;
-    yi += b * s;
+    const double2 w = roots[m];  // (cos, -sin)(2 pi k z / n)
+    xr = fma(a, w.x, xr);
+    xi = fma(a, w.y, xi);
+    yr = fma(b, w.x, yr);
+    yi = fma(b, w.y, yi);
+    m += k;
+    if (m >= n) m -= n;
   }
   double px = xr * xr + xi * xi, py = yr * yr + yi * yi;
   // one-sided power: double every bin but DC (and the Nyquist bin of an even n)
@@ -221,14 +265,25 @@ int pf_spectrum(pf_handle *h, double *sx, double *sy, int64_t nunique) {
   int rc = pf_inner_to_outer(h);
   if (rc) return rc;
   double *d;
-  rc = diag_scratch(h, (size_t)2 * nunique, &d);
+  rc = diag_scratch(h, (size_t)2 * nunique + 2 * (size_t)n, &d);
   if (rc) return rc;
+  {
+    std::vector<double> rt((size_t)2 * n);
+    for (int64_t m = 0; m < n; ++m) {
+      const double ang = 2.0 * M_PI * (double)m / (double)n;
+      rt[2 * m] = cos(ang);
+      rt[2 * m + 1] = -sin(ang);
+    }
+    PF_CUDA(cudaMemcpyAsync(d + 2 * nunique, rt.data(), rt.size() * sizeof(double),
+                            cudaMemcpyHostToDevice, h->stream));
+    PF_CUDA(cudaStreamSynchronize(h->stream));
+  }
   const int64_t plane = (int64_t)p.nx * p.ny;
   const int64_t off = (int64_t)((p.nx - 1) / 2) + (int64_t)p.nx * ((p.ny - 1) / 2);
   const bool mixed = h->p.precision == PF_MIXED;
   k_spectrum<<<(unsigned)((nunique + 127) / 128), 128, 0, h->stream>>>(
       mixed ? nullptr : h->or_, mixed ? nullptr : h->oi_, mixed ? (const float2 *)h->oc32 : nullptr,
-      plane, off, n, nunique, d, d + nunique);
+      plane, off, n, nunique, (const double2 *)(d + 2 * nunique), d, d + nunique);
   PF_LAUNCHED(h);
   PF_CUDA(cudaMemcpyAsync(sx, d, sizeof(double) * nunique, cudaMemcpyDeviceToHost, h->stream));
   PF_CUDA(cudaMemcpyAsync(sy, d + nunique, sizeof(double) * nunique, cudaMemcpyDeviceToHost,

@@ -59,7 +59,9 @@ struct MulTables {
   real ffact;
 };
 
-enum { MID_NONE = 0, MID_PROP = 1, MID_DAMP = 2, MID_SPLIT = 3, MID_RECOMB = 4 };
+enum { MID_NONE = 0, MID_PROP = 1, MID_DAMP = 2, MID_SPLIT = 3, MID_RECOMB = 4,
+       // adjoint of the diffraction step (see diffract_adjoint)
+       MID_ADJ_SPLIT = 5, MID_ADJ_RECOMB = 6, MID_SCALE = 7 };
 
 struct FftArgs {
   cplx *A;
@@ -435,6 +437,17 @@ __device__ __forceinline__ cplx mid_op(const FftArgs &a, int64_t pos, int x, int
   } else if (a.mid == MID_RECOMB) {  // /ffact then + A_nb (diffraction.f90:513-517)
     const cplx b = a.anb[pos];
     v = cplx{v.r / T.ffact + b.r, v.i / T.ffact + b.i};
+  } else if (a.mid == MID_ADJ_SPLIT) {  // keep (1 - m) v for the adjoint recombine
+    const real mk = T.mask[(int64_t)y * T.nx + x];
+    const real nbm = (real)1 - (mk + T.mz[z] * ((real)1 - mk));
+    a.anb[pos] = cplx{nbm * v.r, nbm * v.i};
+  } else if (a.mid == MID_ADJ_RECOMB) {  // m (v / ffact) + (1 - m) v0
+    const real mk = T.mask[(int64_t)y * T.nx + x];
+    const real m = mk + T.mz[z] * ((real)1 - mk);
+    const cplx b = a.anb[pos];
+    v = cplx{m * (v.r / T.ffact) + b.r, m * (v.i / T.ffact) + b.i};
+  } else if (a.mid == MID_SCALE) {
+    v = cplx{v.r / T.ffact, v.i / T.ffact};
   }
   return v;
 }
@@ -793,7 +806,7 @@ static const LongKernel kLongKernels[] = {
 // per-call tables: propagator and damping factors for step h
 __global__ void k_tables(cplx *px, cplx *py, real *dxt, real *dyt, const double *kx,
                          const double *ky, const double *kz, int nx, int ny, int nz, double h,
-                         double sbeta) {
+                         double hd, double sbeta) {
   int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t nxz = (int64_t)nx * nz, nyz = (int64_t)ny * nz;
   if (t < nxz) {
@@ -803,7 +816,7 @@ __global__ void k_tables(cplx *px, cplx *py, real *dxt, real *dyt, const double 
     double s, c;
     sincos(th, &s, &c);
     px[t] = (kzz != 0.0) ? cplx{(real)c, (real)s} : cplx{(real)1, (real)0};
-    dxt[t] = (real)((kzz != 0.0) ? exp(-h * sbeta * fabs(kx[x]) / sqrt(fabs(2.0 * kzz))) : 1.0);
+    dxt[t] = (real)((kzz != 0.0) ? exp(-hd * sbeta * fabs(kx[x]) / sqrt(fabs(2.0 * kzz))) : 1.0);
   } else if (t < nxz + nyz) {
     t -= nxz;
     const int z = (int)(t / ny), y = (int)(t % ny);
@@ -812,7 +825,7 @@ __global__ void k_tables(cplx *px, cplx *py, real *dxt, real *dyt, const double 
     double s, c;
     sincos(th, &s, &c);
     py[t] = (kzz != 0.0) ? cplx{(real)c, (real)s} : cplx{(real)1, (real)0};
-    dyt[t] = (real)((kzz != 0.0) ? exp(-h * sbeta * fabs(ky[y]) / sqrt(fabs(2.0 * kzz))) : 1.0);
+    dyt[t] = (real)((kzz != 0.0) ? exp(-hd * sbeta * fabs(ky[y]) / sqrt(fabs(2.0 * kzz))) : 1.0);
   }
 }
 
@@ -1131,6 +1144,9 @@ static int plane_pass(pf_handle *h, Plan *d, FftArgs a) {
   return PF_OK;
 }
 
+static void base_args(pf_handle *h, Plan *d, real *re, real *im, cplx *oc, FftArgs &a);
+static int run_schedule(pf_handle *h, Plan *d, const FftArgs &a, bool split, bool adjoint);
+
 // Diffract the outer mesh: split real/imaginary arrays (re, im) or, when
 // those are null, the interleaved complex mesh oc (nz2 planes either way).
 static int diffract(pf_handle *h, Plan *&plan, real *re, real *im, cplx *oc, double dz) {
@@ -1141,6 +1157,19 @@ static int diffract(pf_handle *h, Plan *&plan, real *re, real *im, cplx *oc, dou
   }
   Plan *d = plan;
   FftArgs a;
+  base_args(h, d, re, im, oc, a);
+  const bool split = (re != nullptr);
+  const int64_t ntab = (int64_t)(d->nx + d->ny) * d->nz;
+  pf_prof_begin(h, PROF_DIFF);
+  k_tables<<<(unsigned)((ntab + 255) / 256), 256, 0, h->stream>>>(
+      d->px, d->py, d->dxt, d->dyt, d->kx, d->ky, d->kz, d->nx, d->ny, d->nz, dz, dz, p.sbeta);
+  pf_prof_end(h);
+  PF_LAUNCHED(h);
+  return run_schedule(h, d, a, split, false);
+}
+
+static void base_args(pf_handle *h, Plan *d, real *re, real *im, cplx *oc, FftArgs &a) {
+  const pf_params &p = h->p;
   memset(&a, 0, sizeof(a));
   a.A = d->A;
   a.anb = d->anb;
@@ -1158,40 +1187,43 @@ static int diffract(pf_handle *h, Plan *&plan, real *re, real *im, cplx *oc, dou
   a.T.nz = d->nz;
   a.T.qfilter = p.qfilter;
   a.T.ffact = (real)d->ffact;
-  const bool split = (re != nullptr);
-  if (!split) a.A = oc;  // transform the complex outer mesh in place
+  if (re == nullptr) a.A = oc;  // transform the complex outer mesh in place
   a.re_in = re;
   a.im_in = im;
   a.re_out = re;
   a.im_out = im;
   a.mirror = (p.mesh_type == PF_MESH_PERIODIC);
+}
 
-  const int64_t ntab = (int64_t)(d->nx + d->ny) * d->nz;
-  pf_prof_begin(h, PROF_DIFF);
-  k_tables<<<(unsigned)((ntab + 255) / 256), 256, 0, h->stream>>>(
-      d->px, d->py, d->dxt, d->dyt, d->kx, d->ky, d->kz, d->nx, d->ny, d->nz, dz, p.sbeta);
-  pf_prof_end(h);
-  PF_LAUNCHED(h);
-
+// The pass sequence of one diffraction call: the forward step, or (adjoint)
+// the same passes with the adjoint operations in reversed order.
+static int run_schedule(pf_handle *h, Plan *d, const FftArgs &a, bool split, bool adjoint) {
+  // forward: xy fwd | z fwd * prop * z inv | xy inv, split, xy fwd |
+  //          z fwd * damp * z inv | xy inv, + A_nb
+  // adjoint: (A_nb = (1 - m) v) xy fwd | z fwd * damp * z inv |
+  //          xy inv, m v / ffact + A_nb, xy fwd | z fwd * conj(prop) * z inv |
+  //          xy inv, / ffact
+  const int mid2 = adjoint ? MID_DAMP : MID_PROP;
+  const int mid3 = adjoint ? MID_ADJ_RECOMB : MID_SPLIT;
+  const int mid4 = adjoint ? MID_PROP : MID_DAMP;
+  const int mid5 = adjoint ? MID_SCALE : MID_RECOMB;
   if (d->plane) {
-    // five passes: xy fwd | z fwd * prop * z inv | xy inv, split, xy fwd |
-    // z fwd * damp * z inv | xy inv, + A_nb
     struct PStep {
       int plane, dir, mid, second, load_split, store_split;
     };
     const PStep ps[5] = {
         {1, 0, MID_NONE, 0, 1, 0},
-        {0, 0, MID_PROP, 1, 0, 0},
-        {1, 1, MID_SPLIT, 1, 0, 0},
-        {0, 0, MID_DAMP, 1, 0, 0},
-        {1, 1, MID_RECOMB, 0, 0, 1},
+        {0, 0, mid2, 1, 0, 0},
+        {1, 1, mid3, 1, 0, 0},
+        {0, 0, mid4, 1, 0, 0},
+        {1, 1, mid5, 0, 0, 1},
     };
     for (const PStep &s : ps) {
       FftArgs b = a;
       b.dir = s.dir;
       b.mid = s.mid;
       b.second = s.second;
-      b.load_split = split && s.load_split;
+      b.load_split = split && s.load_split && !adjoint;  // the adjoint loads A
       b.store_split = split && s.store_split;
       b.mirror = a.mirror && s.store_split;
       const int rc = s.plane ? plane_pass(h, d, b) : fft_pass(h, d, b, 2);
@@ -1203,22 +1235,22 @@ static int diffract(pf_handle *h, Plan *&plan, real *re, real *im, cplx *oc, dou
     int axis, dir, mid, second, load_split, store_split;
   };
   const Step steps[9] = {
-      {0, 0, MID_NONE, 0, 1, 0},    // x fwd (from re/im)
-      {1, 0, MID_NONE, 0, 0, 0},    // y fwd
-      {2, 0, MID_PROP, 1, 0, 0},    // z fwd, propagate + filter, z inv
-      {1, 1, MID_NONE, 0, 0, 0},    // y inv
-      {0, 1, MID_SPLIT, 1, 0, 0},   // x inv, /ffact, mask split, x fwd
-      {1, 0, MID_NONE, 0, 0, 0},    // y fwd
-      {2, 0, MID_DAMP, 1, 0, 0},    // z fwd, damp, z inv
-      {1, 1, MID_NONE, 0, 0, 0},    // y inv
-      {0, 1, MID_RECOMB, 0, 0, 1},  // x inv, /ffact, + A_nb (to re/im)
+      {0, 0, MID_NONE, 0, 1, 0},  // x fwd (from re/im)
+      {1, 0, MID_NONE, 0, 0, 0},  // y fwd
+      {2, 0, mid2, 1, 0, 0},      // z fwd, propagate + filter (adjoint: damp), z inv
+      {1, 1, MID_NONE, 0, 0, 0},  // y inv
+      {0, 1, mid3, 1, 0, 0},      // x inv, split (adjoint: recombine), x fwd
+      {1, 0, MID_NONE, 0, 0, 0},  // y fwd
+      {2, 0, mid4, 1, 0, 0},      // z fwd, damp (adjoint: conjugate propagator), z inv
+      {1, 1, MID_NONE, 0, 0, 0},  // y inv
+      {0, 1, mid5, 0, 0, 1},      // x inv, recombine (adjoint: scale) (to re/im)
   };
   for (const Step &s : steps) {
     FftArgs b = a;
     b.dir = s.dir;
     b.mid = s.mid;
     b.second = s.second;
-    b.load_split = split && s.load_split;
+    b.load_split = split && s.load_split && !adjoint;
     b.store_split = split && s.store_split;
     // the mirror plane is written by the last pass only
     b.mirror = a.mirror && s.store_split;
@@ -1226,6 +1258,41 @@ static int diffract(pf_handle *h, Plan *&plan, real *re, real *im, cplx *oc, dou
     if (rc) return rc;
   }
   return PF_OK;
+}
+
+// Adjoint (with respect to the real inner product sum re*re' + im*im') of
+// one diffraction step over dz on split re/im arrays of the outer mesh.  The
+// step is A -> Abs(Prop(A)) with Prop = B P F / N (P the propagator and
+// high-pass filter) and Abs(A) = B D F (m A) / N + (1 - m) A (D the damping,
+// m the mask); FFTW's B is the adjoint of F, P's adjoint is the propagator
+// over -dz (the filter and D are real), so the adjoint is
+// Prop^H(Abs^H(v)) with Abs^H(v) = m (B D F v / N) + (1 - m) v.  The periodic
+// mirror plane is not written.
+static int diffract_adjoint(pf_handle *h, Plan *&plan, real *re, real *im, double dz) {
+  const pf_params &p = h->p;
+  if (!plan) {
+    int rc = build_plan(h, plan);
+    if (rc) return rc;
+  }
+  Plan *d = plan;
+  FftArgs a;
+  base_args(h, d, re, im, nullptr, a);
+  a.mirror = 0;
+  const int64_t ntab = (int64_t)(d->nx + d->ny) * d->nz;
+  k_tables<<<(unsigned)((ntab + 255) / 256), 256, 0, h->stream>>>(
+      d->px, d->py, d->dxt, d->dyt, d->kx, d->ky, d->kz, d->nx, d->ny, d->nz, -dz, dz, p.sbeta);
+  PF_LAUNCHED(h);
+  // A = v, A_nb = (1 - m) v
+  {
+    FftArgs b = a;
+    b.load_split = 1;
+    b.store_split = 0;
+    b.mid = MID_ADJ_SPLIT;
+    const unsigned g = (unsigned)((d->n + 255) / 256);
+    k_elementwise<<<g, 256, 0, h->stream>>>(b);
+    PF_LAUNCHED(h);
+  }
+  return run_schedule(h, d, a, true, true);
 }
 
 }  // namespace FFT_NS

@@ -470,6 +470,7 @@ int pf_destroy(pf_handle *h) {
   cudaFree(h->diag);
   cudaFree(h->lat_scratch);
   cudaFree(h->snap);
+  pf_adj_destroy(h->adj);
   cudaFree(h->d_status);
   cudaFree(h->d_red);
   if (h->h_status) cudaFreeHost(h->h_status);
@@ -867,6 +868,19 @@ int pf_run(pf_handle *h, int32_t nsteps, int32_t isteps4diff, int32_t qdiffracti
     istep = last + 1;
   }
   PF_CUDA(cudaStreamSynchronize(h->stream));
+  return PF_OK;
+}
+
+int pf_set_taper_profile(pf_handle *h, int32_t n, const double *z, const double *alpha) {
+  if (!h || n < 0 || (n > 0 && (!z || !alpha)) || n == 1) return PF_BAD_ARG;
+  for (int32_t k = 1; k < n; ++k)
+    if (!(z[k] > z[k - 1])) {
+      h->err = "taper profile abscissae must increase";
+      return PF_BAD_ARG;
+    }
+  h->prof_z.assign(z, z + n);
+  h->prof_a.assign(alpha, alpha + n);
+  if (n > 0) h->n2col = h->n2col0 = alpha[0];
   return PF_OK;
 }
 

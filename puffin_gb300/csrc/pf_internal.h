@@ -95,6 +95,9 @@ struct ProfEvent {
   int cls;
 };
 
+struct AdjCtx;  // adjoint checkpoints and state (adjoint.cu)
+void pf_adj_destroy(AdjCtx *c);
+
 struct pf_handle {
   pf_params p;
   int dev = 0;
@@ -141,12 +144,17 @@ struct pf_handle {
   void *snap = nullptr;
   size_t snap_cap = 0;
 
+  AdjCtx *adj = nullptr;
+
   // completed RK4 steps over the handle's life (the reference's iCsteps); the
   // z2 wrap cadence counts these
   int64_t csteps = 0;
 
   // taper state
   double n2col = 1.0, n2col0 = 1.0, undgrad = 0.0;
+  // piecewise-linear taper profile alpha(z) over control points (empty: the
+  // module's linear taper n2col0 + undgrad (z - sZFS))
+  std::vector<double> prof_z, prof_a;
 
   // device scalars
   unsigned int *d_status = nullptr;
@@ -172,6 +180,10 @@ void pf_prof_flush(pf_handle *h);
 
 // fp64 RK4 step on the device; returns the device status word.
 int pf_rk4_fp64(pf_handle *h, double szl, double hstep, unsigned int *status_out);
+// building blocks of the FP64 step for other drivers (the adjoint)
+void pf_fill_stage_args(pf_handle *h, StageArgs &a, double h6);
+int pf_launch_stage(pf_handle *h, int stage, StageArgs &a);   // k_stage<stage>
+int pf_launch_nodes(pf_handle *h, int stage, NodeArgs &n);    // k_nodes<stage>
 // mixed-precision RK4 step
 int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_out);
 // window management
@@ -180,6 +192,8 @@ int pf_outer_to_inner(pf_handle *h);
 int pf_inner_to_outer(pf_handle *h);
 // diffraction
 int pf_diffract_outer(pf_handle *h, double dz);
+// adjoint of one FP64 diffraction step over dz on split outer-mesh arrays
+int pf_diffract_adjoint_split(pf_handle *h, double *re, double *im, double dz);
 // diffraction of an interleaved complex-float outer mesh (mixed precision)
 int pf_diffract_outer_c32(pf_handle *h, void *outer, double dz);
 void pf_diff_destroy(DiffPlan *d);
@@ -187,6 +201,7 @@ void pf_diff_destroy(DiffPlan *d);
 void pf_stage_coefficients(const pf_params &p, double sz, double n2col, int place,
                            BFieldCoef *bf);
 void pf_taper_stage(pf_handle *h, double sz, double *n2col, int *place);
+double pf_taper_profile_at(const std::vector<double> &z, const std::vector<double> &a, double sz);
 
 #define PF_CUDA(call)                                                     \
   do {                                                                    \

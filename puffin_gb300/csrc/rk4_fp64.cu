@@ -411,9 +411,21 @@ __global__ void __launch_bounds__(256) k_nodes(const NodeArgs a, const double in
 // ---------------------------------------------------------------------------
 
 // getAlpha (wiggler_taper.f90:39-47) + adjUndPlace (puffin_equations.f90:218-254)
+// alpha(z) of a piecewise-linear profile, constant beyond its end points
+double pf_taper_profile_at(const std::vector<double> &z, const std::vector<double> &a, double sz) {
+  const size_t n = z.size();
+  if (sz <= z[0]) return a[0];
+  if (sz >= z[n - 1]) return a[n - 1];
+  const size_t k = (size_t)(std::upper_bound(z.begin(), z.end(), sz) - z.begin()) - 1;
+  const double t = (sz - z[k]) / (z[k + 1] - z[k]);
+  return a[k] + t * (a[k + 1] - a[k]);
+}
+
 void pf_taper_stage(pf_handle *h, double sz, double *n2col, int *place) {
   const pf_params &p = h->p;
-  if ((sz >= p.szfs) && (sz <= p.szfe)) {
+  if (!h->prof_z.empty()) {
+    h->n2col = pf_taper_profile_at(h->prof_z, h->prof_a, sz);
+  } else if ((sz >= p.szfs) && (sz <= p.szfe)) {
     h->n2col = h->n2col0 + h->undgrad * (sz - p.szfs);
   } else if (sz > p.szfe) {
     h->n2col0 = h->n2col;
@@ -614,18 +626,10 @@ static int launch_nodes(pf_handle *h, int stage, NodeArgs &n) {
   return PF_OK;
 }
 
-int pf_rk4_fp64(pf_handle *h, double szl, double hstep, unsigned int *status_out) {
+// Particle, window and physics arguments of the stage kernels for the
+// handle's current state (the per-stage fields are set by the caller).
+void pf_fill_stage_args(pf_handle *h, StageArgs &a, double h6) {
   const pf_params &p = h->p;
-  const double hh = hstep * 0.5, h6 = hstep / 6.0, szh = szl + hh;
-  const double stage_sz[4] = {szl, szh, szh, szl + hstep};
-  const double stage_c[4] = {0.0, hh, hh, hstep};
-  const int nxt = h->cur ^ 1;
-
-  // status_out == nullptr: enqueue only (a step of an asynchronous block;
-  // the caller clears the status word once per block and reads it after)
-  if (status_out) PF_CUDA(cudaMemsetAsync(h->d_status, 0, sizeof(unsigned int), h->stream));
-
-  StageArgs a;
   memset(&a, 0, sizeof(a));
   a.x = h->y[h->cur][0];
   a.y = h->y[h->cur][1];
@@ -673,6 +677,24 @@ int pf_rk4_fp64(pf_handle *h, double szl, double hstep, unsigned int *status_out
   a.fix_e = h->fix_e;
   a.fix_maxexp = h->fix_maxexp;
   a.status = h->d_status;
+}
+
+int pf_launch_stage(pf_handle *h, int stage, StageArgs &a) { return launch_stage(h, stage, a); }
+int pf_launch_nodes(pf_handle *h, int stage, NodeArgs &n) { return launch_nodes(h, stage, n); }
+
+int pf_rk4_fp64(pf_handle *h, double szl, double hstep, unsigned int *status_out) {
+  const pf_params &p = h->p;
+  const double hh = hstep * 0.5, h6 = hstep / 6.0, szh = szl + hh;
+  const double stage_sz[4] = {szl, szh, szh, szl + hstep};
+  const double stage_c[4] = {0.0, hh, hh, hstep};
+  const int nxt = h->cur ^ 1;
+
+  // status_out == nullptr: enqueue only (a step of an asynchronous block;
+  // the caller clears the status word once per block and reads it after)
+  if (status_out) PF_CUDA(cudaMemsetAsync(h->d_status, 0, sizeof(unsigned int), h->stream));
+
+  StageArgs a;
+  pf_fill_stage_args(h, a, h6);
 
   NodeArgs n;
   memset(&n, 0, sizeof(n));

@@ -49,7 +49,9 @@ SYMBOLS = (
     "pf_profile", "pf_profile_read", "pf_rk4_step_noalloc", "pf_power", "pf_num_slices",
     "pf_bunching", "pf_spectrum", "pf_step_count", "pf_set_step_count", "pf_drift",
     "pf_chicane", "pf_quad", "pf_modulation", "pf_match_in", "pf_match_out",
-    "pf_correct_trans", "pf_init_undulator",
+    "pf_correct_trans", "pf_init_undulator", "pf_set_taper_profile", "pf_diffract_adjoint",
+    "pf_adjoint_forward",
+    "pf_adjoint_backward",
 )
 NOALLOC_MAX_PARTICLES = 32768
 NOALLOC_MAX_NODES = 32768
@@ -111,6 +113,11 @@ def load(build_if_missing: bool = False):
         "pf_bunching": (ctypes.c_int, [H, i32, ctypes.c_void_p, i64]),
         "pf_spectrum": (ctypes.c_int, [H, ctypes.c_void_p, ctypes.c_void_p, i64]),
         "pf_step_count": (i64, [H]),
+        "pf_set_taper_profile": (ctypes.c_int, [H, i32, ctypes.c_void_p, ctypes.c_void_p]),
+        "pf_diffract_adjoint": (ctypes.c_int, [H, f64, ctypes.c_void_p, ctypes.c_void_p]),
+        "pf_adjoint_forward": (ctypes.c_int, [H, i32, i32, i32, f64, i32, ctypes.c_void_p,
+                                              ctypes.c_void_p, f64, f64, dp]),
+        "pf_adjoint_backward": (ctypes.c_int, [H, f64, ctypes.c_void_p, i32, dp, dp]),
         "pf_set_step_count": (ctypes.c_int, [H, i64]),
         "pf_drift": (ctypes.c_int, [H, f64, i32]),
         "pf_chicane": (ctypes.c_int, [H, f64, f64, f64, i32]),

@@ -183,6 +183,51 @@ class Puffin:
                                      ctypes.byref(done)))
         return z.value
 
+    def set_taper_profile(self, z=None, alpha=None):
+        """Piecewise-linear alpha(z) through control points (None: the
+        module's linear taper)."""
+        if z is None:
+            self._check(self._lib.pf_set_taper_profile(self._h, 0, None, None))
+            return
+        z = np.ascontiguousarray(z, dtype=np.float64)
+        a = np.ascontiguousarray(alpha, dtype=np.float64)
+        if z.shape != a.shape:
+            raise ValueError("z and alpha need the same length")
+        self._check(self._lib.pf_set_taper_profile(self._h, len(z), z.ctypes.data, a.ctypes.data))
+
+    # -- adjoint (pulse-energy gradients) -------------------------------------------
+    def adjoint_forward(self, nsteps: int, isteps4diff: int, qdiffraction: bool, h: float,
+                        checkpoint_every: int, seed_re, seed_im, seed_amp: float,
+                        chirp: float) -> float:
+        """Pulse energy after nsteps (see pf_adjoint_forward); keeps the
+        checkpoints for adjoint_backward."""
+        sr = np.ascontiguousarray(seed_re, dtype=np.float64)
+        si = np.ascontiguousarray(seed_im, dtype=np.float64)
+        if sr.size != self.n_outer or si.size != self.n_outer:
+            raise ValueError("the seed covers the outer mesh")
+        e = ctypes.c_double()
+        self._check(self._lib.pf_adjoint_forward(self._h, int(nsteps), int(isteps4diff),
+                                                 int(bool(qdiffraction)), float(h),
+                                                 int(checkpoint_every), sr.ctypes.data,
+                                                 si.ctypes.data, float(seed_amp), float(chirp),
+                                                 ctypes.byref(e)))
+        return e.value
+
+    def diffract_adjoint(self, dz: float, re, im):
+        """Adjoint of one diffraction step applied to copies of (re, im)."""
+        r = np.array(re, dtype=np.float64)
+        i = np.array(im, dtype=np.float64)
+        self._check(self._lib.pf_diffract_adjoint(self._h, float(dz), r.ctypes.data, i.ctypes.data))
+        return r, i
+
+    def adjoint_backward(self, ntaper: int, denergy: float = 1.0):
+        """(dE/d taper profile values, dE/d seed_amp, dE/d chirp) times denergy."""
+        g = np.zeros(int(ntaper))
+        gs, gc = ctypes.c_double(), ctypes.c_double()
+        self._check(self._lib.pf_adjoint_backward(self._h, float(denergy), g.ctypes.data,
+                                                  int(ntaper), ctypes.byref(gs), ctypes.byref(gc)))
+        return g, gs.value, gc.value
+
     # -- cumulative step count (iCsteps) -----------------------------------------
     @property
     def step_count(self) -> int:
