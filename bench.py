@@ -64,6 +64,8 @@ def parse():
     ap.add_argument("--np3", type=int, default=2 ** 24,
                     help="macroparticles of the mixed-vs-FP64 leg on the config-1 mesh (0: skip)")
     ap.add_argument("--steps3", type=int, default=32)
+    ap.add_argument("--adjoint-steps", type=int, default=256,
+                    help="steps of the adjoint leg on the 33x33x128 periodic mesh (0: skip)")
     return ap.parse_args()
 
 
@@ -285,6 +287,53 @@ def output_errors(r64, rmx):
     }
 
 
+def adjoint_leg(args, dev):
+    """The adjoint form: periodic 33 x 33 x 128 mesh (129 nodes, 128 unique
+    planes), 2^18 macroparticles, Gaussian seed of waist 1.0 on the resonant
+    carrier, a 16-point taper profile, checkpoints every 64 steps; the forward
+    run with checkpoints, then the backward pass (recompute + adjoint), timed
+    with CUDA events on the library's stream."""
+    import torch
+
+    import puffin_gb300 as P
+    from puffin_gb300 import configs
+
+    w = configs.config4(np_=2 ** 18, nsteps=args.adjoint_steps)
+    p = w.params
+    p.device = dev
+    nx, ny, nz2 = p.nx, p.ny, p.nz2
+    xs = (np.arange(nx) - (nx - 1) / 2) * p.dx
+    ys = (np.arange(ny) - (ny - 1) / 2) * p.dy
+    g = np.exp(-(xs[None, :] ** 2 + ys[:, None] ** 2) / 2.0).ravel()
+    ph = np.arange(nz2) * p.dz2 / (2.0 * p.rho)
+    seed = ((np.cos(ph)[:, None] * g[None, :]).ravel(), (np.sin(ph)[:, None] * g[None, :]).ravel())
+    taper_z = np.linspace(0.0, w.nsteps * w.h, 16)
+    alpha = np.ones(16)
+    with P.Puffin(p) as sim:
+        sim.set_particles(*(w.beam[k] for k in P.PARTICLE_KEYS))
+        sim.set_taper_profile(taper_z, alpha)
+        stream = torch.cuda.ExternalStream(sim.stream_handle, device=dev)
+        run = lambda: sim.adjoint_forward(w.nsteps, w.isteps4diff, True, w.h, 64, seed[0], seed[1],
+                                          1e-2, 0.0)
+        run()                                    # warm-up (plans, allocations)
+        sim.adjoint_backward(16)
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        torch.cuda.synchronize()
+        e[0].record(stream)
+        energy = run()
+        e[1].record(stream)
+        gt, gs, gc = sim.adjoint_backward(16)
+        e[2].record(stream)
+        torch.cuda.synchronize()
+        fwd, bwd = e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])
+    return {
+        "workload": w.name, "macroparticles": w.np, "mesh": [nx, ny, nz2], "steps": w.nsteps,
+        "checkpoint_every": 64, "forward_ms": fwd, "backward_ms": bwd,
+        "backward_over_forward": bwd / fwd, "energy": energy,
+        "grad_seed_amp": gs, "grad_chirp": gc, "grad_taper_norm": float(np.linalg.norm(gt)),
+    }
+
+
 def run_gpu(args, rank, world):
     import torch
 
@@ -331,6 +380,7 @@ def run_gpu(args, rank, world):
     d2h = h2d
     sim.close()
 
+    adj = adjoint_leg(args, dev) if args.adjoint_steps > 0 else None
     rmx = None
     c3 = None
     if not args.no_mixed:
@@ -416,6 +466,8 @@ def run_gpu(args, rank, world):
                          "peak": peak, "unit": "GB/s", "frac": m_ach / peak},
             "clocks": rmx["clocks"],
         }
+    if adj:
+        rec["adjoint"] = adj
     if c3:
         w3 = c3["fp64"]["w"]
         n3 = w3.np

@@ -189,6 +189,15 @@ int64_t pf_num_slices(const pf_handle *h);
 int pf_bunching(pf_handle *h, int32_t harmonic, double *b, int64_t nslices);
 int pf_spectrum(pf_handle *h, double *sx, double *sy, int64_t nunique);
 
+/* How pf_run issues its steps: 0 one step at a time (a host round trip per
+ * step for the status word), 1 asynchronous blocks of steps between two
+ * diffraction calls (one status check per block, the block replayed step by
+ * step if a particle left the window), 2 (default) as 1 with each full block
+ * replayed as a captured CUDA graph whose stage coefficients come from a
+ * device table.  Blocks run asynchronously only while the state they can
+ * change fits in 256 MB (a copy is kept for the replay). */
+int pf_set_launch_mode(pf_handle *h, int32_t mode);
+
 /* Completed RK4 steps counted over the handle's life (the reference's
  * iCsteps, kept across undulator modules): pf_run wraps z2 on the periodic
  * mesh whenever this count reaches a multiple of redist_every
@@ -241,6 +250,20 @@ int pf_init_undulator(pf_handle *h, int32_t und_type, double fx, double fy, doub
  * segment of checkpoint_every steps once.  Both leave the handle's
  * particles at the unchirped beam; the field must be set again before other
  * calls. */
+/* Quiet-start beam on the device (the Halton-sequence branch of the
+ * reference's generator, mp_sequences.f90:126-433, MPfDists.f90:406-620,
+ * noise.f90:25-80): nslices z2 slices with centres z2m[k], width dz2 and
+ * ne[k] electrons, nseq beamlets each from the Halton sequences of bases 2,
+ * 3, 5, 11, 7 (x, y, px, py, gamma; projected on a unit Gaussian, scaled by
+ * sig[5k + d] and shifted by mean[5k + d]) and 13 (z2 offset in the slice).
+ * noise != 0 adds the shot noise (Poisson electron counts, z2 jitter) from a
+ * counter-based generator seeded with seed (the reference seeds from the
+ * clock).  chi = electrons per beamlet * chi_per_electron.  The result
+ * becomes the handle's particles (nslices * nseq of them). */
+int pf_generate_beam(pf_handle *h, int64_t nslices, const double *z2m, const double *ne,
+                     double dz2, int32_t nseq, const double *mean, const double *sig,
+                     int32_t noise, uint64_t seed, double chi_per_electron);
+
 /* Adjoint of one FP64 diffraction step over dz, applied in place to
  * (re, im) on the outer mesh (host or device arrays; the unique z2 planes;
  * the periodic mirror plane is left alone): the conjugate propagator and

@@ -823,3 +823,105 @@ def run_lattice(cfg: Config, beam: Beam, re, im, elements, qdiffraction=True,
         else:
             raise ValueError(kind)
     return sz, csteps
+
+
+# ---------------------------------------------------------------------------
+# Quiet-start beam (mp_sequences.f90:126-433, MPfDists.f90:406-620,
+# noise.f90:25-80) with the library's seeded counter-based generator
+# ---------------------------------------------------------------------------
+def halton(ind: int, base: int) -> float:
+    """halton (mp_sequences.f90:286-305)."""
+    ft, y, it = 1.0, 0.0, ind
+    while it > 0:
+        ft = ft / float(base)
+        y = y + ft * float(it % base)
+        it = it // base
+    return y
+
+
+def project_gauss(seq):
+    """projectRSeq + interp1 (mp_sequences.f90:318-433)."""
+    n = 2000
+    d = (4.0 - (-4.0)) / float(n - 1)
+    yf = [-4.0 + i * d for i in range(n)]
+    cdf = [0.5 * (1.0 + math.erf(v / math.sqrt(2.0))) for v in yf]
+    out = []
+    for v in seq:
+        if cdf[0] < v < cdf[n - 1]:
+            ic = 0
+            while v > cdf[ic]:
+                ic += 1
+            ifl, ifu = ic, ic + 1
+            dx = cdf[ifu] - cdf[ifl]
+            locx = v - cdf[ifl]
+            r = yf[ifl] * (1.0 - locx / dx)
+            r = r + yf[ifu] * locx / dx
+        elif v <= cdf[0]:
+            r = yf[0]
+        else:
+            r = yf[n - 1]
+        out.append(r)
+    return np.array(out)
+
+
+_M64 = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+
+def _mix64(z):
+    with np.errstate(over="ignore"):
+        z = (z + np.uint64(0x9E3779B97F4A7C15)) & _M64
+        z = ((z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)) & _M64
+        z = ((z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)) & _M64
+        return z ^ (z >> np.uint64(31))
+
+
+def _uniform01(seed, i, d):
+    with np.errstate(over="ignore"):
+        k = (np.asarray(i, dtype=np.uint64) * np.uint64(64) + np.uint64(d)) & _M64
+        r = _mix64(np.uint64(seed) ^ _mix64(k))
+    return ((r >> np.uint64(11)).astype(np.float64) + 0.5) * (1.0 / 9007199254740992.0)
+
+
+def generate_beam(z2m, ne, dz2, nseq, mean, sig, noise, seed, chi_per_electron):
+    """Beamlets per slice from the Halton sequences of bases 2, 3, 5, 11, 7
+    (Gaussian) and 13 (z2), with Poisson shot noise; returns a Beam."""
+    z2m = np.asarray(z2m, dtype=np.float64)
+    ne = np.asarray(ne, dtype=np.float64)
+    ns = len(z2m)
+    mean = np.broadcast_to(np.asarray(mean, dtype=np.float64), (ns, 5))
+    sig = np.broadcast_to(np.asarray(sig, dtype=np.float64), (ns, 5))
+    bases = (2, 3, 5, 11, 7, 13)
+    seq = []
+    for d, b in enumerate(bases):
+        v = [halton(j + 1, b) for j in range(nseq)]
+        seq.append(project_gauss(v) if d < 5 else (np.array(v) - 0.5) * dz2)
+    n = ns * nseq
+    i = np.arange(n)
+    k = i // nseq
+    j = i - k * nseq
+    cols = [seq[d][j] * sig[k, d] + mean[k, d] for d in range(5)]
+    z = seq[5][j] + z2m[k]
+    nk = ne[k] / float(nseq)
+    if noise:
+        pk = np.empty(n)
+        small = nk < 12.0
+        # Knuth's product method below a mean of 12
+        for t in np.nonzero(small)[0]:
+            L = math.exp(-nk[t])
+            p, c = 1.0, 0
+            for it in range(60):
+                p *= float(_uniform01(seed, t, 2 + it))
+                if p <= L:
+                    break
+                c += 1
+            pk[t] = c
+        big = ~small
+        u1 = _uniform01(seed, i[big], 0)
+        u2 = _uniform01(seed, i[big], 1)
+        g = np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * math.pi * u2)
+        pk[big] = np.floor(nk[big] + np.sqrt(nk[big]) * g + 0.5)
+        moved = pk > 0.0
+        nk = np.where(moved, pk, nk)
+        u = _uniform01(seed, i, 63)
+        z = np.where(moved, z + (u - 0.5) * dz2 / np.sqrt(nk), z)
+    return Beam(cols[0], cols[1], z, cols[2], cols[3], cols[4], nk * chi_per_electron)

@@ -6,7 +6,8 @@ from .lib import (FP64, MESH_PERIODIC, MESH_TEMPORAL, MIXED, UND_CURVED, UND_HEL
 from .puffin import PARTICLE_KEYS, Puffin, PuffinError, rk4_step_noalloc  # noqa: F401
 from . import lattice  # noqa: F401
 from . import adjoint  # noqa: F401
+from . import h5dump  # noqa: F401
 
-__all__ = ["lattice", "adjoint", "Puffin", "PuffinError", "rk4_step_noalloc", "Params", "default_params", "load", "library_path",
+__all__ = ["lattice", "adjoint", "h5dump", "Puffin", "PuffinError", "rk4_step_noalloc", "Params", "default_params", "load", "library_path",
            "PARTICLE_KEYS", "FP64", "MIXED", "MESH_TEMPORAL", "MESH_PERIODIC",
            "UND_PUFFIN", "UND_HELICAL", "UND_PLANEPOLE", "UND_CURVED"]

@@ -17,8 +17,11 @@ CSRC = os.path.join(PKG, "csrc")
 OUT = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT, "libpuffgpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# host code rounds operation by operation (no FMA contraction on either the
+# x86 or the Arm host), as the reference's and the oracle's code do
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-              "-Xcompiler", "-Wall", "--expt-relaxed-constexpr"]
+              "-Xcompiler", "-Wall", "-Xcompiler", "-ffp-contract=off",
+              "--expt-relaxed-constexpr"]
 
 
 def nvcc() -> str:

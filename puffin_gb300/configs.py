@@ -182,3 +182,25 @@ def config3(np_=2 ** 24, seed=SEED, nsteps=2000):
     w = config1(np_=np_, seed=seed, nsteps=nsteps)
     w.name = "config3: config1 mesh, 2^24 macroparticles"
     return w
+
+
+def config4(np_=2 ** 18, seed=SEED, nsteps=3000):
+    """The adjoint form's mesh: periodic helical 33 x 33 x 129 nodes (128
+    unique planes over 8 resonant wavelengths), dx = dy = 0.2, rho = 0.005,
+    aw = 1, gamma_r = 500, 32 steps per period, diffraction every 16 steps,
+    the config-1 beam at 2^18 macroparticles (sigma 1.0, |x|,|y| <= 1.35)."""
+    w = config1(np_=np_, seed=seed, nsteps=nsteps)
+    p = w.params
+    lamr = 4.0 * PUFFIN_PI * p.rho
+    p.nx = p.ny = 33
+    p.nz2 = 129
+    p.dz2 = 8.0 * lamr / 128.0
+    p.sperwaves = 8.0
+    rng = np.random.default_rng(seed)
+    lz2 = (p.nz2 - 1) * p.dz2
+    w.beam["z2"] = _quiet_z2(rng, np_, 0.0, lz2)
+    w.beam["chi"] = np.full(np_, 2.0 * math.pi * lz2 / np_)
+    n = p.nx * p.ny * p.nz2
+    w.field = (np.zeros(n), np.zeros(n))
+    w.name = "config4: periodic helical 33x33x128 (adjoint form)"
+    return w

@@ -471,6 +471,10 @@ int pf_destroy(pf_handle *h) {
   cudaFree(h->lat_scratch);
   cudaFree(h->snap);
   pf_adj_destroy(h->adj);
+  if (h->gexec) cudaGraphExecDestroy(h->gexec);
+  cudaFree(h->coef_dev);
+  if (h->coef_host) cudaFreeHost(h->coef_host);
+  cudaFree(h->step_ctr);
   cudaFree(h->d_status);
   cudaFree(h->d_red);
   if (h->h_status) cudaFreeHost(h->h_status);
@@ -754,6 +758,101 @@ static int block_snapshot(pf_handle *h, bool save) {
   return PF_OK;
 }
 
+// A block of len RK4 steps (len even, no wrap inside) as one CUDA-graph
+// launch.  The graph is captured once per (block length, buffers) and
+// replayed; the per-(step, stage) coefficients reach the kernels through a
+// device table uploaded before each launch, indexed by a device step counter
+// that the last node kernel of every step advances.  *szl advances to the
+// block's last step (whose position update, diffraction and wrap the caller
+// does after the status check).
+static int run_block_graph(pf_handle *h, int len, double hstep, double *szl) {
+  const bool mixed = (h->p.precision == PF_MIXED);
+  const size_t entry = mixed ? pf_step_coefficients_f_bytes() : 4 * sizeof(StageCoef);
+  const size_t bytes = entry * (size_t)len;
+  if (h->coef_cap < bytes) {
+    cudaFree(h->coef_dev);
+    if (h->coef_host) cudaFreeHost(h->coef_host);
+    h->coef_dev = h->coef_host = nullptr;
+    h->coef_cap = 0;
+    PF_CUDA(cudaMalloc(&h->coef_dev, bytes));
+    PF_CUDA(cudaMallocHost(&h->coef_host, bytes));
+    h->coef_cap = bytes;
+    if (h->gexec) {  // the captured graph reads the old table
+      cudaGraphExecDestroy(h->gexec);
+      h->gexec = nullptr;
+    }
+  }
+  if (!h->step_ctr) PF_CUDA(cudaMalloc(&h->step_ctr, sizeof(int)));
+  const void *key[6] = {h->y[0][0], h->y[1][0], mixed ? h->w32 : (const void *)h->wr,
+                        (const void *)(intptr_t)h->np, (const void *)(intptr_t)h->nwin,
+                        (const void *)(intptr_t)(h->nix * 65536 + h->niy)};
+  bool same = h->gexec && h->g_len == len && h->g_cur == h->cur;
+  for (int k = 0; k < 6; ++k) same = same && (h->g_key[k] == key[k]);
+  const double szl0 = *szl;
+  if (!same) {
+    if (h->gexec) {
+      cudaGraphExecDestroy(h->gexec);
+      h->gexec = nullptr;
+    }
+    // capture: the drivers' host-side work runs (taper state and buffer
+    // parity advance), so both are restored afterwards
+    const double n2col = h->n2col, n2col0 = h->n2col0, undgrad = h->undgrad;
+    const int cur = h->cur;
+    const int64_t launches = h->launches;
+    cudaGraph_t g = nullptr;
+    PF_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    h->capturing = true;
+    int rc = PF_OK;
+    double z = szl0;
+    for (int k = 0; k < len && rc == PF_OK; ++k) {
+      unsigned int *none = nullptr;
+      rc = mixed ? pf_rk4_mixed(h, z, hstep, none) : pf_rk4_fp64(h, z, hstep, none);
+      z = z + hstep;
+    }
+    h->capturing = false;
+    const cudaError_t ce = cudaStreamEndCapture(h->stream, &g);
+    h->g_nlaunch = h->launches - launches;
+    h->launches = launches;
+    h->n2col = n2col;
+    h->n2col0 = n2col0;
+    h->undgrad = undgrad;
+    h->cur = cur;
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (ce != cudaSuccess) {
+      h->err = std::string("step-block capture: ") + cudaGetErrorString(ce);
+      if (g) cudaGraphDestroy(g);
+      return PF_CUDA_ERR;
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&h->gexec, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) {
+      h->gexec = nullptr;
+      h->err = std::string("step-block graph: ") + cudaGetErrorString(ie);
+      return PF_CUDA_ERR;
+    }
+    h->g_len = len;
+    h->g_cur = h->cur;
+    for (int k = 0; k < 6; ++k) h->g_key[k] = key[k];
+  }
+  // this block's coefficients (the taper state advances as the steps do)
+  double z = szl0;
+  for (int k = 0; k < len; ++k) {
+    char *dst = (char *)h->coef_host + entry * (size_t)k;
+    if (mixed) pf_step_coefficients_f(h, z, hstep, dst);
+    else pf_step_coefficients(h, z, hstep, (StageCoef *)dst);
+    if (k < len - 1) z = z + hstep;
+  }
+  *szl = z;
+  PF_CUDA(cudaMemcpyAsync(h->coef_dev, h->coef_host, bytes, cudaMemcpyHostToDevice, h->stream));
+  PF_CUDA(cudaMemsetAsync(h->step_ctr, 0, sizeof(int), h->stream));
+  PF_CUDA(cudaGraphLaunch(h->gexec, h->stream));
+  h->launches += h->g_nlaunch;
+  return PF_OK;
+}
+
 int pf_run(pf_handle *h, int32_t nsteps, int32_t isteps4diff, int32_t qdiffraction,
            double hstep, double *szl, int32_t *steps_done) {
   if (!h || !szl || nsteps < 0 || (qdiffraction && isteps4diff < 1)) return PF_BAD_ARG;
@@ -779,7 +878,7 @@ int pf_run(pf_handle *h, int32_t nsteps, int32_t isteps4diff, int32_t qdiffracti
   // when the saved state is small (launch-bound problems); larger problems
   // gain nothing from it and run step by step.
   size_t wb;
-  const bool async_blocks = block_state_bytes(h, &wb) <= ((size_t)256 << 20);
+  const bool async_blocks = h->launch_mode >= 1 && block_state_bytes(h, &wb) <= ((size_t)256 << 20);
   auto after_step = [&](int istep) -> int {
     *szl = *szl + hstep;
     if (qdiffraction && (istep % isteps4diff == 0 || istep == nsteps)) {
@@ -828,19 +927,30 @@ int pf_run(pf_handle *h, int32_t nsteps, int32_t isteps4diff, int32_t qdiffracti
     rc = block_snapshot(h, true);
     if (rc) return rc;
     PF_CUDA(cudaMemsetAsync(h->d_status, 0, sizeof(unsigned int), h->stream));
-    for (int k = istep; k <= last; ++k) {
-      unsigned int *none = nullptr;
-      rc = (h->p.precision == PF_MIXED) ? pf_rk4_mixed(h, *szl, hstep, none)
-                                        : pf_rk4_fp64(h, *szl, hstep, none);
+    const int len = last - istep + 1;
+    bool wrap_inside = false;
+    for (int k = 1; k < len; ++k) wrap_inside |= ((csteps0 + k) % redist == 0);
+    if (h->use_graphs && !h->prof && h->g_warm && len == isteps4diff && len % 2 == 0 &&
+        !wrap_inside) {
+      rc = run_block_graph(h, len, hstep, szl);
       if (rc) return rc;
-      if (k < last) {
-        *szl = *szl + hstep;
-        h->csteps++;
-        if (h->csteps % redist == 0) {
-          rc = pf_wrap_z2(h);
-          if (rc) return rc;
+      h->csteps += len - 1;
+    } else {
+      for (int k = istep; k <= last; ++k) {
+        unsigned int *none = nullptr;
+        rc = (h->p.precision == PF_MIXED) ? pf_rk4_mixed(h, *szl, hstep, none)
+                                          : pf_rk4_fp64(h, *szl, hstep, none);
+        if (rc) return rc;
+        if (k < last) {
+          *szl = *szl + hstep;
+          h->csteps++;
+          if (h->csteps % redist == 0) {
+            rc = pf_wrap_z2(h);
+            if (rc) return rc;
+          }
         }
       }
+      h->g_warm = true;  // kernel attributes are set: later blocks may be captured
     }
     PF_CUDA(cudaMemcpyAsync(h->h_status, h->d_status, sizeof(unsigned int),
                             cudaMemcpyDeviceToHost, h->stream));
@@ -881,6 +991,13 @@ int pf_set_taper_profile(pf_handle *h, int32_t n, const double *z, const double 
   h->prof_z.assign(z, z + n);
   h->prof_a.assign(alpha, alpha + n);
   if (n > 0) h->n2col = h->n2col0 = alpha[0];
+  return PF_OK;
+}
+
+int pf_set_launch_mode(pf_handle *h, int32_t mode) {
+  if (!h || mode < 0 || mode > 2) return PF_BAD_ARG;
+  h->launch_mode = mode;
+  h->use_graphs = (mode == 2);
   return PF_OK;
 }
 

@@ -44,7 +44,17 @@ struct BFieldCoef {
 };
 
 // Everything a stage kernel needs, passed by value.
+// Per-(step, stage) coefficients read from device memory by the stage kernels
+// when pf_run replays a captured step block (the values the host would pass
+// as kernel arguments otherwise).
+struct StageCoef {
+  BFieldCoef bf;
+  double n2col, kn2col;
+};
+
 struct StageArgs {
+  const StageCoef *coef_tab;  // non-null: coefficients at coef_tab[*step_ctr * 4 + stage - 1]
+  const int *step_ctr;
   // particle arrays
   const double *x, *y, *z2, *px, *py, *gam, *chi;
   const double *kin[6];   // derivative used to form the stage state (stage > 1)
@@ -74,6 +84,7 @@ struct StageArgs {
 };
 
 struct NodeArgs {
+  int *step_ctr;              // non-null: stage 4 advances it once per step
   int64_t n;                  // window nodes
   unsigned long long *acc_lo_r, *acc_hi_r, *acc_lo_i, *acc_hi_i;
   double *wr, *wi;            // window field state (ac_rfield_in)
@@ -146,6 +157,21 @@ struct pf_handle {
 
   AdjCtx *adj = nullptr;
 
+  // graph replay of pf_run's step blocks: the captured block, what it was
+  // captured for, and the coefficient table it reads
+  cudaGraphExec_t gexec = nullptr;
+  int g_len = 0, g_cur = -1;
+  const void *g_key[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  void *coef_dev = nullptr;   // device table (StageCoef or its FP32 form)
+  void *coef_host = nullptr;  // pinned host staging of the table
+  size_t coef_cap = 0;
+  int *step_ctr = nullptr;
+  bool capturing = false;     // the step drivers emit table reads while set
+  bool use_graphs = true;
+  int launch_mode = 2;        // pf_set_launch_mode
+  bool g_warm = false;        // an uncaptured block ran first (kernel attributes set)
+  int64_t g_nlaunch = 0;      // kernels in the captured block
+
   // completed RK4 steps over the handle's life (the reference's iCsteps); the
   // z2 wrap cadence counts these
   int64_t csteps = 0;
@@ -186,6 +212,10 @@ int pf_launch_stage(pf_handle *h, int stage, StageArgs &a);   // k_stage<stage>
 int pf_launch_nodes(pf_handle *h, int stage, NodeArgs &n);    // k_nodes<stage>
 // mixed-precision RK4 step
 int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_out);
+// stage-coefficient table entries of one step (4 entries), FP64 and FP32 forms
+void pf_step_coefficients(pf_handle *h, double szl, double hstep, StageCoef *out);
+void pf_step_coefficients_f(pf_handle *h, double szl, double hstep, void *out);
+size_t pf_step_coefficients_f_bytes();
 // window management
 int pf_window_from_particles(pf_handle *h, int *nix, int *niy);
 int pf_outer_to_inner(pf_handle *h);

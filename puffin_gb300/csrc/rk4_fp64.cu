@@ -285,14 +285,16 @@ __device__ __forceinline__ void stage_particle(const StageArgs &a, const int64_t
   double k[6];
   if (a.electrons_evolve) {
     double bx, by, bz;
-    bfield(a.bf, X, Y, bx, by, bz);
+    const StageCoef *tc = a.coef_tab ? a.coef_tab + (*a.step_ctr) * 4 + (STAGE - 1) : nullptr;
+    bfield(tc ? tc->bf : a.bf, X, Y, bx, by, bz);
+    const double n2col = tc ? tc->n2col : a.n2col, kn2col = tc ? tc->kn2col : a.kn2col;
     const double ep = p2 * a.eta_k2;           // eta p2 / kappa^2
-    const double cz = a.kn2col * qrG * bz;     // kappa (1 + eta p2) / Gamma alpha bz
+    const double cz = kn2col * qrG * bz;       // kappa (1 + eta p2) / Gamma alpha bz
     k[2] = p2;
     k[0] = a.dxc * qrG * PX;
     k[1] = -(a.dxc * qrG * PY);
-    k[3] = a.sInv2rho * (a.n2col * by - ep * fr) + cz * PY;
-    k[4] = a.sInv2rho * (a.n2col * bx - ep * fi) - cz * PX;
+    k[3] = a.sInv2rho * (n2col * by - ep * fr) + cz * PY;
+    k[4] = a.sInv2rho * (n2col * bx - ep * fi) - cz * PX;
     k[5] = -(a.rho2 * qrG * (PX * fr + PY * fi));
   } else {
 #pragma unroll
@@ -401,6 +403,7 @@ __global__ void __launch_bounds__(256) k_nodes(const NodeArgs a, const double in
       a.wr[n] = wr + a.h6 * (a.d0r[n] + dr + 2.0 * a.d12r[n]);
       a.wi[n] = wi + a.h6 * (a.d0i[n] + di + 2.0 * a.d12i[n]);
     }
+    if (a.step_ctr && n == 0) *a.step_ctr += 1;
   }
 }
 
@@ -680,6 +683,21 @@ void pf_fill_stage_args(pf_handle *h, StageArgs &a, double h6) {
 }
 
 int pf_launch_stage(pf_handle *h, int stage, StageArgs &a) { return launch_stage(h, stage, a); }
+
+// The four stage-coefficient entries of one step at local zbar szl
+// (advances the taper state as the step itself does).
+void pf_step_coefficients(pf_handle *h, double szl, double hstep, StageCoef *out) {
+  const double hh = hstep * 0.5, szh = szl + hh;
+  const double stage_sz[4] = {szl, szh, szh, szl + hstep};
+  for (int s = 0; s < 4; ++s) {
+    double n2col;
+    int place;
+    pf_taper_stage(h, stage_sz[s], &n2col, &place);
+    out[s].n2col = n2col;
+    out[s].kn2col = h->p.kappa * n2col;
+    pf_stage_coefficients(h->p, stage_sz[s], n2col, place, &out[s].bf);
+  }
+}
 int pf_launch_nodes(pf_handle *h, int stage, NodeArgs &n) { return launch_nodes(h, stage, n); }
 
 int pf_rk4_fp64(pf_handle *h, double szl, double hstep, unsigned int *status_out) {
@@ -695,6 +713,10 @@ int pf_rk4_fp64(pf_handle *h, double szl, double hstep, unsigned int *status_out
 
   StageArgs a;
   pf_fill_stage_args(h, a, h6);
+  if (h->capturing) {
+    a.coef_tab = (const StageCoef *)h->coef_dev;
+    a.step_ctr = h->step_ctr;
+  }
 
   NodeArgs n;
   memset(&n, 0, sizeof(n));
@@ -714,6 +736,7 @@ int pf_rk4_fp64(pf_handle *h, double szl, double hstep, unsigned int *status_out
   n.h6 = h6;
   n.fix_e = h->fix_e;
   n.status = h->d_status;
+  if (h->capturing) n.step_ctr = h->step_ctr;
 
   for (int s = 1; s <= 4; ++s) {
     double n2col;

@@ -22,7 +22,8 @@
 // that), which is accurate to a few ulps in FP64 and needs no square root or
 // division.
 //
-// Deposit: each block of 2048 macroparticles (4 per thread) accumulates its
+// Deposit: each block of up to 2048 macroparticles (up to 4 per thread; fewer
+// for beams too small to fill the SMs) accumulates its
 // contributions to the three z2 planes from the lowest plane its particles
 // start from in a shared-memory tile, deposited as each macroparticle's
 // slopes are computed (nothing per particle is kept, which keeps the kernel
@@ -57,6 +58,8 @@ struct BFieldF {
 };
 
 struct MixArgs {
+  const void *coef_tab;  // non-null: StageCoefF at [*step_ctr * 4 + stage - 1]
+  const int *step_ctr;
   const double *x, *y, *z2, *px, *py, *gam, *chi;
   // slopes: FP32 arrays for x, y, px, py, Gamma (index 2 unused), FP64 for z2
   const float *kin_f[6];
@@ -71,6 +74,7 @@ struct MixArgs {
   int64_t np;
   double cstate, h6;
   float cstate_f, eta_f, inv_dx_f, inv_dy_f, hx_dx, hy_dy, inv_dz2_f;
+  int ppt;             // macroparticles per thread (1..MX_PPT)
   int fixE;            // tile fixed-point exponent
   float tile_vmax;     // contributions at or above this go to HBM
   double aw2g, g02;    // aw^2 / gamma0^2, 1 / gamma0^2
@@ -93,6 +97,13 @@ struct MixNodeArgs {
   float2 *acc, *w, *as, *d0, *d12;
   float coef, h6;
   const unsigned int *status;
+  int *step_ctr;  // non-null: stage 4 advances it once per step
+};
+
+// per-(step, stage) coefficients of a replayed step block (FP32 form)
+struct StageCoefF {
+  BFieldF bf;
+  float n2col, kn2col;
 };
 
 __device__ __forceinline__ void bfield_f(const BFieldF &b, float x, float y, float &bx, float &by,
@@ -261,8 +272,8 @@ __global__ void __launch_bounds__(MX_THREADS) k_stage_mixed(const MixArgs a) {
     __syncthreads();
     int my_pzlo = INT_MAX;
 #pragma unroll
-    for (int q = 0; q < MX_PPT; ++q) {
-      const int64_t i = (int64_t)blockIdx.x * (MX_THREADS * MX_PPT) + q * MX_THREADS + threadIdx.x;
+    for (int q = 0; q < a.ppt; ++q) {
+      const int64_t i = (int64_t)blockIdx.x * (MX_THREADS * a.ppt) + q * MX_THREADS + threadIdx.x;
       if (halted || i >= a.np) continue;
       // an estimate is enough: a wrong origin only sends deposits to HBM
       const float fz = floorf(d2f_rn(a.z2[i]) * a.inv_dz2_f);
@@ -281,8 +292,8 @@ __global__ void __launch_bounds__(MX_THREADS) k_stage_mixed(const MixArgs a) {
   const int pzlo = a.tile ? s_pzlo : 0;
 
 #pragma unroll 1
-  for (int q = 0; q < MX_PPT; ++q) {
-    const int64_t i = (int64_t)blockIdx.x * (MX_THREADS * MX_PPT) + q * MX_THREADS + threadIdx.x;
+  for (int q = 0; q < a.ppt; ++q) {
+    const int64_t i = (int64_t)blockIdx.x * (MX_THREADS * a.ppt) + q * MX_THREADS + threadIdx.x;
     if (halted || i >= a.np) continue;
     // FP64 state; stage values of z2, Gamma, px, py in FP64, of x, y in FP32
     const double x0 = a.x[i], yv0 = a.y[i], z0 = a.z2[i], px0 = a.px[i], py0 = a.py[i],
@@ -423,14 +434,17 @@ __global__ void __launch_bounds__(MX_THREADS) k_stage_mixed(const MixArgs a) {
     double kz = 0.0;
     if (a.electrons_evolve) {
       float bx, by, bz;
-      bfield_f(a.bf, X, Y, bx, by, bz);
+      const StageCoefF *tc =
+          a.coef_tab ? (const StageCoefF *)a.coef_tab + (*a.step_ctr) * 4 + (STAGE - 1) : nullptr;
+      bfield_f(tc ? tc->bf : a.bf, X, Y, bx, by, bz);
+      const float n2col = tc ? tc->n2col : a.n2col, kn2col = tc ? tc->kn2col : a.kn2col;
       const float ep = p2f * a.eta_k2;
-      const float cz = a.kn2col * qrG * bz;
+      const float cz = kn2col * qrG * bz;
       kz = p2;
       k[0] = a.dxc * qrG * PX;
       k[1] = -(a.dxc * qrG * PY);
-      k[3] = a.sInv2rho * (a.n2col * by - ep * fr) + cz * PY;
-      k[4] = a.sInv2rho * (a.n2col * bx - ep * fi) - cz * PX;
+      k[3] = a.sInv2rho * (n2col * by - ep * fr) + cz * PY;
+      k[4] = a.sInv2rho * (n2col * bx - ep * fi) - cz * PX;
       k[5] = -(a.rho2 * qrG * (PX * fr + PY * fi));
     }
     constexpr int kF[5] = {0, 1, 3, 4, 5};
@@ -501,6 +515,7 @@ __global__ void __launch_bounds__(256) k_nodes_mixed(const MixNodeArgs a) {
       const float2 d0 = a.d0[n], e = a.d12[n];
       a.w[n] = make_float2(w.x + a.h6 * (d0.x + d.x + 2.f * e.x), w.y + a.h6 * (d0.y + d.y + 2.f * e.y));
     }
+    if (a.step_ctr && n == 0) *a.step_ctr += 1;
   }
 }
 
@@ -533,6 +548,25 @@ BFieldF to_float(const BFieldCoef &b) {
 }
 
 }  // namespace
+
+// FP32 stage-coefficient entries of one step (advances the taper state)
+void pf_step_coefficients_f(pf_handle *h, double szl, double hstep, void *out_) {
+  StageCoefF *out = (StageCoefF *)out_;
+  const double hh = hstep * 0.5, szh = szl + hh;
+  const double stage_sz[4] = {szl, szh, szh, szl + hstep};
+  for (int s = 0; s < 4; ++s) {
+    double n2col;
+    int place;
+    pf_taper_stage(h, stage_sz[s], &n2col, &place);
+    BFieldCoef bf;
+    pf_stage_coefficients(h->p, stage_sz[s], n2col, place, &bf);
+    out[s].bf = to_float(bf);
+    out[s].n2col = (float)n2col;
+    out[s].kn2col = (float)(h->p.kappa * n2col);
+  }
+}
+
+size_t pf_step_coefficients_f_bytes() { return 4 * sizeof(StageCoefF); }
 
 int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_out) {
   const pf_params &p = h->p;
@@ -594,6 +628,10 @@ int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_ou
   a.electrons_evolve = p.electrons_evolve;
   a.coupling = p.coupling;
   a.status = h->d_status;
+  if (h->capturing) {
+    a.coef_tab = h->coef_dev;
+    a.step_ctr = h->step_ctr;
+  }
   const int ntr = h->nix * h->niy;
   const size_t tile_bytes = (size_t)4 * MX_TILE_PLANES * ntr * sizeof(int);
   {
@@ -618,6 +656,7 @@ int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_ou
   n.d12 = (float2 *)h->d12_32;
   n.h6 = (float)(hstep / 6.0);
   n.status = h->d_status;
+  if (h->capturing) n.step_ctr = h->step_ctr;
 
   static bool attr_set = false;
   if (!attr_set) {
@@ -630,7 +669,10 @@ int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_ou
       PF_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
     attr_set = true;
   }
-  const int64_t per_block = (int64_t)MX_THREADS * MX_PPT;
+  // up to MX_PPT macroparticles per thread, fewer when the beam is too small
+  // to give every SM two blocks
+  a.ppt = (int)std::max<int64_t>(1, std::min<int64_t>(MX_PPT, h->np / ((int64_t)152 * 2 * MX_THREADS)));
+  const int64_t per_block = (int64_t)MX_THREADS * a.ppt;
   const unsigned pg = (unsigned)std::max<int64_t>(1, (h->np + per_block - 1) / per_block);
   const unsigned ng = (unsigned)std::max<int64_t>(1, (h->nwin + 255) / 256);
   const bool oned = p.one_d != 0;

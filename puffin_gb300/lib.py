@@ -50,7 +50,7 @@ SYMBOLS = (
     "pf_bunching", "pf_spectrum", "pf_step_count", "pf_set_step_count", "pf_drift",
     "pf_chicane", "pf_quad", "pf_modulation", "pf_match_in", "pf_match_out",
     "pf_correct_trans", "pf_init_undulator", "pf_set_taper_profile", "pf_diffract_adjoint",
-    "pf_adjoint_forward",
+    "pf_adjoint_forward", "pf_generate_beam", "pf_set_launch_mode",
     "pf_adjoint_backward",
 )
 NOALLOC_MAX_PARTICLES = 32768
@@ -114,6 +114,10 @@ def load(build_if_missing: bool = False):
         "pf_spectrum": (ctypes.c_int, [H, ctypes.c_void_p, ctypes.c_void_p, i64]),
         "pf_step_count": (i64, [H]),
         "pf_set_taper_profile": (ctypes.c_int, [H, i32, ctypes.c_void_p, ctypes.c_void_p]),
+        "pf_set_launch_mode": (ctypes.c_int, [H, i32]),
+        "pf_generate_beam": (ctypes.c_int, [H, i64, ctypes.c_void_p, ctypes.c_void_p, f64, i32,
+                                            ctypes.c_void_p, ctypes.c_void_p, i32,
+                                            ctypes.c_uint64, f64]),
         "pf_diffract_adjoint": (ctypes.c_int, [H, f64, ctypes.c_void_p, ctypes.c_void_p]),
         "pf_adjoint_forward": (ctypes.c_int, [H, i32, i32, i32, f64, i32, ctypes.c_void_p,
                                               ctypes.c_void_p, f64, f64, dp]),

@@ -195,6 +195,57 @@ class Puffin:
             raise ValueError("z and alpha need the same length")
         self._check(self._lib.pf_set_taper_profile(self._h, len(z), z.ctypes.data, a.ctypes.data))
 
+    def set_launch_mode(self, mode: int):
+        """0 step by step, 1 asynchronous step blocks, 2 blocks as CUDA graphs."""
+        self._check(self._lib.pf_set_launch_mode(self._h, int(mode)))
+
+    # -- Puffin dump files ----------------------------------------------------------
+    def load_dump(self, particles_path=None, field_path=None):
+        """Start from the reference's HDF5 dumps (particle and/or field file);
+        returns the resume attributes of the particle file (iCsteps, zbarLocal,
+        ...) and sets the cumulative step count from iCsteps."""
+        from . import h5dump
+        attrs = {}
+        if particles_path is not None:
+            beam, attrs = h5dump.read_particles(particles_path)
+            self.set_particles(*(beam[k] for k in PARTICLE_KEYS))
+            if "iCsteps" in attrs:
+                self.step_count = int(attrs["iCsteps"])
+        if field_path is not None:
+            re, im, _, fattrs = h5dump.read_field(field_path)
+            self.set_field(re, im)
+            attrs = attrs or fattrs
+        return attrs
+
+    def save_dump(self, particles_path=None, field_path=None, attrs=None):
+        """Write the particles and/or the field in the reference's dump layout."""
+        from . import h5dump
+        a = dict(attrs or {})
+        a.setdefault("iCsteps", self.step_count)
+        if particles_path is not None:
+            h5dump.write_particles(particles_path, self.get_particles(), a)
+        if field_path is not None:
+            re, im = self.get_field()
+            p = self.params
+            h5dump.write_field(field_path, re, im, (p.nx, p.ny, p.nz2), a)
+
+    # -- beam generation ------------------------------------------------------------
+    def generate_beam(self, z2m, ne, dz2: float, nseq: int, mean, sig, noise: bool = True,
+                      seed: int = 0x5EED, chi_per_electron: float = 1.0):
+        """Quiet-start Halton beamlets per z2 slice with shot noise (see
+        pf_generate_beam); mean and sig are (nslices, 5) arrays over x, y,
+        px, py, gamma (or 5 values for every slice)."""
+        z2m = np.ascontiguousarray(z2m, dtype=np.float64)
+        ne = np.ascontiguousarray(ne, dtype=np.float64)
+        ns = len(z2m)
+        m = np.ascontiguousarray(np.broadcast_to(np.asarray(mean, dtype=np.float64), (ns, 5)))
+        s = np.ascontiguousarray(np.broadcast_to(np.asarray(sig, dtype=np.float64), (ns, 5)))
+        self._check(self._lib.pf_generate_beam(self._h, ns, z2m.ctypes.data, ne.ctypes.data,
+                                               float(dz2), int(nseq), m.ctypes.data,
+                                               s.ctypes.data, int(bool(noise)),
+                                               int(seed) & (2 ** 64 - 1),
+                                               float(chi_per_electron)))
+
     # -- adjoint (pulse-energy gradients) -------------------------------------------
     def adjoint_forward(self, nsteps: int, isteps4diff: int, qdiffraction: bool, h: float,
                         checkpoint_every: int, seed_re, seed_im, seed_amp: float,

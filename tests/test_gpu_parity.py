@@ -281,6 +281,44 @@ def test_run_with_diffraction_matches_oracle():
     field_close(gf, (re, im), 1e-9)
 
 
+@pytest.mark.parametrize("precision", [P.FP64, P.MIXED])
+def test_run_graph_blocks_match_step_by_step(precision):
+    """pf_run replays its 8-step blocks as captured CUDA graphs with the stage
+    coefficients from a device table; the result matches the same schedule
+    driven one call at a time (rk4par, diffractIM, wrap): bit for bit in
+    FP64."""
+    w = configs.config1(np_=8192, seed=41, nsteps=64)
+    w.params.precision = precision
+    field = random_field(w.params, 3, amp=1e-2)
+    h = w.h
+    with P.Puffin(w.params) as sim:
+        sim.set_particles(*(w.beam[k] for k in P.PARTICLE_KEYS))
+        sim.set_field(*field)
+        sim.und_section(64, 8, True, h)
+        got, gf = sim.get_particles(), sim.get_field()
+    with P.Puffin(w.params) as sim:
+        sim.set_particles(*(w.beam[k] for k in P.PARTICLE_KEYS))
+        sim.set_field(*field)
+        sim.diffractIM(8 * h / 2)
+        szl = 0.0
+        for i in range(1, 65):
+            assert sim.rk4par(szl, h)
+            szl = szl + h
+            if i % 8 == 0:
+                sim.diffractIM(8 * h / 2 + (8 * h / 2 if i < 64 else 0.0))
+            if i % 60 == 0:
+                sim.wrap_z2()
+        want, wf = sim.get_particles(), sim.get_field()
+    if precision == P.FP64:  # the fixed-point deposit makes FP64 runs reproducible bit for bit
+        for k in ("x", "y", "z2", "px", "py", "gam"):
+            np.testing.assert_array_equal(got[k], want[k], err_msg=k)
+        np.testing.assert_array_equal(gf[0], wf[0])
+        np.testing.assert_array_equal(gf[1], wf[1])
+    else:  # FP32 atomics land in any order: FP32 rounding, grown over 64 steps
+        assert_beam_close(got, oracle_beam(want), rtol=1e-5, atol=1e-8)
+        field_close(gf, wf, 1e-4)
+
+
 def test_deposit_is_bit_reproducible():
     w = configs.config1(np_=20000, seed=3, nsteps=4)
     field = random_field(w.params, 2)
@@ -399,3 +437,31 @@ def test_device_arrays_round_trip():
     torch.cuda.synchronize()
     for k in P.PARTICLE_KEYS:
         assert torch.equal(out[k], t[k])
+
+
+@pytest.mark.parametrize("noise", [False, True])
+def test_generate_beam_matches_oracle(noise):
+    """The device beam generator against the oracle's restatement: the quiet
+    beam bit for bit, the shot noise to the transcendental functions' last
+    bits (normal branch) and exactly where the counts agree."""
+    ns, nseq = 64, 200
+    z2m = (np.arange(ns) + 0.5) * 0.05
+    ne = np.where(np.arange(ns) % 2 == 0, 8.0e4, 900.0)   # 400 and 4.5 per beamlet
+    mean = np.stack([np.zeros(ns), np.full(ns, 0.2), np.zeros(ns), np.zeros(ns),
+                     1.0 + 1e-3 * np.arange(ns)], axis=1)
+    sig = np.array([0.8, 0.6, 0.01, 0.02, 5e-4])
+    p = P.default_params(rho=0.005, eta=1e-5, kappa=0.2, nx=31, ny=31, nz2=80, dx=0.3, dy=0.3,
+                         dz2=0.05)
+    with P.Puffin(p) as sim:
+        sim.generate_beam(z2m, ne, 0.05, nseq, mean, sig, noise=noise, seed=99, chi_per_electron=3.0)
+        got = sim.get_particles()
+    want = O.generate_beam(z2m, ne, 0.05, nseq, mean, sig, noise, 99, 3.0)
+    for k in ("x", "y", "px", "py", "gam"):
+        np.testing.assert_array_equal(got[k], getattr(want, k), err_msg=k)
+    if not noise:
+        np.testing.assert_array_equal(got["z2"], want.z2)
+        np.testing.assert_array_equal(got["chi"], want.chi)
+    else:
+        same = got["chi"] == want.chi
+        assert np.mean(same) > 0.999
+        np.testing.assert_allclose(got["z2"][same], want.z2[same], rtol=0, atol=1e-15)
