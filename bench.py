@@ -64,6 +64,9 @@ def parse():
     ap.add_argument("--np3", type=int, default=2 ** 24,
                     help="macroparticles of the mixed-vs-FP64 leg on the config-1 mesh (0: skip)")
     ap.add_argument("--steps3", type=int, default=32)
+    ap.add_argument("--batch-n", type=int, default=128,
+                    help="instances of the batched form (0: skip the leg)")
+    ap.add_argument("--batch-steps", type=int, default=32)
     ap.add_argument("--adjoint-steps", type=int, default=256,
                     help="steps of the adjoint leg on the 33x33x128 periodic mesh (0: skip)")
     return ap.parse_args()
@@ -334,6 +337,78 @@ def adjoint_leg(args, dev):
     }
 
 
+def batch_leg(args, dev):
+    """The batched form: args.batch_n independent periodic single-slice
+    instances (macroparticles log-uniform in [2^14, 2^20], meshes
+    {17, 33, 65}^2 x {32, 64, 128}, rho, detuning, aw and undulator type drawn
+    from the seed), 32 steps per period, diffraction every 16 steps.  Per
+    precision: every instance alone through pf_run (its CUDA-graph blocks),
+    then all of them as one batch (autotuned), each for args.batch_steps
+    steps after a 16-step warm-up; wall-clock time around each, both ending
+    with the device idle.  The state continues from one timing to the next
+    (the rate does not depend on it)."""
+    import torch
+
+    import puffin_gb300 as P
+    from puffin_gb300 import configs
+
+    ws = configs.config5(n_inst=args.batch_n, nsteps=args.batch_steps)
+    total = sum(w.np for w in ws)
+    out = {"workload": f"{len(ws)} periodic single-slice instances (batched form)",
+           "instances": len(ws), "macroparticles_total": total,
+           "macroparticles_min": min(w.np for w in ws), "macroparticles_max": max(w.np for w in ws),
+           "steps": args.batch_steps, "warmup_steps": 16, "diffraction_every": 16,
+           "timing": "wall clock around the run calls (host and device)", "unit": UNIT}
+    launches = 0
+    for name, prec in (("fp64", P.FP64), ("mixed", P.MIXED)):
+        sims = []
+        try:
+            for w in ws:
+                w.params.precision = prec
+                w.params.device = dev
+                sim = P.Puffin(w.params)
+                sim.set_particles(*(w.beam[k] for k in P.PARTICLE_KEYS))
+                sims.append(sim)
+            hs = np.array([w.h for w in ws])
+            z = np.zeros(len(ws))
+            for i, sim in enumerate(sims):        # warm-up: plans, graphs
+                z[i] = sim.und_section(16, 16, True, ws[i].h, z[i])
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for i, sim in enumerate(sims):
+                z[i] = sim.und_section(args.batch_steps, 16, True, ws[i].h, z[i])
+            torch.cuda.synchronize()
+            t_single = time.perf_counter() - t0
+            launches += sum(s.kernel_launches for s in sims)
+            with P.Batch(sims) as b:
+                t0 = time.perf_counter()
+                shape = b.tune(hs, z)
+                t_tune = time.perf_counter() - t0
+                z, _ = b.run(16, 16, True, hs, z)   # warm-up: graph capture
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                z, _ = b.run(args.batch_steps, 16, True, hs, z)
+                torch.cuda.synchronize()
+                t_batch = time.perf_counter() - t0
+                launches += b.kernel_launches
+            modes = shape.pop("modes")
+            out[name] = {
+                "one_at_a_time": {"value": total * args.batch_steps / t_single,
+                                  "ms_per_step": 1e3 * t_single / args.batch_steps},
+                "batched": {"value": total * args.batch_steps / t_batch,
+                            "ms_per_step": 1e3 * t_batch / args.batch_steps},
+                "speedup": t_single / t_batch,
+                "tuned_shape": shape,
+                "tuned_modes": {str(int(m)): int(c) for m, c in zip(*np.unique(modes, return_counts=True))},
+                "tune_seconds": t_tune,
+            }
+        finally:
+            for s in sims:
+                s.close()
+    out["gpu_launches"] = launches
+    return out
+
+
 def run_gpu(args, rank, world):
     import torch
 
@@ -381,6 +456,7 @@ def run_gpu(args, rank, world):
     sim.close()
 
     adj = adjoint_leg(args, dev) if args.adjoint_steps > 0 else None
+    bat = batch_leg(args, dev) if args.batch_n > 0 else None
     rmx = None
     c3 = None
     if not args.no_mixed:
@@ -468,6 +544,9 @@ def run_gpu(args, rank, world):
         }
     if adj:
         rec["adjoint"] = adj
+    if bat:
+        rec["gpu_launches"] += bat.pop("gpu_launches")
+        rec["batched"] = bat
     if c3:
         w3 = c3["fp64"]["w"]
         n3 = w3.np

@@ -275,6 +275,45 @@ int pf_adjoint_forward(pf_handle *h, int32_t nsteps, int32_t isteps4diff, int32_
 int pf_adjoint_backward(pf_handle *h, double denergy, double *g_taper, int32_t ntaper,
                         double *g_seed, double *g_chirp);
 
+/* Batched runs (no counterpart in the reference, which runs one simulation
+ * per process).  A batch groups n independent instances -- handles created
+ * with pf_create on one device, one precision, 3D, each with its particles
+ * and field set -- and advances them together: every RK4 stage of every
+ * instance in one launch over (instance, range) tiles, the blocks of steps
+ * between diffraction calls replayed as one CUDA graph.  Each instance
+ * follows pf_run's schedule exactly (UndSection, undulator.f90:33-358):
+ * pf_batch_run(b, nsteps, isteps4diff, qdiffraction, hstep, szl, status)
+ * does what pf_run(inst[i], nsteps, isteps4diff, qdiffraction, hstep[i],
+ * &szl[i], NULL) does for every i (FP64: the same bits), with hstep and szl
+ * per instance.  status[i] (may be NULL) receives each instance's pf_status;
+ * an instance that fails stops, the others go on; the return value is the
+ * first failing instance's status (PF_OK when none failed).  The handles stay
+ * owned by the caller and must outlive the batch; while a batch call runs,
+ * their work is queued on the batch's stream.
+ *
+ * pf_batch_tune times candidate launch shapes on the instances' current
+ * state (restored afterwards) and keeps the fastest: per instance the deposit
+ * mode (direct atomics, or a shared-memory tile over ranges of 1024..8192
+ * macroparticles), for the batch the macroparticles per direct tile, the FP64
+ * stage block size, the node tile length and persistent or per-tile grids.
+ * pf_batch_get_shape / pf_batch_set_shape read and override them: shape5 =
+ * {stage threads (128 or 256), macroparticles per direct tile, nodes per node
+ * tile, stage grid (0 one block per tile, -1 persistent), node grid}, modes =
+ * per instance 0 (direct) or the tile range length. */
+typedef struct pf_batch pf_batch;
+int pf_batch_create(pf_handle *const *handles, int32_t n, pf_batch **out);
+int pf_batch_destroy(pf_batch *b);
+int pf_batch_run(pf_batch *b, int32_t nsteps, int32_t isteps4diff, int32_t qdiffraction,
+                 const double *hstep, double *szl, int32_t *status);
+int pf_batch_tune(pf_batch *b, const double *hstep, const double *szl, int32_t repeats);
+int pf_batch_get_shape(const pf_batch *b, int64_t *shape5, int64_t *modes);
+int pf_batch_set_shape(pf_batch *b, const int64_t *shape5, const int64_t *modes);
+/* on = 0: launch the kernels of each block directly instead of a graph */
+int pf_batch_use_graphs(pf_batch *b, int32_t on);
+int64_t pf_batch_launches(const pf_batch *b);
+void *pf_batch_stream(const pf_batch *b);
+const char *pf_batch_last_error(const pf_batch *b);
+
 /* Block until all work queued by the handle is done. */
 int pf_sync(pf_handle *h);
 

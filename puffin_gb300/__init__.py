@@ -7,7 +7,8 @@ from .puffin import PARTICLE_KEYS, Puffin, PuffinError, rk4_step_noalloc  # noqa
 from . import lattice  # noqa: F401
 from . import adjoint  # noqa: F401
 from . import h5dump  # noqa: F401
+from .batch import Batch  # noqa: F401
 
-__all__ = ["lattice", "adjoint", "h5dump", "Puffin", "PuffinError", "rk4_step_noalloc", "Params", "default_params", "load", "library_path",
+__all__ = ["lattice", "adjoint", "h5dump", "Batch", "Puffin", "PuffinError", "rk4_step_noalloc", "Params", "default_params", "load", "library_path",
            "PARTICLE_KEYS", "FP64", "MIXED", "MESH_TEMPORAL", "MESH_PERIODIC",
            "UND_PUFFIN", "UND_HELICAL", "UND_PLANEPOLE", "UND_CURVED"]

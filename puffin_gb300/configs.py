@@ -204,3 +204,53 @@ def config4(np_=2 ** 18, seed=SEED, nsteps=3000):
     w.field = (np.zeros(n), np.zeros(n))
     w.name = "config4: periodic helical 33x33x128 (adjoint form)"
     return w
+
+
+def config5(n_inst=128, seed=SEED, nsteps=1000, np_range=(2 ** 14, 2 ** 20)):
+    """The batched form: n_inst independent periodic single-slice instances.
+    Per instance, from the seed: macroparticles log-uniform in np_range;
+    transverse mesh nx = ny in {17, 33, 65} with dx chosen so the inner-window
+    rule fits the beam (|x|, |y| <= 1.35 sigma, sigma 1.0) on the mesh; z2
+    mesh of {32, 64, 128} unique planes at 16 per resonant wavelength;
+    rho uniform in [0.002, 0.01]; energy detuning uniform in +-2 rho; aw
+    uniform in [0.7, 1.5]; helical or planepole with equal odds.  32 steps per
+    period (h = 4 pi rho / 32), diffraction every 16 steps.  Returns the list
+    of workloads (each with its own params, h and beam)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    lo, hi = math.log(np_range[0]), math.log(np_range[1])
+    for k in range(n_inst):
+        np_ = int(round(math.exp(rng.uniform(lo, hi))))
+        nx = int(rng.choice([17, 33, 65]))
+        nunique = int(rng.choice([32, 64, 128]))
+        rho = float(rng.uniform(0.002, 0.01))
+        detune = float(rng.uniform(-2.0 * rho, 2.0 * rho))
+        aw = float(rng.uniform(0.7, 1.5))
+        und = L.UND_HELICAL if rng.random() < 0.5 else L.UND_PLANEPOLE
+        gr = 500.0
+        lamr = 4.0 * PUFFIN_PI * rho
+        dz2 = lamr / 16.0
+        nz2 = nunique + 1
+        # window rule 2 (ceil(1.35 / dx) + 3) <= nx - 1
+        dx = 1.35 / ((nx - 1) / 2 - 3.5)
+        p = _base_params(rho, aw, gr, und, nx, nx, nz2, dx, dx, dz2, L.MESH_PERIODIC,
+                         sperwaves=nunique / 16.0, szfs=0.0, szfe=nsteps * lamr / 32.0)
+        lz2 = nunique * dz2
+        x = rng.standard_normal(np_ * 2)
+        x = x[np.abs(x) <= 1.35][:np_]
+        y = rng.standard_normal(np_ * 2)
+        y = y[np.abs(y) <= 1.35][:np_]
+        beam = {
+            "x": x.copy(), "y": y.copy(),
+            "z2": _quiet_z2(rng, np_, 0.0, lz2),
+            "px": 0.01 * rng.standard_normal(np_), "py": 0.01 * rng.standard_normal(np_),
+            "gam": 1.0 + detune + 5e-4 * rng.standard_normal(np_),
+            "chi": np.full(np_, 2.0 * math.pi * lz2 / np_),
+        }
+        match_in(p, beam)
+        n = p.nx * p.ny * p.nz2
+        und_name = "helical" if und == L.UND_HELICAL else "planepole"
+        out.append(Workload(f"batch instance {k}: periodic {und_name} {nx}x{nx}x{nunique}, "
+                            f"rho={rho:.4f}, aw={aw:.3f}, detuning={detune:+.4f}, np={np_}",
+                            p, lamr / 32.0, nsteps, 16, True, beam, (np.zeros(n), np.zeros(n))))
+    return out

@@ -700,9 +700,9 @@ int pf_redistribute(pf_handle *h) {
   return PF_OK;
 }
 
-int pf_diffract(pf_handle *h, double dz) {
-  if (!h) return PF_BAD_ARG;
-  cudaSetDevice(h->dev);
+}  // extern "C"
+
+int pf_diffract_enqueue(pf_handle *h, double dz) {
   int rc = pf_inner_to_outer(h);
   if (rc) return rc;
   rc = (h->p.precision == PF_MIXED) ? pf_diffract_outer_c32(h, h->oc32, dz)
@@ -712,10 +712,22 @@ int pf_diffract(pf_handle *h, double dz) {
     rc = pf_outer_to_inner(h);
     if (rc) return rc;
   }
+  return PF_OK;
+}
+
+extern "C" {
+
+int pf_diffract(pf_handle *h, double dz) {
+  if (!h) return PF_BAD_ARG;
+  cudaSetDevice(h->dev);
+  const int rc = pf_diffract_enqueue(h, dz);
+  if (rc) return rc;
   PF_CUDA(cudaStreamSynchronize(h->stream));
   pf_prof_flush(h);
   return PF_OK;
 }
+
+}  // extern "C"
 
 // Bytes of the state an asynchronous block can change: the current particle
 // buffers and the window field.
@@ -726,7 +738,7 @@ static size_t block_state_bytes(const pf_handle *h, size_t *wbytes) {
 }
 
 // Copy the block state to (save) or from (restore) the snapshot buffer.
-static int block_snapshot(pf_handle *h, bool save) {
+int pf_block_snapshot(pf_handle *h, bool save) {
   size_t wb;
   const size_t need = block_state_bytes(h, &wb);
   if (save && h->snap_cap < need) {
@@ -853,6 +865,56 @@ static int run_block_graph(pf_handle *h, int len, double hstep, double *szl) {
   return PF_OK;
 }
 
+void pf_sched_init(pf_handle *h, RunSched &s, int32_t nsteps, int32_t isteps4diff,
+                   int32_t qdiffraction, double hstep, double *szl, int32_t *steps_done) {
+  s.nsteps = nsteps;
+  s.isteps4diff = isteps4diff;
+  s.qdiffraction = qdiffraction;
+  s.hstep = hstep;
+  s.dzds = qdiffraction ? (double)isteps4diff * hstep / 2.0 : 0.0;
+  s.redist = h->p.redist_every > 0 ? h->p.redist_every : 60;
+  s.szl = szl;
+  s.steps_done = steps_done;
+  s.sync = true;
+}
+
+// What follows step istep of UndSection's loop (undulator.f90:214-330): the
+// position, the diffraction of the step's end (the half step owed plus the
+// next half step), the cumulative count and the periodic wrap.
+int pf_sched_after_step(pf_handle *h, RunSched &s, int istep) {
+  *s.szl = *s.szl + s.hstep;
+  if (s.qdiffraction && (istep % s.isteps4diff == 0 || istep == s.nsteps)) {
+    const double dzdf = s.dzds;
+    if (istep == s.nsteps) s.dzds = 0.0;
+    else if (istep + s.isteps4diff <= s.nsteps) s.dzds = (double)s.isteps4diff * s.hstep / 2;
+    else s.dzds = (double)(s.nsteps - istep) * s.hstep / 2;
+    const int r = s.sync ? pf_diffract(h, dzdf + s.dzds) : pf_diffract_enqueue(h, dzdf + s.dzds);
+    if (r) return r;
+  }
+  h->csteps++;
+  if (h->csteps % s.redist == 0) {
+    const int r = pf_wrap_z2(h);
+    if (r) return r;
+  }
+  if (s.steps_done) *s.steps_done = istep;
+  return PF_OK;
+}
+
+// One step with the reference's window retries (undulator.f90:196-212).
+int pf_sched_eager_step(pf_handle *h, RunSched &s, int istep) {
+  int tries = 0;
+  for (;;) {
+    int r = pf_rk4_step(h, *s.szl, s.hstep);
+    if (r == PF_OK) break;
+    if (r != PF_OUT_OF_WINDOW || ++tries > 3) return r;
+    r = pf_redistribute(h);  // getInNode + getLocalFieldIndices
+    if (r) return r;
+  }
+  return pf_sched_after_step(h, s, istep);
+}
+
+extern "C" {
+
 int pf_run(pf_handle *h, int32_t nsteps, int32_t isteps4diff, int32_t qdiffraction,
            double hstep, double *szl, int32_t *steps_done) {
   if (!h || !szl || nsteps < 0 || (qdiffraction && isteps4diff < 1)) return PF_BAD_ARG;
@@ -862,14 +924,14 @@ int pf_run(pf_handle *h, int32_t nsteps, int32_t isteps4diff, int32_t qdiffracti
     return PF_STATE;
   }
   cudaSetDevice(h->dev);
-  double dzds = 0.0;
+  RunSched sc;
+  pf_sched_init(h, sc, nsteps, isteps4diff, qdiffraction, hstep, szl, steps_done);
   int rc;
   if (qdiffraction) {
-    dzds = (double)isteps4diff * hstep / 2.0;
-    rc = pf_diffract(h, dzds);
+    rc = pf_diffract(h, sc.dzds);
     if (rc) return rc;
   }
-  const int redist = h->p.redist_every > 0 ? h->p.redist_every : 60;
+  const int redist = sc.redist;
   // Steps between two diffraction calls run as one asynchronous block: the
   // kernels of every step are queued without a host round trip and the status
   // word is read once at the end (a failed step makes the rest of the block a
@@ -879,42 +941,13 @@ int pf_run(pf_handle *h, int32_t nsteps, int32_t isteps4diff, int32_t qdiffracti
   // gain nothing from it and run step by step.
   size_t wb;
   const bool async_blocks = h->launch_mode >= 1 && block_state_bytes(h, &wb) <= ((size_t)256 << 20);
-  auto after_step = [&](int istep) -> int {
-    *szl = *szl + hstep;
-    if (qdiffraction && (istep % isteps4diff == 0 || istep == nsteps)) {
-      double dzdf = dzds;
-      if (istep == nsteps) dzds = 0.0;
-      else if (istep + isteps4diff <= nsteps) dzds = (double)isteps4diff * hstep / 2;
-      else dzds = (double)(nsteps - istep) * hstep / 2;
-      int r = pf_diffract(h, dzdf + dzds);
-      if (r) return r;
-    }
-    h->csteps++;
-    if (h->csteps % redist == 0) {
-      int r = pf_wrap_z2(h);
-      if (r) return r;
-    }
-    if (steps_done) *steps_done = istep;
-    return PF_OK;
-  };
-  auto eager_step = [&](int istep) -> int {
-    int tries = 0;
-    for (;;) {
-      int r = pf_rk4_step(h, *szl, hstep);
-      if (r == PF_OK) break;
-      if (r != PF_OUT_OF_WINDOW || ++tries > 3) return r;
-      r = pf_redistribute(h);  // getInNode + getLocalFieldIndices
-      if (r) return r;
-    }
-    return after_step(istep);
-  };
   int istep = 1;
   while (istep <= nsteps) {
     // the block ends at the next diffraction step (or after 16 steps)
     int last = qdiffraction ? std::min<int>(nsteps, ((istep - 1) / isteps4diff + 1) * isteps4diff)
                             : std::min<int>(nsteps, istep + 15);
     if (!async_blocks || last == istep) {
-      rc = eager_step(istep);
+      rc = pf_sched_eager_step(h, sc, istep);
       if (rc) return rc;
       ++istep;
       continue;
@@ -924,7 +957,7 @@ int pf_run(pf_handle *h, int32_t nsteps, int32_t isteps4diff, int32_t qdiffracti
     const double szl0 = *szl, n2col = h->n2col, n2col0 = h->n2col0, undgrad = h->undgrad;
     const int64_t csteps0 = h->csteps;
     const int cur0 = h->cur;
-    rc = block_snapshot(h, true);
+    rc = pf_block_snapshot(h, true);
     if (rc) return rc;
     PF_CUDA(cudaMemsetAsync(h->d_status, 0, sizeof(unsigned int), h->stream));
     const int len = last - istep + 1;
@@ -957,14 +990,14 @@ int pf_run(pf_handle *h, int32_t nsteps, int32_t isteps4diff, int32_t qdiffracti
     PF_CUDA(cudaStreamSynchronize(h->stream));
     pf_prof_flush(h);
     if (*h->h_status == 0u) {
-      rc = after_step(last);  // last step's position, diffraction and wrap
+      rc = pf_sched_after_step(h, sc, last);  // last step's position, diffraction and wrap
       if (rc) return rc;
       istep = last + 1;
       continue;
     }
     // replay the block step by step from the saved state
     h->cur = cur0;
-    rc = block_snapshot(h, false);
+    rc = pf_block_snapshot(h, false);
     if (rc) return rc;
     *szl = szl0;
     h->n2col = n2col;
@@ -972,7 +1005,7 @@ int pf_run(pf_handle *h, int32_t nsteps, int32_t isteps4diff, int32_t qdiffracti
     h->undgrad = undgrad;
     h->csteps = csteps0;
     for (int k = istep; k <= last; ++k) {
-      rc = eager_step(k);
+      rc = pf_sched_eager_step(h, sc, k);
       if (rc) return rc;
     }
     istep = last + 1;

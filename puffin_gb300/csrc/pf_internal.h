@@ -97,6 +97,21 @@ struct NodeArgs {
   const unsigned int *status;
 };
 
+// One unit of work of a batched launch: a range of macroparticles (or of
+// window nodes) of one instance of the batch.
+struct BatchTile {
+  int32_t inst, pad;
+  int64_t begin, end;
+};
+
+// Per-instance arguments of the batched periodic z2 wrap.
+struct WrapArgs {
+  double *z2[2];     // z2 of both particle buffers
+  int64_t csteps0;   // cumulative steps before the block
+  double lenz2;
+  int redist, cur0, periodic, pad;
+};
+
 struct DiffPlan;  // FFT plan (fft.cu)
 
 enum { PROF_STAGE = 0, PROF_NODES = 1, PROF_FFT = 2, PROF_DIFF = 3, PROF_OTHER = 4, PROF_N = 5 };
@@ -210,6 +225,38 @@ int pf_rk4_fp64(pf_handle *h, double szl, double hstep, unsigned int *status_out
 void pf_fill_stage_args(pf_handle *h, StageArgs &a, double h6);
 int pf_launch_stage(pf_handle *h, int stage, StageArgs &a);   // k_stage<stage>
 int pf_launch_nodes(pf_handle *h, int stage, NodeArgs &n);    // k_nodes<stage>
+// stage-kernel pointers of stage s (1..4) for particle buffer cur
+void pf_stage_pointers(pf_handle *h, StageArgs &a, int s, int cur);
+// node-kernel arguments of the handle's window
+void pf_fill_node_args(pf_handle *h, NodeArgs &n, double hstep);
+// batched FP64 launches over (instance, range) tiles; dense-mode shared
+// bytes of an instance's window (0: above the shared-memory limit)
+cudaError_t pf_stage_batch(cudaStream_t st, int stage, bool tile, const StageArgs *args,
+                           const BatchTile *tiles, int ntiles, int grid, int threads, size_t smem);
+cudaError_t pf_nodes_batch(cudaStream_t st, int stage, const NodeArgs *args,
+                           const BatchTile *tiles, int ntiles, int grid, int threads,
+                           int *step_ctr);
+cudaError_t pf_wrap_batch(cudaStream_t st, const WrapArgs *args, const BatchTile *tiles,
+                          int ntiles, int grid, const int *step_ctr);
+size_t pf_stage_tile_smem(const pf_handle *h);
+// blocks of a kernel resident on the current device at once (grid < 0 of the
+// batched launchers: a persistent grid)
+int pf_resident_blocks(const void *kernel, int threads, size_t smem);
+constexpr int PF_FT_PPB = 8192;  // largest dense-mode tile of the FP64 stage
+// batched mixed-precision launches (rk4_mixed.cu); the argument records are
+// opaque to the callers
+constexpr int PF_MX_THREADS = 512, PF_MX_PPT = 4;
+size_t pf_mixed_stage_args_bytes();
+size_t pf_mixed_node_args_bytes();
+size_t pf_mixed_tile_smem(const pf_handle *h);
+void pf_mixed_fill_stage(pf_handle *h, int stage, int cur, double hstep, int tile,
+                         const void *coef_tab, const int *step_ctr, unsigned *status, void *out);
+void pf_mixed_fill_nodes(pf_handle *h, int stage, double hstep, unsigned *status, void *out);
+cudaError_t pf_mixed_stage_batch(cudaStream_t st, int stage, const void *args,
+                                 const BatchTile *tiles, int ntiles, int grid, size_t smem);
+cudaError_t pf_mixed_nodes_batch(cudaStream_t st, int stage, const void *args,
+                                 const BatchTile *tiles, int ntiles, int grid, int threads,
+                                 int *step_ctr);
 // mixed-precision RK4 step
 int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_out);
 // stage-coefficient table entries of one step (4 entries), FP64 and FP32 forms
@@ -222,6 +269,25 @@ int pf_outer_to_inner(pf_handle *h);
 int pf_inner_to_outer(pf_handle *h);
 // diffraction
 int pf_diffract_outer(pf_handle *h, double dz);
+// inner2Outer + diffraction + outer2Inner queued on the handle's stream
+int pf_diffract_enqueue(pf_handle *h, double dz);
+// save (restore) the particles and the window field of an asynchronous block
+int pf_block_snapshot(pf_handle *h, bool save);
+
+// The schedule of pf_run (UndSection's loop) for one handle.
+struct RunSched {
+  int32_t nsteps = 0, isteps4diff = 1, qdiffraction = 0;
+  double hstep = 0.0;
+  double dzds = 0.0;  // half diffraction step owed by the previous call
+  int redist = 60;
+  double *szl = nullptr;
+  int32_t *steps_done = nullptr;
+  bool sync = true;   // false: diffraction is queued without waiting
+};
+void pf_sched_init(pf_handle *h, RunSched &s, int32_t nsteps, int32_t isteps4diff,
+                   int32_t qdiffraction, double hstep, double *szl, int32_t *steps_done);
+int pf_sched_after_step(pf_handle *h, RunSched &s, int istep);
+int pf_sched_eager_step(pf_handle *h, RunSched &s, int istep);
 // adjoint of one FP64 diffraction step over dz on split outer-mesh arrays
 int pf_diffract_adjoint_split(pf_handle *h, double *re, double *im, double dz);
 // diffraction of an interleaved complex-float outer mesh (mixed precision)

@@ -129,7 +129,7 @@ __device__ __forceinline__ double fix_to_double(u64 lo, u64 hi, double inv_scale
 // Integer addition is associative, so the tile and its flush to HBM give the
 // same bits as the direct atomics, whatever the order.
 constexpr int FT_PLANES = 3;
-constexpr int FT_PPB = 8192;  // macroparticles per block in the dense mode
+constexpr int FT_PPB = PF_FT_PPB;  // macroparticles per block in the dense mode
 constexpr int FT_THREADS = 256;
 
 struct FixTile {
@@ -318,6 +318,51 @@ __device__ __forceinline__ void stage_particle(const StageArgs &a, const int64_t
   }
 }
 
+// Dense mode of one block: macroparticles i0..i1-1 deposit into a shared
+// tile of FT_PLANES planes from the lowest plane they start from (z2 only
+// moves forward within a step, p2 > 0); the tile is then added to the window
+// accumulators, one pair of atomics per node.  Every thread of the block
+// calls it (it holds block barriers).
+template <int STAGE, bool ONED>
+__device__ __forceinline__ void stage_tile_block(const StageArgs &a, const int64_t i0,
+                                                 const int64_t i1, u64 *ftile, int &s_pzlo) {
+  const int ntr = (int)(a.nix * a.niy);
+  const int tn = FT_PLANES * ntr;
+  for (int k = threadIdx.x; k < 4 * tn; k += blockDim.x) ftile[k] = 0ull;
+  if (threadIdx.x == 0) s_pzlo = INT_MAX;
+  __syncthreads();
+  const bool halted = (*((volatile unsigned int *)a.status) != 0u);
+  int my = INT_MAX;
+  if (!halted) {
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+      const double fz = floor(a.z2[i] * a.inv_dz2);
+      if (!(fabs(fz) < 2.0e9)) continue;
+      int m = (int)fz;
+      if (a.periodic) {
+        m %= (int)a.npl;
+        if (m < 0) m += (int)a.npl;
+      }
+      my = min(my, m);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) my = min(my, __shfl_xor_sync(0xffffffffu, my, o));
+  if ((threadIdx.x & 31) == 0 && my != INT_MAX) atomicMin(&s_pzlo, my);
+  __syncthreads();
+  const FixTile t{ftile, ftile + tn, ftile + 2 * tn, ftile + 3 * tn, s_pzlo, ntr};
+  if (!halted)
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x)
+      stage_particle<STAGE, ONED, true>(a, i, t);
+  __syncthreads();
+  if (t.pzlo == INT_MAX) return;
+  for (int k = threadIdx.x; k < tn; k += blockDim.x) {
+    const int64_t plane = (int64_t)t.pzlo + k / ntr;
+    if (plane >= a.npl) break;
+    const int64_t node = plane * ntr + (k % ntr);
+    fix_add(a.acc_lo_r, a.acc_hi_r, node, t.lo_r[k], t.hi_r[k]);
+    fix_add(a.acc_lo_i, a.acc_hi_i, node, t.lo_i[k], t.hi_i[k]);
+  }
+}
+
 template <int STAGE, bool ONED, bool TILE = false>
 __global__ void __launch_bounds__(256) k_stage(const StageArgs a) {
   if constexpr (!TILE) {
@@ -326,56 +371,50 @@ __global__ void __launch_bounds__(256) k_stage(const StageArgs a) {
     if (*((volatile unsigned int *)a.status) != 0u) return;
     stage_particle<STAGE, ONED, false>(a, i, FixTile{});
   } else {
-    // dense mode: FT_PPB consecutive macroparticles per block deposit into
-    // a shared tile of FT_PLANES planes from the lowest plane they start
-    // from (z2 only moves forward within a step, p2 > 0); the tile is then
-    // added to the window accumulators, one pair of atomics per node
     extern __shared__ u64 ftile[];
     __shared__ int s_pzlo;
-    const int ntr = (int)(a.nix * a.niy);
-    const int tn = FT_PLANES * ntr;
-    for (int k = threadIdx.x; k < 4 * tn; k += FT_THREADS) ftile[k] = 0ull;
-    if (threadIdx.x == 0) s_pzlo = INT_MAX;
-    __syncthreads();
     const int64_t i0 = (int64_t)blockIdx.x * FT_PPB;
-    const int64_t i1 = min(a.np, i0 + FT_PPB);
-    const bool halted = (*((volatile unsigned int *)a.status) != 0u);
-    int my = INT_MAX;
-    if (!halted) {
-      for (int64_t i = i0 + threadIdx.x; i < i1; i += FT_THREADS) {
-        const double fz = floor(a.z2[i] * a.inv_dz2);
-        if (!(fabs(fz) < 2.0e9)) continue;
-        int m = (int)fz;
-        if (a.periodic) {
-          m %= (int)a.npl;
-          if (m < 0) m += (int)a.npl;
-        }
-        my = min(my, m);
-      }
+    stage_tile_block<STAGE, ONED>(a, i0, min(a.np, i0 + FT_PPB), ftile, s_pzlo);
+  }
+}
+
+// Batched stage: the tiles (instance, macroparticle range) of many
+// independent instances in one launch; a block walks the tiles
+// blockIdx.x, blockIdx.x + gridDim.x, ... and stages the arguments of each
+// tile's instance in shared memory.  TILE: the dense-mode deposit.
+template <int STAGE, bool TILE>
+__global__ void __launch_bounds__(256, 3) k_stage_batch(const StageArgs *__restrict__ args,
+                                                     const BatchTile *__restrict__ tiles,
+                                                     const int ntiles) {
+  __shared__ __align__(16) u64 sa_raw[sizeof(StageArgs) / 8];
+  __shared__ int s_pzlo;
+  extern __shared__ u64 ftile[];
+  static_assert(sizeof(StageArgs) % 8 == 0, "StageArgs is copied as 64-bit words");
+  const StageArgs &sa = *reinterpret_cast<const StageArgs *>(sa_raw);
+  int cur = -1;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const BatchTile tl = tiles[t];
+    if (tl.inst != cur) {
+      __syncthreads();  // the previous tile is done with the arguments
+      const u64 *src = reinterpret_cast<const u64 *>(args + tl.inst);
+      for (int k = threadIdx.x; k < (int)(sizeof(StageArgs) / 8); k += blockDim.x) sa_raw[k] = src[k];
+      cur = tl.inst;
+      __syncthreads();
     }
-    for (int o = 16; o > 0; o >>= 1) my = min(my, __shfl_xor_sync(0xffffffffu, my, o));
-    if ((threadIdx.x & 31) == 0 && my != INT_MAX) atomicMin(&s_pzlo, my);
-    __syncthreads();
-    const FixTile t{ftile, ftile + tn, ftile + 2 * tn, ftile + 3 * tn, s_pzlo, ntr};
-    if (!halted)
-      for (int64_t i = i0 + threadIdx.x; i < i1; i += FT_THREADS)
-        stage_particle<STAGE, ONED, true>(a, i, t);
-    __syncthreads();
-    if (t.pzlo == INT_MAX) return;
-    for (int k = threadIdx.x; k < tn; k += FT_THREADS) {
-      const int64_t plane = (int64_t)t.pzlo + k / ntr;
-      if (plane >= a.npl) break;
-      const int64_t node = plane * ntr + (k % ntr);
-      fix_add(a.acc_lo_r, a.acc_hi_r, node, t.lo_r[k], t.hi_r[k]);
-      fix_add(a.acc_lo_i, a.acc_hi_i, node, t.lo_i[k], t.hi_i[k]);
+    if constexpr (TILE) {
+      stage_tile_block<STAGE, false>(sa, tl.begin, tl.end, ftile, s_pzlo);
+      __syncthreads();  // the tile is reused by the next range
+    } else {
+      if (*((volatile unsigned int *)sa.status) != 0u) continue;
+      for (int64_t i = tl.begin + threadIdx.x; i < tl.end; i += blockDim.x)
+        stage_particle<STAGE, false, false>(sa, i, FixTile{});
     }
   }
 }
 
 template <int STAGE>
-__global__ void __launch_bounds__(256) k_nodes(const NodeArgs a, const double inv_scale) {
-  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= a.n) return;
+__device__ __forceinline__ void node_update(const NodeArgs &a, const int64_t n,
+                                            const double inv_scale) {
   const double dr = fix_to_double(a.acc_lo_r[n], a.acc_hi_r[n], inv_scale);
   const double di = fix_to_double(a.acc_lo_i[n], a.acc_hi_i[n], inv_scale);
   a.acc_lo_r[n] = 0ull;
@@ -403,7 +442,47 @@ __global__ void __launch_bounds__(256) k_nodes(const NodeArgs a, const double in
       a.wr[n] = wr + a.h6 * (a.d0r[n] + dr + 2.0 * a.d12r[n]);
       a.wi[n] = wi + a.h6 * (a.d0i[n] + di + 2.0 * a.d12i[n]);
     }
-    if (a.step_ctr && n == 0) *a.step_ctr += 1;
+  }
+}
+
+template <int STAGE>
+__global__ void __launch_bounds__(256) k_nodes(const NodeArgs a, const double inv_scale) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= a.n) return;
+  node_update<STAGE>(a, n, inv_scale);
+  if (STAGE == 4 && a.step_ctr && n == 0) *a.step_ctr += 1;
+}
+
+// Batched node update over (instance, node range) tiles; the last stage
+// advances the batch's step counter once.
+template <int STAGE>
+__global__ void __launch_bounds__(256) k_nodes_batch(const NodeArgs *__restrict__ args,
+                                                     const BatchTile *__restrict__ tiles,
+                                                     const int ntiles, int *step_ctr) {
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const BatchTile tl = tiles[t];
+    const NodeArgs a = args[tl.inst];
+    const double inv_scale = ldexp(1.0, -a.fix_e);
+    for (int64_t n = tl.begin + threadIdx.x; n < tl.end; n += blockDim.x)
+      node_update<STAGE>(a, n, inv_scale);
+  }
+  if (STAGE == 4 && step_ctr && blockIdx.x == 0 && threadIdx.x == 0) *step_ctr += 1;
+}
+
+// Batched periodic z2 wrap after a step of a block: instance i wraps when
+// its cumulative step count (csteps0 + steps done in the block) is a
+// multiple of its cadence; the current buffer after k steps is cur0 ^ (k & 1).
+__global__ void __launch_bounds__(256) k_wrap_batch(const WrapArgs *__restrict__ args,
+                                                    const BatchTile *__restrict__ tiles,
+                                                    const int ntiles, const int *step_ctr) {
+  const int k = *step_ctr;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const BatchTile tl = tiles[t];
+    const WrapArgs a = args[tl.inst];
+    if (!a.periodic || (a.csteps0 + k) % a.redist != 0) continue;
+    double *z2 = ((a.cur0 ^ (k & 1)) != 0) ? a.z2[1] : a.z2[0];
+    for (int64_t i = tl.begin + threadIdx.x; i < tl.end; i += blockDim.x)
+      z2[i] = z2[i] - (floor(z2[i] / a.lenz2) * a.lenz2);
   }
 }
 
@@ -684,6 +763,116 @@ void pf_fill_stage_args(pf_handle *h, StageArgs &a, double h6) {
 
 int pf_launch_stage(pf_handle *h, int stage, StageArgs &a) { return launch_stage(h, stage, a); }
 
+void pf_stage_pointers(pf_handle *h, StageArgs &a, int s, int cur) {
+  const int nxt = cur ^ 1;
+  a.x = h->y[cur][0];
+  a.y = h->y[cur][1];
+  a.z2 = h->y[cur][2];
+  a.px = h->y[cur][3];
+  a.py = h->y[cur][4];
+  a.gam = h->y[cur][5];
+  a.ar = (s == 1) ? h->wr : h->asr;
+  a.ai = (s == 1) ? h->wi : h->asi;
+  for (int j = 0; j < 6; ++j) {
+    a.kin[j] = (s == 2) ? h->k1[j] : (s == 3) ? h->ka[j] : (s == 4) ? h->kb[j] : nullptr;
+    a.kout[j] = (s == 1) ? h->k1[j] : (s == 3) ? h->kb[j] : nullptr;
+    a.kacc[j] = (s >= 2) ? h->ka[j] : nullptr;
+    a.k1[j] = h->k1[j];
+    a.ynext[j] = h->y[nxt][j];
+  }
+}
+
+void pf_fill_node_args(pf_handle *h, NodeArgs &n, double hstep) {
+  memset(&n, 0, sizeof(n));
+  n.n = h->nwin;
+  n.acc_lo_r = h->acc;
+  n.acc_hi_r = h->acc + h->wcap;
+  n.acc_lo_i = h->acc + 2 * h->wcap;
+  n.acc_hi_i = h->acc + 3 * h->wcap;
+  n.wr = h->wr;
+  n.wi = h->wi;
+  n.asr = h->asr;
+  n.asi = h->asi;
+  n.d0r = h->d0r;
+  n.d0i = h->d0i;
+  n.d12r = h->d12r;
+  n.d12i = h->d12i;
+  n.h6 = hstep / 6.0;
+  n.fix_e = h->fix_e;
+  n.status = h->d_status;
+}
+
+int pf_resident_blocks(const void *kernel, int threads, size_t smem) {
+  int dev = 0, nsm = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
+  return std::max(1, nsm * std::max(1, per_sm));
+}
+
+size_t pf_stage_tile_smem(const pf_handle *h) {
+  const size_t bytes = (size_t)4 * FT_PLANES * h->nix * h->niy * sizeof(u64);
+  return bytes <= 96 * 1024 ? bytes : 0;
+}
+
+cudaError_t pf_stage_batch(cudaStream_t st, int stage, bool tile, const StageArgs *args,
+                           const BatchTile *tiles, int ntiles, int grid, int threads, size_t smem) {
+  static std::once_flag once;
+  static cudaError_t attr = cudaSuccess;
+  std::call_once(once, [] {
+    const void *fns[] = {(const void *)k_stage_batch<1, true>, (const void *)k_stage_batch<2, true>,
+                         (const void *)k_stage_batch<3, true>, (const void *)k_stage_batch<4, true>};
+    for (const void *f : fns) {
+      const cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
+      if (e != cudaSuccess) attr = e;
+    }
+  });
+  if (attr != cudaSuccess) return attr;
+  if (ntiles <= 0) return cudaSuccess;
+  if (grid < 0) {  // persistent: the blocks that fit on the device at once
+    const void *f = tile ? (const void *)k_stage_batch<1, true> : (const void *)k_stage_batch<1, false>;
+    grid = pf_resident_blocks(f, threads, tile ? smem : 0);
+  }
+  const unsigned g = (unsigned)(grid == 0 ? ntiles : std::max(1, std::min(grid, ntiles)));
+#define PF_BATCH_CASE(S)                                                                   \
+  case S:                                                                                  \
+    if (tile) k_stage_batch<S, true><<<g, threads, smem, st>>>(args, tiles, ntiles);       \
+    else k_stage_batch<S, false><<<g, threads, 0, st>>>(args, tiles, ntiles);              \
+    break;
+  switch (stage) {
+    PF_BATCH_CASE(1)
+    PF_BATCH_CASE(2)
+    PF_BATCH_CASE(3)
+    PF_BATCH_CASE(4)
+  }
+#undef PF_BATCH_CASE
+  return cudaGetLastError();
+}
+
+cudaError_t pf_nodes_batch(cudaStream_t st, int stage, const NodeArgs *args,
+                           const BatchTile *tiles, int ntiles, int grid, int threads,
+                           int *step_ctr) {
+  if (ntiles <= 0) return cudaSuccess;
+  if (grid < 0) grid = pf_resident_blocks((const void *)k_nodes_batch<1>, threads, 0);
+  const unsigned g = (unsigned)(grid == 0 ? ntiles : std::max(1, std::min(grid, ntiles)));
+  switch (stage) {
+    case 1: k_nodes_batch<1><<<g, threads, 0, st>>>(args, tiles, ntiles, nullptr); break;
+    case 2: k_nodes_batch<2><<<g, threads, 0, st>>>(args, tiles, ntiles, nullptr); break;
+    case 3: k_nodes_batch<3><<<g, threads, 0, st>>>(args, tiles, ntiles, nullptr); break;
+    default: k_nodes_batch<4><<<g, threads, 0, st>>>(args, tiles, ntiles, step_ctr); break;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t pf_wrap_batch(cudaStream_t st, const WrapArgs *args, const BatchTile *tiles,
+                          int ntiles, int grid, const int *step_ctr) {
+  if (ntiles <= 0) return cudaSuccess;
+  if (grid < 0) grid = pf_resident_blocks((const void *)k_wrap_batch, 256, 0);
+  const unsigned g = (unsigned)(grid == 0 ? ntiles : std::max(1, std::min(grid, ntiles)));
+  k_wrap_batch<<<g, 256, 0, st>>>(args, tiles, ntiles, step_ctr);
+  return cudaGetLastError();
+}
+
 // The four stage-coefficient entries of one step at local zbar szl
 // (advances the taper state as the step itself does).
 void pf_step_coefficients(pf_handle *h, double szl, double hstep, StageCoef *out) {
@@ -719,23 +908,7 @@ int pf_rk4_fp64(pf_handle *h, double szl, double hstep, unsigned int *status_out
   }
 
   NodeArgs n;
-  memset(&n, 0, sizeof(n));
-  n.n = h->nwin;
-  n.acc_lo_r = a.acc_lo_r;
-  n.acc_hi_r = a.acc_hi_r;
-  n.acc_lo_i = a.acc_lo_i;
-  n.acc_hi_i = a.acc_hi_i;
-  n.wr = h->wr;
-  n.wi = h->wi;
-  n.asr = h->asr;
-  n.asi = h->asi;
-  n.d0r = h->d0r;
-  n.d0i = h->d0i;
-  n.d12r = h->d12r;
-  n.d12i = h->d12i;
-  n.h6 = h6;
-  n.fix_e = h->fix_e;
-  n.status = h->d_status;
+  pf_fill_node_args(h, n, hstep);
   if (h->capturing) n.step_ctr = h->step_ctr;
 
   for (int s = 1; s <= 4; ++s) {
@@ -746,15 +919,7 @@ int pf_rk4_fp64(pf_handle *h, double szl, double hstep, unsigned int *status_out
     a.kn2col = p.kappa * n2col;
     pf_stage_coefficients(p, stage_sz[s - 1], n2col, place, &a.bf);
     a.cstate = stage_c[s - 1];
-    a.ar = (s == 1) ? h->wr : h->asr;
-    a.ai = (s == 1) ? h->wi : h->asi;
-    for (int j = 0; j < 6; ++j) {
-      a.kin[j] = (s == 2) ? h->k1[j] : (s == 3) ? h->ka[j] : (s == 4) ? h->kb[j] : nullptr;
-      a.kout[j] = (s == 1) ? h->k1[j] : (s == 3) ? h->kb[j] : nullptr;
-      a.kacc[j] = (s >= 2) ? h->ka[j] : nullptr;
-      a.k1[j] = h->k1[j];
-      a.ynext[j] = h->y[nxt][j];
-    }
+    pf_stage_pointers(h, a, s, h->cur);
     int rc = launch_stage(h, s, a);
     if (rc) return rc;
     // the next stage's field is A0 + hh*d0, A0 + hh*d1, A0 + h*d2

@@ -43,6 +43,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <mutex>
 
 #include "pf_internal.h"
 
@@ -251,9 +252,12 @@ __device__ __forceinline__ bool cell_split(double t, int &ip, float &fr) {
   return true;
 }
 
+// One block's macroparticles i0 + q MX_THREADS + threadIdx.x (q < ppt,
+// below i1).  Every thread of the block calls it (it holds block barriers
+// when the tile is on).
 template <int STAGE, bool ONED>
-__global__ void __launch_bounds__(MX_THREADS) k_stage_mixed(const MixArgs a) {
-  extern __shared__ __align__(16) float tile[];  // [2][planes*ntr] (sum, comp) float2 each
+__device__ __forceinline__ void mixed_block(const MixArgs &a, const int64_t i0, const int64_t i1,
+                                            const int ppt, float *tile, int &s_pzlo) {
   const int ntr = a.nix * a.niy;
   const int tile_n = MX_TILE_PLANES * ntr;
   // [re hi | im hi | re lo | im lo], tile_n words each
@@ -261,7 +265,6 @@ __global__ void __launch_bounds__(MX_THREADS) k_stage_mixed(const MixArgs a) {
   int *thi_i = thi_r + tile_n;
   unsigned *tlo_r = reinterpret_cast<unsigned *>(thi_i + tile_n);
   unsigned *tlo_i = tlo_r + tile_n;
-  __shared__ int s_pzlo;
 
   const bool halted = (*((volatile unsigned int *)a.status) != 0u);
   if (a.tile) {
@@ -272,9 +275,9 @@ __global__ void __launch_bounds__(MX_THREADS) k_stage_mixed(const MixArgs a) {
     __syncthreads();
     int my_pzlo = INT_MAX;
 #pragma unroll
-    for (int q = 0; q < a.ppt; ++q) {
-      const int64_t i = (int64_t)blockIdx.x * (MX_THREADS * a.ppt) + q * MX_THREADS + threadIdx.x;
-      if (halted || i >= a.np) continue;
+    for (int q = 0; q < ppt; ++q) {
+      const int64_t i = i0 + q * MX_THREADS + threadIdx.x;
+      if (halted || i >= i1) continue;
       // an estimate is enough: a wrong origin only sends deposits to HBM
       const float fz = floorf(d2f_rn(a.z2[i]) * a.inv_dz2_f);
       if (!(fabsf(fz) < 1.0e9f)) continue;
@@ -292,9 +295,9 @@ __global__ void __launch_bounds__(MX_THREADS) k_stage_mixed(const MixArgs a) {
   const int pzlo = a.tile ? s_pzlo : 0;
 
 #pragma unroll 1
-  for (int q = 0; q < a.ppt; ++q) {
-    const int64_t i = (int64_t)blockIdx.x * (MX_THREADS * a.ppt) + q * MX_THREADS + threadIdx.x;
-    if (halted || i >= a.np) continue;
+  for (int q = 0; q < ppt; ++q) {
+    const int64_t i = i0 + q * MX_THREADS + threadIdx.x;
+    if (halted || i >= i1) continue;
     // FP64 state; stage values of z2, Gamma, px, py in FP64, of x, y in FP32
     const double x0 = a.x[i], yv0 = a.y[i], z0 = a.z2[i], px0 = a.px[i], py0 = a.py[i],
                  g0 = a.gam[i];
@@ -494,9 +497,7 @@ __global__ void __launch_bounds__(MX_THREADS) k_stage_mixed(const MixArgs a) {
 }
 
 template <int STAGE>
-__global__ void __launch_bounds__(256) k_nodes_mixed(const MixNodeArgs a) {
-  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= a.n) return;
+__device__ __forceinline__ void node_update_mixed(const MixNodeArgs &a, const int64_t n) {
   const float2 d = a.acc[n];
   a.acc[n] = make_float2(0.f, 0.f);
   const float2 w = a.w[n];
@@ -515,9 +516,65 @@ __global__ void __launch_bounds__(256) k_nodes_mixed(const MixNodeArgs a) {
       const float2 d0 = a.d0[n], e = a.d12[n];
       a.w[n] = make_float2(w.x + a.h6 * (d0.x + d.x + 2.f * e.x), w.y + a.h6 * (d0.y + d.y + 2.f * e.y));
     }
-    if (a.step_ctr && n == 0) *a.step_ctr += 1;
   }
 }
+
+template <int STAGE>
+__global__ void __launch_bounds__(256) k_nodes_mixed(const MixNodeArgs a) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= a.n) return;
+  node_update_mixed<STAGE>(a, n);
+  if (STAGE == 4 && a.step_ctr && n == 0) *a.step_ctr += 1;
+}
+
+template <int STAGE, bool ONED>
+__global__ void __launch_bounds__(MX_THREADS) k_stage_mixed(const MixArgs a) {
+  extern __shared__ __align__(16) float tile[];
+  __shared__ int s_pzlo;
+  const int64_t i0 = (int64_t)blockIdx.x * (MX_THREADS * a.ppt);
+  mixed_block<STAGE, ONED>(a, i0, min(a.np, i0 + (int64_t)MX_THREADS * a.ppt), a.ppt, tile, s_pzlo);
+}
+
+// Batched mixed stage over (instance, macroparticle range) tiles of at most
+// MX_THREADS * MX_PPT macroparticles; the arguments of each tile's instance
+// are staged in shared memory.
+template <int STAGE>
+__global__ void __launch_bounds__(MX_THREADS) k_stage_mixed_batch(const MixArgs *__restrict__ args,
+                                                                  const BatchTile *__restrict__ tiles,
+                                                                  const int ntiles) {
+  extern __shared__ __align__(16) float tile[];
+  __shared__ int s_pzlo;
+  __shared__ __align__(16) unsigned long long sa_raw[sizeof(MixArgs) / 8];
+  static_assert(sizeof(MixArgs) % 8 == 0, "MixArgs is copied as 64-bit words");
+  const MixArgs &sa = *reinterpret_cast<const MixArgs *>(sa_raw);
+  int cur = -1;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const BatchTile tl = tiles[t];
+    __syncthreads();  // the previous range is done with the arguments and the tile
+    if (tl.inst != cur) {
+      const unsigned long long *src = reinterpret_cast<const unsigned long long *>(args + tl.inst);
+      for (int k = threadIdx.x; k < (int)(sizeof(MixArgs) / 8); k += MX_THREADS) sa_raw[k] = src[k];
+      cur = tl.inst;
+      __syncthreads();
+    }
+    const int ppt = (int)((tl.end - tl.begin + MX_THREADS - 1) / MX_THREADS);
+    mixed_block<STAGE, false>(sa, tl.begin, tl.end, ppt, tile, s_pzlo);
+  }
+}
+
+// Batched mixed node update over (instance, node range) tiles.
+template <int STAGE>
+__global__ void __launch_bounds__(256) k_nodes_mixed_batch(const MixNodeArgs *__restrict__ args,
+                                                           const BatchTile *__restrict__ tiles,
+                                                           const int ntiles, int *step_ctr) {
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const BatchTile tl = tiles[t];
+    const MixNodeArgs a = args[tl.inst];
+    for (int64_t n = tl.begin + threadIdx.x; n < tl.end; n += blockDim.x) node_update_mixed<STAGE>(a, n);
+  }
+  if (STAGE == 4 && step_ctr && blockIdx.x == 0 && threadIdx.x == 0) *step_ctr += 1;
+}
+
 
 BFieldF to_float(const BFieldCoef &b) {
   BFieldF f;
@@ -568,24 +625,10 @@ void pf_step_coefficients_f(pf_handle *h, double szl, double hstep, void *out_) 
 
 size_t pf_step_coefficients_f_bytes() { return 4 * sizeof(StageCoefF); }
 
-int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_out) {
+// Stage arguments of the handle's state that do not change between stages.
+static void fill_mix_args(pf_handle *h, MixArgs &a, double hstep) {
   const pf_params &p = h->p;
-  const double hh = hstep * 0.5, szh = szl + hh;
-  const double stage_sz[4] = {szl, szh, szh, szl + hstep};
-  const double stage_c[4] = {0.0, hh, hh, hstep};
-  const int nxt = h->cur ^ 1;
-  // status_out == nullptr: enqueue only (a step of an asynchronous block;
-  // the caller clears the status word once per block and reads it after)
-  if (status_out) PF_CUDA(cudaMemsetAsync(h->d_status, 0, sizeof(unsigned int), h->stream));
-
-  MixArgs a;
   memset(&a, 0, sizeof(a));
-  a.x = h->y[h->cur][0];
-  a.y = h->y[h->cur][1];
-  a.z2 = h->y[h->cur][2];
-  a.px = h->y[h->cur][3];
-  a.py = h->y[h->cur][4];
-  a.gam = h->y[h->cur][5];
   a.chi = h->chi;
   a.np = h->np;
   a.h6 = hstep / 6.0;
@@ -628,12 +671,6 @@ int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_ou
   a.electrons_evolve = p.electrons_evolve;
   a.coupling = p.coupling;
   a.status = h->d_status;
-  if (h->capturing) {
-    a.coef_tab = h->coef_dev;
-    a.step_ctr = h->step_ctr;
-  }
-  const int ntr = h->nix * h->niy;
-  const size_t tile_bytes = (size_t)4 * MX_TILE_PLANES * ntr * sizeof(int);
   {
     // |chi/dV3 (1 + eta p2)/Gamma p w| below 16 chi_max/dV3 for |p| (1+eta p2)/Gamma < 16;
     // the rest goes to HBM
@@ -643,10 +680,42 @@ int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_ou
     a.fixE = 39 - e;
     a.tile_vmax = (float)ldexp(1.0, e);
   }
-  a.tile = tile_bytes <= 96 * 1024 ? 1 : 0;
-  const size_t smem = a.tile ? tile_bytes : 0;
+  a.tile = pf_mixed_tile_smem(h) > 0 ? 1 : 0;
+}
 
-  MixNodeArgs n;
+// Per-stage fields: the state and slope arrays of stage s for buffer cur.
+static void mix_stage_pointers(pf_handle *h, MixArgs &a, int s, int cur, double hstep) {
+  const double hh = hstep * 0.5;
+  const double stage_c[4] = {0.0, hh, hh, hstep};
+  const int nxt = cur ^ 1;
+  a.x = h->y[cur][0];
+  a.y = h->y[cur][1];
+  a.z2 = h->y[cur][2];
+  a.px = h->y[cur][3];
+  a.py = h->y[cur][4];
+  a.gam = h->y[cur][5];
+  a.cstate = stage_c[s - 1];
+  a.cstate_f = (float)stage_c[s - 1];
+  a.as = (const float2 *)((s == 1) ? h->w32 : h->as32);
+  // the slope arrays are FP64-sized; in this mode they hold FP32 values,
+  // except the z2 slope
+  double *const *kin = (s == 2) ? h->k1 : (s == 3) ? h->ka : (s == 4) ? h->kb : nullptr;
+  double *const *kout = (s == 1) ? h->k1 : (s == 3) ? h->kb : nullptr;
+  double *const *kacc = (s >= 2) ? h->ka : nullptr;
+  for (int j = 0; j < 6; ++j) {
+    a.kin_f[j] = kin ? (const float *)kin[j] : nullptr;
+    a.kout_f[j] = kout ? (float *)kout[j] : nullptr;
+    a.kacc_f[j] = kacc ? (float *)kacc[j] : nullptr;
+    a.k1_f[j] = (const float *)h->k1[j];
+    a.ynext[j] = h->y[nxt][j];
+  }
+  a.kin_z = kin ? kin[2] : nullptr;
+  a.kout_z = kout ? kout[2] : nullptr;
+  a.kacc_z = kacc ? kacc[2] : nullptr;
+  a.k1_z = h->k1[2];
+}
+
+static void fill_mix_nodes(pf_handle *h, MixNodeArgs &n, int s, double hstep) {
   memset(&n, 0, sizeof(n));
   n.n = h->nwin;
   n.acc = (float2 *)h->acc32;
@@ -655,20 +724,111 @@ int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_ou
   n.d0 = (float2 *)h->d0_32;
   n.d12 = (float2 *)h->d12_32;
   n.h6 = (float)(hstep / 6.0);
+  n.coef = (float)((s == 3) ? hstep : hstep * 0.5);
   n.status = h->d_status;
-  if (h->capturing) n.step_ctr = h->step_ctr;
+}
 
-  static bool attr_set = false;
-  if (!attr_set) {
+size_t pf_mixed_tile_smem(const pf_handle *h) {
+  const size_t bytes = (size_t)4 * MX_TILE_PLANES * h->nix * h->niy * sizeof(int);
+  return bytes <= 96 * 1024 ? bytes : 0;
+}
+
+size_t pf_mixed_stage_args_bytes() { return sizeof(MixArgs); }
+size_t pf_mixed_node_args_bytes() { return sizeof(MixNodeArgs); }
+
+void pf_mixed_fill_stage(pf_handle *h, int stage, int cur, double hstep, int tile,
+                         const void *coef_tab, const int *step_ctr, unsigned *status, void *out) {
+  MixArgs a;
+  fill_mix_args(h, a, hstep);
+  mix_stage_pointers(h, a, stage, cur, hstep);
+  a.tile = tile && pf_mixed_tile_smem(h) > 0 ? 1 : 0;
+  a.ppt = MX_PPT;
+  a.coef_tab = coef_tab;
+  a.step_ctr = step_ctr;
+  a.status = status;
+  memcpy(out, &a, sizeof(a));
+}
+
+void pf_mixed_fill_nodes(pf_handle *h, int stage, double hstep, unsigned *status, void *out) {
+  MixNodeArgs n;
+  fill_mix_nodes(h, n, stage, hstep);
+  n.status = status;
+  memcpy(out, &n, sizeof(n));
+}
+
+static cudaError_t mixed_attrs() {
+  static std::once_flag once;
+  static cudaError_t attr = cudaSuccess;
+  std::call_once(once, [] {
     // the tile may exceed the 48 KB default of dynamic shared memory
     const void *fns[] = {(const void *)k_stage_mixed<1, false>, (const void *)k_stage_mixed<2, false>,
                          (const void *)k_stage_mixed<3, false>, (const void *)k_stage_mixed<4, false>,
                          (const void *)k_stage_mixed<1, true>,  (const void *)k_stage_mixed<2, true>,
-                         (const void *)k_stage_mixed<3, true>,  (const void *)k_stage_mixed<4, true>};
-    for (const void *f : fns)
-      PF_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
-    attr_set = true;
+                         (const void *)k_stage_mixed<3, true>,  (const void *)k_stage_mixed<4, true>,
+                         (const void *)k_stage_mixed_batch<1>,  (const void *)k_stage_mixed_batch<2>,
+                         (const void *)k_stage_mixed_batch<3>,  (const void *)k_stage_mixed_batch<4>};
+    for (const void *f : fns) {
+      const cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
+      if (e != cudaSuccess) attr = e;
+    }
+  });
+  return attr;
+}
+
+cudaError_t pf_mixed_stage_batch(cudaStream_t st, int stage, const void *args,
+                                 const BatchTile *tiles, int ntiles, int grid, size_t smem) {
+  const cudaError_t e = mixed_attrs();
+  if (e != cudaSuccess) return e;
+  if (ntiles <= 0) return cudaSuccess;
+  if (grid < 0) grid = pf_resident_blocks((const void *)k_stage_mixed_batch<1>, MX_THREADS, smem);
+  const unsigned g = (unsigned)(grid == 0 ? ntiles : std::max(1, std::min(grid, ntiles)));
+  const MixArgs *a = (const MixArgs *)args;
+  switch (stage) {
+    case 1: k_stage_mixed_batch<1><<<g, MX_THREADS, smem, st>>>(a, tiles, ntiles); break;
+    case 2: k_stage_mixed_batch<2><<<g, MX_THREADS, smem, st>>>(a, tiles, ntiles); break;
+    case 3: k_stage_mixed_batch<3><<<g, MX_THREADS, smem, st>>>(a, tiles, ntiles); break;
+    default: k_stage_mixed_batch<4><<<g, MX_THREADS, smem, st>>>(a, tiles, ntiles); break;
   }
+  return cudaGetLastError();
+}
+
+cudaError_t pf_mixed_nodes_batch(cudaStream_t st, int stage, const void *args,
+                                 const BatchTile *tiles, int ntiles, int grid, int threads,
+                                 int *step_ctr) {
+  if (ntiles <= 0) return cudaSuccess;
+  if (grid < 0) grid = pf_resident_blocks((const void *)k_nodes_mixed_batch<1>, threads, 0);
+  const unsigned g = (unsigned)(grid == 0 ? ntiles : std::max(1, std::min(grid, ntiles)));
+  const MixNodeArgs *a = (const MixNodeArgs *)args;
+  switch (stage) {
+    case 1: k_nodes_mixed_batch<1><<<g, threads, 0, st>>>(a, tiles, ntiles, nullptr); break;
+    case 2: k_nodes_mixed_batch<2><<<g, threads, 0, st>>>(a, tiles, ntiles, nullptr); break;
+    case 3: k_nodes_mixed_batch<3><<<g, threads, 0, st>>>(a, tiles, ntiles, nullptr); break;
+    default: k_nodes_mixed_batch<4><<<g, threads, 0, st>>>(a, tiles, ntiles, step_ctr); break;
+  }
+  return cudaGetLastError();
+}
+
+int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_out) {
+  const pf_params &p = h->p;
+  const double hh = hstep * 0.5, szh = szl + hh;
+  const double stage_sz[4] = {szl, szh, szh, szl + hstep};
+  const int nxt = h->cur ^ 1;
+  // status_out == nullptr: enqueue only (a step of an asynchronous block;
+  // the caller clears the status word once per block and reads it after)
+  if (status_out) PF_CUDA(cudaMemsetAsync(h->d_status, 0, sizeof(unsigned int), h->stream));
+
+  MixArgs a;
+  fill_mix_args(h, a, hstep);
+  if (h->capturing) {
+    a.coef_tab = h->coef_dev;
+    a.step_ctr = h->step_ctr;
+  }
+  const size_t smem = a.tile ? pf_mixed_tile_smem(h) : 0;
+  MixNodeArgs n;
+  fill_mix_nodes(h, n, 1, hstep);
+  if (h->capturing) n.step_ctr = h->step_ctr;
+
+  PF_CUDA(mixed_attrs());
   // up to MX_PPT macroparticles per thread, fewer when the beam is too small
   // to give every SM two blocks
   a.ppt = (int)std::max<int64_t>(1, std::min<int64_t>(MX_PPT, h->np / ((int64_t)152 * 2 * MX_THREADS)));
@@ -685,25 +845,7 @@ int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_ou
     a.bf = to_float(bf);
     a.n2col = (float)n2col;
     a.kn2col = (float)(p.kappa * n2col);
-    a.cstate = stage_c[s - 1];
-    a.cstate_f = (float)stage_c[s - 1];
-    a.as = (const float2 *)((s == 1) ? h->w32 : h->as32);
-    // the slope arrays are FP64-sized; in this mode they hold FP32 values,
-    // except the z2 slope
-    double *const *kin = (s == 2) ? h->k1 : (s == 3) ? h->ka : (s == 4) ? h->kb : nullptr;
-    double *const *kout = (s == 1) ? h->k1 : (s == 3) ? h->kb : nullptr;
-    double *const *kacc = (s >= 2) ? h->ka : nullptr;
-    for (int j = 0; j < 6; ++j) {
-      a.kin_f[j] = kin ? (const float *)kin[j] : nullptr;
-      a.kout_f[j] = kout ? (float *)kout[j] : nullptr;
-      a.kacc_f[j] = kacc ? (float *)kacc[j] : nullptr;
-      a.k1_f[j] = (const float *)h->k1[j];
-      a.ynext[j] = h->y[nxt][j];
-    }
-    a.kin_z = kin ? kin[2] : nullptr;
-    a.kout_z = kout ? kout[2] : nullptr;
-    a.kacc_z = kacc ? kacc[2] : nullptr;
-    a.k1_z = h->k1[2];
+    mix_stage_pointers(h, a, s, h->cur, hstep);
     if (h->np > 0) {
       pf_prof_begin(h, PROF_STAGE);
 #define PF_MIX_CASE(S)                                                                 \

@@ -51,7 +51,9 @@ SYMBOLS = (
     "pf_chicane", "pf_quad", "pf_modulation", "pf_match_in", "pf_match_out",
     "pf_correct_trans", "pf_init_undulator", "pf_set_taper_profile", "pf_diffract_adjoint",
     "pf_adjoint_forward", "pf_generate_beam", "pf_set_launch_mode",
-    "pf_adjoint_backward",
+    "pf_adjoint_backward", "pf_batch_create", "pf_batch_destroy", "pf_batch_run",
+    "pf_batch_tune", "pf_batch_get_shape", "pf_batch_set_shape", "pf_batch_use_graphs",
+    "pf_batch_launches", "pf_batch_stream", "pf_batch_last_error",
 )
 NOALLOC_MAX_PARTICLES = 32768
 NOALLOC_MAX_NODES = 32768
@@ -131,6 +133,17 @@ def load(build_if_missing: bool = False):
         "pf_match_out": (ctypes.c_int, [H, f64]),
         "pf_correct_trans": (ctypes.c_int, [H]),
         "pf_init_undulator": (ctypes.c_int, [H, i32, f64, f64, f64, f64, f64, f64, i32, f64, i32]),
+        "pf_batch_create": (ctypes.c_int, [ctypes.c_void_p, i32, ctypes.POINTER(H)]),
+        "pf_batch_destroy": (ctypes.c_int, [H]),
+        "pf_batch_run": (ctypes.c_int, [H, i32, i32, i32, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_void_p]),
+        "pf_batch_tune": (ctypes.c_int, [H, ctypes.c_void_p, ctypes.c_void_p, i32]),
+        "pf_batch_get_shape": (ctypes.c_int, [H, ctypes.c_void_p, ctypes.c_void_p]),
+        "pf_batch_set_shape": (ctypes.c_int, [H, ctypes.c_void_p, ctypes.c_void_p]),
+        "pf_batch_use_graphs": (ctypes.c_int, [H, i32]),
+        "pf_batch_launches": (i64, [H]),
+        "pf_batch_stream": (ctypes.c_void_p, [H]),
+        "pf_batch_last_error": (ctypes.c_char_p, [H]),
         "pf_rk4_step_noalloc": (ctypes.c_int, [P, dp, dp, f64, f64, i64] + [ctypes.c_void_p] * 9
                                 + [i32, i32, ctypes.c_void_p]),
     }

@@ -1,0 +1,165 @@
+"""Batched runs against the same instances run one at a time.
+
+Every instance of a batch follows pf_run's schedule, so in FP64 (integer
+fixed-point deposit) the batch must give the same bits as und_section on
+each instance alone, whatever the launch shapes (graphs or not, tuned or
+not).  The mixed-precision batch deposits with float atomics whose order
+varies: it is compared at rtol 1e-5 / atol 1e-8 on the particles and 1e-4
+of the largest field value.
+
+Instances: the batched form's recipe at small sizes (macroparticles
+log-uniform in [2^10, 2^13], meshes {17, 33, 65}^2 x {32, 64, 128}), 40
+steps with diffraction every 16 (two graph blocks and a short block), and a
+wrap cadence of 12 steps on half of them so that wraps fall inside blocks.
+"""
+import numpy as np
+import pytest
+
+import puffin_gb300 as P
+from puffin_gb300 import configs
+
+pytestmark = pytest.mark.gpu
+NSTEPS, EVERY = 40, 16
+
+
+def _instances(n=6, seed=7, precision=P.FP64, np_range=(2 ** 10, 2 ** 13)):
+    ws = configs.config5(n_inst=n, seed=seed, nsteps=NSTEPS, np_range=np_range)
+    for k, w in enumerate(ws):
+        w.params.precision = precision
+        if k % 2:
+            w.params.redist_every = 12
+    return ws
+
+
+def _make(w, field_scale=1e-3):
+    sim = P.Puffin(w.params)
+    sim.set_particles(*(w.beam[k] for k in P.PARTICLE_KEYS))
+    rng = np.random.default_rng(int(w.np))
+    n = len(w.field[0])
+    sim.set_field(field_scale * rng.standard_normal(n), field_scale * rng.standard_normal(n))
+    return sim
+
+
+def _state(sim):
+    return sim.get_particles(), sim.get_field(), sim.step_count
+
+
+def _single(ws):
+    out = []
+    for w in ws:
+        with _make(w) as sim:
+            z = sim.und_section(NSTEPS, EVERY, True, w.h)
+            out.append((_state(sim), z))
+    return out
+
+
+def _assert_same(got, want, exact, tag):
+    (gp, gf, gc), gz = got
+    (wp, wf, wc), wz = want
+    assert gc == wc, tag
+    assert gz == wz, tag
+    for k in ("x", "y", "z2", "px", "py", "gam"):
+        if exact:
+            np.testing.assert_array_equal(gp[k], wp[k], err_msg=f"{tag} {k}")
+        else:
+            np.testing.assert_allclose(gp[k], wp[k], rtol=1e-5, atol=1e-8, err_msg=f"{tag} {k}")
+    for a, b in zip(gf, wf):
+        if exact:
+            np.testing.assert_array_equal(a, b, err_msg=f"{tag} field")
+        else:
+            np.testing.assert_allclose(a, b, rtol=0, atol=1e-4 * np.max(np.abs(b)),
+                                       err_msg=f"{tag} field")
+
+
+def _batch_run(ws, graphs=True, tune=False, shape=None):
+    sims = [_make(w) for w in ws]
+    hs = np.array([w.h for w in ws])
+    try:
+        with P.Batch(sims) as b:
+            b.use_graphs(graphs)
+            if tune:
+                b.tune(hs)
+            if shape:
+                b.set_shape(**shape)
+            z, st = b.run(NSTEPS, EVERY, True, hs, raise_on_error=False)
+            launches = b.kernel_launches
+        res = [(_state(s), float(z[i])) for i, s in enumerate(sims)]
+    finally:
+        for s in sims:
+            s.close()
+    return res, st, launches
+
+
+@pytest.mark.parametrize("graphs", [True, False])
+def test_fp64_batch_matches_single_runs_bitwise(graphs):
+    ws = _instances()
+    want = _single(ws)
+    got, st, launches = _batch_run(ws, graphs=graphs)
+    assert np.all(st == 0)
+    for i, (g, w) in enumerate(zip(got, want)):
+        _assert_same(g, w, True, f"instance {i}")
+    # one launch per stage kind and step (plus wraps), not per instance
+    assert launches <= NSTEPS * (4 * 3 + 1)
+
+
+def test_fp64_batch_shapes_keep_the_bits():
+    ws = _instances(n=4, seed=11)
+    want = _single(ws)
+    for shape in ({"stage_tile": 256, "stage_grid": -1, "node_tile": 1024, "node_grid": -1},
+                  {"stage_threads": 128, "stage_tile": 4096, "modes": [0, 0, 0, 0]},
+                  {"modes": [2048, 0, 8192, 4096]}):
+        if "modes" in shape and any(m > 0 for m in shape["modes"]):
+            # shared-tile modes only where the instance's window fits the tile
+            shape = dict(shape)
+            shape["modes"] = [m if w.params.nx <= 17 else 0 for m, w in zip(shape["modes"], ws)]
+        got, st, _ = _batch_run(ws, shape=shape)
+        assert np.all(st == 0)
+        for i, (g, w) in enumerate(zip(got, want)):
+            _assert_same(g, w, True, f"{shape} instance {i}")
+
+
+def test_fp64_batch_tuned():
+    ws = _instances(n=5, seed=13)
+    want = _single(ws)
+    got, st, _ = _batch_run(ws, tune=True)
+    assert np.all(st == 0)
+    for i, (g, w) in enumerate(zip(got, want)):
+        _assert_same(g, w, True, f"instance {i}")
+
+
+def test_mixed_batch_matches_single_runs():
+    ws = _instances(n=5, seed=17, precision=P.MIXED)
+    want = _single(ws)
+    got, st, _ = _batch_run(ws, tune=True)
+    assert np.all(st == 0)
+    for i, (g, w) in enumerate(zip(got, want)):
+        _assert_same(g, w, False, f"instance {i}")
+
+
+def test_window_replay_and_failure_isolation():
+    """Instance 0 starts with a window smaller than its beam: its first block
+    fails, is replayed step by step and redistributes (as pf_run does).
+    Instance 1 has a macroparticle outside the mesh: it fails with
+    PF_OUT_OF_WINDOW after the retries, and the others finish."""
+    ws = _instances(n=4, seed=19)
+    ws[0].params.nx = ws[0].params.ny = 65
+    ws[0].params.dx = ws[0].params.dy = 0.2
+    ws[0].params.nix = ws[0].params.niy = 9
+    n1 = len(ws[1].field[0])
+    ws[1].params.nix = ws[1].params.niy = 9
+    ws[1].beam["x"][5] = 100.0
+    for w in (ws[0], ws[1]):
+        n = w.params.nx * w.params.ny * w.params.nz2
+        w.field = (np.zeros(n), np.zeros(n))
+    assert len(ws[1].field[0]) == n1
+    with _make(ws[0]) as sim:
+        assert sim.window == (9, 9)
+        z = sim.und_section(NSTEPS, EVERY, True, ws[0].h)
+        assert sim.window != (9, 9)
+        want0 = (_state(sim), z)
+    want = [want0, None] + _single(ws[2:])
+    got, st, _ = _batch_run(ws)
+    assert st[0] == 0 and st[2] == 0 and st[3] == 0
+    assert st[1] == P.lib.PF_OUT_OF_WINDOW
+    for i in (0, 2, 3):
+        _assert_same(got[i], want[i], True, f"instance {i}")
