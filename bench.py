@@ -67,6 +67,13 @@ def parse():
     ap.add_argument("--batch-n", type=int, default=128,
                     help="instances of the batched form (0: skip the leg)")
     ap.add_argument("--batch-steps", type=int, default=32)
+    ap.add_argument("--batch-only", action="store_true",
+                    help="run only the batched-form leg and print its record")
+    ap.add_argument("--batch-precisions", default="fp64,mixed")
+    ap.add_argument("--no-batch-single", action="store_true",
+                    help="skip the one-at-a-time comparison of the batched form")
+    ap.add_argument("--no-batch-tune", action="store_true",
+                    help="batched form with the default shapes (persistent grids)")
     ap.add_argument("--adjoint-steps", type=int, default=256,
                     help="steps of the adjoint leg on the 33x33x128 periodic mesh (0: skip)")
     return ap.parse_args()
@@ -360,7 +367,9 @@ def batch_leg(args, dev):
            "steps": args.batch_steps, "warmup_steps": 16, "diffraction_every": 16,
            "timing": "wall clock around the run calls (host and device)", "unit": UNIT}
     launches = 0
-    for name, prec in (("fp64", P.FP64), ("mixed", P.MIXED)):
+    precs = {"fp64": P.FP64, "mixed": P.MIXED}
+    for name in args.batch_precisions.split(","):
+        prec = precs[name]
         sims = []
         try:
             for w in ws:
@@ -371,18 +380,24 @@ def batch_leg(args, dev):
                 sims.append(sim)
             hs = np.array([w.h for w in ws])
             z = np.zeros(len(ws))
-            for i, sim in enumerate(sims):        # warm-up: plans, graphs
-                z[i] = sim.und_section(16, 16, True, ws[i].h, z[i])
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            for i, sim in enumerate(sims):
-                z[i] = sim.und_section(args.batch_steps, 16, True, ws[i].h, z[i])
-            torch.cuda.synchronize()
-            t_single = time.perf_counter() - t0
-            launches += sum(s.kernel_launches for s in sims)
+            t_single = None
+            if not args.no_batch_single:
+                for i, sim in enumerate(sims):        # warm-up: plans, graphs
+                    z[i] = sim.und_section(16, 16, True, ws[i].h, z[i])
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                for i, sim in enumerate(sims):
+                    z[i] = sim.und_section(args.batch_steps, 16, True, ws[i].h, z[i])
+                torch.cuda.synchronize()
+                t_single = time.perf_counter() - t0
+                launches += sum(s.kernel_launches for s in sims)
             with P.Batch(sims) as b:
                 t0 = time.perf_counter()
-                shape = b.tune(hs, z)
+                if args.no_batch_tune:
+                    b.set_shape(stage_grid=-1, node_grid=-1)
+                    shape = b.shape()
+                else:
+                    shape = b.tune(hs, z)
                 t_tune = time.perf_counter() - t0
                 z, _ = b.run(16, 16, True, hs, z)   # warm-up: graph capture
                 torch.cuda.synchronize()
@@ -393,11 +408,12 @@ def batch_leg(args, dev):
                 launches += b.kernel_launches
             modes = shape.pop("modes")
             out[name] = {
-                "one_at_a_time": {"value": total * args.batch_steps / t_single,
-                                  "ms_per_step": 1e3 * t_single / args.batch_steps},
+                "one_at_a_time": None if t_single is None else {
+                    "value": total * args.batch_steps / t_single,
+                    "ms_per_step": 1e3 * t_single / args.batch_steps},
                 "batched": {"value": total * args.batch_steps / t_batch,
                             "ms_per_step": 1e3 * t_batch / args.batch_steps},
-                "speedup": t_single / t_batch,
+                "speedup": None if t_single is None else t_single / t_batch,
                 "tuned_shape": shape,
                 "tuned_modes": {str(int(m)): int(c) for m, c in zip(*np.unique(modes, return_counts=True))},
                 "tune_seconds": t_tune,
@@ -455,8 +471,6 @@ def run_gpu(args, rank, world):
     d2h = h2d
     sim.close()
 
-    adj = adjoint_leg(args, dev) if args.adjoint_steps > 0 else None
-    bat = batch_leg(args, dev) if args.batch_n > 0 else None
     rmx = None
     c3 = None
     if not args.no_mixed:
@@ -468,6 +482,9 @@ def run_gpu(args, rank, world):
                 c3[name] = _time_path(args, dev, prec, world, "config3", args.steps3, args.warmup)
                 c3[name]["sim"].close()
 
+    # the forms that hold many buffers run last
+    adj = adjoint_leg(args, dev) if args.adjoint_steps > 0 else None
+    bat = batch_leg(args, dev) if args.batch_n > 0 else None
     times = torch.tensor([ms, e2e_ms, rmx["ms"] if rmx else 0.0,
                           c3["fp64"]["ms"] if c3 else 0.0, c3["mixed"]["ms"] if c3 else 0.0],
                          dtype=torch.float64, device=f"cuda:{dev}")
@@ -595,6 +612,14 @@ def main():
     if args.impl == "reference":
         if rank == 0:
             print(json.dumps(run_reference(args)), flush=True)
+        return
+    if args.batch_only:
+        import torch
+        dev = int(os.environ.get("LOCAL_RANK", "0"))
+        torch.cuda.set_device(dev)
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "unit": UNIT, "batched": batch_leg(args, dev)}),
+                  flush=True)
         return
     if world > 1:
         import torch

@@ -412,16 +412,29 @@ __global__ void __launch_bounds__(256, 3) k_stage_batch(const StageArgs *__restr
   }
 }
 
+// Every input of the node is loaded before the first store (the arrays
+// could alias as far as the compiler knows), so a thread waits for HBM once.
 template <int STAGE>
 __device__ __forceinline__ void node_update(const NodeArgs &a, const int64_t n,
                                             const double inv_scale) {
-  const double dr = fix_to_double(a.acc_lo_r[n], a.acc_hi_r[n], inv_scale);
-  const double di = fix_to_double(a.acc_lo_i[n], a.acc_hi_i[n], inv_scale);
+  const u64 lr = a.acc_lo_r[n], hr = a.acc_hi_r[n], li = a.acc_lo_i[n], hi = a.acc_hi_i[n];
+  const double wr = a.wr[n], wi = a.wi[n];
+  double e0r = 0.0, e0i = 0.0, e12r = 0.0, e12i = 0.0;
+  if (STAGE == 3 || STAGE == 4) {
+    e12r = a.d12r[n];
+    e12i = a.d12i[n];
+  }
+  if (STAGE == 4) {
+    e0r = a.d0r[n];
+    e0i = a.d0i[n];
+  }
+  const unsigned st = (STAGE == 4) ? *a.status : 0u;
+  const double dr = fix_to_double(lr, hr, inv_scale);
+  const double di = fix_to_double(li, hi, inv_scale);
   a.acc_lo_r[n] = 0ull;
   a.acc_hi_r[n] = 0ull;
   a.acc_lo_i[n] = 0ull;
   a.acc_hi_i[n] = 0ull;
-  const double wr = a.wr[n], wi = a.wi[n];
   if (STAGE == 1) {
     a.d0r[n] = dr;
     a.d0i[n] = di;
@@ -435,12 +448,12 @@ __device__ __forceinline__ void node_update(const NodeArgs &a, const int64_t n,
   } else if (STAGE == 3) {
     a.asr[n] = wr + a.coef * dr;
     a.asi[n] = wi + a.coef * di;
-    a.d12r[n] = a.d12r[n] + dr;
-    a.d12i[n] = a.d12i[n] + di;
+    a.d12r[n] = e12r + dr;
+    a.d12i[n] = e12i + di;
   } else {
-    if (*a.status == 0u) {
-      a.wr[n] = wr + a.h6 * (a.d0r[n] + dr + 2.0 * a.d12r[n]);
-      a.wi[n] = wi + a.h6 * (a.d0i[n] + di + 2.0 * a.d12i[n]);
+    if (st == 0u) {
+      a.wr[n] = wr + a.h6 * (e0r + dr + 2.0 * e12r);
+      a.wi[n] = wi + a.h6 * (e0i + di + 2.0 * e12i);
     }
   }
 }

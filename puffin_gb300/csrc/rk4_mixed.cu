@@ -496,11 +496,17 @@ __device__ __forceinline__ void mixed_block(const MixArgs &a, const int64_t i0, 
   }
 }
 
+// Every input of the node is loaded before the first store (the arrays
+// could alias as far as the compiler knows), so a thread waits for HBM once.
 template <int STAGE>
 __device__ __forceinline__ void node_update_mixed(const MixNodeArgs &a, const int64_t n) {
   const float2 d = a.acc[n];
-  a.acc[n] = make_float2(0.f, 0.f);
   const float2 w = a.w[n];
+  float2 e12 = make_float2(0.f, 0.f), d0 = make_float2(0.f, 0.f);
+  if (STAGE == 3 || STAGE == 4) e12 = a.d12[n];
+  if (STAGE == 4) d0 = a.d0[n];
+  const unsigned st = (STAGE == 4) ? *a.status : 0u;
+  a.acc[n] = make_float2(0.f, 0.f);
   if (STAGE == 1) {
     a.d0[n] = d;
     a.as[n] = make_float2(w.x + a.coef * d.x, w.y + a.coef * d.y);
@@ -509,13 +515,10 @@ __device__ __forceinline__ void node_update_mixed(const MixNodeArgs &a, const in
     a.as[n] = make_float2(w.x + a.coef * d.x, w.y + a.coef * d.y);
   } else if (STAGE == 3) {
     a.as[n] = make_float2(w.x + a.coef * d.x, w.y + a.coef * d.y);
-    const float2 e = a.d12[n];
-    a.d12[n] = make_float2(e.x + d.x, e.y + d.y);
+    a.d12[n] = make_float2(e12.x + d.x, e12.y + d.y);
   } else {
-    if (*a.status == 0u) {
-      const float2 d0 = a.d0[n], e = a.d12[n];
-      a.w[n] = make_float2(w.x + a.h6 * (d0.x + d.x + 2.f * e.x), w.y + a.h6 * (d0.y + d.y + 2.f * e.y));
-    }
+    if (st == 0u)
+      a.w[n] = make_float2(w.x + a.h6 * (d0.x + d.x + 2.f * e12.x), w.y + a.h6 * (d0.y + d.y + 2.f * e12.y));
   }
 }
 
