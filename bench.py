@@ -64,6 +64,9 @@ def parse():
     ap.add_argument("--np3", type=int, default=2 ** 24,
                     help="macroparticles of the mixed-vs-FP64 leg on the config-1 mesh (0: skip)")
     ap.add_argument("--steps3", type=int, default=32)
+    ap.add_argument("--fidelity-np", type=int, default=2 ** 20,
+                    help="macroparticles of the mixed-vs-FP64 saturation leg (0: skip)")
+    ap.add_argument("--fidelity-steps", type=int, default=6000)
     ap.add_argument("--batch-n", type=int, default=128,
                     help="instances of the batched form (0: skip the leg)")
     ap.add_argument("--batch-steps", type=int, default=32)
@@ -344,6 +347,42 @@ def adjoint_leg(args, dev):
     }
 
 
+def fidelity_leg(args, dev):
+    """The mixed form's physics targets: the config-1 mesh (periodic
+    helical 21 x 21 x 64, rho 0.005, gamma_r 500) at args.fidelity_np
+    macroparticles run to saturation in FP64 and in mixed precision from the
+    same beam, the pulse energy sampled every 16 steps; the power gain length
+    of the exponential regime (fit of ln E between 1e-3 and 1e-1 of the
+    saturated energy) and the saturated energy (top of the first synchrotron
+    oscillation) of the mixed run against the FP64 run."""
+    import puffin_gb300 as P
+    from puffin_gb300 import configs, fel
+
+    curves = {}
+    t = {}
+    for name, prec in (("fp64", P.FP64), ("mixed", P.MIXED)):
+        w = configs.config1(np_=args.fidelity_np, nsteps=args.fidelity_steps)
+        w.params.precision = prec
+        w.params.device = dev
+        t0 = time.perf_counter()
+        curves[name] = fel.power_curve(w.params, w.beam, w.field, w.h, args.fidelity_steps)
+        t[name] = time.perf_counter() - t0
+    z = curves["fp64"][0]
+    cmp = fel.compare(z, curves["fp64"][1], curves["mixed"][1])
+    return {
+        "workload": "config-1 mesh run to saturation (periodic helical 21x21x64, rho 0.005)",
+        "macroparticles": args.fidelity_np, "steps": args.fidelity_steps,
+        "zbar_end": float(z[-1]), "sample_every_steps": 16,
+        "reference": "FP64 path (the oracle's GPU twin)",
+        "gain_length": cmp["gain_length"], "saturated_energy": cmp["saturated_energy"],
+        "max_energy": cmp["max_energy"],
+        "targets": {"gain_length_rel": 5e-3, "saturated_power_rel": 1e-2},
+        "within_targets": bool(abs(cmp["gain_length"]["rel_diff"]) <= 5e-3
+                               and abs(cmp["saturated_energy"]["rel_diff"]) <= 1e-2),
+        "wall_seconds": t,
+    }
+
+
 def batch_leg(args, dev):
     """The batched form: args.batch_n independent periodic single-slice
     instances (macroparticles log-uniform in [2^14, 2^20], meshes
@@ -483,6 +522,7 @@ def run_gpu(args, rank, world):
                 c3[name]["sim"].close()
 
     # the forms that hold many buffers run last
+    fid = fidelity_leg(args, dev) if args.fidelity_np > 0 and not args.no_mixed else None
     adj = adjoint_leg(args, dev) if args.adjoint_steps > 0 else None
     bat = batch_leg(args, dev) if args.batch_n > 0 else None
     times = torch.tensor([ms, e2e_ms, rmx["ms"] if rmx else 0.0,
@@ -559,6 +599,8 @@ def run_gpu(args, rank, world):
                          "peak": peak, "unit": "GB/s", "frac": m_ach / peak},
             "clocks": rmx["clocks"],
         }
+    if fid:
+        rec["mixed_fidelity"] = fid
     if adj:
         rec["adjoint"] = adj
     if bat:

@@ -95,3 +95,21 @@ def test_mixed_run_power_matches_fp64():
     assert abs(pw["mixed"] - pw["fp64"]) <= 1e-4 * pw["fp64"]
     np.testing.assert_allclose(outs["mixed"][0]["z2"], outs["fp64"][0]["z2"], rtol=1e-7, atol=1e-9)
     np.testing.assert_allclose(outs["mixed"][0]["gam"], outs["fp64"][0]["gam"], rtol=1e-7, atol=1e-9)
+
+
+def test_mixed_gain_length_and_saturation_match_fp64():
+    """The mixed form's physics targets on the config-1 mesh run to
+    saturation from a shot-noise start (2^16 macroparticles, 5120 steps,
+    zbar 0 to 10): power gain length of the exponential regime within 0.5 %
+    and saturated energy within 1 % of the FP64 run."""
+    from puffin_gb300 import fel
+    w = configs.config1(np_=2 ** 16, nsteps=5120)
+    curves = {}
+    for name, prm in (("fp64", w.params), ("mixed", mixed(w.params))):
+        curves[name] = fel.power_curve(prm, w.beam, w.field, w.h, w.nsteps)
+    z = curves["fp64"][0]
+    c = fel.compare(z, curves["fp64"][1], curves["mixed"][1])
+    zs = c["saturated_energy"]["zbar_ref"]
+    assert zs < z[-1] - 0.5, "the run must pass the first saturation"
+    assert abs(c["gain_length"]["rel_diff"]) <= 5e-3, c
+    assert abs(c["saturated_energy"]["rel_diff"]) <= 1e-2, c
