@@ -267,6 +267,8 @@ def _time_path(args, dev, precision, world, workload="config2", steps=None, warm
             step()
         e1.record(stream)
         torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
     ms = e0.elapsed_time(e1)
     out = {
         "w": w, "sim": sim, "step": step, "stream": stream, "win": win, "ms": ms,
@@ -298,6 +300,28 @@ def output_errors(r64, rmx):
         "spectrum_rel_l2": float(np.linalg.norm(smx - s64) / max(np.linalg.norm(s64), 1e-300)),
         "after_steps": r64["warmup"] + r64["steps"],
     }
+
+
+def max_over_ranks(values, world, device=None):
+    """Element-wise maximum over the ranks of a list of times (the slowest
+    rank sets the job's time); with one process the values come back as
+    they are.  The reduction runs on `device` (the GPU under NCCL; the host
+    under gloo)."""
+    if world <= 1:
+        return [float(v) for v in values]
+    import torch
+    import torch.distributed as dist
+    if device is None or dist.get_backend() == "gloo":
+        device = "cpu"
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.cpu()]
+
+
+def whole_job_rate(units_per_rank, steps, world, ms):
+    """Whole-job throughput: the units every rank processed per step, times
+    the ranks and the steps, over the (maximum) time."""
+    return world * units_per_rank * steps / (ms * 1e-3)
 
 
 def adjoint_leg(args, dev):
@@ -505,6 +529,8 @@ def run_gpu(args, rank, world):
         assert lib.pf_get_field(sim._h, fre.ctypes.data, fim.ctypes.data) == 0
     t1.record(stream)
     torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
     e2e_ms = max(t0.elapsed_time(t1), 1e-9)
     h2d = 7 * 8 * n + 2 * 8 * sim.n_outer
     d2h = h2d
@@ -525,17 +551,14 @@ def run_gpu(args, rank, world):
     fid = fidelity_leg(args, dev) if args.fidelity_np > 0 and not args.no_mixed else None
     adj = adjoint_leg(args, dev) if args.adjoint_steps > 0 else None
     bat = batch_leg(args, dev) if args.batch_n > 0 else None
-    times = torch.tensor([ms, e2e_ms, rmx["ms"] if rmx else 0.0,
-                          c3["fp64"]["ms"] if c3 else 0.0, c3["mixed"]["ms"] if c3 else 0.0],
-                         dtype=torch.float64, device=f"cuda:{dev}")
-    if world > 1:
-        torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
-    ms, e2e_ms, mx_ms, c3_64_ms, c3_mx_ms = (float(v) for v in times)
+    ms, e2e_ms, mx_ms, c3_64_ms, c3_mx_ms = max_over_ranks(
+        [ms, e2e_ms, rmx["ms"] if rmx else 0.0, c3["fp64"]["ms"] if c3 else 0.0,
+         c3["mixed"]["ms"] if c3 else 0.0], world, f"cuda:{dev}")
     if rank != 0:
         return None
 
-    value = world * n * args.steps / (ms * 1e-3)
-    e2e_value = world * n * args.e2e_steps / (e2e_ms * 1e-3) if args.e2e_steps > 0 else None
+    value = whole_job_rate(n, args.steps, world, ms)
+    e2e_value = whole_job_rate(n, args.e2e_steps, world, e2e_ms) if args.e2e_steps > 0 else None
     peak, peak_kind = measured_peaks()
     stage_ms, stage_n = r64["kernel"]["stage"]
     stage_avg = stage_ms / max(1, stage_n)
@@ -587,7 +610,7 @@ def run_gpu(args, rank, world):
         m_ach = n * BYTES_PER_PARTICLE_STAGE / (mavg * 1e-3) / 1e9
         mk = {k: v[0] for k, v in rmx["kernel"].items()}
         rec["mixed"] = {
-            "value": world * n * args.steps / (mx_ms * 1e-3), "unit": UNIT,
+            "value": whole_job_rate(n, args.steps, world, mx_ms), "unit": UNIT,
             "ms_per_step": mx_ms / args.steps, "speedup_vs_fp64": ms / mx_ms,
             "dtype": "f32 field/weights/deposit/FFT, f64 state/p2/RK4 combination",
             "power_rel_error_vs_fp64": abs(rmx["power"] - r64["power"]) / max(r64["power"], 1e-300),
@@ -613,10 +636,10 @@ def run_gpu(args, rank, world):
             "workload": w3.name, "macroparticles": n3,
             "mesh": [w3.params.nx, w3.params.ny, w3.params.nz2],
             "steps": args.steps3, "warmup": args.warmup,
-            "fp64": {"value": world * n3 * args.steps3 / (c3_64_ms * 1e-3),
+            "fp64": {"value": whole_job_rate(n3, args.steps3, world, c3_64_ms),
                      "ms_per_step": c3_64_ms / args.steps3,
                      "kernel_ms": {k: v[0] for k, v in c3["fp64"]["kernel"].items()}},
-            "mixed": {"value": world * n3 * args.steps3 / (c3_mx_ms * 1e-3),
+            "mixed": {"value": whole_job_rate(n3, args.steps3, world, c3_mx_ms),
                       "ms_per_step": c3_mx_ms / args.steps3,
                       "kernel_ms": {k: v[0] for k, v in c3["mixed"]["kernel"].items()}},
             "speedup_vs_fp64": c3_64_ms / c3_mx_ms,
