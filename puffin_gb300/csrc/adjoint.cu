@@ -328,8 +328,11 @@ __global__ void k_adj_nodes(int64_t n, const double *lwr, const double *lwi, dou
   nui[t] = ca * lwi[t] + cb * ai;
   lsr[t] += ar;
   lsi[t] += ai;
-  lar[t] = 0.0;
-  lai[t] = 0.0;
+  // zeros computed from the loaded values, so that the stores issue once
+  // the loads have returned (a constant store to an address whose load is
+  // in flight is several times slower)
+  lar[t] = ar - ar;
+  lai[t] = ai - ai;
 }
 
 __global__ void k_scale2(int64_t n, const double *xr, const double *xi, double *yr, double *yi,

@@ -506,7 +506,6 @@ __device__ __forceinline__ void node_update_mixed(const MixNodeArgs &a, const in
   if (STAGE == 3 || STAGE == 4) e12 = a.d12[n];
   if (STAGE == 4) d0 = a.d0[n];
   const unsigned st = (STAGE == 4) ? *a.status : 0u;
-  a.acc[n] = make_float2(0.f, 0.f);
   if (STAGE == 1) {
     a.d0[n] = d;
     a.as[n] = make_float2(w.x + a.coef * d.x, w.y + a.coef * d.y);
@@ -520,6 +519,11 @@ __device__ __forceinline__ void node_update_mixed(const MixNodeArgs &a, const in
     if (st == 0u)
       a.w[n] = make_float2(w.x + a.h6 * (d0.x + d.x + 2.f * e12.x), w.y + a.h6 * (d0.y + d.y + 2.f * e12.y));
   }
+  // The accumulator is cleared last, with zeros computed from the loaded
+  // value (d - d is +0 for the finite sums of a run): a store of a constant
+  // to an address whose load is still in flight is several times slower on
+  // this GPU than the same store issued once the load has returned.
+  a.acc[n] = make_float2(d.x - d.x, d.y - d.y);
 }
 
 template <int STAGE>
