@@ -77,6 +77,8 @@ struct FftArgs {
   int second;    // run the opposite transform after the mid operation
   int load_split, store_split;
   int mirror;    // periodic: also write plane nz (mirror of plane 0) of the output
+  // four-step z2 transform: w_N^(b k1) at [k1 * N2 + b], forward and backward
+  const cplx *tw4f, *tw4b;
 };
 
 __device__ __forceinline__ int64_t line_base(const AxisPlan &p, int64_t L) {
@@ -555,9 +557,9 @@ __global__ void k_elementwise(const FftArgs a) {
 
 // ---- in-place kernels specialised per transform length ------------------------
 // The transverse-plane kernel (a whole nx*ny plane per block: the x and y
-// transforms of one pass over HBM) and the long-line kernel (G adjacent z2
-// lines per block, so that every 32-byte sector of the strided z2 axis is
-// used in full) hold their data in a single shared buffer.  A pass stages the
+// transforms of one pass over HBM) and the four-step z2 kernels (G adjacent
+// z2 lines per block, so that the strided z2 axis is read in whole 256-byte
+// segments) hold their data in a single shared buffer.  A pass stages the
 // inputs of each thread's butterflies in registers, the block syncs, and the
 // outputs overwrite the inputs.  Lengths, radices and line counts are
 // template constants, so each pass is straight-line code with constant index
@@ -740,42 +742,75 @@ __global__ void __launch_bounds__(PT, 1) k_fft_plane(const FftArgs a) {
   for (int t = threadIdx.x; t < plane; t += PT) store(a, off + t, buf[sw(t)]);
 }
 
-// Long lines (the z2 axis): G adjacent lines per block, lines padded by one
-// element in shared memory; consecutive threads load consecutive lines,
-// which are adjacent in HBM.
-template <int N, int G>
-__global__ void __launch_bounds__(PT, 1) k_fft_long(const FftArgs a) {
+// The z2 axis as a four-step transform, N = N1 * N2: z = N2 a + b
+// (a < N1, b < N2), kz = k1 + N1 k2, and
+//   X[k1 + N1 k2] = sum_b w_N2^(b k2) w_N^(b k1) sum_a x[N2 a + b] w_N1^(a k1).
+// The fused pass "forward, mid operation at kz, inverse" of a diffraction
+// step becomes three kernels, each reading and writing the mesh once, in
+// place:
+//   STEP 0, block (b, lines): DFT over a -> k1, times w_N^(b k1); element k1
+//           goes to plane N2 k1 + b;
+//   STEP 1, block (k1, lines): DFT over b -> k2 (plane N2 k1 + k2 holds
+//           kz = k1 + N1 k2), the mid operation, inverse DFT over k2 -> b,
+//           times w_N^(-b k1);
+//   STEP 2, block (b, lines): inverse DFT over k1 -> a (plane N2 a + b).
+// A block holds G adjacent lines (adjacent in HBM: whole 256-byte segments
+// per plane) of one short transform, about 33 KB, so several blocks share an
+// SM.  The short transforms are the in-place shared-memory passes above, with
+// their plans in a.ax (length N1) and a.ay (length N2).
+template <int N1, int N2, int G, int STEP>
+__global__ void __launch_bounds__(PT) k_z4(const FftArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx *buf = reinterpret_cast<cplx *>(smem_raw);
-  const AxisPlan &p = a.ax;
-  constexpr int ls = N + 1;
-  const int64_t L0 = (int64_t)blockIdx.x * G;
-  const int nl = (int)min((int64_t)G, p.nlines - L0);
-  for (int t = threadIdx.x; t < nl * N; t += PT) {
+  constexpr int M = (STEP == 1) ? N2 : N1;  // length of this step's transforms
+  constexpr int ls = M + 1;
+  const int64_t plane = (int64_t)a.T.nx * a.T.ny;  // = number of lines
+  const int64_t ngroups = (plane + G - 1) / G;
+  const int64_t grp = (int64_t)blockIdx.x % ngroups;
+  const int f = (int)((int64_t)blockIdx.x / ngroups);  // b (steps 0, 2) or k1 (step 1)
+  const int64_t L0 = grp * G;
+  const int nl = (int)min((int64_t)G, plane - L0);
+  auto pos_of = [&](int l, int j) -> int64_t {
+    const int64_t pz = (STEP == 1) ? (int64_t)N2 * f + j : (int64_t)N2 * j + f;
+    return pz * plane + L0 + l;
+  };
+  for (int t = threadIdx.x; t < nl * M; t += PT) {
     const int l = t % nl, j = t / nl;
-    load_async(buf + sw(l * ls + j), a, line_base(p, L0 + l) + (int64_t)j * p.stride);
+    load_async(buf + sw(l * ls + j), a, pos_of(l, j));
   }
   cp_async_wait_all();
   __syncthreads();
-  if (a.dir) ip_transform<N, G, true>(buf, nl, ls, 1, a.tw_b, p);
-  else ip_transform<N, G, false>(buf, nl, ls, 1, a.tw_f, p);
-  if (a.mid != MID_NONE) {
-    for (int t = threadIdx.x; t < nl * N; t += PT) {
-      const int l = t / N, j = t - l * N;
-      int x, y, z;
-      coords(p, a.T, L0 + l, j, x, y, z);
-      const int64_t pos = line_base(p, L0 + l) + (int64_t)j * p.stride;
-      buf[sw(l * ls + j)] = mid_op(a, pos, x, y, z, buf[sw(l * ls + j)]);
+  if constexpr (STEP == 0) {
+    ip_transform<N1, G, false>(buf, nl, ls, 1, a.tw_f, a.ax);
+    // consecutive threads take adjacent lines: one twiddle per warp, and
+    // conflict-free shared slots (line stride M + 1)
+    for (int t = threadIdx.x; t < nl * M; t += PT) {
+      const int l = t % nl, k1 = t / nl;
+      buf[sw(l * ls + k1)] = cmul(buf[sw(l * ls + k1)], a.tw4f[k1 * N2 + f]);
     }
     __syncthreads();
-    if (a.second) {
-      if (!a.dir) ip_transform<N, G, true>(buf, nl, ls, 1, a.tw_b, p);
-      else ip_transform<N, G, false>(buf, nl, ls, 1, a.tw_f, p);
+  } else if constexpr (STEP == 1) {
+    ip_transform<N2, G, false>(buf, nl, ls, 1, a.tw_f, a.ay);
+    // adjacent lines are adjacent x: coalesced reads of the (x, kz) tables
+    for (int t = threadIdx.x; t < nl * M; t += PT) {
+      const int l = t % nl, k2 = t / nl;
+      const int64_t L = L0 + l;
+      buf[sw(l * ls + k2)] = mid_op(a, 0, (int)(L % a.T.nx), (int)(L / a.T.nx), f + N1 * k2,
+                                    buf[sw(l * ls + k2)]);
     }
+    __syncthreads();
+    ip_transform<N2, G, true>(buf, nl, ls, 1, a.tw_b, a.ay);
+    for (int t = threadIdx.x; t < nl * M; t += PT) {
+      const int l = t % nl, b = t / nl;
+      buf[sw(l * ls + b)] = cmul(buf[sw(l * ls + b)], a.tw4b[f * N2 + b]);
+    }
+    __syncthreads();
+  } else {
+    ip_transform<N1, G, true>(buf, nl, ls, 1, a.tw_b, a.ax);
   }
-  for (int t = threadIdx.x; t < nl * N; t += PT) {
+  for (int t = threadIdx.x; t < nl * M; t += PT) {
     const int l = t % nl, j = t / nl;
-    store(a, line_base(p, L0 + l) + (int64_t)j * p.stride, buf[sw(l * ls + j)]);
+    store(a, pos_of(l, j), buf[sw(l * ls + j)]);
   }
 }
 
@@ -786,10 +821,6 @@ struct PlaneKernel {
   int nx, ny;
   FftKernel fn;
 };
-struct LongKernel {
-  int n, g;
-  FftKernel fn;
-};
 
 static const PlaneKernel kPlaneKernels[] = {
     {17, 17, k_fft_plane<17, 17>}, {21, 21, k_fft_plane<21, 21>}, {33, 33, k_fft_plane<33, 33>},
@@ -798,10 +829,17 @@ static const PlaneKernel kPlaneKernels[] = {
     {129, 129, k_fft_plane<129, 129>},
 #endif
 };
-static const LongKernel kLongKernels[] = {
-    {2048, (sizeof(real) == 4) ? 4 : 2, k_fft_long<2048, (sizeof(real) == 4) ? 4 : 2>},
-    {4096, (sizeof(real) == 4) ? 4 : 2, k_fft_long<4096, (sizeof(real) == 4) ? 4 : 2>},
+// four-step z2 transforms (N = n1 * n2) with g lines per block
+constexpr int ZG = (sizeof(real) == 4) ? 64 : 32;
+struct Z4Kernel {
+  int n1, n2, g;
+  FftKernel k[3];
 };
+static const Z4Kernel kZ4Kernels[] = {
+    {64, 64, ZG, {k_z4<64, 64, ZG, 0>, k_z4<64, 64, ZG, 1>, k_z4<64, 64, ZG, 2>}},
+    {64, 32, ZG, {k_z4<64, 32, ZG, 0>, k_z4<64, 32, ZG, 1>, k_z4<64, 32, ZG, 2>}},
+};
+
 
 // per-call tables: propagator and damping factors for step h
 __global__ void k_tables(cplx *px, cplx *py, real *dxt, real *dyt, const double *kx,
@@ -838,9 +876,10 @@ struct Plan {
   size_t smem[3] = {0, 0, 0};
   FftKernel plane = nullptr;  // x and y in one k_fft_plane pass
   size_t plane_smem = 0;
-  FftKernel zlong = nullptr;  // z2 with k_fft_long
-  AxisPlan axl;               // the z2 plan of k_fft_long (its own lines per block)
-  size_t zlong_smem = 0;
+  const Z4Kernel *z4 = nullptr;  // four-step z2 transform, when N factors
+  AxisPlan z4p1, z4p2;            // plans of the N1 and N2 transforms
+  cplx *tw4 = nullptr;            // w_N^(b k1), forward then backward
+  size_t z4_smem = 0;
   cplx *A = nullptr, *anb = nullptr;
   cplx *tw = nullptr;  // forward block then backward block
   size_t ntw = 0;
@@ -855,7 +894,7 @@ struct Plan {
 static void destroy(Plan *d) {
   if (!d) return;
   void *ptrs[] = {d->A, d->anb, d->tw, d->px, d->py, d->dxt, d->dyt,
-                  d->kx, d->ky, d->kz, d->mask, d->mz, d->zflag};
+                  d->kx, d->ky, d->kz, d->mask, d->mz, d->zflag, d->tw4};
   for (void *q : ptrs) cudaFree(q);
   delete d;
 }
@@ -1013,17 +1052,54 @@ static int build_plan(pf_handle *h, Plan *&out) {
                                    max_smem));
     }
   if (d->plane_smem > (size_t)max_smem) d->plane = nullptr;
-  // long z2 lines: G adjacent lines per block fill whole 32-byte sectors
-  for (const LongKernel &k : kLongKernels)
-    if (k.n == d->nz && d->ax[2].lpb < k.g && d->ax[2].nlines >= k.g) {
-      d->zlong = k.fn;
-      d->axl = d->ax[2];
-      d->axl.lpb = k.g;
-      d->zlong_smem = (((size_t)k.g * (k.n + 1) + 15) / 16) * 16 * sizeof(cplx);
-      PF_CUDA(cudaFuncSetAttribute((const void *)k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   max_smem));
+  // four-step z2 transform: sub-plans of lengths N1 and N2 (their twiddles
+  // appended to the pass tables) and the w_N^(b k1) table
+  std::vector<cplx> tw4;
+  for (const Z4Kernel &k : kZ4Kernels)
+    if (k.n1 * k.n2 == d->nz && !d->z4) {
+      AxisPlan *sp[2] = {&d->z4p1, &d->z4p2};
+      const int sn[2] = {k.n1, k.n2};
+      for (int q = 0; q < 2; ++q) {
+        AxisPlan &ap = *sp[q];
+        memset(&ap, 0, sizeof(ap));
+        ap.axis = 2;
+        ap.n = sn[q];
+        const std::vector<int> f = factorize(sn[q]);
+        ap.npass = (int)f.size();
+        int ns = 1;
+        for (int ps = 0; ps < ap.npass; ++ps) {
+          const int R = f[ps];
+          ap.radix[ps] = R;
+          ap.ns[ps] = ns;
+          ap.twoff[ps] = (int)tab.size();
+          for (int kk = 0; kk < ns; ++kk)
+            for (int r = 0; r < R; ++r) {
+              const double ang = -2.0 * PF_FULL_PI * (double)(kk * r) / (double)(ns * R);
+              tab.push_back(cplx{(real)cos(ang), (real)sin(ang)});
+              tabb.push_back(cplx{(real)cos(ang), (real)-sin(ang)});
+            }
+          ns *= R;
+        }
+      }
+      tw4.resize((size_t)2 * d->nz);
+      for (int k1 = 0; k1 < k.n1; ++k1)
+        for (int b = 0; b < k.n2; ++b) {
+          const double ang = -2.0 * PF_FULL_PI * (double)(b * k1) / (double)d->nz;
+          tw4[(size_t)k1 * k.n2 + b] = cplx{(real)cos(ang), (real)sin(ang)};
+          tw4[(size_t)d->nz + (size_t)k1 * k.n2 + b] = cplx{(real)cos(ang), (real)-sin(ang)};
+        }
+      const int m = std::max(k.n1, k.n2);
+      d->z4_smem = (((size_t)k.g * (m + 1) + 15) / 16) * 16 * sizeof(cplx);
+      if (d->z4_smem > (size_t)max_smem) continue;
+      for (int q = 0; q < 3; ++q)
+        PF_CUDA(cudaFuncSetAttribute((const void *)k.k[q],
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+      d->z4 = &k;
     }
-  if (d->zlong_smem > (size_t)max_smem) d->zlong = nullptr;
+  if (d->z4) {
+    PF_CUDA(cudaMalloc(&d->tw4, tw4.size() * sizeof(cplx)));
+    PF_CUDA(cudaMemcpy(d->tw4, tw4.data(), tw4.size() * sizeof(cplx), cudaMemcpyHostToDevice));
+  }
   d->ntw = tab.size();
   if (d->ntw) {
     PF_CUDA(cudaMalloc(&d->tw, 2 * d->ntw * sizeof(cplx)));
@@ -1116,13 +1192,21 @@ static int fft_pass(pf_handle *h, Plan *d, FftArgs a, int axis) {
     }
     return PF_OK;
   }
-  if (axis == 2 && d->zlong) {
-    a.ax = d->axl;
-    const int64_t blocks = (a.ax.nlines + a.ax.lpb - 1) / a.ax.lpb;
-    pf_prof_begin(h, PROF_FFT);
-    d->zlong<<<(unsigned)blocks, PT, d->zlong_smem, h->stream>>>(a);
-    pf_prof_end(h);
-    PF_LAUNCHED(h);
+  if (axis == 2 && d->z4 && a.dir == 0 && a.second && !a.load_split && !a.store_split &&
+      (a.mid == MID_PROP || a.mid == MID_DAMP)) {
+    const Z4Kernel &k = *d->z4;
+    a.ax = d->z4p1;
+    a.ay = d->z4p2;
+    a.tw4f = d->tw4;
+    a.tw4b = d->tw4 + d->nz;
+    const int64_t ngroups = ((int64_t)d->nx * d->ny + k.g - 1) / k.g;
+    for (int q = 0; q < 3; ++q) {
+      const int64_t blocks = ngroups * (q == 1 ? k.n1 : k.n2);
+      pf_prof_begin(h, PROF_FFT);
+      k.k[q]<<<(unsigned)blocks, PT, d->z4_smem, h->stream>>>(a);
+      pf_prof_end(h);
+      PF_LAUNCHED(h);
+    }
     return PF_OK;
   }
   const int64_t blocks = (a.ax.nlines + a.ax.lpb - 1) / a.ax.lpb;
