@@ -759,59 +759,57 @@ __global__ void __launch_bounds__(PT, 1) k_fft_plane(const FftArgs a) {
 // SM.  The short transforms are the in-place shared-memory passes above, with
 // their plans in a.ax (length N1) and a.ay (length N2).
 template <int N1, int N2, int G, int STEP>
-__global__ void __launch_bounds__(PT) k_z4(const FftArgs a) {
+__global__ void __launch_bounds__(PT, (sizeof(real) == 4) ? 3 : 2) k_z4(const FftArgs a) {
+  static_assert(PT % G == 0, "a thread keeps one line of its group");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx *buf = reinterpret_cast<cplx *>(smem_raw);
   constexpr int M = (STEP == 1) ? N2 : N1;  // length of this step's transforms
   constexpr int ls = M + 1;
+  constexpr int JS = PT / G;                 // element stride of a thread's loops
   const int64_t plane = (int64_t)a.T.nx * a.T.ny;  // = number of lines
   const int64_t ngroups = (plane + G - 1) / G;
   const int64_t grp = (int64_t)blockIdx.x % ngroups;
   const int f = (int)((int64_t)blockIdx.x / ngroups);  // b (steps 0, 2) or k1 (step 1)
   const int64_t L0 = grp * G;
   const int nl = (int)min((int64_t)G, plane - L0);
-  auto pos_of = [&](int l, int j) -> int64_t {
+  // every element loop: consecutive threads take adjacent lines (adjacent in
+  // HBM, conflict-free shared slots), and a thread's line never changes
+  const int l = threadIdx.x % G, j0 = threadIdx.x / G;
+  const bool on = l < nl;
+  auto pos_of = [&](int j) -> int64_t {
     const int64_t pz = (STEP == 1) ? (int64_t)N2 * f + j : (int64_t)N2 * j + f;
     return pz * plane + L0 + l;
   };
-  for (int t = threadIdx.x; t < nl * M; t += PT) {
-    const int l = t % nl, j = t / nl;
-    load_async(buf + sw(l * ls + j), a, pos_of(l, j));
-  }
+  if (on)
+    for (int j = j0; j < M; j += JS) load_async(buf + sw(l * ls + j), a, pos_of(j));
   cp_async_wait_all();
   __syncthreads();
   if constexpr (STEP == 0) {
     ip_transform<N1, G, false>(buf, nl, ls, 1, a.tw_f, a.ax);
-    // consecutive threads take adjacent lines: one twiddle per warp, and
-    // conflict-free shared slots (line stride M + 1)
-    for (int t = threadIdx.x; t < nl * M; t += PT) {
-      const int l = t % nl, k1 = t / nl;
-      buf[sw(l * ls + k1)] = cmul(buf[sw(l * ls + k1)], a.tw4f[k1 * N2 + f]);
-    }
+    if (on)
+      for (int k1 = j0; k1 < M; k1 += JS)
+        buf[sw(l * ls + k1)] = cmul(buf[sw(l * ls + k1)], a.tw4f[k1 * N2 + f]);
     __syncthreads();
   } else if constexpr (STEP == 1) {
     ip_transform<N2, G, false>(buf, nl, ls, 1, a.tw_f, a.ay);
-    // adjacent lines are adjacent x: coalesced reads of the (x, kz) tables
-    for (int t = threadIdx.x; t < nl * M; t += PT) {
-      const int l = t % nl, k2 = t / nl;
-      const int64_t L = L0 + l;
-      buf[sw(l * ls + k2)] = mid_op(a, 0, (int)(L % a.T.nx), (int)(L / a.T.nx), f + N1 * k2,
-                                    buf[sw(l * ls + k2)]);
+    if (on) {
+      // adjacent lines are adjacent x: coalesced reads of the (x, kz) tables
+      const int L = (int)(L0 + l);
+      const int x = L % a.T.nx, y = L / a.T.nx;
+      for (int k2 = j0; k2 < M; k2 += JS)
+        buf[sw(l * ls + k2)] = mid_op(a, 0, x, y, f + N1 * k2, buf[sw(l * ls + k2)]);
     }
     __syncthreads();
     ip_transform<N2, G, true>(buf, nl, ls, 1, a.tw_b, a.ay);
-    for (int t = threadIdx.x; t < nl * M; t += PT) {
-      const int l = t % nl, b = t / nl;
-      buf[sw(l * ls + b)] = cmul(buf[sw(l * ls + b)], a.tw4b[f * N2 + b]);
-    }
+    if (on)
+      for (int b = j0; b < M; b += JS)
+        buf[sw(l * ls + b)] = cmul(buf[sw(l * ls + b)], a.tw4b[f * N2 + b]);
     __syncthreads();
   } else {
     ip_transform<N1, G, true>(buf, nl, ls, 1, a.tw_b, a.ax);
   }
-  for (int t = threadIdx.x; t < nl * M; t += PT) {
-    const int l = t % nl, j = t / nl;
-    store(a, pos_of(l, j), buf[sw(l * ls + j)]);
-  }
+  if (on)
+    for (int j = j0; j < M; j += JS) store(a, pos_of(j), buf[sw(l * ls + j)]);
 }
 
 // Instantiated transverse planes (square meshes of the workloads) and long
