@@ -45,6 +45,10 @@ sys.path.insert(0, ROOT)
 METRIC = "macroparticle-RK4-steps/s: mixed vs FP64 on GB300 at stated power error"
 UNIT = "macroparticle-steps/s"
 BYTES_PER_PARTICLE_STAGE = 104          # 56 B read + 48 B write (416 B per step)
+# DRAM read + write of one FP64 stage launch per macroparticle, from one ncu
+# capture of k_stage<3> on 2^22 macroparticles (the traffic grows with the
+# macroparticles; the window field is read from L2)
+TRAFFIC_PER_PARTICLE_STAGE = 807.2e6 / 4194304
 FLOPS_PER_PARTICLE_STAGE = 166          # ~664 FP64 flop per particle-step
 
 
@@ -598,7 +602,10 @@ def run_gpu(args, rank, world):
         "kernel_ms": kern,
         "roofline": {"kernel": "k_stage (fused FP64 RK4 stage)", "bound": "hbm",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_kind": f"{peak_kind} copy bandwidth (burst)", "traffic": None,
+                     "peak_kind": f"{peak_kind} copy bandwidth (burst)",
+                     "traffic": n * TRAFFIC_PER_PARTICLE_STAGE,
+                     "traffic_source": "ncu dram bytes of k_stage<3> at 2^22 macroparticles, "
+                                       "scaled to the launch's macroparticles",
                      "fp64": {"achieved_tflops": fp64_achieved, "peak_tflops": dgemm_tflops,
                               "peak_kind": "measured cuBLAS DGEMM 4096^3",
                               "frac": fp64_achieved / dgemm_tflops}},
