@@ -30,6 +30,7 @@
 
 #include <algorithm>
 #include <map>
+#include <mutex>
 #include <string>
 #include <tuple>
 #include <vector>
@@ -52,6 +53,20 @@ constexpr int64_t WRAP_TILE = 16384;
 // macroparticles per shared-tile range; cached by instance shape
 typedef std::tuple<int, int, int, int64_t, int64_t> ModeKey;  // precision, nix, niy, npl, np
 std::map<ModeKey, int64_t> g_mode_cache;
+std::mutex g_mode_mutex;  // batches may be tuned from several host threads
+
+bool cached_mode(const ModeKey &key, int64_t *mode) {
+  std::lock_guard<std::mutex> lock(g_mode_mutex);
+  auto it = g_mode_cache.find(key);
+  if (it == g_mode_cache.end()) return false;
+  *mode = it->second;
+  return true;
+}
+
+void cache_mode(const ModeKey &key, int64_t mode) {
+  std::lock_guard<std::mutex> lock(g_mode_mutex);
+  g_mode_cache[key] = mode;
+}
 
 }  // namespace
 
@@ -755,11 +770,7 @@ int pf_batch_tune(pf_batch *b, const double *hstep, const double *szl, int32_t r
     for (int i = 0; i < b->n && out == PF_OK; ++i) {
       const pf_handle *h = b->inst[i];
       const ModeKey key{b->mixed ? 1 : 0, h->nix, h->niy, (int)h->npl, h->np};
-      auto it = g_mode_cache.find(key);
-      if (it != g_mode_cache.end()) {
-        b->mode[i] = it->second;
-        continue;
-      }
+      if (cached_mode(key, &b->mode[i])) continue;
       std::vector<int64_t> mine;
       for (int64_t m : cand)
         if (m == 0 || inst_tile_smem(b, h) > 0) mine.push_back(m);
@@ -783,7 +794,7 @@ int pf_batch_tune(pf_batch *b, const double *hstep, const double *szl, int32_t r
         }
       }
       b->mode[i] = best_mode;
-      g_mode_cache[key] = best_mode;
+      if (out == PF_OK) cache_mode(key, best_mode);
     }
     b->active = act0;
   }

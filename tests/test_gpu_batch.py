@@ -163,3 +163,29 @@ def test_window_replay_and_failure_isolation():
     assert st[1] == P.lib.PF_OUT_OF_WINDOW
     for i in (0, 2, 3):
         _assert_same(got[i], want[i], True, f"instance {i}")
+
+
+def test_temporal_and_mixed_eager_batch():
+    """A temporal-mesh instance (no wrap) beside periodic ones, FP64, and the
+    mixed batch with direct launches instead of graphs."""
+    ws = _instances(n=3, seed=23)
+    t = ws[1]
+    t.params.mesh_type = P.MESH_TEMPORAL
+    # 128 planes (8 resonant wavelengths): the beam slips 1.25 wavelengths
+    # forward in z2 over the 40 steps and must stay on the mesh
+    t.params.nz2 = 129
+    n = t.params.nx * t.params.ny * t.params.nz2
+    t.field = (np.zeros(n), np.zeros(n))
+    lz2 = (t.params.nz2 - 1) * t.params.dz2
+    t.beam["z2"] = 0.1 * lz2 + 0.3 * lz2 * (t.beam["z2"] - t.beam["z2"].min()) / np.ptp(t.beam["z2"])
+    want = _single(ws)
+    got, st, _ = _batch_run(ws)
+    assert np.all(st == 0)
+    for i, (g, w) in enumerate(zip(got, want)):
+        _assert_same(g, w, True, f"instance {i}")
+    ws = _instances(n=4, seed=29, precision=P.MIXED)
+    want = _single(ws)
+    got, st, _ = _batch_run(ws, graphs=False)
+    assert np.all(st == 0)
+    for i, (g, w) in enumerate(zip(got, want)):
+        _assert_same(g, w, False, f"instance {i}")
