@@ -29,10 +29,11 @@
 // slopes are computed (nothing per particle is kept, which keeps the kernel
 // near 64 registers and two 512-thread blocks per SM).  The tile sums are
 // exact: each FP32 contribution is converted to a fixed-point integer
-// v * 2^E (|v * 2^E| < 2^39, E chosen per beam from max chi/dV3) split into
-// a signed high part (v >> 20) and a 20-bit low part, which are added with
-// two non-returning 32-bit shared-memory reductions into separate words; up
-// to 2048 low parts of < 2^20 cannot overflow 32 bits, so no carry is lost.
+// v * 2^E truncated (|v * 2^E| < 2^31, E chosen per beam from max
+// chi/dV3, one float-to-int conversion) split into a signed high part
+// (v >> 20) and a 20-bit low part, which are added with two non-returning
+// 32-bit shared-memory reductions into separate words; up to 2048 low parts
+// of < 2^20 cannot overflow 32 bits, so no carry is lost.
 // The flush forms (sum_hi 2^20 + sum_lo) 2^-E in FP32 once per node and adds
 // it to HBM with one float atomic per component.  Contributions
 // outside the tile, or larger than the tile's range, go straight to HBM.
@@ -77,7 +78,9 @@ struct MixArgs {
   float cstate_f, eta_f, inv_dx_f, inv_dy_f, hx_dx, hy_dy, inv_dz2_f;
   int ppt;             // macroparticles per thread (1..MX_PPT)
   int fixE;            // tile fixed-point exponent
+  float fix_scale;     // 2^fixE
   float tile_vmax;     // contributions at or above this go to HBM
+  float npl_f, inv_npl_f;  // planes held (periodic plane estimate of the tile origin)
   double aw2g, g02;    // aw^2 / gamma0^2, 1 / gamma0^2
   double ser[7];       // binomial coefficients of 1/sqrt(1-u) - 1, times 1/eta
   const float2 *as;  // stage field (window, interleaved complex)
@@ -150,24 +153,16 @@ __device__ __forceinline__ void bfield_f(const BFieldF &b, float x, float y, flo
   }
 }
 
-// v * 2^E truncated toward zero, from the bits of v (integer operations);
-// the caller guarantees |v * 2^E| < 2^39
-__device__ __forceinline__ long long f2fix(float v, int E) {
-  const unsigned u = __float_as_uint(v);
-  const int ex = (int)((u >> 23) & 0xffu);
-  if (ex == 0) return 0;
-  const long long m = (long long)((u & 0x7fffffu) | 0x800000u);
-  const int sh = ex - 150 + E;  // v * 2^E = m * 2^sh
-  const long long r = (sh >= 0) ? (m << sh) : (sh > -24 ? (m >> -sh) : 0);
-  return (u >> 31) ? -r : r;
-}
+// v * 2^E truncated toward zero (scale = 2^E, so the product is exact);
+// the caller guarantees |v * 2^E| < 2^31
+__device__ __forceinline__ int f2fix(float v, float scale) { return __float2int_rz(v * scale); }
 
 // exact shared-tile add of a fixed-point value: high part (signed) and the
 // 20-bit low part into separate 32-bit words, non-returning reductions
-__device__ __forceinline__ void tile_add(int *hi, unsigned *lo, long long r) {
+__device__ __forceinline__ void tile_add(int *hi, unsigned *lo, int r) {
   if (r == 0) return;
-  atomicAdd(hi, (int)(r >> 20));
-  atomicAdd(lo, (unsigned)(r & 0xFFFFFll));
+  atomicAdd(hi, r >> 20);
+  atomicAdd(lo, (unsigned)r & 0xFFFFFu);
 }
 
 __device__ __forceinline__ void global_add(float2 *a, float2 v) {
@@ -279,14 +274,10 @@ __device__ __forceinline__ void mixed_block(const MixArgs &a, const int64_t i0, 
       const int64_t i = i0 + q * MX_THREADS + threadIdx.x;
       if (halted || i >= i1) continue;
       // an estimate is enough: a wrong origin only sends deposits to HBM
-      const float fz = floorf(d2f_rn(a.z2[i]) * a.inv_dz2_f);
-      if (!(fabsf(fz) < 1.0e9f)) continue;
-      int m = (int)fz;
-      if (a.periodic) {
-        m %= (int)a.npl;
-        if (m < 0) m += (int)a.npl;
-      }
-      my_pzlo = min(my_pzlo, m);
+      float fz = floorf(d2f_rn(a.z2[i]) * a.inv_dz2_f);
+      if (!(fabsf(fz) < 1.0e7f)) continue;
+      if (a.periodic) fz = fmaxf(fz - a.npl_f * floorf(fz * a.inv_npl_f), 0.f);
+      my_pzlo = min(my_pzlo, (int)fz);
     }
     for (int o = 16; o > 0; o >>= 1) my_pzlo = min(my_pzlo, __shfl_xor_sync(0xffffffffu, my_pzlo, o));
     if ((threadIdx.x & 31) == 0 && my_pzlo != INT_MAX) atomicMin(&s_pzlo, my_pzlo);
@@ -347,8 +338,12 @@ __device__ __forceinline__ void mixed_block(const MixArgs &a, const int64_t i0, 
     if (!ok) {
       atomicOr(a.status, ST_OUT_OF_Z2);
     } else if (a.periodic) {
-      int m = iz % (int)a.npl;
-      if (m < 0) m += (int)a.npl;
+      const int npl = (int)a.npl;
+      int m = iz;
+      if ((unsigned)m >= (unsigned)npl) {  // z2 outside the first period (rare)
+        m %= npl;
+        if (m < 0) m += npl;
+      }
       pz0 = m;
       pz1 = (m + 1 == a.npl) ? 0 : m + 1;
     } else if (!(iz >= 0 && iz + 1 < a.nz2)) {
@@ -420,8 +415,8 @@ __device__ __forceinline__ void mixed_block(const MixArgs &a, const int64_t i0, 
           if (a.tile && tp >= 0 && tp < MX_TILE_PLANES && fabsf(vr) < a.tile_vmax &&
               fabsf(vi) < a.tile_vmax) {
             const int ti = tp * ntr + (int)node;
-            tile_add(thi_r + ti, tlo_r + ti, f2fix(vr, a.fixE));
-            tile_add(thi_i + ti, tlo_i + ti, f2fix(vi, a.fixE));
+            tile_add(thi_r + ti, tlo_r + ti, f2fix(vr, a.fix_scale));
+            tile_add(thi_i + ti, tlo_i + ti, f2fix(vi, a.fix_scale));
           } else {
             global_add(a.acc + (int64_t)plane * ntr + node, make_float2(vr, vi));
           }
@@ -483,11 +478,11 @@ __device__ __forceinline__ void mixed_block(const MixArgs &a, const int64_t i0, 
   if (a.tile) {
     __syncthreads();
     if (pzlo != INT_MAX) {
+      // (hi 2^20 + lo) 2^-E in FP32 (the accumulators are FP32)
+      const float shi = ldexpf(1.f, 20 - a.fixE), slo = ldexpf(1.f, -a.fixE);
       for (int t = threadIdx.x; t < tile_n; t += MX_THREADS) {
         const int plane = pzlo + t / ntr;
         if (plane >= a.npl) break;
-        // (hi 2^20 + lo) 2^-E in FP32 (the accumulators are FP32)
-        const float shi = ldexpf(1.f, 20 - a.fixE), slo = ldexpf(1.f, -a.fixE);
         const float2 v = make_float2(fmaf((float)thi_r[t], shi, (float)tlo_r[t] * slo),
                                      fmaf((float)thi_i[t], shi, (float)tlo_i[t] * slo));
         if (v.x != 0.f || v.y != 0.f) global_add(a.acc + (int64_t)plane * ntr + (t - (plane - pzlo) * ntr), v);
@@ -646,6 +641,8 @@ static void fill_mix_args(pf_handle *h, MixArgs &a, double hstep) {
   a.nz2 = p.nz2;
   a.periodic = (p.mesh_type == PF_MESH_PERIODIC);
   a.one_d = p.one_d;
+  a.npl_f = (float)h->npl;
+  a.inv_npl_f = 1.0f / (float)h->npl;
   a.halfx = ((double)(h->nix - 1) / 2.0) * p.dx;
   a.halfy = ((double)(h->niy - 1) / 2.0) * p.dy;
   a.inv_dx = 1.0 / p.dx;
@@ -684,10 +681,13 @@ static void fill_mix_args(pf_handle *h, MixArgs &a, double hstep) {
     const double vmax = 16.0 * h->chi_max / (p.dx * p.dy * p.dz2);
     int e = 0;
     frexp(vmax > 0.0 ? vmax : 1.0, &e);  // vmax < 2^e
-    a.fixE = 39 - e;
+    a.fixE = 31 - e;
+    a.fix_scale = (float)ldexp(1.0, a.fixE);
     a.tile_vmax = (float)ldexp(1.0, e);
   }
-  a.tile = pf_mixed_tile_smem(h) > 0 ? 1 : 0;
+  // the tile needs a window that fits shared memory and a scale 2^E that is
+  // a normal float (beams with any usable charge weights)
+  a.tile = (pf_mixed_tile_smem(h) > 0 && a.fixE >= -126 && a.fixE <= 127) ? 1 : 0;
 }
 
 // Per-stage fields: the state and slope arrays of stage s for buffer cur.
@@ -748,7 +748,7 @@ void pf_mixed_fill_stage(pf_handle *h, int stage, int cur, double hstep, int til
   MixArgs a;
   fill_mix_args(h, a, hstep);
   mix_stage_pointers(h, a, stage, cur, hstep);
-  a.tile = tile && pf_mixed_tile_smem(h) > 0 ? 1 : 0;
+  a.tile = (tile && a.tile) ? 1 : 0;
   a.ppt = MX_PPT;
   a.coef_tab = coef_tab;
   a.step_ctr = step_ctr;
