@@ -394,6 +394,30 @@ __device__ __forceinline__ void mixed_block(const MixArgs &a, const int64_t i0, 
         const float dw = d2f_rn(a.chi[i]) * a.inv_dV3 * qrG;
         const float sr = dw * PX, si = dw * PY;
         const int nc = ONED ? 2 : 8;
+        const int tp0 = pz0 - pzlo, tp1 = pz1 - pzlo;
+        if (a.tile && (unsigned)tp0 < (unsigned)MX_TILE_PLANES &&
+            (unsigned)tp1 < (unsigned)MX_TILE_PLANES && fabsf(sr) < a.tile_vmax &&
+            fabsf(si) < a.tile_vmax) {
+          // the common case: both planes in the tile, and every corner's
+          // |w s| <= |s| fits the tile's range (0 <= w <= 1)
+          const int t0 = tp0 * ntr + (ONED ? 0 : (int)b0), t1 = tp1 * ntr + (ONED ? 0 : (int)b0);
+#pragma unroll
+          for (int c = 0; c < 8; ++c) {
+            if (c >= nc) break;
+            float w;
+            int ti;
+            if (ONED) {
+              w = (c == 0) ? zw1 : zw2;
+              ti = (c == 0) ? t0 : t1;
+            } else {
+              const int cx = c & 1, cy = (c >> 1) & 1, cz = c >> 2;
+              w = (cx ? x2 : x1) * (cy ? y2 : y1) * (cz ? zw2 : zw1);
+              ti = (cz ? t1 : t0) + cx + cy * a.nix;
+            }
+            tile_add(thi_r + ti, tlo_r + ti, f2fix(w * sr, a.fix_scale));
+            tile_add(thi_i + ti, tlo_i + ti, f2fix(w * si, a.fix_scale));
+          }
+        } else {
 #pragma unroll
         for (int c = 0; c < 8; ++c) {
           if (c >= nc) break;
@@ -420,6 +444,7 @@ __device__ __forceinline__ void mixed_block(const MixArgs &a, const int64_t i0, 
           } else {
             global_add(a.acc + (int64_t)plane * ntr + node, make_float2(vr, vi));
           }
+        }
         }
       }
     }
