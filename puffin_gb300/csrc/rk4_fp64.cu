@@ -72,6 +72,40 @@ __device__ __forceinline__ void bfield(const BFieldCoef &b, double x, double y,
   }
 }
 
+// Integer part and fraction of t (0 <= t < 2^52, or a zero of either sign)
+// from the bits of t, with integer operations only: the same values as
+// floor(t) and t - floor(t) (both exact), without the FP64 pipe the stage
+// kernel is bound by.  False for negative, non-finite or larger t.
+__device__ __forceinline__ bool split_cell(double t, int64_t &ip, double &fr) {
+  const u64 b = (u64)__double_as_longlong(t);
+  if ((b << 1) == 0ull) {  // +0 or -0: floor is 0 (-0), t - floor(t) is +0
+    ip = 0;
+    fr = 0.0;
+    return true;
+  }
+  if (b >> 63) return false;
+  const int e = (int)((b >> 52) & 0x7ffull) - 1023;
+  if (e > 51) return false;  // >= 2^52, infinity, NaN
+  if (e < 0) {
+    ip = 0;
+    fr = t;
+    return true;
+  }
+  const u64 m = (b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+  const int sh = 52 - e;  // 1 .. 52
+  ip = (int64_t)(m >> sh);
+  const u64 fb = m & ((1ull << sh) - 1ull);  // fraction * 2^sh
+  if (fb == 0ull) {
+    fr = 0.0;
+    return true;
+  }
+  const int lz = __clzll((long long)fb);  // >= 12
+  const int ex = (63 - lz) - sh;         // fraction = 1.xxx * 2^ex
+  const u64 mant = (fb << (lz + 1)) >> 12;
+  fr = __longlong_as_double((long long)(((u64)(ex + 1023) << 52) | mant));
+  return true;
+}
+
 // Exact conversion of c * 2^E (truncated toward zero) to a two's-complement
 // 128-bit integer (hi:lo).  Returns false when |c * 2^E| >= 2^maxexp.
 __device__ __forceinline__ bool to_fix(double c, int E, int maxexp, u64 &lo, u64 &hi) {
@@ -174,27 +208,47 @@ __device__ __forceinline__ void stage_particle(const StageArgs &a, const int64_t
   bool ok = true;
   int64_t pz0 = 0, pz1 = 0;
   {
+    // the cell index and fraction from the bits (integer operations, the
+    // same values as floor and subtraction); FP64 floor where the bits
+    // cannot give them (negative or very large z2)
     const double tz = Z2 * a.inv_dz2;
-    const double fz = floor(tz);
-    const double z2n = fz + 1.0;
-    const double zw2 = tz - fz;
-    if (a.periodic) {
-      if (!(fabs(z2n) < 9.0e15)) {
-        ok = false;
-        atomicOr(a.status, ST_OUT_OF_Z2);
-      } else {
-        int64_t m = ((int64_t)z2n - 1) % a.npl;
-        if (m < 0) m += a.npl;
+    int64_t izc;
+    double zw2;
+    if (split_cell(tz, izc, zw2)) {
+      if (a.periodic) {
+        int64_t m = izc;  // z2n - 1
+        if ((uint64_t)m >= (uint64_t)a.npl) m %= a.npl;
         pz0 = m;
         pz1 = (m + 1 == a.npl) ? 0 : m + 1;
-      }
-    } else {
-      if (!(z2n >= 1.0 && z2n < (double)a.nz2)) {
+      } else if (!(izc + 1 < a.nz2)) {
         ok = false;
         atomicOr(a.status, ST_OUT_OF_Z2);
       } else {
-        pz0 = (int64_t)z2n - 1;
+        pz0 = izc;
         pz1 = pz0 + 1;
+      }
+    } else {
+      const double fz = floor(tz);
+      const double z2n = fz + 1.0;
+      zw2 = tz - fz;
+      if (a.periodic) {
+        if (!(fabs(z2n) < 9.0e15)) {
+          ok = false;
+          atomicOr(a.status, ST_OUT_OF_Z2);
+        } else {
+          int64_t m = ((int64_t)z2n - 1) % a.npl;
+          if (m < 0) m += a.npl;
+          pz0 = m;
+          pz1 = (m + 1 == a.npl) ? 0 : m + 1;
+        }
+      } else {
+        if (!(z2n >= 1.0 && z2n < (double)a.nz2)) {
+          ok = false;
+          atomicOr(a.status, ST_OUT_OF_Z2);
+        } else {
+          pz0 = (int64_t)z2n - 1;
+          pz1 = pz0 + 1;
+        }
       }
     }
     if (ONED) {
@@ -204,21 +258,22 @@ __device__ __forceinline__ void stage_particle(const StageArgs &a, const int64_t
       node[0] = pz0;
       node[1] = pz1;
     } else {
+      // a coordinate whose bits give no cell (negative, non-finite, huge)
+      // is outside the window, as floor + 1 < 1 or >= nix would say
       const double tx = (X + a.halfx) * a.inv_dx;
-      const double fx = floor(tx);
-      const double xn = fx + 1.0;
-      const double x2 = tx - fx, x1 = 1.0 - x2;
       const double ty = (Y + a.halfy) * a.inv_dy;
-      const double fy = floor(ty);
-      const double yn = fy + 1.0;
-      const double y2 = ty - fy, y1 = 1.0 - y2;
+      int64_t ixc = -1, iyc = -1;
+      double x2 = 0.0, y2 = 0.0;
+      const bool okx = split_cell(tx, ixc, x2) && ixc + 1 < a.nix;
+      const bool oky = split_cell(ty, iyc, y2) && iyc + 1 < a.niy;
+      const double x1 = 1.0 - x2, y1 = 1.0 - y2;
       const double zw1 = 1.0 - zw2;
-      if (!(xn >= 1.0 && xn < (double)a.nix && yn >= 1.0 && yn < (double)a.niy)) {
+      if (!(okx && oky)) {
         ok = false;
         atomicOr(a.status, ST_OUT_OF_WINDOW);
       }
       const int64_t ntr = a.nix * a.niy;
-      const int64_t ix = ok ? (int64_t)xn - 1 : 0, iy = ok ? (int64_t)yn - 1 : 0;
+      const int64_t ix = ok ? ixc : 0, iy = ok ? iyc : 0;
       const int64_t b0 = ix + iy * a.nix + pz0 * ntr, b1 = ix + iy * a.nix + pz1 * ntr;
       const double x1y1 = x1 * y1, x2y1 = x2 * y1, x1y2 = x1 * y2, x2y2 = x2 * y2;
       w[0] = x1y1 * zw1;

@@ -314,8 +314,9 @@ def test_run_graph_blocks_match_step_by_step(precision):
             np.testing.assert_array_equal(got[k], want[k], err_msg=k)
         np.testing.assert_array_equal(gf[0], wf[0])
         np.testing.assert_array_equal(gf[1], wf[1])
-    else:  # FP32 atomics land in any order: FP32 rounding, grown over 64 steps
-        assert_beam_close(got, oracle_beam(want), rtol=1e-5, atol=1e-8)
+    else:  # FP32 atomics land in any order: FP32 rounding, grown over 64 steps,
+        # to 1e-5 of each coordinate's scale (momenta ~1e-2: atol 1e-7)
+        assert_beam_close(got, oracle_beam(want), rtol=1e-5, atol=1e-7)
         field_close(gf, wf, 1e-4)
 
 
