@@ -133,6 +133,34 @@ def _beam3d(p, n, seed, zlo, zhi, sig=1.0):
     return beam
 
 
+def test_cell_edges_and_periodic_images():
+    """The cell index and fraction come from the bits of the scaled
+    coordinate: macroparticles exactly on cell boundaries (transverse and
+    z2), at negative z2 and beyond the first period of the periodic mesh
+    (their images), against the oracle's floor arithmetic at 1e-12."""
+    w = configs.config1(np_=4096, seed=5, nsteps=2)
+    p = w.params
+    beam = {k: v.copy() for k, v in w.beam.items()}
+    n = len(beam["x"])
+    lz2 = (p.nz2 - 1) * p.dz2
+    rng = np.random.default_rng(9)
+    k = np.arange(n)
+    # a quarter on z2 cell boundaries, a quarter shifted by -1 or +2 periods
+    on = k % 4 == 0
+    beam["z2"][on] = np.round(beam["z2"][on] / p.dz2) * p.dz2
+    img = k % 4 == 1
+    beam["z2"][img] += np.where(rng.random(img.sum()) < 0.5, -lz2, 2.0 * lz2)
+    # transverse boundaries: x on a node of the window (cells of dx = 0.2)
+    xb = k % 4 == 2
+    beam["x"][xb] = np.round(beam["x"][xb] / p.dx) * p.dx
+    beam["y"][xb] = np.round(beam["y"][xb] / p.dy) * p.dy
+    field = random_field(p, 4, amp=1e-2)
+    got, gf, (nix, niy), _ = run_gpu_steps(p, beam, field, w.h, 2)
+    b, of, _ = run_oracle_steps(p, beam, field, w.h, 2, nix, niy)
+    assert_beam_close(got, b, rtol=1e-12, atol=1e-15)
+    field_close(gf, of, 1e-12)
+
+
 @pytest.mark.parametrize("place_sz", [0.0, 0.05, 0.9])
 def test_one_step_planepole_taper_ends_focusing(place_sz):
     """Temporal mesh, planepole with undulator ends (start/main/end sections),
