@@ -419,7 +419,7 @@ __device__ __forceinline__ void stage_tile_block(const StageArgs &a, const int64
 }
 
 template <int STAGE, bool ONED, bool TILE = false>
-__global__ void __launch_bounds__(256) k_stage(const StageArgs a) {
+__global__ void __launch_bounds__(256, TILE ? 2 : 4) k_stage(const StageArgs a) {
   if constexpr (!TILE) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.np) return;
