@@ -474,7 +474,7 @@ __device__ __forceinline__ void store(const FftArgs &a, int64_t pos, cplx v) {
   }
 }
 
-__global__ void __launch_bounds__(NTHREADS) k_fft(const FftArgs a) {
+__global__ void __launch_bounds__(NTHREADS, (sizeof(real) == 8) ? 3 : 1) k_fft(const FftArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx *smem_all = reinterpret_cast<cplx *>(smem_raw);
   const AxisPlan &p = a.ax;
@@ -1029,7 +1029,9 @@ static int build_plan(pf_handle *h, Plan *&out) {
     }
     // lines per block: about 2048 points per block, adjacent lines for the
     // strided axes, two buffers within the shared-memory limit
-    lpb = std::max<int64_t>(1, 2048 / ap.n);
+    // (FP64: about 1400 points, so that three blocks share an SM: measured
+    // 5 % faster than two blocks of 2048 points, and faster than four)
+    lpb = std::max<int64_t>(1, (sizeof(real) == 8 ? 1400 : 2048) / ap.n);
     lpb = std::min<int64_t>(lpb, ap.nlines);
     auto bytes = [&](int64_t lp) { return (size_t)(2 * lp * ap.n + scratch) * sizeof(cplx); };
     while (lpb > 1 && bytes(lpb) > (size_t)max_smem) --lpb;
