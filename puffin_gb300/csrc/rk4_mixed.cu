@@ -555,7 +555,7 @@ __global__ void __launch_bounds__(256) k_nodes_mixed(const MixNodeArgs a) {
 }
 
 template <int STAGE, bool ONED>
-__global__ void __launch_bounds__(MX_THREADS) k_stage_mixed(const MixArgs a) {
+__global__ void __launch_bounds__(MX_THREADS, 3) k_stage_mixed(const MixArgs a) {
   extern __shared__ __align__(16) float tile[];
   __shared__ int s_pzlo;
   const int64_t i0 = (int64_t)blockIdx.x * (MX_THREADS * a.ppt);
@@ -566,7 +566,7 @@ __global__ void __launch_bounds__(MX_THREADS) k_stage_mixed(const MixArgs a) {
 // MX_THREADS * MX_PPT macroparticles; the arguments of each tile's instance
 // are staged in shared memory.
 template <int STAGE>
-__global__ void __launch_bounds__(MX_THREADS) k_stage_mixed_batch(const MixArgs *__restrict__ args,
+__global__ void __launch_bounds__(MX_THREADS, 3) k_stage_mixed_batch(const MixArgs *__restrict__ args,
                                                                   const BatchTile *__restrict__ tiles,
                                                                   const int ntiles) {
   extern __shared__ __align__(16) float tile[];
