@@ -419,7 +419,7 @@ __device__ __forceinline__ void stage_tile_block(const StageArgs &a, const int64
 }
 
 template <int STAGE, bool ONED, bool TILE = false>
-__global__ void __launch_bounds__(256, TILE ? 2 : 4) k_stage(const StageArgs a) {
+__global__ void __launch_bounds__(256, TILE ? 3 : 4) k_stage(const StageArgs a) {
   if constexpr (!TILE) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.np) return;
@@ -438,7 +438,7 @@ __global__ void __launch_bounds__(256, TILE ? 2 : 4) k_stage(const StageArgs a) 
 // blockIdx.x, blockIdx.x + gridDim.x, ... and stages the arguments of each
 // tile's instance in shared memory.  TILE: the dense-mode deposit.
 template <int STAGE, bool TILE>
-__global__ void __launch_bounds__(256, 3) k_stage_batch(const StageArgs *__restrict__ args,
+__global__ void __launch_bounds__(256, 4) k_stage_batch(const StageArgs *__restrict__ args,
                                                      const BatchTile *__restrict__ tiles,
                                                      const int ntiles) {
   __shared__ __align__(16) u64 sa_raw[sizeof(StageArgs) / 8];
