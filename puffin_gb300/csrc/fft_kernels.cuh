@@ -759,7 +759,7 @@ __global__ void __launch_bounds__(PT, 1) k_fft_plane(const FftArgs a) {
 // SM.  The short transforms are the in-place shared-memory passes above, with
 // their plans in a.ax (length N1) and a.ay (length N2).
 template <int N1, int N2, int G, int STEP>
-__global__ void __launch_bounds__(PT, (sizeof(real) == 4) ? 3 : 2) k_z4(const FftArgs a) {
+__global__ void __launch_bounds__(PT, (sizeof(real) == 4) ? 4 : 3) k_z4(const FftArgs a) {
   static_assert(PT % G == 0, "a thread keeps one line of its group");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx *buf = reinterpret_cast<cplx *>(smem_raw);
