@@ -32,7 +32,7 @@ def nvcc() -> str:
 
 
 def _deps():
-    return (glob.glob(os.path.join(CSRC, "*.h")) +
+    return (glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh")) +
             [os.path.join(ROOT, "include", "puffgpu.h"), __file__])
 
 
