@@ -9,9 +9,12 @@ merged diffraction call (dz = 8 h), exactly as UndSection schedules them.
 
 * value  -- particle-steps/s with the state resident in HBM (CUDA events on
             the library's stream around K steps, after W warm-up steps);
-* e2e    -- the same metric through the C ABI with host buffers: every step
-            copies the particles and the field in from pinned host memory and
-            reads both back (the drop-in call pattern of a host driver);
+* e2e    -- the same metric through the C ABI with host buffers, in the
+            reference's data flow: every step copies the particles and the
+            inner-window field (the arrays rk4par advances) in from pinned
+            host memory and reads them back; around each diffraction call the
+            outer field goes in and comes back as well (inner2Outer /
+            diffractIM / outer2Inner);
 * roofline -- the dominant kernel (the fused RK4 stage kernel) timed live
             with CUDA events; algorithmic bytes 104 B per particle per stage
             (416 B per particle-step over 4 stages);
@@ -275,7 +278,7 @@ def _time_path(args, dev, precision, world, workload="config2", steps=None, warm
             torch.distributed.barrier()
     ms = e0.elapsed_time(e1)
     out = {
-        "w": w, "sim": sim, "step": step, "stream": stream, "win": win, "ms": ms,
+        "w": w, "sim": sim, "step": step, "state": state, "stream": stream, "win": win, "ms": ms,
         "launches": sim.kernel_launches - launches0, "clocks": clk.summary(),
         "kernel": {name: sim.profile_read(cls) for name, cls in
                    (("stage", L.PROF_STAGE), ("nodes", L.PROF_NODES), ("fft", L.PROF_FFT),
@@ -506,7 +509,11 @@ def run_gpu(args, rank, world):
     ms = r64["ms"]
     every = w.isteps4diff
 
-    # end to end through the C ABI with host buffers
+    # end to end through the C ABI with host buffers, in UndSection's data
+    # flow: every step hands in the particles (7 arrays) and the inner-window
+    # field (the arrays rk4par advances) from pinned host memory and reads the
+    # six evolving particle arrays and the window back; the outer field goes
+    # in before and comes back after each diffraction call (every 8th step)
     n = w.np
     pin = {k: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy() for k in P.PARTICLE_KEYS}
     fre = torch.empty(sim.n_outer, dtype=torch.float64, pin_memory=True).numpy()
@@ -519,6 +526,14 @@ def run_gpu(args, rank, world):
     fim[:] = i_
     lib = L.load()
     ptrs = [pin[k].ctypes.data for k in P.PARTICLE_KEYS]
+    # the window that the host state needs (set_particles may grow it once)
+    assert lib.pf_set_particles(sim._h, n, *ptrs) == 0
+    nw = sim.n_window
+    wre = torch.empty(nw, dtype=torch.float64, pin_memory=True).numpy()
+    wim = torch.empty(nw, dtype=torch.float64, pin_memory=True).numpy()
+    assert lib.pf_get_window_field(sim._h, wre.ctypes.data, wim.ctypes.data) == 0
+    state64 = r64["state"]
+    n_diff = 0
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
@@ -526,18 +541,30 @@ def run_gpu(args, rank, world):
     t1 = torch.cuda.Event(enable_timing=True)
     t0.record(stream)
     for _ in range(max(0, args.e2e_steps)):
+        diff = (state64["i"] + 1) % every == 0
+        if diff:
+            assert lib.pf_set_field(sim._h, fre.ctypes.data, fim.ctypes.data) == 0
+        assert lib.pf_set_window_field(sim._h, wre.ctypes.data, wim.ctypes.data) == 0
         assert lib.pf_set_particles(sim._h, n, *ptrs) == 0
-        assert lib.pf_set_field(sim._h, fre.ctypes.data, fim.ctypes.data) == 0
+        if lib.pf_window_nodes(sim._h) != nw:
+            raise RuntimeError("the inner window changed size during the end-to-end steps")
         step()
-        assert lib.pf_get_particles(sim._h, *ptrs) == 0
-        assert lib.pf_get_field(sim._h, fre.ctypes.data, fim.ctypes.data) == 0
+        if lib.pf_window_nodes(sim._h) != nw:
+            raise RuntimeError("the inner window changed size during the end-to-end steps")
+        assert lib.pf_get_particles(sim._h, *ptrs[:6], None) == 0
+        assert lib.pf_get_window_field(sim._h, wre.ctypes.data, wim.ctypes.data) == 0
+        if diff:
+            assert lib.pf_get_field(sim._h, fre.ctypes.data, fim.ctypes.data) == 0
+            n_diff += 1
     t1.record(stream)
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
     e2e_ms = max(t0.elapsed_time(t1), 1e-9)
-    h2d = 7 * 8 * n + 2 * 8 * sim.n_outer
-    d2h = h2d
+    k_e2e = max(1, args.e2e_steps)
+    h2d = (7 * 8 * n + 2 * 8 * nw) + 2 * 8 * sim.n_outer * n_diff / k_e2e
+    d2h = (6 * 8 * n + 2 * 8 * nw) + 2 * 8 * sim.n_outer * n_diff / k_e2e
+    e2e_diff_calls = n_diff
     sim.close()
 
     rmx = None
@@ -596,7 +623,11 @@ def run_gpu(args, rank, world):
             "l2": "inputs larger than L2 (particle state 470 MB, field 1.09 GB per array pair)",
         },
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "steps": args.e2e_steps},
+                "d2h_bytes_per_step": d2h, "steps": args.e2e_steps,
+                "diffraction_calls": e2e_diff_calls,
+                "per_step": "particles (7 arrays in, 6 out) and the inner-window field, "
+                            "in and out; the outer field in and out around each "
+                            "diffraction call"},
         "gpu_launches": r64["launches"] + (rmx["launches"] if rmx else 0)
         + (c3["fp64"]["launches"] + c3["mixed"]["launches"] if c3 else 0),
         "kernel_ms": kern,

@@ -114,7 +114,11 @@ void pf_default_params(pf_params *p);
 int pf_create(const pf_params *p, pf_handle **out);
 int pf_destroy(pf_handle *h);
 
-/* Particles: host arrays (copied in/out) or device arrays (device-to-device). */
+/* Particles: host arrays (copied in/out) or device arrays (device-to-device).
+ * pf_set_particles also computes the inner window the particles need
+ * (getInNode, parallel/para_field.f90:1432-1508) when the handle has none
+ * yet or the current one is too small; a larger current window is kept (the
+ * reference recomputes it only at redistribution: pf_redistribute). */
 int pf_set_particles(pf_handle *h, int64_t n, const double *x, const double *y,
                      const double *z2, const double *px, const double *py,
                      const double *gam, const double *chi);
@@ -132,6 +136,24 @@ int pf_set_field(pf_handle *h, const double *re, const double *im);
 int pf_get_field(pf_handle *h, double *re, double *im);
 int pf_set_field_dev(pf_handle *h, const double *re, const double *im);
 int pf_get_field_dev(pf_handle *h, double *re, double *im);
+
+/* Inner-window field: the arrays rk4par advances (ac_rfield_in /
+ * ac_ifield_in, puffin/lib/interaction/puffin_mpi_RK4.f90:38, filled by
+ * outer2Inner and read back by inner2Outer, parallel/para_field.f90:1352-1429).
+ * pf_window_nodes() values each: nix * niy * planes, x fastest, planes = nz2
+ * (temporal mesh) or nz2 - 1 (periodic), the window centred in the outer
+ * mesh.  pf_set_window_field replaces the window that the next pf_rk4_step
+ * advances; pf_diffract and pf_get_field copy the window into the outer
+ * mesh first, as UndSection's inner2Outer does.  A driver that keeps the
+ * window between steps exchanges only these arrays and the particles per
+ * step, and the outer field around diffraction calls.  PF_STATE before the
+ * particles (and so the window) are set; the window changes size only in
+ * pf_set_particles and pf_redistribute. */
+int pf_set_window_field(pf_handle *h, const double *re, const double *im);
+int pf_get_window_field(pf_handle *h, double *re, double *im);
+int pf_set_window_field_dev(pf_handle *h, const double *re, const double *im);
+int pf_get_window_field_dev(pf_handle *h, double *re, double *im);
+int64_t pf_window_nodes(const pf_handle *h);
 
 /* Taper state (n2col, n2col0, undgrad). */
 int pf_set_taper(pf_handle *h, double n2col, double n2col0, double undgrad);

@@ -338,7 +338,9 @@ static int set_window(pf_handle *h, int nix, int niy) {
   return pf_outer_to_inner(h);
 }
 
-static int choose_window(pf_handle *h) {
+// grow_only: keep the current window while it is at least as large as the
+// one the particles need
+static int choose_window(pf_handle *h, bool grow_only) {
   int nix = h->p.nix, niy = h->p.niy;
   if (nix <= 0 || niy <= 0) {
     int rc = pf_window_from_particles(h, &nix, &niy);
@@ -348,6 +350,7 @@ static int choose_window(pf_handle *h) {
     h->err = "inner window larger than the mesh";
     return PF_BAD_ARG;
   }
+  if (grow_only && h->nwin > 0 && nix <= h->nix && niy <= h->niy) return PF_OK;
   return set_window(h, nix, niy);
 }
 
@@ -518,7 +521,10 @@ static int set_particles_impl(pf_handle *h, int64_t n, const double *const src[7
   const double smax = chimax / (h->p.dx * h->p.dy * h->p.dz2);
   const int e_s = (smax > 0.0 && isfinite(smax)) ? ilogb(smax) + 1 : 0;
   h->fix_e = h->fix_maxexp - 16 - e_s;
-  return choose_window(h);
+  // getInNode for the first particles; afterwards the window only grows here
+  // (the reference recomputes it at redistribution, pf_redistribute), so a
+  // driver that hands the state in every step keeps one window
+  return choose_window(h, true);
 }
 
 int pf_set_particles(pf_handle *h, int64_t n, const double *x, const double *y,
@@ -629,6 +635,70 @@ int pf_get_field(pf_handle *h, double *re, double *im) {
 int pf_get_field_dev(pf_handle *h, double *re, double *im) {
   return get_field_impl(h, re, im, cudaMemcpyDeviceToDevice);
 }
+
+// the inner-window field (ac_rfield_in / ac_ifield_in) in outer2Inner's layout
+static int set_window_field_impl(pf_handle *h, const double *re, const double *im,
+                                 cudaMemcpyKind kind) {
+  if (!h || !re || !im) return PF_BAD_ARG;
+  if (h->nwin == 0) {
+    h->err = "pf_set_window_field: no inner window (particles not set)";
+    return PF_STATE;
+  }
+  cudaSetDevice(h->dev);
+  const size_t b = sizeof(double) * (size_t)h->nwin;
+  if (h->p.precision == PF_MIXED) {
+    if (!h->staging) PF_CUDA(cudaMalloc(&h->staging, 2 * sizeof(double) * (size_t)h->nouter));
+    PF_CUDA(cudaMemcpyAsync(h->staging, re, b, kind, h->stream));
+    PF_CUDA(cudaMemcpyAsync(h->staging + h->nwin, im, b, kind, h->stream));
+    k_to_c32<<<grid_for(h->nwin, 256), 256, 0, h->stream>>>((float2 *)h->w32, h->staging,
+                                                           h->staging + h->nwin, h->nwin);
+    PF_LAUNCHED(h);
+  } else {
+    PF_CUDA(cudaMemcpyAsync(h->wr, re, b, kind, h->stream));
+    PF_CUDA(cudaMemcpyAsync(h->wi, im, b, kind, h->stream));
+  }
+  h->window_valid = true;
+  PF_CUDA(cudaStreamSynchronize(h->stream));
+  return PF_OK;
+}
+
+static int get_window_field_impl(pf_handle *h, double *re, double *im, cudaMemcpyKind kind) {
+  if (!h || !re || !im) return PF_BAD_ARG;
+  if (h->nwin == 0) {
+    h->err = "pf_get_window_field: no inner window (particles not set)";
+    return PF_STATE;
+  }
+  cudaSetDevice(h->dev);
+  const size_t b = sizeof(double) * (size_t)h->nwin;
+  if (h->p.precision == PF_MIXED) {
+    if (!h->staging) PF_CUDA(cudaMalloc(&h->staging, 2 * sizeof(double) * (size_t)h->nouter));
+    k_from_c32<<<grid_for(h->nwin, 256), 256, 0, h->stream>>>(
+        (const float2 *)h->w32, h->staging, h->staging + h->nwin, h->nwin);
+    PF_LAUNCHED(h);
+    PF_CUDA(cudaMemcpyAsync(re, h->staging, b, kind, h->stream));
+    PF_CUDA(cudaMemcpyAsync(im, h->staging + h->nwin, b, kind, h->stream));
+  } else {
+    PF_CUDA(cudaMemcpyAsync(re, h->wr, b, kind, h->stream));
+    PF_CUDA(cudaMemcpyAsync(im, h->wi, b, kind, h->stream));
+  }
+  PF_CUDA(cudaStreamSynchronize(h->stream));
+  return PF_OK;
+}
+
+int pf_set_window_field(pf_handle *h, const double *re, const double *im) {
+  return set_window_field_impl(h, re, im, cudaMemcpyHostToDevice);
+}
+int pf_get_window_field(pf_handle *h, double *re, double *im) {
+  return get_window_field_impl(h, re, im, cudaMemcpyDeviceToHost);
+}
+int pf_set_window_field_dev(pf_handle *h, const double *re, const double *im) {
+  return set_window_field_impl(h, re, im, cudaMemcpyDeviceToDevice);
+}
+int pf_get_window_field_dev(pf_handle *h, double *re, double *im) {
+  return get_window_field_impl(h, re, im, cudaMemcpyDeviceToDevice);
+}
+
+int64_t pf_window_nodes(const pf_handle *h) { return h ? h->nwin : -1; }
 
 int pf_set_taper(pf_handle *h, double n2col, double n2col0, double undgrad) {
   if (!h) return PF_BAD_ARG;

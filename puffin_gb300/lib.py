@@ -53,7 +53,9 @@ SYMBOLS = (
     "pf_adjoint_forward", "pf_generate_beam", "pf_set_launch_mode",
     "pf_adjoint_backward", "pf_batch_create", "pf_batch_destroy", "pf_batch_run",
     "pf_batch_tune", "pf_batch_get_shape", "pf_batch_set_shape", "pf_batch_use_graphs",
-    "pf_batch_launches", "pf_batch_stream", "pf_batch_last_error",
+    "pf_batch_launches", "pf_batch_stream", "pf_batch_last_error", "pf_set_window_field",
+    "pf_get_window_field", "pf_set_window_field_dev", "pf_get_window_field_dev",
+    "pf_window_nodes",
 )
 NOALLOC_MAX_PARTICLES = 32768
 NOALLOC_MAX_NODES = 32768
@@ -98,6 +100,11 @@ def load(build_if_missing: bool = False):
         "pf_set_taper": (ctypes.c_int, [H, f64, f64, f64]),
         "pf_get_taper": (ctypes.c_int, [H, dp, dp, dp]),
         "pf_get_window": (ctypes.c_int, [H, ctypes.POINTER(i32), ctypes.POINTER(i32)]),
+        "pf_set_window_field": (ctypes.c_int, [H, ctypes.c_void_p, ctypes.c_void_p]),
+        "pf_get_window_field": (ctypes.c_int, [H, ctypes.c_void_p, ctypes.c_void_p]),
+        "pf_set_window_field_dev": (ctypes.c_int, [H, ctypes.c_void_p, ctypes.c_void_p]),
+        "pf_get_window_field_dev": (ctypes.c_int, [H, ctypes.c_void_p, ctypes.c_void_p]),
+        "pf_window_nodes": (i64, [H]),
         "pf_rk4_step": (ctypes.c_int, [H, f64, f64]),
         "pf_redistribute": (ctypes.c_int, [H]),
         "pf_wrap_z2": (ctypes.c_int, [H]),

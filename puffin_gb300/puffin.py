@@ -137,6 +137,36 @@ class Puffin:
         self._check(self._lib.pf_get_field(self._h, re.ctypes.data, im.ctypes.data))
         return re, im
 
+    @property
+    def n_window(self) -> int:
+        """Values per array of the inner-window field (nix * niy * planes)."""
+        return int(self._lib.pf_window_nodes(self._h))
+
+    def set_window_field(self, re, im):
+        """Replace the inner-window field that the next rk4par advances
+        (ac_rfield_in / ac_ifield_in; outer2Inner's layout, x fastest)."""
+        if _is_torch_cuda(re) and _is_torch_cuda(im):
+            (re, pr), (im, pi) = _dev(re), _dev(im)
+            fn = self._lib.pf_set_window_field_dev
+        else:
+            (re, pr), (im, pi) = _host(re), _host(im)
+            fn = self._lib.pf_set_window_field
+        n = self.n_window
+        if re.size != n or im.size != n:
+            raise ValueError(f"window field arrays must hold nix*niy*planes = {n} values")
+        self._check(fn(self._h, pr, pi))
+
+    def get_window_field(self, out=None):
+        if out is not None and _is_torch_cuda(out[0]):
+            self._check(self._lib.pf_get_window_field_dev(self._h, _dev(out[0])[1],
+                                                          _dev(out[1])[1]))
+            return out
+        n = self.n_window
+        re = np.empty(n)
+        im = np.empty(n)
+        self._check(self._lib.pf_get_window_field(self._h, re.ctypes.data, im.ctypes.data))
+        return re, im
+
     # -- taper / window ---------------------------------------------------------
     def set_taper(self, n2col, n2col0, undgrad):
         self._check(self._lib.pf_set_taper(self._h, n2col, n2col0, undgrad))
