@@ -1,13 +1,14 @@
 // Mixed-precision RK4 macroparticle push.
 //
 // FP64: the particle state (x, y, z2, px, py, Gamma) in HBM and every RK4
-// stage combination y + h/6 (k1 + k4 + 2 (k2 + k3)); the stage values of z2,
-// Gamma, px and py; p2 (the z2 velocity, which sets the ponderomotive phase)
-// and the z2 cell index and fraction.
-// FP32: the field window, the transverse stage coordinates and interpolation
-// weights, the gather, the source term and its deposit, the b-fields, the
-// momentum/energy equations, and the slopes of x, y, px, py and Gamma (the
-// z2 slope p2 stays FP64).
+// stage combination y + h/6 (k1 + k4 + 2 (k2 + k3)); the stage values of z2
+// and Gamma; p2 (the z2 velocity, which sets the ponderomotive phase) and the
+// z2 cell index and fraction.
+// FP32: the field window, the transverse stage coordinates and momenta
+// (px^2 + py^2 enters p2 as a 1e-4 correction, so FP32 keeps u to ~1e-11)
+// and interpolation weights, the gather, the source term and its deposit, the
+// b-fields, the momentum/energy equations, and the slopes of x, y, px, py and
+// Gamma (the z2 slope p2 stays FP64).
 //
 // GB300 issues FP64 at 1/64 of the FP32 rate, so this kernel is bound by its
 // FP64 instruction count: conversions between FP32 and FP64 are done with
@@ -17,9 +18,10 @@
 // p2 (gamma_to_p2.f90:84-85) is (1/sqrt(1-u) - 1)/eta with
 // u = (1 + aw^2 p_perp^2)/(gamma0^2 Gamma^2) of order 1e-7: the reference form
 // cancels 7 digits.  Here r - 1 = 1/sqrt(1-u) - 1 is summed as its binomial
-// series u/2 + 3u^2/8 + 5u^3/16 + ... (five terms for u < 1e-4, seven for
+// series u/2 + 3u^2/8 + 5u^3/16 + ... (below u = 2e-6 as (u/2)(1 + c) with
+// the small correction c in FP32; five terms for u < 1e-4, seven for
 // u < 1e-3, truncation below 1e-16 of the result; the reference form above
-// that), which is accurate to a few ulps in FP64 and needs no square root or
+// that), which is accurate to 1e-13 or better and needs no square root or
 // division.
 //
 // Deposit: each block of up to 2048 macroparticles (up to 4 per thread; fewer
@@ -76,6 +78,7 @@ struct MixArgs {
   int64_t np;
   double cstate, h6;
   float cstate_f, eta_f, inv_dx_f, inv_dy_f, hx_dx, hy_dy, inv_dz2_f;
+  float ser_r1, ser_r2;  // ser[1] / ser[0], ser[2] / ser[0]
   int ppt;             // macroparticles per thread (1..MX_PPT)
   int fixE;            // tile fixed-point exponent
   float fix_scale;     // 2^fixE
@@ -201,8 +204,16 @@ __device__ __forceinline__ float d2f_rn(double d) {
 // folded into the coefficients c[k] = C(2k+2, k+1) / 4^(k+1) / eta:
 // three terms for u < 2e-6, five for u < 1e-4, seven for u < 1e-3 (the
 // truncation stays below 1e-17 of the result), the closed form above
-__device__ __forceinline__ double p2_series(double u, const double *c, double inv_eta) {
-  if (u < 2.0e-6) return u * fma(fma(c[2], u, c[1]), u, c[0]);
+__device__ __forceinline__ double p2_series(double u, const double *c, double inv_eta, float r1,
+                                            float r2) {
+  if (u < 2.0e-6) {
+    // u c0 (1 + (c1/c0) u + (c2/c0) u^2) with the correction (below 2e-6) in
+    // FP32: its rounding is below 1e-13 of p2; two FP64 operations
+    const float uf = d2f_rn(u);
+    const float corr = uf * fmaf(r2, uf, r1);
+    const double uc = u * c[0];
+    return fma(uc, f2d(corr), uc);
+  }
   if (u < 1.0e-4) {
     double s = c[4];
     s = fma(s, u, c[3]);
@@ -289,13 +300,13 @@ __device__ __forceinline__ void mixed_block(const MixArgs &a, const int64_t i0, 
   for (int q = 0; q < ppt; ++q) {
     const int64_t i = i0 + q * MX_THREADS + threadIdx.x;
     if (halted || i >= i1) continue;
-    // FP64 state; stage values of z2, Gamma, px, py in FP64, of x, y in FP32
+    // FP64 state; stage values of z2 and Gamma in FP64, of x, y, px, py in FP32
     const double x0 = a.x[i], yv0 = a.y[i], z0 = a.z2[i], px0 = a.px[i], py0 = a.py[i],
                  g0 = a.gam[i];
     float kin[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     double kz_in = 0.0;
-    double zs = z0, gs = g0, pxs = px0, pys = py0;
-    float X = d2f_rn(x0), Y = d2f_rn(yv0);
+    double zs = z0, gs = g0;
+    float X = d2f_rn(x0), Y = d2f_rn(yv0), PX = d2f_rn(px0), PY = d2f_rn(py0);
     if (STAGE > 1) {
       kin[0] = a.kin_f[0][i];
       kin[1] = a.kin_f[1][i];
@@ -305,18 +316,20 @@ __device__ __forceinline__ void mixed_block(const MixArgs &a, const int64_t i0, 
       kz_in = a.kin_z[i];
       zs = fma(a.cstate, kz_in, z0);
       gs = fma(a.cstate, f2d(kin[5]), g0);
-      pxs = fma(a.cstate, f2d(kin[3]), px0);
-      pys = fma(a.cstate, f2d(kin[4]), py0);
+      PX = fmaf(a.cstate_f, kin[3], PX);
+      PY = fmaf(a.cstate_f, kin[4], PY);
       X = fmaf(a.cstate_f, kin[0], X);
       Y = fmaf(a.cstate_f, kin[1], Y);
     }
-    const float Gf = d2f_rn(gs), PX = d2f_rn(pxs), PY = d2f_rn(pys);
+    const float Gf = d2f_rn(gs);
     // 1/Gamma: FP32 reciprocal and one FP64 Newton step (relative error ~1e-14)
     const float rGf = __frcp_rn(Gf);
     double rG = f2d(rGf);
     rG = fma(rG, fma(-gs, rG, 1.0), rG);
-    const double u = fma(a.aw2g, fma(pxs, pxs, pys * pys), a.g02) * (rG * rG);
-    const double p2 = p2_series(u, a.ser, a.inv_eta);
+    // px^2 + py^2 in FP32: aw^2 (px^2 + py^2) is ~1e-4 of 1 + aw^2 (px^2 + py^2),
+    // so its rounding stays near 1e-11 of u
+    const double u = fma(a.aw2g, f2d(fmaf(PX, PX, PY * PY)), a.g02) * (rG * rG);
+    const double p2 = p2_series(u, a.ser, a.inv_eta, a.ser_r1, a.ser_r2);
     const float p2f = d2f_rn(p2);
     const float qrG = fmaf(a.eta_f, p2f, 1.f) * rGf;
 
@@ -686,6 +699,8 @@ static void fill_mix_args(pf_handle *h, MixArgs &a, double hstep) {
     const double cb[7] = {1.0 / 2.0, 3.0 / 8.0, 5.0 / 16.0, 35.0 / 128.0, 63.0 / 256.0,
                           231.0 / 1024.0, 429.0 / 2048.0};
     for (int k = 0; k < 7; ++k) a.ser[k] = cb[k] / p.eta;
+    a.ser_r1 = (float)(cb[1] / cb[0]);
+    a.ser_r2 = (float)(cb[2] / cb[0]);
   }
   a.inv_g02 = 1.0 / (p.gamma_r * p.gamma_r);
   a.aw2 = p.aw * p.aw;
