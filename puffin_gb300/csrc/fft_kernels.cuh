@@ -600,11 +600,18 @@ __device__ __forceinline__ int sw(int i) {
   return (sizeof(real) == 4) ? (i ^ ((i >> 4) & 15)) : (i ^ ((i >> 3) & 7));
 }
 
-template <int N, int NL, int R, int NS, bool INV>
+// LM (line-major thread order): consecutive threads take adjacent lines at
+// the same butterfly and the slots are not swizzled.  A warp's accesses are
+// then to slots ls apart, which no two lanes of a 128-byte wavefront share a
+// bank on when ls is 1 (interleaved lines) or odd.  Else consecutive threads
+// take consecutive butterflies of a line and the XOR swizzle spreads their
+// strided accesses (about two wavefronts per ideal one remain).
+template <int N, int NL, int R, int NS, bool INV, bool LM = false>
 __device__ __forceinline__ void ip_pass(cplx *buf, int nl, int ls, int es, const cplx *tw) {
   constexpr int NB = N / R;
   constexpr int MAXB = (NL * NB + PT - 1) / PT;
-  const int total = nl * NB;
+  const int total = LM ? NL * NB : nl * NB;
+  auto slot = [](int i) { return LM ? i : sw(i); };
   int obase[MAXB];
   if constexpr (R == 2 || R == 4 || R == 8) {
     cplx v[MAXB][R];
@@ -612,12 +619,12 @@ __device__ __forceinline__ void ip_pass(cplx *buf, int nl, int ls, int es, const
     for (int b = 0; b < MAXB; ++b) {
       const int t = threadIdx.x + b * PT;
       obase[b] = -1;
-      if (t < total) {
-        const int l = t / NB, j = t - l * NB;
+      const int l = LM ? t % NL : t / NB, j = LM ? t / NL : t - (t / NB) * NB;
+      if (t < total && (!LM || l < nl)) {
         const int k = j % NS;
         const int src = l * ls + j * es;
 #pragma unroll
-        for (int r = 0; r < R; ++r) v[b][r] = buf[sw(src + r * NB * es)];
+        for (int r = 0; r < R; ++r) v[b][r] = buf[slot(src + r * NB * es)];
         if constexpr (NS > 1) {
 #pragma unroll
           for (int r = 1; r < R; ++r) v[b][r] = cmul(v[b][r], tw[k * R + r]);
@@ -631,7 +638,7 @@ __device__ __forceinline__ void ip_pass(cplx *buf, int nl, int ls, int es, const
       if (obase[b] < 0) continue;
       dft_regs<R, INV>(v[b]);
 #pragma unroll
-      for (int r = 0; r < R; ++r) buf[sw(obase[b] + r * NS * es)] = v[b][r];
+      for (int r = 0; r < R; ++r) buf[slot(obase[b] + r * NS * es)] = v[b][r];
     }
     __syncthreads();
   } else {
@@ -643,14 +650,14 @@ __device__ __forceinline__ void ip_pass(cplx *buf, int nl, int ls, int es, const
     for (int b = 0; b < MAXB; ++b) {
       const int t = threadIdx.x + b * PT;
       obase[b] = -1;
-      if (t < total) {
-        const int l = t / NB, j = t - l * NB;
+      const int l = LM ? t % NL : t / NB, j = LM ? t / NL : t - (t / NB) * NB;
+      if (t < total && (!LM || l < nl)) {
         const int k = j % NS;
         const int src = l * ls + j * es;
-        x0[b] = buf[sw(src)];
+        x0[b] = buf[slot(src)];
 #pragma unroll
         for (int q = 1; q <= H; ++q) {
-          cplx u = buf[sw(src + q * NB * es)], w = buf[sw(src + (R - q) * NB * es)];
+          cplx u = buf[slot(src + q * NB * es)], w = buf[slot(src + (R - q) * NB * es)];
           if constexpr (NS > 1) {
             u = cmul(u, tw[k * R + q]);
             w = cmul(w, tw[k * R + R - q]);
@@ -670,7 +677,7 @@ __device__ __forceinline__ void ip_pass(cplx *buf, int nl, int ls, int es, const
       cplx s0 = x0[b];
 #pragma unroll
       for (int q = 0; q < H; ++q) s0 = cadd(s0, av[b][q]);
-      buf[sw(o)] = s0;
+      buf[slot(o)] = s0;
       // every thread runs the same (q, j) sequence: the root is an immediate
       // constant-bank operand
 #pragma unroll
@@ -687,11 +694,11 @@ __device__ __forceinline__ void ip_pass(cplx *buf, int nl, int ls, int es, const
           S.i = fma(bv[b][j - 1].i, sn, S.i);
         }
         if (!INV) {
-          buf[sw(o + q * ds)] = cplx{C.r + S.i, C.i - S.r};
-          buf[sw(o + (R - q) * ds)] = cplx{C.r - S.i, C.i + S.r};
+          buf[slot(o + q * ds)] = cplx{C.r + S.i, C.i - S.r};
+          buf[slot(o + (R - q) * ds)] = cplx{C.r - S.i, C.i + S.r};
         } else {
-          buf[sw(o + q * ds)] = cplx{C.r - S.i, C.i + S.r};
-          buf[sw(o + (R - q) * ds)] = cplx{C.r + S.i, C.i - S.r};
+          buf[slot(o + q * ds)] = cplx{C.r - S.i, C.i + S.r};
+          buf[slot(o + (R - q) * ds)] = cplx{C.r + S.i, C.i - S.r};
         }
       }
     }
@@ -700,23 +707,26 @@ __device__ __forceinline__ void ip_pass(cplx *buf, int nl, int ls, int es, const
 }
 
 // all passes of a length-N transform over (at most) NL lines
-template <int N, int NL, bool INV, int K = 0>
+template <int N, int NL, bool INV, bool LM = false, int K = 0>
 __device__ __forceinline__ void ip_transform(cplx *buf, int nl, int ls, int es, const cplx *tw,
                                              const AxisPlan &p) {
   if constexpr (K < fac_count(N)) {
-    ip_pass<N, NL, fac_radix(N, K), fac_ns(N, K), INV>(buf, nl, ls, es, tw + p.twoff[K]);
-    ip_transform<N, NL, INV, K + 1>(buf, nl, ls, es, tw, p);
+    ip_pass<N, NL, fac_radix(N, K), fac_ns(N, K), INV, LM>(buf, nl, ls, es, tw + p.twoff[K]);
+    ip_transform<N, NL, INV, LM, K + 1>(buf, nl, ls, es, tw, p);
   }
 }
 
+// line-major thread order, unswizzled slots: the x lines are NX apart (odd
+// on every instantiated plane), the y lines adjacent
 template <int NX, int NY>
 __device__ __forceinline__ void xy_transform(cplx *buf, const FftArgs &a, bool inv) {
+  static_assert(NX % 2 == 1, "conflict-free line-major passes need an odd row length");
   if (!inv) {
-    ip_transform<NX, NY, false>(buf, NY, NX, 1, a.tw_f, a.ax);
-    ip_transform<NY, NX, false>(buf, NX, 1, NX, a.tw_f, a.ay);
+    ip_transform<NX, NY, false, true>(buf, NY, NX, 1, a.tw_f, a.ax);
+    ip_transform<NY, NX, false, true>(buf, NX, 1, NX, a.tw_f, a.ay);
   } else {
-    ip_transform<NY, NX, true>(buf, NX, 1, NX, a.tw_b, a.ay);
-    ip_transform<NX, NY, true>(buf, NY, NX, 1, a.tw_b, a.ax);
+    ip_transform<NY, NX, true, true>(buf, NX, 1, NX, a.tw_b, a.ay);
+    ip_transform<NX, NY, true, true>(buf, NY, NX, 1, a.tw_b, a.ax);
   }
 }
 
@@ -729,17 +739,17 @@ __global__ void __launch_bounds__(PT, 1) k_fft_plane(const FftArgs a) {
   constexpr int plane = NX * NY;
   const int z = blockIdx.x;
   const int64_t off = (int64_t)z * plane;
-  for (int t = threadIdx.x; t < plane; t += PT) load_async(buf + sw(t), a, off + t);
+  for (int t = threadIdx.x; t < plane; t += PT) load_async(buf + t, a, off + t);
   cp_async_wait_all();
   __syncthreads();
   xy_transform<NX, NY>(buf, a, a.dir != 0);
   if (a.mid != MID_NONE) {
     for (int t = threadIdx.x; t < plane; t += PT)
-      buf[sw(t)] = mid_op(a, off + t, t % NX, t / NX, z, buf[sw(t)]);
+      buf[t] = mid_op(a, off + t, t % NX, t / NX, z, buf[t]);
     __syncthreads();
     if (a.second) xy_transform<NX, NY>(buf, a, a.dir == 0);
   }
-  for (int t = threadIdx.x; t < plane; t += PT) store(a, off + t, buf[sw(t)]);
+  for (int t = threadIdx.x; t < plane; t += PT) store(a, off + t, buf[t]);
 }
 
 // The z2 axis as a four-step transform, N = N1 * N2: z = N2 a + b
@@ -764,7 +774,6 @@ __global__ void __launch_bounds__(PT, (sizeof(real) == 4) ? 4 : 3) k_z4(const Ff
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx *buf = reinterpret_cast<cplx *>(smem_raw);
   constexpr int M = (STEP == 1) ? N2 : N1;  // length of this step's transforms
-  constexpr int ls = M + 1;
   constexpr int JS = PT / G;                 // element stride of a thread's loops
   const int64_t plane = (int64_t)a.T.nx * a.T.ny;  // = number of lines
   const int64_t ngroups = (plane + G - 1) / G;
@@ -772,8 +781,10 @@ __global__ void __launch_bounds__(PT, (sizeof(real) == 4) ? 4 : 3) k_z4(const Ff
   const int f = (int)((int64_t)blockIdx.x / ngroups);  // b (steps 0, 2) or k1 (step 1)
   const int64_t L0 = grp * G;
   const int nl = (int)min((int64_t)G, plane - L0);
-  // every element loop: consecutive threads take adjacent lines (adjacent in
-  // HBM, conflict-free shared slots), and a thread's line never changes
+  // the G lines interleaved in shared memory (element j of line l at
+  // j * G + l): every element loop and every butterfly pass has consecutive
+  // threads on adjacent lines (adjacent in HBM, consecutive shared slots: no
+  // bank conflicts), and a thread's line never changes in the element loops
   const int l = threadIdx.x % G, j0 = threadIdx.x / G;
   const bool on = l < nl;
   auto pos_of = [&](int j) -> int64_t {
@@ -781,35 +792,35 @@ __global__ void __launch_bounds__(PT, (sizeof(real) == 4) ? 4 : 3) k_z4(const Ff
     return pz * plane + L0 + l;
   };
   if (on)
-    for (int j = j0; j < M; j += JS) load_async(buf + sw(l * ls + j), a, pos_of(j));
+    for (int j = j0; j < M; j += JS) load_async(buf + j * G + l, a, pos_of(j));
   cp_async_wait_all();
   __syncthreads();
   if constexpr (STEP == 0) {
-    ip_transform<N1, G, false>(buf, nl, ls, 1, a.tw_f, a.ax);
+    ip_transform<N1, G, false, true>(buf, nl, 1, G, a.tw_f, a.ax);
     if (on)
       for (int k1 = j0; k1 < M; k1 += JS)
-        buf[sw(l * ls + k1)] = cmul(buf[sw(l * ls + k1)], a.tw4f[k1 * N2 + f]);
+        buf[k1 * G + l] = cmul(buf[k1 * G + l], a.tw4f[k1 * N2 + f]);
     __syncthreads();
   } else if constexpr (STEP == 1) {
-    ip_transform<N2, G, false>(buf, nl, ls, 1, a.tw_f, a.ay);
+    ip_transform<N2, G, false, true>(buf, nl, 1, G, a.tw_f, a.ay);
     if (on) {
       // adjacent lines are adjacent x: coalesced reads of the (x, kz) tables
       const int L = (int)(L0 + l);
       const int x = L % a.T.nx, y = L / a.T.nx;
       for (int k2 = j0; k2 < M; k2 += JS)
-        buf[sw(l * ls + k2)] = mid_op(a, 0, x, y, f + N1 * k2, buf[sw(l * ls + k2)]);
+        buf[k2 * G + l] = mid_op(a, 0, x, y, f + N1 * k2, buf[k2 * G + l]);
     }
     __syncthreads();
-    ip_transform<N2, G, true>(buf, nl, ls, 1, a.tw_b, a.ay);
+    ip_transform<N2, G, true, true>(buf, nl, 1, G, a.tw_b, a.ay);
     if (on)
       for (int b = j0; b < M; b += JS)
-        buf[sw(l * ls + b)] = cmul(buf[sw(l * ls + b)], a.tw4b[f * N2 + b]);
+        buf[b * G + l] = cmul(buf[b * G + l], a.tw4b[f * N2 + b]);
     __syncthreads();
   } else {
-    ip_transform<N1, G, true>(buf, nl, ls, 1, a.tw_b, a.ax);
+    ip_transform<N1, G, true, true>(buf, nl, 1, G, a.tw_b, a.ax);
   }
   if (on)
-    for (int j = j0; j < M; j += JS) store(a, pos_of(j), buf[sw(l * ls + j)]);
+    for (int j = j0; j < M; j += JS) store(a, pos_of(j), buf[j * G + l]);
 }
 
 // Instantiated transverse planes (square meshes of the workloads) and long
@@ -1089,7 +1100,7 @@ static int build_plan(pf_handle *h, Plan *&out) {
           tw4[(size_t)d->nz + (size_t)k1 * k.n2 + b] = cplx{(real)cos(ang), (real)-sin(ang)};
         }
       const int m = std::max(k.n1, k.n2);
-      d->z4_smem = (((size_t)k.g * (m + 1) + 15) / 16) * 16 * sizeof(cplx);
+      d->z4_smem = (((size_t)k.g * m + 15) / 16) * 16 * sizeof(cplx);
       if (d->z4_smem > (size_t)max_smem) continue;
       for (int q = 0; q < 3; ++q)
         PF_CUDA(cudaFuncSetAttribute((const void *)k.k[q],
