@@ -107,6 +107,11 @@ __global__ void k_to_c32(float2 *o, const double *re, const double *im, int64_t 
   if (t < n) o[t] = make_float2((float)re[t], (float)im[t]);
 }
 
+__global__ void k_to_f32(float *o, const double *v, int64_t n) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) o[t] = (float)v[t];
+}
+
 __global__ void k_from_c32(const float2 *o, double *re, double *im, int64_t n) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < n) {
@@ -188,7 +193,9 @@ static void free_particles(pf_handle *h) {
     h->k1[j] = h->ka[j] = h->kb[j] = nullptr;
   }
   cudaFree(h->chi);
+  cudaFree(h->chi_f);
   h->chi = nullptr;
+  h->chi_f = nullptr;
   h->cap = 0;
 }
 
@@ -222,6 +229,8 @@ static int alloc_particles(pf_handle *h, int64_t n) {
     PF_CUDA(cudaMalloc(&h->kb[j], b));
   }
   PF_CUDA(cudaMalloc(&h->chi, b));
+  if (h->p.precision == PF_MIXED)
+    PF_CUDA(cudaMalloc(&h->chi_f, sizeof(float) * (size_t)std::max<int64_t>(n, 1)));
   h->cap = n;
   return PF_OK;
 }
@@ -501,6 +510,10 @@ static int set_particles_impl(pf_handle *h, int64_t n, const double *const src[7
     for (int j = 0; j < 6; ++j)
       PF_CUDA(cudaMemcpyAsync(h->y[h->cur][j], src[j], b, kind, h->stream));
     PF_CUDA(cudaMemcpyAsync(h->chi, src[6], b, kind, h->stream));
+    if (h->chi_f) {
+      k_to_f32<<<grid_for(n, 256), 256, 0, h->stream>>>(h->chi_f, h->chi, n);
+      PF_LAUNCHED(h);
+    }
   }
   // fixed-point scale of the deposit from max |chi| / dV3
   double chimax = 0.0;

@@ -139,6 +139,7 @@ struct pf_handle {
   double *y[2][6] = {};       // double-buffered x, y, z2, px, py, gamma
   int cur = 0;
   double *chi = nullptr;
+  float *chi_f = nullptr;  // FP32 copy of chi (mixed precision), set with the particles
   double *k1[6] = {}, *ka[6] = {}, *kb[6] = {};
   int fix_e = 0, fix_maxexp = 126;
   double chi_max = 0.0;

@@ -64,7 +64,8 @@ struct BFieldF {
 struct MixArgs {
   const void *coef_tab;  // non-null: StageCoefF at [*step_ctr * 4 + stage - 1]
   const int *step_ctr;
-  const double *x, *y, *z2, *px, *py, *gam, *chi;
+  const double *x, *y, *z2, *px, *py, *gam;
+  const float *chi_f;  // chi rounded to FP32 (set with the particles)
   // slopes: FP32 arrays for x, y, px, py, Gamma (index 2 unused), FP64 for z2
   const float *kin_f[6];
   const double *kin_z;
@@ -279,19 +280,24 @@ __device__ __forceinline__ void mixed_block(const MixArgs &a, const int64_t i0, 
     for (int t = threadIdx.x; t < 4 * tile_n; t += MX_THREADS) thi_r[t] = 0;
     if (threadIdx.x == 0) s_pzlo = INT_MAX;
     __syncthreads();
-    int my_pzlo = INT_MAX;
+    // an estimate is enough (a wrong origin only sends deposits to HBM): the
+    // smallest z2 of the warp's particles, as the integer order of the bits
+    // of z2 >= 0, converted once per warp
+    long long kmin = LLONG_MAX;
 #pragma unroll
     for (int q = 0; q < ppt; ++q) {
       const int64_t i = i0 + q * MX_THREADS + threadIdx.x;
       if (halted || i >= i1) continue;
-      // an estimate is enough: a wrong origin only sends deposits to HBM
-      float fz = floorf(d2f_rn(a.z2[i]) * a.inv_dz2_f);
-      if (!(fabsf(fz) < 1.0e7f)) continue;
-      if (a.periodic) fz = fmaxf(fz - a.npl_f * floorf(fz * a.inv_npl_f), 0.f);
-      my_pzlo = min(my_pzlo, (int)fz);
+      kmin = min(kmin, __double_as_longlong(a.z2[i]));
     }
-    for (int o = 16; o > 0; o >>= 1) my_pzlo = min(my_pzlo, __shfl_xor_sync(0xffffffffu, my_pzlo, o));
-    if ((threadIdx.x & 31) == 0 && my_pzlo != INT_MAX) atomicMin(&s_pzlo, my_pzlo);
+    for (int o = 16; o > 0; o >>= 1) kmin = min(kmin, __shfl_xor_sync(0xffffffffu, kmin, o));
+    if ((threadIdx.x & 31) == 0 && kmin != LLONG_MAX) {
+      float fz = floorf(d2f_rn(__longlong_as_double(kmin)) * a.inv_dz2_f);
+      if (fabsf(fz) < 1.0e7f) {
+        if (a.periodic) fz = fmaxf(fz - a.npl_f * floorf(fz * a.inv_npl_f), 0.f);
+        atomicMin(&s_pzlo, (int)fz);
+      }
+    }
     __syncthreads();
   }
   const int pzlo = a.tile ? s_pzlo : 0;
@@ -404,7 +410,7 @@ __device__ __forceinline__ void mixed_block(const MixArgs &a, const int64_t i0, 
       }
       if (a.field_evolve) {
         // deposit (chi/dV3) (1 + eta p2)/Gamma p w_c to the 8 (2 on 1D) nodes
-        const float dw = d2f_rn(a.chi[i]) * a.inv_dV3 * qrG;
+        const float dw = a.chi_f[i] * a.inv_dV3 * qrG;
         const float sr = dw * PX, si = dw * PY;
         const int nc = ONED ? 2 : 8;
         const int tp0 = pz0 - pzlo, tp1 = pz1 - pzlo;
@@ -669,7 +675,7 @@ size_t pf_step_coefficients_f_bytes() { return 4 * sizeof(StageCoefF); }
 static void fill_mix_args(pf_handle *h, MixArgs &a, double hstep) {
   const pf_params &p = h->p;
   memset(&a, 0, sizeof(a));
-  a.chi = h->chi;
+  a.chi_f = h->chi_f;
   a.np = h->np;
   a.h6 = hstep / 6.0;
   a.acc = (float2 *)h->acc32;
