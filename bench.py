@@ -49,9 +49,10 @@ METRIC = "macroparticle-RK4-steps/s: mixed vs FP64 on GB300 at stated power erro
 UNIT = "macroparticle-steps/s"
 BYTES_PER_PARTICLE_STAGE = 104          # 56 B read + 48 B write (416 B per step)
 # DRAM read + write of one FP64 stage launch per macroparticle, from one ncu
-# capture of k_stage<3> on 2^22 macroparticles (the traffic grows with the
-# macroparticles; the window field is read from L2)
-TRAFFIC_PER_PARTICLE_STAGE = 807.2e6 / 4194304
+# capture of k_stage<3> on 2^22 macroparticles over 129 x 129 x 2048 planes
+# (the config-2 density; the traffic grows with the macroparticles, the
+# window field is mostly read from L2)
+TRAFFIC_PER_PARTICLE_STAGE = 881.5e6 / 4194304
 FLOPS_PER_PARTICLE_STAGE = 166          # ~664 FP64 flop per particle-step
 
 
@@ -635,8 +636,9 @@ def run_gpu(args, rank, world):
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": f"{peak_kind} copy bandwidth (burst)",
                      "traffic": n * TRAFFIC_PER_PARTICLE_STAGE,
-                     "traffic_source": "ncu dram bytes of k_stage<3> at 2^22 macroparticles, "
-                                       "scaled to the launch's macroparticles",
+                     "traffic_source": "ncu dram bytes of k_stage<3> at 2^22 macroparticles "
+                                       "on 129x129x2048 planes, scaled to the launch's "
+                                       "macroparticles",
                      "fp64": {"achieved_tflops": fp64_achieved, "peak_tflops": dgemm_tflops,
                               "peak_kind": "measured cuBLAS DGEMM 4096^3",
                               "frac": fp64_achieved / dgemm_tflops}},
