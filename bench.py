@@ -85,8 +85,9 @@ def parse():
                     help="skip the one-at-a-time comparison of the batched form")
     ap.add_argument("--no-batch-tune", action="store_true",
                     help="batched form with the default shapes (persistent grids)")
-    ap.add_argument("--adjoint-steps", type=int, default=256,
-                    help="steps of the adjoint leg on the 33x33x128 periodic mesh (0: skip)")
+    ap.add_argument("--adjoint-steps", type=int, default=3000,
+                    help="steps of the adjoint leg on the 33x33x128 periodic mesh (0: skip); "
+                         "3000 is the adjoint form's full run")
     return ap.parse_args()
 
 
