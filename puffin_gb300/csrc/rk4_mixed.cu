@@ -163,8 +163,8 @@ __device__ __forceinline__ int f2fix(float v, float scale) { return __float2int_
 
 // exact shared-tile add of a fixed-point value: high part (signed) and the
 // 20-bit low part into separate 32-bit words, non-returning reductions
+// (straight-line: a zero contribution adds zero)
 __device__ __forceinline__ void tile_add(int *hi, unsigned *lo, int r) {
-  if (r == 0) return;
   atomicAdd(hi, r >> 20);
   atomicAdd(lo, (unsigned)r & 0xFFFFFu);
 }
@@ -500,22 +500,25 @@ __device__ __forceinline__ void mixed_block(const MixArgs &a, const int64_t i0, 
       a.kacc_z[i] = kz;
     } else if (STAGE == 3) {
 #pragma unroll
+      // k2 is read again here rather than kept live through the body (the
+      // kernel runs at 40 registers)
       for (int t = 0; t < 5; ++t) {
         a.kout_f[kF[t]][i] = k[kF[t]];
-        a.kacc_f[kF[t]][i] = kin[kF[t]] + k[kF[t]];
+        a.kacc_f[kF[t]][i] = a.kin_f[kF[t]][i] + k[kF[t]];
       }
       a.kout_z[i] = kz;
-      a.kacc_z[i] = kz_in + kz;
+      a.kacc_z[i] = a.kin_z[i] + kz;
     } else {
-      // y + h/6 (k1 + k4 + 2 (k2 + k3)): the slope sum in FP32, the update in FP64
-      const double y0[6] = {x0, yv0, z0, px0, py0, g0};
+      // y + h/6 (k1 + k4 + 2 (k2 + k3)): the slope sum in FP32, the update in
+      // FP64 on the state read again (not kept live through the body)
+      const double y0[6] = {a.x[i], a.y[i], a.z2[i], a.px[i], a.py[i], a.gam[i]};
 #pragma unroll
       for (int t = 0; t < 5; ++t) {
         const int j = kF[t];
         const float sum = a.k1_f[j][i] + k[j] + 2.f * a.kacc_f[j][i];
         a.ynext[j][i] = fma(a.h6, f2d(sum), y0[j]);
       }
-      a.ynext[2][i] = fma(a.h6, a.k1_z[i] + kz + 2.0 * a.kacc_z[i], z0);
+      a.ynext[2][i] = fma(a.h6, a.k1_z[i] + kz + 2.0 * a.kacc_z[i], y0[2]);
     }
   }
 
