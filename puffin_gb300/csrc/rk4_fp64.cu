@@ -363,12 +363,16 @@ __device__ __forceinline__ void stage_particle(const StageArgs &a, const int64_t
     } else if (STAGE == 2) {
       a.kacc[j][i] = k[j];
     } else if (STAGE == 3) {
+      // k2 and (stage 4) the state are read again here rather than held
+      // live through the body: the same values, fewer registers
       a.kout[j][i] = k[j];
-      a.kacc[j][i] = kin[j] + k[j];
+      a.kacc[j][i] = a.kin[j][i] + k[j];
     } else {
       const double k1 = a.k1[j][i];
       const double k23 = a.kacc[j][i];
-      a.ynext[j][i] = y0[j] + a.h6 * (k1 + k[j] + 2.0 * k23);
+      const double yj = (j == 0) ? a.x[i] : (j == 1) ? a.y[i] : (j == 2) ? a.z2[i]
+                      : (j == 3) ? a.px[i] : (j == 4) ? a.py[i] : a.gam[i];
+      a.ynext[j][i] = yj + a.h6 * (k1 + k[j] + 2.0 * k23);
     }
   }
 }
