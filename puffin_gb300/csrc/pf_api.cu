@@ -194,8 +194,10 @@ static void free_particles(pf_handle *h) {
   }
   cudaFree(h->chi);
   cudaFree(h->chi_f);
+  cudaFree(h->base4);
   h->chi = nullptr;
   h->chi_f = nullptr;
+  h->base4 = nullptr;
   h->cap = 0;
 }
 
@@ -229,8 +231,10 @@ static int alloc_particles(pf_handle *h, int64_t n) {
     PF_CUDA(cudaMalloc(&h->kb[j], b));
   }
   PF_CUDA(cudaMalloc(&h->chi, b));
-  if (h->p.precision == PF_MIXED)
+  if (h->p.precision == PF_MIXED) {
     PF_CUDA(cudaMalloc(&h->chi_f, sizeof(float) * (size_t)std::max<int64_t>(n, 1)));
+    PF_CUDA(cudaMalloc(&h->base4, sizeof(float4) * (size_t)std::max<int64_t>(n, 1)));
+  }
   h->cap = n;
   return PF_OK;
 }

@@ -140,6 +140,7 @@ struct pf_handle {
   int cur = 0;
   double *chi = nullptr;
   float *chi_f = nullptr;  // FP32 copy of chi (mixed precision), set with the particles
+  float4 *base4 = nullptr; // FP32 x, y, px, py of the step's start state (mixed; stage 1 writes it)
   double *k1[6] = {}, *ka[6] = {}, *kb[6] = {};
   int fix_e = 0, fix_maxexp = 126;
   double chi_max = 0.0;

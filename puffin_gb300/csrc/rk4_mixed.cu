@@ -66,6 +66,7 @@ struct MixArgs {
   const int *step_ctr;
   const double *x, *y, *z2, *px, *py, *gam;
   const float *chi_f;  // chi rounded to FP32 (set with the particles)
+  float4 *base4;       // x, y, px, py of the step's start state in FP32 (stage 1 writes)
   // slopes: FP32 arrays for x, y, px, py, Gamma (index 2 unused), FP64 for z2
   const float *kin_f[6];
   const double *kin_z;
@@ -306,13 +307,26 @@ __device__ __forceinline__ void mixed_block(const MixArgs &a, const int64_t i0, 
   for (int q = 0; q < ppt; ++q) {
     const int64_t i = i0 + q * MX_THREADS + threadIdx.x;
     if (halted || i >= i1) continue;
-    // FP64 state; stage values of z2 and Gamma in FP64, of x, y, px, py in FP32
-    const double x0 = a.x[i], yv0 = a.y[i], z0 = a.z2[i], px0 = a.px[i], py0 = a.py[i],
-                 g0 = a.gam[i];
+    // FP64 state; stage values of z2 and Gamma in FP64, of x, y, px, py in
+    // FP32 from their FP32 roundings, which stage 1 keeps for the later stages
+    const double z0 = a.z2[i], g0 = a.gam[i];
     float kin[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     double kz_in = 0.0;
     double zs = z0, gs = g0;
-    float X = d2f_rn(x0), Y = d2f_rn(yv0), PX = d2f_rn(px0), PY = d2f_rn(py0);
+    float X, Y, PX, PY;
+    if (STAGE == 1) {
+      X = d2f_rn(a.x[i]);
+      Y = d2f_rn(a.y[i]);
+      PX = d2f_rn(a.px[i]);
+      PY = d2f_rn(a.py[i]);
+      a.base4[i] = make_float4(X, Y, PX, PY);
+    } else {
+      const float4 b = a.base4[i];
+      X = b.x;
+      Y = b.y;
+      PX = b.z;
+      PY = b.w;
+    }
     if (STAGE > 1) {
       kin[0] = a.kin_f[0][i];
       kin[1] = a.kin_f[1][i];
@@ -750,6 +764,7 @@ static void mix_stage_pointers(pf_handle *h, MixArgs &a, int s, int cur, double 
   a.px = h->y[cur][3];
   a.py = h->y[cur][4];
   a.gam = h->y[cur][5];
+  a.base4 = h->base4;
   a.cstate = stage_c[s - 1];
   a.cstate_f = (float)stage_c[s - 1];
   a.as = (const float2 *)((s == 1) ? h->w32 : h->as32);
