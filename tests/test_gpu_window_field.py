@@ -139,3 +139,94 @@ def test_host_driver_matches_resident_run_bitwise():
     np.testing.assert_array_equal(got_f[0], want_f[0])
     np.testing.assert_array_equal(got_f[1], want_f[1])
     np.testing.assert_array_equal(outer[0], want_f[0])
+
+
+def test_host_driver_golden_1d_run():
+    """The reference's own 1D end-to-end case (test/testMPIIntegration.pf)
+    driven through the host pattern: particles and the window field (here
+    the whole 1D field, one node per z2 plane) handed in and read back around
+    every rk4par call; the result matches the reference's golden dump to its
+    own 1e-10."""
+    import os
+    from tests import golden_beam as GB
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "f1main_expected.npz"))
+    cfg, h = GB.config()
+    ob = GB.initial_beam(cfg, g["electrons"][:, 6])
+    beam = {k: getattr(ob, k).copy() for k in P.PARTICLE_KEYS}
+    p = P.default_params(rho=cfg.rho, aw=cfg.aw, gamma_r=cfg.gamma_r, eta=cfg.eta,
+                         kappa=cfg.kappa, fx=cfg.fx, fy=cfg.fy, und_type=P.UND_PUFFIN,
+                         nx=1, ny=1, nz2=cfg.nz2, dx=1.0, dy=1.0, dz2=cfg.dz2, one_d=1,
+                         szfs=0.0, szfe=cfg.szfe)
+    with P.Puffin(p) as sim:
+        sim.set_particles(*(beam[k] for k in P.PARTICLE_KEYS))
+        sim.set_field(np.zeros(cfg.nz2), np.zeros(cfg.nz2))
+        assert sim.window == (1, 1) and sim.n_window == cfg.nz2
+        win = sim.get_window_field()
+        szl = 0.0
+        for _ in range(GB.NSTEPS):
+            sim.set_window_field(*win)
+            sim.set_particles(*(beam[k] for k in P.PARTICLE_KEYS))
+            assert sim.rk4par(szl, h)
+            szl += h
+            got = sim.get_particles()
+            for k in P.PARTICLE_KEYS:
+                beam[k] = got[k]
+            win = sim.get_window_field()
+        taper = sim.get_taper()
+    b = O.Beam(*(beam[k] for k in P.PARTICLE_KEYS))
+    O.match_out(cfg, b, szl, taper[0])
+    O.correct_trans(b)
+    e = g["electrons"]
+    for j, k in enumerate(("x", "y", "z2", "px", "py", "gam")):
+        np.testing.assert_allclose(getattr(b, k), e[:, j], rtol=0, atol=1e-10, err_msg=k)
+    np.testing.assert_allclose(win[0], g["aperp"][0], rtol=0, atol=1e-10)
+    np.testing.assert_allclose(win[1], g["aperp"][1], rtol=0, atol=1e-10)
+
+
+def test_host_driver_mixed_matches_resident_run():
+    """The same host pattern on the mixed path (FP32 window field: the FP64
+    host copy holds FP32 values, so the hand-over is exact): 12 steps with
+    diffraction every 4 against the resident mixed run, to the mixed path's
+    own run-to-run spread (FP32 atomics land in any order)."""
+    w, field = _setup(P.MIXED, seed=21)
+    h, every, nsteps = w.h, 4, 12
+    with P.Puffin(w.params) as sim:
+        sim.set_particles(*(w.beam[k] for k in P.PARTICLE_KEYS))
+        sim.set_field(*field)
+        szl = 0.0
+        for i in range(1, nsteps + 1):
+            assert sim.rk4par(szl, h)
+            szl += h
+            if i % every == 0:
+                sim.diffractIM(every * h)
+        want_p, want_f = sim.get_particles(), sim.get_field()
+    beam = {k: np.array(w.beam[k]) for k in P.PARTICLE_KEYS}
+    with P.Puffin(w.params) as sim:
+        sim.set_particles(*(beam[k] for k in P.PARTICLE_KEYS))
+        sim.set_field(*field)
+        outer = sim.get_field()
+        win = sim.get_window_field()
+        szl = 0.0
+        for i in range(1, nsteps + 1):
+            diff = i % every == 0
+            if diff:
+                sim.set_field(*outer)
+            sim.set_window_field(*win)
+            sim.set_particles(*(beam[k] for k in P.PARTICLE_KEYS))
+            assert sim.rk4par(szl, h)
+            szl += h
+            if diff:
+                sim.diffractIM(every * h)
+            got = sim.get_particles()
+            for k in P.PARTICLE_KEYS:
+                beam[k] = got[k]
+            win = sim.get_window_field()
+            if diff:
+                outer = sim.get_field()
+    for k in ("x", "y", "z2", "px", "py", "gam"):
+        # the tolerances of the mixed graph-block test: FP32 rounding of
+        # differently ordered atomics, to 1e-5 of each coordinate's scale
+        np.testing.assert_allclose(beam[k], want_p[k], rtol=1e-5, atol=1e-7, err_msg=k)
+    scale = max(np.max(np.abs(want_f[0])), np.max(np.abs(want_f[1])))
+    np.testing.assert_allclose(outer[0], want_f[0], rtol=0, atol=1e-4 * scale)
+    np.testing.assert_allclose(outer[1], want_f[1], rtol=0, atol=1e-4 * scale)
