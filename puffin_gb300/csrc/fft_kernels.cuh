@@ -46,6 +46,7 @@ struct AxisPlan {
   int64_t nlines;
   int lpb;
   int axis;         // 0 x, 1 y, 2 z
+  int pfa;          // 1: n = 129 = 3 * 43 as a prime-factor transform (k_fft)
 };
 
 struct MulTables {
@@ -362,11 +363,119 @@ __device__ __forceinline__ void stockham_pass(const cplx *in, cplx *out, int n, 
   }
 }
 
+// n = 129 = 3 * 43 as a prime-factor (Good-Thomas) transform: input
+// element (n1, n2) at (43 n1 + 3 n2) mod 129, output (k1, k2) at
+// (43 k1 + 87 k2) mod 129 (87 = 3 * (3^-1 mod 43)), so that the 3-point and
+// 43-point DFTs need no twiddle factors between them (the mixed-radix form
+// multiplies 126 values per line by twiddles).  Pass 1: the 43 three-point
+// DFTs over n1, written as Y[k1][n2] at k1 * 43 + n2.
+template <bool INV>
+__device__ __forceinline__ void pfa129_pass3(const cplx *in, cplx *out, int nl) {
+  const real c = c_roots[root_off(3) + 1].r, sn = c_roots[root_off(3) + 1].i;
+  for (int t = threadIdx.x; t < nl * 43; t += NTHREADS) {
+    const int l = t / 43, n2 = t - l * 43;
+    const cplx *src = in + l * 129;
+    const int i0 = 3 * n2;
+    int i1 = i0 + 43, i2 = i0 + 86;
+    if (i1 >= 129) i1 -= 129;
+    if (i2 >= 129) i2 -= 129;
+    const cplx x0 = src[i0], u = src[i1], w = src[i2];
+    const cplx av = cadd(u, w), bv = csub(u, w);
+    cplx C = x0;
+    C.r = fma(av.r, c, C.r);
+    C.i = fma(av.i, c, C.i);
+    const cplx S{bv.r * sn, bv.i * sn};
+    cplx *dst = out + l * 129 + n2;
+    dst[0] = cadd(x0, av);
+    if (!INV) {
+      dst[43] = cplx{C.r + S.i, C.i - S.r};
+      dst[86] = cplx{C.r - S.i, C.i + S.r};
+    } else {
+      dst[43] = cplx{C.r - S.i, C.i + S.r};
+      dst[86] = cplx{C.r + S.i, C.i - S.r};
+    }
+  }
+}
+
+// Pass 2: the three 43-point DFTs over n2 (contiguous inputs Y[k1][.]),
+// outputs to (43 k1 + 87 k2) mod 129; the butterfly shared by odd_groups(43)
+// threads as in odd_pass_shared.
+template <bool INV>
+__device__ __forceinline__ void pfa129_pass43(const cplx *in, cplx *out, int nl, cplx *scratch) {
+  constexpr int R = 43, H = 21;
+  constexpr int G = odd_groups(R);
+  constexpr int OFF = root_off(R);
+  constexpr int BPR = NTHREADS / G;
+  const int nbt = nl * 3;
+  const int btl = threadIdx.x / G, g = threadIdx.x - (threadIdx.x / G) * G;
+  for (int base = 0; base < nbt; base += BPR) {
+    const int bt = base + btl;
+    const bool act = (btl < BPR) && (bt < nbt);
+    int l = 0, j = 0;
+    cplx *ab = scratch + btl * R;
+    if (act) {
+      l = bt / 3;
+      j = bt - l * 3;
+      const cplx *src = in + l * 129 + j * 43;
+      for (int jj = g + 1; jj <= H; jj += G) {
+        const cplx u = src[jj], w = src[R - jj];
+        ab[jj - 1] = cadd(u, w);
+        ab[H + jj - 1] = csub(u, w);
+      }
+    }
+    __syncthreads();
+    if (act) {
+      const cplx x0 = in[l * 129 + j * 43];
+      cplx *dst = out + l * 129;
+      const int k0 = 43 * j;
+      if (g == 0) {
+        cplx s0 = x0;
+#pragma unroll
+        for (int jj = 0; jj < H; ++jj) s0 = cadd(s0, ab[jj]);
+        dst[k0] = s0;
+      }
+#pragma unroll 1
+      for (int q = g + 1; q <= H; q += G) {
+        cplx C = x0, S{(real)0, (real)0};
+        int m = 0;
+#pragma unroll
+        for (int jj = 1; jj <= H; ++jj) {
+          m += q;
+          if (m >= R) m -= R;
+          const real c = c_roots[OFF + m].r;
+          const real sn = c_roots[OFF + m].i;
+          const cplx av = ab[jj - 1], bv = ab[H + jj - 1];
+          C.r = fma(av.r, c, C.r);
+          C.i = fma(av.i, c, C.i);
+          S.r = fma(bv.r, sn, S.r);
+          S.i = fma(bv.i, sn, S.i);
+        }
+        const int kq = (k0 + 87 * q) % 129, kr = (k0 + 87 * (R - q)) % 129;
+        if (!INV) {
+          dst[kq] = cplx{C.r + S.i, C.i - S.r};
+          dst[kr] = cplx{C.r - S.i, C.i + S.r};
+        } else {
+          dst[kq] = cplx{C.r - S.i, C.i + S.r};
+          dst[kr] = cplx{C.r + S.i, C.i - S.r};
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // All passes of one transform; returns the buffer that holds the result.
 template <bool INV>
 __device__ __noinline__ cplx *transform(cplx *buf0, cplx *buf1, cplx *scratch, const AxisPlan &p,
                                         int nl, const cplx *tw) {
   cplx *in = buf0, *out = buf1;
+  if (p.pfa) {
+    pfa129_pass3<INV>(in, out, nl);
+    __syncthreads();
+    pfa129_pass43<INV>(out, in, nl, scratch);
+    __syncthreads();
+    return in;
+  }
   for (int ps = 0; ps < p.npass; ++ps) {
     const int R = p.radix[ps], Ns = p.ns[ps];
     const cplx *twp = tw + p.twoff[ps];
@@ -1021,6 +1130,7 @@ static int build_plan(pf_handle *h, Plan *&out) {
       return PF_BAD_ARG;
     }
     ap.npass = (int)f.size();
+    ap.pfa = (ap.n == 129) ? 1 : 0;
     int scratch = 0;
     for (int r : f) scratch = std::max(scratch, odd_scratch(r));
     int ns = 1;
