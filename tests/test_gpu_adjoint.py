@@ -5,7 +5,7 @@ against pf_run on the same inputs.
 Workload: the config-1 mesh (periodic, helical, 21 x 21 x 64 unique planes),
 4096 macroparticles, 32 steps with diffraction every 8 and checkpoints every
 8, a 16-point taper profile, a Gaussian seed (waist 1.0) at amplitude 1e-2
-and an energy chirp.  Tolerance (the benchmark spec): the adjoint gradient within
+and an energy chirp.  Tolerance (the adjoint form's target): the adjoint gradient within
 1e-4 relative of central differences with steps of 1e-6, for every component
 larger than 1e-3 of the largest.
 """
