@@ -25,7 +25,7 @@ merged diffraction call (dz = 8 h), exactly as UndSection schedules them.
 Fortran + MPI + FFTW-MPI + parallel HDF5 and cannot be built here, so the
 oracle restatement stands in) and prints its own line.
 
-N > 1 (torchrun): the path does not shard in this build, so N independent
+N > 1 (torchrun): the path does not shard here, so N independent
 replicas run one per GPU ("replicas only"); value sums over ranks and the
 time is the maximum over ranks.
 """

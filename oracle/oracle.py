@@ -1,8 +1,8 @@
 """CPU oracle for the Puffin hot path (TEST INFRASTRUCTURE ONLY).
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline
-leg may import this module, and only as the checker: the GPU library never
-calls it.  It restates the reference's algorithm on the CPU:
+leg may import this module, and only to compare against: the GPU library
+never calls it.  It restates the reference's algorithm on the CPU:
 
 * the RK4 particle/field push (``puffin_oracle.c``, reached through ctypes);
 * the diffraction step in numpy (``diffract``), following
