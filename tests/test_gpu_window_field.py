@@ -230,3 +230,29 @@ def test_host_driver_mixed_matches_resident_run():
     scale = max(np.max(np.abs(want_f[0])), np.max(np.abs(want_f[1])))
     np.testing.assert_allclose(outer[0], want_f[0], rtol=0, atol=1e-4 * scale)
     np.testing.assert_allclose(outer[1], want_f[1], rtol=0, atol=1e-4 * scale)
+
+
+def test_set_particles_keeps_a_covering_window():
+    """pf_set_particles computes the window (getInNode) for the first beam,
+    grows it for a wider one and keeps it for a narrower one; pf_redistribute
+    recomputes it from the particles, as the reference does."""
+    w, field = _setup(P.FP64, seed=31, np_=2048)
+    beam = {k: np.array(v) for k, v in w.beam.items()}
+    narrow = dict(beam, x=0.5 * beam["x"], y=0.5 * beam["y"])
+    with P.Puffin(w.params) as sim:
+        sim.set_particles(*(narrow[k] for k in P.PARTICLE_KEYS))
+        sim.set_field(*field)
+        w0 = sim.window
+        sim.set_particles(*(beam[k] for k in P.PARTICLE_KEYS))
+        w1 = sim.window
+        assert w1[0] > w0[0] and w1[1] > w0[1]
+        sim.set_particles(*(narrow[k] for k in P.PARTICLE_KEYS))
+        assert sim.window == w1
+        sim.redistribute()
+        assert sim.window == w0
+        # the field survives the window changes (inner2Outer before each)
+        fr, fi = sim.get_field()
+    cfg = oracle_config(w.params)
+    re, im = _mirrored(cfg, field)
+    np.testing.assert_array_equal(fr, re)
+    np.testing.assert_array_equal(fi, im)
