@@ -434,6 +434,9 @@ __device__ __forceinline__ void mixed_block(const MixArgs &a, const int64_t i0, 
           // the common case: both planes in the tile, and every corner's
           // |w s| <= |s| fits the tile's range (0 <= w <= 1)
           const int t0 = tp0 * ntr + (ONED ? 0 : (int)b0), t1 = tp1 * ntr + (ONED ? 0 : (int)b0);
+          // the source scaled to the tile's fixed point once (a power of two:
+          // exact), so each corner is one product and one conversion
+          const float srs = sr * a.fix_scale, sis = si * a.fix_scale;
 #pragma unroll
           for (int c = 0; c < 8; ++c) {
             if (c >= nc) break;
@@ -447,8 +450,8 @@ __device__ __forceinline__ void mixed_block(const MixArgs &a, const int64_t i0, 
               w = (cx ? x2 : x1) * (cy ? y2 : y1) * (cz ? zw2 : zw1);
               ti = (cz ? t1 : t0) + cx + cy * a.nix;
             }
-            tile_add(thi_r + ti, tlo_r + ti, f2fix(w * sr, a.fix_scale));
-            tile_add(thi_i + ti, tlo_i + ti, f2fix(w * si, a.fix_scale));
+            tile_add(thi_r + ti, tlo_r + ti, __float2int_rz(w * srs));
+            tile_add(thi_i + ti, tlo_i + ti, __float2int_rz(w * sis));
           }
         } else {
 #pragma unroll
