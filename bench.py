@@ -513,10 +513,11 @@ def run_gpu(args, rank, world):
     every = w.isteps4diff
 
     # end to end through the C ABI with host buffers, in UndSection's data
-    # flow: every step hands in the particles (7 arrays) and the inner-window
-    # field (the arrays rk4par advances) from pinned host memory and reads the
-    # six evolving particle arrays and the window back; the outer field goes
-    # in before and comes back after each diffraction call (every 8th step)
+    # flow: every step hands in the six evolving particle arrays (chi, which
+    # rk4par never changes, is handed in once before the steps) and the
+    # inner-window field (the arrays rk4par advances) from pinned host memory
+    # and reads them back; the outer field goes in before and comes back
+    # after each diffraction call (every 8th step)
     n = w.np
     pin = {k: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy() for k in P.PARTICLE_KEYS}
     fre = torch.empty(sim.n_outer, dtype=torch.float64, pin_memory=True).numpy()
@@ -549,7 +550,7 @@ def run_gpu(args, rank, world):
         if diff:
             assert lib.pf_set_field(sim._h, fre.ctypes.data, fim.ctypes.data) == 0
         assert lib.pf_set_window_field(sim._h, wre.ctypes.data, wim.ctypes.data) == 0
-        assert lib.pf_set_particles(sim._h, n, *ptrs) == 0
+        assert lib.pf_set_particles(sim._h, n, *ptrs[:6], None) == 0   # chi kept
         step()
         if lib.pf_window_nodes(sim._h) != nw:
             # the particles needed a larger window (pf_set_particles) or a
@@ -570,7 +571,7 @@ def run_gpu(args, rank, world):
         torch.distributed.barrier()
     e2e_ms = max(t0.elapsed_time(t1), 1e-9)
     k_e2e = max(1, args.e2e_steps)
-    h2d = (7 * 8 * n + 2 * 8 * nw) + 2 * 8 * sim.n_outer * n_diff / k_e2e
+    h2d = (6 * 8 * n + 2 * 8 * nw) + 2 * 8 * sim.n_outer * n_diff / k_e2e
     d2h = (6 * 8 * n + 2 * 8 * nw) + 2 * 8 * sim.n_outer * n_diff / k_e2e
     e2e_diff_calls = n_diff
     sim.close()
@@ -633,9 +634,9 @@ def run_gpu(args, rank, world):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "steps": args.e2e_steps,
                 "diffraction_calls": e2e_diff_calls, "window_changes": window_changes,
-                "per_step": "particles (7 arrays in, 6 out) and the inner-window field, "
-                            "in and out; the outer field in and out around each "
-                            "diffraction call"},
+                "per_step": "the six evolving particle arrays and the inner-window "
+                            "field, in and out (chi handed in once before the steps); "
+                            "the outer field in and out around each diffraction call"},
         "gpu_launches": r64["launches"] + (rmx["launches"] if rmx else 0)
         + (c3["fp64"]["launches"] + c3["mixed"]["launches"] if c3 else 0),
         "kernel_ms": kern,

@@ -118,7 +118,10 @@ int pf_destroy(pf_handle *h);
  * pf_set_particles also computes the inner window the particles need
  * (getInNode, parallel/para_field.f90:1432-1508) when the handle has none
  * yet or the current one is too small; a larger current window is kept (the
- * reference recomputes it only at redistribution: pf_redistribute). */
+ * reference recomputes it only at redistribution: pf_redistribute).  chi may
+ * be NULL to keep the handle's chi (rk4par never changes it) when n is the
+ * current macroparticle count, else PF_BAD_ARG; pf_get_particles skips every
+ * NULL destination. */
 int pf_set_particles(pf_handle *h, int64_t n, const double *x, const double *y,
                      const double *z2, const double *px, const double *py,
                      const double *gam, const double *chi);

@@ -502,8 +502,16 @@ int pf_destroy(pf_handle *h) {
 static int set_particles_impl(pf_handle *h, int64_t n, const double *const src[7],
                               cudaMemcpyKind kind) {
   if (!h || n < 0) return PF_BAD_ARG;
-  for (int j = 0; j < 7; ++j)
+  for (int j = 0; j < 6; ++j)
     if (n > 0 && !src[j]) return PF_BAD_ARG;
+  // chi == NULL keeps the handle's chi (and its fixed-point scale): only for
+  // the same macroparticles, as a driver that hands the state in every step
+  // passes them (rk4par never changes chi)
+  const bool keep_chi = (src[6] == nullptr);
+  if (n > 0 && keep_chi && !(h->particles_set && n == h->np)) {
+    h->err = "pf_set_particles: chi may be NULL only to keep the current macroparticles' chi";
+    return PF_BAD_ARG;
+  }
   cudaSetDevice(h->dev);
   int rc = alloc_particles(h, n);
   if (rc) return rc;
@@ -513,12 +521,15 @@ static int set_particles_impl(pf_handle *h, int64_t n, const double *const src[7
   if (n > 0) {
     for (int j = 0; j < 6; ++j)
       PF_CUDA(cudaMemcpyAsync(h->y[h->cur][j], src[j], b, kind, h->stream));
-    PF_CUDA(cudaMemcpyAsync(h->chi, src[6], b, kind, h->stream));
-    if (h->chi_f) {
-      k_to_f32<<<grid_for(n, 256), 256, 0, h->stream>>>(h->chi_f, h->chi, n);
-      PF_LAUNCHED(h);
+    if (!keep_chi) {
+      PF_CUDA(cudaMemcpyAsync(h->chi, src[6], b, kind, h->stream));
+      if (h->chi_f) {
+        k_to_f32<<<grid_for(n, 256), 256, 0, h->stream>>>(h->chi_f, h->chi, n);
+        PF_LAUNCHED(h);
+      }
     }
   }
+  if (keep_chi && n > 0) return choose_window(h, true);
   // fixed-point scale of the deposit from max |chi| / dV3
   double chimax = 0.0;
   if (n > 0) {

@@ -88,8 +88,9 @@ class Puffin:
         raise PuffinError(rc, self._lib.pf_last_error(self._h).decode())
 
     # -- particles --------------------------------------------------------------
-    def set_particles(self, x, y, z2, px, py, gam, chi):
-        arrs = [x, y, z2, px, py, gam, chi]
+    def set_particles(self, x, y, z2, px, py, gam, chi=None):
+        """chi=None keeps the handle's chi (same macroparticle count)."""
+        arrs = [x, y, z2, px, py, gam] + ([] if chi is None else [chi])
         if all(_is_torch_cuda(a) for a in arrs):
             keep = [_dev(a) for a in arrs]
             fn = self._lib.pf_set_particles_dev
@@ -99,7 +100,8 @@ class Puffin:
         n = len(keep[0][0])
         if any(len(k[0]) != n for k in keep):
             raise ValueError("particle arrays differ in length")
-        self._check(fn(self._h, n, *(k[1] for k in keep)))
+        ptrs = [k[1] for k in keep] + ([None] if chi is None else [])
+        self._check(fn(self._h, n, *ptrs))
 
     @property
     def n_particles(self):

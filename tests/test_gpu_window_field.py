@@ -165,7 +165,8 @@ def test_host_driver_golden_1d_run():
         szl = 0.0
         for _ in range(GB.NSTEPS):
             sim.set_window_field(*win)
-            sim.set_particles(*(beam[k] for k in P.PARTICLE_KEYS))
+            # chi, which rk4par never changes, stays on the device
+            sim.set_particles(*(beam[k] for k in P.PARTICLE_KEYS[:6]))
             assert sim.rk4par(szl, h)
             szl += h
             got = sim.get_particles()
@@ -256,3 +257,17 @@ def test_set_particles_keeps_a_covering_window():
     re, im = _mirrored(cfg, field)
     np.testing.assert_array_equal(fr, re)
     np.testing.assert_array_equal(fi, im)
+
+
+def test_keeping_chi_needs_the_same_macroparticles():
+    w, field = _setup(P.FP64, seed=33, np_=1024)
+    b = w.beam
+    with P.Puffin(w.params) as sim:
+        with pytest.raises(P.PuffinError):      # no chi on the handle yet
+            sim.set_particles(*(b[k] for k in P.PARTICLE_KEYS[:6]))
+        sim.set_particles(*(b[k] for k in P.PARTICLE_KEYS))
+        sim.set_particles(*(b[k] for k in P.PARTICLE_KEYS[:6]))
+        with pytest.raises(P.PuffinError):      # a different count needs its chi
+            sim.set_particles(*(b[k][:-1] for k in P.PARTICLE_KEYS[:6]))
+        got = sim.get_particles()
+    np.testing.assert_array_equal(got["chi"], b["chi"])
