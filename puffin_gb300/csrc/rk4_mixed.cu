@@ -24,7 +24,7 @@
 // that), which is accurate to 1e-13 or better and needs no square root or
 // division.
 //
-// Deposit: each block of up to 2048 macroparticles (up to 4 per thread; fewer
+// Deposit: each block of up to 3072 macroparticles (up to 6 per thread; fewer
 // for beams too small to fill the SMs) accumulates its
 // contributions to the three z2 planes from the lowest plane its particles
 // start from in a shared-memory tile, deposited as each macroparticle's
@@ -34,8 +34,9 @@
 // v * 2^E truncated (|v * 2^E| < 2^31, E chosen per beam from max
 // chi/dV3, one float-to-int conversion) split into a signed high part
 // (v >> 20) and a 20-bit low part, which are added with two non-returning
-// 32-bit shared-memory reductions into separate words; up to 2048 low parts
-// of < 2^20 cannot overflow 32 bits, so no carry is lost.
+// 32-bit shared-memory reductions into separate words; the 3072 low parts
+// (< 2^20 each) a node can receive from one block stay below 2^32 (up to
+// 4096 would), so no carry is lost.
 // The flush forms (sum_hi 2^20 + sum_lo) 2^-E in FP32 once per node and adds
 // it to HBM with one float atomic per component.  Contributions
 // outside the tile, or larger than the tile's range, go straight to HBM.
@@ -53,7 +54,9 @@
 namespace {
 
 constexpr int MX_THREADS = 512;
-constexpr int MX_PPT = 4;  // macroparticles per thread
+constexpr int MX_PPT = 6;  // macroparticles per thread
+// the unsigned low words of the exact tile hold up to 4096 parts below 2^20
+static_assert(MX_THREADS * MX_PPT <= 4096, "tile low words could carry");
 constexpr int MX_TILE_PLANES = 3;
 
 struct BFieldF {
