@@ -766,7 +766,8 @@ int pf_batch_tune(pf_batch *b, const double *hstep, const double *szl, int32_t r
   {
     std::vector<char> act0 = b->active;
     const std::vector<int64_t> cand =
-        b->mixed ? std::vector<int64_t>{0, 1024, 2048, 3072} : std::vector<int64_t>{0, 2048, 4096, 8192};
+        b->mixed ? std::vector<int64_t>{0, 1024, 2048, 3072, 4096}
+                 : std::vector<int64_t>{0, 2048, 4096, 8192};
     for (int i = 0; i < b->n && out == PF_OK; ++i) {
       const pf_handle *h = b->inst[i];
       const ModeKey key{b->mixed ? 1 : 0, h->nix, h->niy, (int)h->npl, h->np};

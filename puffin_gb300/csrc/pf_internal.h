@@ -247,7 +247,7 @@ int pf_resident_blocks(const void *kernel, int threads, size_t smem);
 constexpr int PF_FT_PPB = 8192;  // largest dense-mode tile of the FP64 stage
 // batched mixed-precision launches (rk4_mixed.cu); the argument records are
 // opaque to the callers
-constexpr int PF_MX_THREADS = 512, PF_MX_PPT = 6;
+constexpr int PF_MX_THREADS = 512, PF_MX_PPT = 8;
 size_t pf_mixed_stage_args_bytes();
 size_t pf_mixed_node_args_bytes();
 size_t pf_mixed_tile_smem(const pf_handle *h);

@@ -24,7 +24,8 @@
 // that), which is accurate to 1e-13 or better and needs no square root or
 // division.
 //
-// Deposit: each block of up to 3072 macroparticles (up to 6 per thread; fewer
+// Deposit: each block of up to 3072 macroparticles (6 per thread; 8 for beams
+// dense along z2; fewer
 // for beams too small to fill the SMs) accumulates its
 // contributions to the three z2 planes from the lowest plane its particles
 // start from in a shared-memory tile, deposited as each macroparticle's
@@ -34,9 +35,9 @@
 // v * 2^E truncated (|v * 2^E| < 2^31, E chosen per beam from max
 // chi/dV3, one float-to-int conversion) split into a signed high part
 // (v >> 20) and a 20-bit low part, which are added with two non-returning
-// 32-bit shared-memory reductions into separate words; the 3072 low parts
-// (< 2^20 each) a node can receive from one block stay below 2^32 (up to
-// 4096 would), so no carry is lost.
+// 32-bit shared-memory reductions into separate words; the at most 4096 low
+// parts (< 2^20 each) a node can receive from one block stay below 2^32, so
+// no carry is lost.
 // The flush forms (sum_hi 2^20 + sum_lo) 2^-E in FP32 once per node and adds
 // it to HBM with one float atomic per component.  Contributions
 // outside the tile, or larger than the tile's range, go straight to HBM.
@@ -54,7 +55,7 @@
 namespace {
 
 constexpr int MX_THREADS = 512;
-constexpr int MX_PPT = 6;  // macroparticles per thread
+constexpr int MX_PPT = 8;  // macroparticles per thread, at most
 // the unsigned low words of the exact tile hold up to 4096 parts below 2^20
 static_assert(MX_THREADS * MX_PPT <= 4096, "tile low words could carry");
 constexpr int MX_TILE_PLANES = 3;
@@ -906,9 +907,13 @@ int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_ou
   if (h->capturing) n.step_ctr = h->step_ctr;
 
   PF_CUDA(mixed_attrs());
-  // up to MX_PPT macroparticles per thread, fewer when the beam is too small
-  // to give every SM two blocks
-  a.ppt = (int)std::max<int64_t>(1, std::min<int64_t>(MX_PPT, h->np / ((int64_t)152 * 2 * MX_THREADS)));
+  // six macroparticles per thread (3072 per block), eight for beams dense
+  // along z2 (a block then still spans a fraction of a plane; six and eight
+  // measured best for the config-2 and the config-1-mesh 2^24 beams), fewer
+  // when the beam is too small to give every SM two blocks
+  const int64_t per_plane = h->np / std::max<int64_t>(1, (int64_t)h->npl);
+  const int64_t want = (per_plane >= (int64_t)16 * MX_THREADS) ? MX_PPT : 6;
+  a.ppt = (int)std::max<int64_t>(1, std::min<int64_t>(want, h->np / ((int64_t)152 * 2 * MX_THREADS)));
   const int64_t per_block = (int64_t)MX_THREADS * a.ppt;
   const unsigned pg = (unsigned)std::max<int64_t>(1, (h->np + per_block - 1) / per_block);
   const unsigned ng = (unsigned)std::max<int64_t>(1, (h->nwin + 255) / 256);
