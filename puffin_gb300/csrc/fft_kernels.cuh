@@ -1,3 +1,4 @@
+#include <type_traits>
 // FFT diffraction kernels and host plan, instantiated once per real type
 // (included by fft.cu with FFT_T = double / float and FFT_NS = fft64 / fft32).
 
@@ -715,8 +716,16 @@ __device__ __forceinline__ int sw(int i) {
 // bank on when ls is 1 (interleaved lines) or odd.  Else consecutive threads
 // take consecutive butterflies of a line and the XOR swizzle spreads their
 // strided accesses (about two wavefronts per ideal one remain).
-template <int N, int NL, int R, int NS, bool INV, bool LM = false>
-__device__ __forceinline__ void ip_pass(cplx *buf, int nl, int ls, int es, const cplx *tw) {
+// element-wise operation applied to the outputs of a transform's last pass
+// (line l, element e of the line), in place of a separate pass over shared
+// memory; NoPost leaves them
+struct NoPost {
+  __device__ __forceinline__ cplx operator()(int, int, cplx v) const { return v; }
+};
+
+template <int N, int NL, int R, int NS, bool INV, bool LM = false, class Post = NoPost>
+__device__ __forceinline__ void ip_pass(cplx *buf, int nl, int ls, int es, const cplx *tw,
+                                        const Post &post = Post()) {
   constexpr int NB = N / R;
   constexpr int MAXB = (NL * NB + PT - 1) / PT;
   const int total = LM ? NL * NB : nl * NB;
@@ -724,6 +733,7 @@ __device__ __forceinline__ void ip_pass(cplx *buf, int nl, int ls, int es, const
   int obase[MAXB];
   if constexpr (R == 2 || R == 4 || R == 8) {
     cplx v[MAXB][R];
+    int lb[MAXB], eb[MAXB];
 #pragma unroll
     for (int b = 0; b < MAXB; ++b) {
       const int t = threadIdx.x + b * PT;
@@ -738,7 +748,9 @@ __device__ __forceinline__ void ip_pass(cplx *buf, int nl, int ls, int es, const
 #pragma unroll
           for (int r = 1; r < R; ++r) v[b][r] = cmul(v[b][r], tw[k * R + r]);
         }
-        obase[b] = l * ls + ((j / NS) * NS * R + k) * es;
+        lb[b] = l;
+        eb[b] = (j / NS) * NS * R + k;
+        obase[b] = l * ls + eb[b] * es;
       }
     }
     __syncthreads();
@@ -747,10 +759,12 @@ __device__ __forceinline__ void ip_pass(cplx *buf, int nl, int ls, int es, const
       if (obase[b] < 0) continue;
       dft_regs<R, INV>(v[b]);
 #pragma unroll
-      for (int r = 0; r < R; ++r) buf[slot(obase[b] + r * NS * es)] = v[b][r];
+      for (int r = 0; r < R; ++r)
+        buf[slot(obase[b] + r * NS * es)] = post(lb[b], eb[b] + r * NS, v[b][r]);
     }
     __syncthreads();
   } else {
+    static_assert(std::is_same<Post, NoPost>::value, "output operations on radix 2, 4, 8 passes only");
     constexpr int H = (R - 1) / 2;
     constexpr int OFF = root_off(R);
     static_assert(OFF >= 0, "radix without an unrolled butterfly");
@@ -816,12 +830,16 @@ __device__ __forceinline__ void ip_pass(cplx *buf, int nl, int ls, int es, const
 }
 
 // all passes of a length-N transform over (at most) NL lines
-template <int N, int NL, bool INV, bool LM = false, int K = 0>
+template <int N, int NL, bool INV, bool LM = false, int K = 0, class Post = NoPost>
 __device__ __forceinline__ void ip_transform(cplx *buf, int nl, int ls, int es, const cplx *tw,
-                                             const AxisPlan &p) {
+                                             const AxisPlan &p, const Post &post = Post()) {
   if constexpr (K < fac_count(N)) {
-    ip_pass<N, NL, fac_radix(N, K), fac_ns(N, K), INV, LM>(buf, nl, ls, es, tw + p.twoff[K]);
-    ip_transform<N, NL, INV, LM, K + 1>(buf, nl, ls, es, tw, p);
+    if constexpr (K + 1 == fac_count(N))
+      ip_pass<N, NL, fac_radix(N, K), fac_ns(N, K), INV, LM>(buf, nl, ls, es, tw + p.twoff[K],
+                                                             post);
+    else
+      ip_pass<N, NL, fac_radix(N, K), fac_ns(N, K), INV, LM>(buf, nl, ls, es, tw + p.twoff[K]);
+    ip_transform<N, NL, INV, LM, K + 1>(buf, nl, ls, es, tw, p, post);
   }
 }
 
@@ -877,6 +895,26 @@ __global__ void __launch_bounds__(PT, 1) k_fft_plane(const FftArgs a) {
 // per plane) of one short transform, about 33 KB, so several blocks share an
 // SM.  The short transforms are the in-place shared-memory passes above, with
 // their plans in a.ax (length N1) and a.ay (length N2).
+// output operations of the four-step kernels: the twiddle tw[e * s + c] of
+// element e, and the propagator / damping of kz = f + n1 * e at the line's
+// (x, y) (adjacent lines are adjacent x: coalesced reads of the tables)
+struct Z4Twiddle {
+  const cplx *tw;
+  int s, c;
+  __device__ __forceinline__ cplx operator()(int, int e, cplx v) const {
+    return cmul(v, tw[e * s + c]);
+  }
+};
+struct Z4Mid {
+  const FftArgs *a;
+  int L0, f, n1;
+  __device__ __forceinline__ cplx operator()(int l, int e, cplx v) const {
+    const int L = L0 + l;
+    const int x = L % a->T.nx, y = L / a->T.nx;
+    return mid_op(*a, 0, x, y, f + n1 * e, v);
+  }
+};
+
 template <int N1, int N2, int G, int STEP>
 __global__ void __launch_bounds__(PT, (sizeof(real) == 4) ? 4 : 3) k_z4(const FftArgs a) {
   static_assert(PT % G == 0, "a thread keeps one line of its group");
@@ -904,7 +942,18 @@ __global__ void __launch_bounds__(PT, (sizeof(real) == 4) ? 4 : 3) k_z4(const Ff
     for (int j = j0; j < M; j += JS) load_async(buf + j * G + l, a, pos_of(j));
   cp_async_wait_all();
   __syncthreads();
-  if constexpr (STEP == 0) {
+  // FP32 (LSU-bound): the twiddles and the propagator / damping are applied
+  // as the last radix pass writes its outputs (Z4Twiddle, Z4Mid); FP64
+  // (FP64-bound, and short of registers for the fused form): separate
+  // element passes
+  constexpr bool FUSED = sizeof(real) == 4;
+  if constexpr (STEP == 0 && FUSED) {
+    ip_transform<N1, G, false, true>(buf, nl, 1, G, a.tw_f, a.ax, Z4Twiddle{a.tw4f, N2, f});
+  } else if constexpr (STEP == 1 && FUSED) {
+    ip_transform<N2, G, false, true>(buf, nl, 1, G, a.tw_f, a.ay,
+                                     Z4Mid{&a, (int)L0, f, N1});
+    ip_transform<N2, G, true, true>(buf, nl, 1, G, a.tw_b, a.ay, Z4Twiddle{a.tw4b, 1, f * N2});
+  } else if constexpr (STEP == 0) {
     ip_transform<N1, G, false, true>(buf, nl, 1, G, a.tw_f, a.ax);
     if (on)
       for (int k1 = j0; k1 < M; k1 += JS)
@@ -913,7 +962,6 @@ __global__ void __launch_bounds__(PT, (sizeof(real) == 4) ? 4 : 3) k_z4(const Ff
   } else if constexpr (STEP == 1) {
     ip_transform<N2, G, false, true>(buf, nl, 1, G, a.tw_f, a.ay);
     if (on) {
-      // adjacent lines are adjacent x: coalesced reads of the (x, kz) tables
       const int L = (int)(L0 + l);
       const int x = L % a.T.nx, y = L / a.T.nx;
       for (int k2 = j0; k2 < M; k2 += JS)
