@@ -171,9 +171,11 @@ struct FixTile {
   int pzlo, ntr;
 };
 
+// tc: this step's coefficients of a replayed step block (read once per
+// thread or staged once per block by the caller), null outside graphs
 template <int STAGE, bool ONED, bool TILE>
 __device__ __forceinline__ void stage_particle(const StageArgs &a, const int64_t i,
-                                               const FixTile &t) {
+                                               const FixTile &t, const StageCoef *tc) {
   const double y0[6] = {a.x[i], a.y[i], a.z2[i], a.px[i], a.py[i], a.gam[i]};
   double s[6];
   double kin[6];
@@ -340,7 +342,6 @@ __device__ __forceinline__ void stage_particle(const StageArgs &a, const int64_t
   double k[6];
   if (a.electrons_evolve) {
     double bx, by, bz;
-    const StageCoef *tc = a.coef_tab ? a.coef_tab + (*a.step_ctr) * 4 + (STAGE - 1) : nullptr;
     bfield(tc ? tc->bf : a.bf, X, Y, bx, by, bz);
     const double n2col = tc ? tc->n2col : a.n2col, kn2col = tc ? tc->kn2col : a.kn2col;
     const double ep = p2 * a.eta_k2;           // eta p2 / kappa^2
@@ -387,9 +388,14 @@ __device__ __forceinline__ void stage_tile_block(const StageArgs &a, const int64
                                                  const int64_t i1, u64 *ftile, int &s_pzlo) {
   const int ntr = (int)(a.nix * a.niy);
   const int tn = FT_PLANES * ntr;
+  __shared__ StageCoef s_coef;  // a replayed block's coefficients, staged once
   for (int k = threadIdx.x; k < 4 * tn; k += blockDim.x) ftile[k] = 0ull;
-  if (threadIdx.x == 0) s_pzlo = INT_MAX;
+  if (threadIdx.x == 0) {
+    s_pzlo = INT_MAX;
+    if (a.coef_tab) s_coef = a.coef_tab[(*a.step_ctr) * 4 + (STAGE - 1)];
+  }
   __syncthreads();
+  const StageCoef *tc = a.coef_tab ? &s_coef : nullptr;
   const bool halted = (*((volatile unsigned int *)a.status) != 0u);
   int my = INT_MAX;
   if (!halted) {
@@ -410,7 +416,7 @@ __device__ __forceinline__ void stage_tile_block(const StageArgs &a, const int64
   const FixTile t{ftile, ftile + tn, ftile + 2 * tn, ftile + 3 * tn, s_pzlo, ntr};
   if (!halted)
     for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x)
-      stage_particle<STAGE, ONED, true>(a, i, t);
+      stage_particle<STAGE, ONED, true>(a, i, t, tc);
   __syncthreads();
   if (t.pzlo == INT_MAX) return;
   for (int k = threadIdx.x; k < tn; k += blockDim.x) {
@@ -428,7 +434,8 @@ __global__ void __launch_bounds__(256, TILE ? 3 : 4) k_stage(const StageArgs a) 
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.np) return;
     if (*((volatile unsigned int *)a.status) != 0u) return;
-    stage_particle<STAGE, ONED, false>(a, i, FixTile{});
+    const StageCoef *tc = a.coef_tab ? a.coef_tab + (*a.step_ctr) * 4 + (STAGE - 1) : nullptr;
+    stage_particle<STAGE, ONED, false>(a, i, FixTile{}, tc);
   } else {
     extern __shared__ u64 ftile[];
     __shared__ int s_pzlo;
@@ -450,6 +457,7 @@ __global__ void __launch_bounds__(256, 4) k_stage_batch(const StageArgs *__restr
   extern __shared__ u64 ftile[];
   static_assert(sizeof(StageArgs) % 8 == 0, "StageArgs is copied as 64-bit words");
   const StageArgs &sa = *reinterpret_cast<const StageArgs *>(sa_raw);
+  __shared__ StageCoef s_coef;  // the tile's instance's coefficients (replayed blocks)
   int cur = -1;
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const BatchTile tl = tiles[t];
@@ -457,6 +465,10 @@ __global__ void __launch_bounds__(256, 4) k_stage_batch(const StageArgs *__restr
       __syncthreads();  // the previous tile is done with the arguments
       const u64 *src = reinterpret_cast<const u64 *>(args + tl.inst);
       for (int k = threadIdx.x; k < (int)(sizeof(StageArgs) / 8); k += blockDim.x) sa_raw[k] = src[k];
+      if (threadIdx.x == 0) {
+        const StageArgs &g = args[tl.inst];
+        if (g.coef_tab) s_coef = g.coef_tab[(*g.step_ctr) * 4 + (STAGE - 1)];
+      }
       cur = tl.inst;
       __syncthreads();
     }
@@ -465,8 +477,9 @@ __global__ void __launch_bounds__(256, 4) k_stage_batch(const StageArgs *__restr
       __syncthreads();  // the tile is reused by the next range
     } else {
       if (*((volatile unsigned int *)sa.status) != 0u) continue;
+      const StageCoef *tc = sa.coef_tab ? &s_coef : nullptr;
       for (int64_t i = tl.begin + threadIdx.x; i < tl.end; i += blockDim.x)
-        stage_particle<STAGE, false, false>(sa, i, FixTile{});
+        stage_particle<STAGE, false, false>(sa, i, FixTile{}, tc);
     }
   }
 }
