@@ -589,8 +589,10 @@ int pf_batch_create(pf_handle *const *handles, int32_t n, pf_batch **out) {
     pf_batch_destroy(b);
     return PF_CUDA_ERR;
   }
-  // default deposit modes: the dense rule of the single-instance path
+  // default deposit modes: the dense rule of the single-instance path; the
+  // batch keeps its instances' macroparticle order (no z2 ordering)
   for (int i = 0; i < n; ++i) {
+    handles[i]->sort_z2 = false;
     const pf_handle *h = handles[i];
     const int64_t ntr = (int64_t)h->nix * h->niy;
     const bool dense = mixed ? pf_mixed_tile_smem(h) > 0

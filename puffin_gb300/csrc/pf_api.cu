@@ -195,9 +195,12 @@ static void free_particles(pf_handle *h) {
   cudaFree(h->chi);
   cudaFree(h->chi_f);
   cudaFree(h->base4);
+  cudaFree(h->perm);
   h->chi = nullptr;
   h->chi_f = nullptr;
   h->base4 = nullptr;
+  h->perm = nullptr;
+  h->permuted = false;
   h->cap = 0;
 }
 
@@ -486,6 +489,7 @@ int pf_destroy(pf_handle *h) {
   cudaFree(h->diag);
   cudaFree(h->lat_scratch);
   cudaFree(h->snap);
+  cudaFree(h->plane_off);
   pf_adj_destroy(h->adj);
   if (h->gexec) cudaGraphExecDestroy(h->gexec);
   cudaFree(h->coef_dev);
@@ -498,6 +502,8 @@ int pf_destroy(pf_handle *h) {
   delete h;
   return PF_OK;
 }
+
+__global__ void k_unpermute(const double *src, const int32_t *perm, double *dst, int64_t n);
 
 static int set_particles_impl(pf_handle *h, int64_t n, const double *const src[7],
                               cudaMemcpyKind kind) {
@@ -515,6 +521,19 @@ static int set_particles_impl(pf_handle *h, int64_t n, const double *const src[7
   cudaSetDevice(h->dev);
   int rc = alloc_particles(h, n);
   if (rc) return rc;
+  if (h->permuted && src[6] == nullptr && n > 0 && n == h->np) {
+    // the kept chi goes back to the caller's order with the new arrays
+    cudaSetDevice(h->dev);
+    k_unpermute<<<grid_for(n, 256), 256, 0, h->stream>>>(h->chi, h->perm, h->kb[0], n);
+    PF_LAUNCHED(h);
+    PF_CUDA(cudaMemcpyAsync(h->chi, h->kb[0], sizeof(double) * (size_t)n,
+                            cudaMemcpyDeviceToDevice, h->stream));
+    if (h->chi_f) {
+      k_to_f32<<<grid_for(n, 256), 256, 0, h->stream>>>(h->chi_f, h->chi, n);
+      PF_LAUNCHED(h);
+    }
+  }
+  h->permuted = false;
   h->np = n;
   h->particles_set = true;
   const size_t b = sizeof(double) * (size_t)n;
@@ -569,14 +588,151 @@ int pf_set_particles_dev(pf_handle *h, int64_t n, const double *x, const double 
   return set_particles_impl(h, n, s, cudaMemcpyDeviceToDevice);
 }
 
+// ---------------------------------------------------------------------------
+// z2 ordering: a counting sort of the macroparticles over the z2 planes (the
+// FEL bunching spreads runs of consecutive macroparticles over many planes,
+// which defeats the stage kernels' block tiles); the caller's order is kept
+// in perm and restored by pf_get_particles.
+__device__ __forceinline__ int sort_plane(double z2, double inv_dz2, int npl, int periodic) {
+  const double f = floor(z2 * inv_dz2);
+  int p = (fabs(f) < 2.0e9) ? (int)f : 0;
+  if (periodic) {
+    p %= npl;
+    if (p < 0) p += npl;
+  }
+  return min(max(p, 0), npl - 1);
+}
+
+__global__ void k_iota32(int32_t *p, int64_t n) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) p[t] = (int32_t)t;
+}
+
+// one atomic per distinct plane of a warp (the arrays are mostly z2-ordered)
+__device__ __forceinline__ int warp_plane_add(int *cnt, int plane, bool on) {
+  const unsigned act = __ballot_sync(0xffffffffu, on);
+  if (!on) return 0;
+  const unsigned peers = __match_any_sync(act, plane);
+  const int leader = __ffs(peers) - 1;
+  const int lane = threadIdx.x & 31;
+  const int rank = __popc(peers & ((1u << lane) - 1u));
+  int base = 0;
+  if (lane == leader) base = atomicAdd(cnt + plane, __popc(peers));
+  base = __shfl_sync(peers, base, leader);
+  return base + rank;
+}
+
+__global__ void k_plane_count(const double *z2, int64_t n, double inv_dz2, int npl, int periodic,
+                              int *cnt) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool on = t < n;
+  const int p = on ? sort_plane(z2[t], inv_dz2, npl, periodic) : 0;
+  warp_plane_add(cnt, p, on);
+}
+
+__global__ void k_plane_scan(int *cnt, int npl) {  // exclusive, one thread
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int run = 0;
+  for (int k = 0; k < npl; ++k) {
+    const int c = cnt[k];
+    cnt[k] = run;
+    run += c;
+  }
+}
+
+struct SortArrays {
+  const double *src[7];
+  double *dst[7];
+  const int32_t *perm_src;
+  int32_t *perm_dst;
+};
+
+__global__ void k_plane_scatter(const SortArrays a, int64_t n, double inv_dz2, int npl,
+                                int periodic, int *off) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool on = t < n;
+  const int p = on ? sort_plane(a.src[2][t], inv_dz2, npl, periodic) : 0;
+  const int pos = warp_plane_add(off, p, on);
+  if (!on) return;
+#pragma unroll
+  for (int j = 0; j < 7; ++j) a.dst[j][pos] = a.src[j][t];
+  a.perm_dst[pos] = a.perm_src[t];
+}
+
+__global__ void k_unpermute(const double *src, const int32_t *perm, double *dst, int64_t n) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) dst[perm[t]] = src[t];
+}
+
+// Between steps only: the slope arrays (k1, ka) and the other state buffer
+// are free then and hold the sorted copy, which is copied back in place (the
+// arrays keep their addresses, so captured step blocks stay valid).
+int pf_sort_z2(pf_handle *h) {
+  if (!h->sort_z2 || h->np < ((int64_t)1 << 15) || h->p.one_d || h->npl < 2) return PF_OK;
+  if (h->np >= ((int64_t)1 << 31)) return PF_OK;
+  const int npl = (int)h->npl;
+  const int periodic = (h->p.mesh_type == PF_MESH_PERIODIC);
+  const double inv_dz2 = 1.0 / h->p.dz2;
+  const int64_t n = h->np;
+  if (!h->perm) PF_CUDA(cudaMalloc(&h->perm, sizeof(int32_t) * (size_t)h->cap));
+  if (!h->permuted) {
+    k_iota32<<<grid_for(n, 256), 256, 0, h->stream>>>(h->perm, n);
+    PF_LAUNCHED(h);
+  }
+  if (h->plane_cap < npl) {
+    cudaFree(h->plane_off);
+    h->plane_off = nullptr;
+    PF_CUDA(cudaMalloc(&h->plane_off, sizeof(int) * (size_t)npl));
+    h->plane_cap = npl;
+  }
+  PF_CUDA(cudaMemsetAsync(h->plane_off, 0, sizeof(int) * (size_t)npl, h->stream));
+  k_plane_count<<<grid_for(n, 256), 256, 0, h->stream>>>(h->y[h->cur][2], n, inv_dz2, npl,
+                                                         periodic, h->plane_off);
+  PF_LAUNCHED(h);
+  k_plane_scan<<<1, 32, 0, h->stream>>>(h->plane_off, npl);
+  PF_LAUNCHED(h);
+  SortArrays a;
+  const int nxt = 1 - h->cur;
+  for (int j = 0; j < 6; ++j) {
+    a.src[j] = h->y[h->cur][j];
+    a.dst[j] = h->y[nxt][j];
+  }
+  a.src[6] = h->chi;
+  a.dst[6] = h->k1[0];
+  a.perm_src = h->perm;
+  a.perm_dst = reinterpret_cast<int32_t *>(h->ka[0]);
+  k_plane_scatter<<<grid_for(n, 256), 256, 0, h->stream>>>(a, n, inv_dz2, npl, periodic,
+                                                           h->plane_off);
+  PF_LAUNCHED(h);
+  const size_t b = sizeof(double) * (size_t)n;
+  for (int j = 0; j < 6; ++j)
+    PF_CUDA(cudaMemcpyAsync(h->y[h->cur][j], h->y[nxt][j], b, cudaMemcpyDeviceToDevice, h->stream));
+  PF_CUDA(cudaMemcpyAsync(h->chi, h->k1[0], b, cudaMemcpyDeviceToDevice, h->stream));
+  PF_CUDA(cudaMemcpyAsync(h->perm, h->ka[0], sizeof(int32_t) * (size_t)n,
+                          cudaMemcpyDeviceToDevice, h->stream));
+  if (h->chi_f) {
+    k_to_f32<<<grid_for(n, 256), 256, 0, h->stream>>>(h->chi_f, h->chi, n);
+    PF_LAUNCHED(h);
+  }
+  h->permuted = true;
+  return PF_OK;
+}
+
 static int get_particles_impl(pf_handle *h, double *const dst[7], cudaMemcpyKind kind) {
   if (!h) return PF_BAD_ARG;
   cudaSetDevice(h->dev);
   const size_t b = sizeof(double) * (size_t)h->np;
   if (h->np > 0) {
-    for (int j = 0; j < 6; ++j)
-      if (dst[j]) PF_CUDA(cudaMemcpyAsync(dst[j], h->y[h->cur][j], b, kind, h->stream));
-    if (dst[6]) PF_CUDA(cudaMemcpyAsync(dst[6], h->chi, b, kind, h->stream));
+    for (int j = 0; j < 7; ++j) {
+      if (!dst[j]) continue;
+      const double *src = (j < 6) ? h->y[h->cur][j] : h->chi;
+      if (h->permuted) {  // back to the caller's order through a free slope array
+        k_unpermute<<<grid_for(h->np, 256), 256, 0, h->stream>>>(src, h->perm, h->kb[0], h->np);
+        PF_LAUNCHED(h);
+        src = h->kb[0];
+      }
+      PF_CUDA(cudaMemcpyAsync(dst[j], src, b, kind, h->stream));
+    }
   }
   PF_CUDA(cudaStreamSynchronize(h->stream));
   return PF_OK;
@@ -993,6 +1149,11 @@ int pf_sched_after_step(pf_handle *h, RunSched &s, int istep) {
   if (h->csteps % s.redist == 0) {
     const int r = pf_wrap_z2(h);
     if (r) return r;
+  }
+  if (h->csteps - h->last_sort >= s.redist || h->csteps < h->last_sort) {
+    const int r = pf_sort_z2(h);
+    if (r) return r;
+    h->last_sort = h->csteps;
   }
   if (s.steps_done) *s.steps_done = istep;
   return PF_OK;

@@ -157,6 +157,13 @@ struct pf_handle {
   unsigned long long *acc = nullptr;       // 4 * wcap words
   bool window_valid = false;  // window holds the outer mesh's current values
 
+  // z2 ordering of the macroparticles (pf_run, at the wrap cadence): slot k
+  // holds the caller's macroparticle perm[k] while `permuted`
+  int32_t *perm = nullptr;
+  int *plane_off = nullptr;
+  int64_t plane_cap = 0, last_sort = 0;
+  bool permuted = false, sort_z2 = true;
+
   // mixed precision: interleaved complex-float outer mesh and window arrays
   void *oc32 = nullptr;
   void *w32 = nullptr, *as32 = nullptr, *d0_32 = nullptr, *d12_32 = nullptr, *acc32 = nullptr;
