@@ -121,7 +121,9 @@ int pf_destroy(pf_handle *h);
  * reference recomputes it only at redistribution: pf_redistribute).  chi may
  * be NULL to keep the handle's chi (rk4par never changes it) when n is the
  * current macroparticle count, else PF_BAD_ARG; pf_get_particles skips every
- * NULL destination. */
+ * NULL destination.  pf_run may re-order the macroparticles on the device by
+ * z2 plane (beams of 2^15 or more, at the wrap cadence); pf_get_particles
+ * always returns them in the order pf_set_particles received them. */
 int pf_set_particles(pf_handle *h, int64_t n, const double *x, const double *y,
                      const double *z2, const double *px, const double *py,
                      const double *gam, const double *chi);

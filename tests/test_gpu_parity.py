@@ -494,3 +494,49 @@ def test_generate_beam_matches_oracle(noise):
         same = got["chi"] == want.chi
         assert np.mean(same) > 0.999
         np.testing.assert_allclose(got["z2"][same], want.z2[same], rtol=0, atol=1e-15)
+
+
+@pytest.mark.parametrize("precision", [P.FP64, P.MIXED])
+def test_run_with_z2_ordering_matches_step_by_step(precision):
+    """pf_run re-orders beams of 2^15 macroparticles or more by z2 plane at
+    the wrap cadence (the caller's order is restored by pf_get_particles);
+    130 steps (two orderings) against the same schedule driven one call at a
+    time, which never re-orders: bit for bit in FP64."""
+    w = configs.config1(np_=2 ** 15, seed=43, nsteps=130)
+    w.params.precision = precision
+    field = random_field(w.params, 5, amp=1e-2)
+    h = w.h
+    with P.Puffin(w.params) as sim:
+        sim.set_particles(*(w.beam[k] for k in P.PARTICLE_KEYS))
+        sim.set_field(*field)
+        sim.und_section(130, 10, True, h)
+        got, gf = sim.get_particles(), sim.get_field()
+        # a second read and a chi-keeping hand-over see the caller's order too
+        again = sim.get_particles()
+        sim.set_particles(*(got[k] for k in P.PARTICLE_KEYS[:6]))
+        kept = sim.get_particles()
+    for k in P.PARTICLE_KEYS:
+        np.testing.assert_array_equal(again[k], got[k], err_msg=k)
+        np.testing.assert_array_equal(kept[k], got[k], err_msg=k)
+    np.testing.assert_array_equal(got["chi"], w.beam["chi"])
+    with P.Puffin(w.params) as sim:
+        sim.set_particles(*(w.beam[k] for k in P.PARTICLE_KEYS))
+        sim.set_field(*field)
+        sim.diffractIM(10 * h / 2)
+        szl = 0.0
+        for i in range(1, 131):
+            assert sim.rk4par(szl, h)
+            szl = szl + h
+            if i % 10 == 0:
+                sim.diffractIM(10 * h / 2 + (10 * h / 2 if i < 130 else 0.0))
+            if i % 60 == 0:
+                sim.wrap_z2()
+        want, wf = sim.get_particles(), sim.get_field()
+    if precision == P.FP64:
+        for k in ("x", "y", "z2", "px", "py", "gam"):
+            np.testing.assert_array_equal(got[k], want[k], err_msg=k)
+        np.testing.assert_array_equal(gf[0], wf[0])
+        np.testing.assert_array_equal(gf[1], wf[1])
+    else:
+        assert_beam_close(got, oracle_beam(want), rtol=1e-5, atol=1e-7)
+        field_close(gf, wf, 1e-4)
