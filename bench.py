@@ -19,11 +19,14 @@ merged diffraction call (dz = 8 h), exactly as UndSection schedules them.
             with CUDA events; algorithmic bytes 104 B per particle per stage
             (416 B per particle-step over 4 stages);
 * cpu_baseline -- the CPU restatement of the same step (oracle/), timed on the
-            host cores on a bounded sample and extrapolated to the workload.
+            host cores on one diffraction block of the full workload (8 RK4
+            steps and their diffraction call).
 
-``--impl reference`` times the CPU implementation alone (the reference is
-Fortran + MPI + FFTW-MPI + parallel HDF5 and cannot be built here, so the
-oracle restatement stands in) and prints its own line.
+``--impl reference`` times the CPU implementation alone on the same workload
+and schedule, W warm-up and K timed steps (the reference is Fortran + MPI +
+FFTW-MPI + parallel HDF5 and cannot be built here, so the oracle
+restatement stands in; the CUDA library is not loaded) and prints its own
+line.
 
 N > 1 (torchrun): the path does not shard here, so N independent
 replicas run one per GPU ("replicas only"); value sums over ranks and the
@@ -69,7 +72,6 @@ def parse():
                     help="z2 nodes of the mesh (smaller only for profiling captures)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision leg")
-    ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--np3", type=int, default=2 ** 24,
                     help="macroparticles of the mixed-vs-FP64 leg on the config-1 mesh (0: skip)")
     ap.add_argument("--steps3", type=int, default=32)
@@ -158,66 +160,106 @@ def measured_peaks():
 
 
 # ---------------------------------------------------------------------------
-def cpu_baseline(w, seconds):
-    """Time the CPU restatement (oracle/) on the host cores on a bounded
-    sample of the workload and extrapolate to the full macroparticle count:
-    RK4 step time = a + b * Np from two sample sizes, plus one diffraction
-    per 8 steps (numpy restatement with scipy's multithreaded FFT)."""
+def oracle_steps(w, steps, warmup):
+    """The CPU restatement (oracle/) of the timed step on the whole workload,
+    with the GPU arm's schedule: `warmup` untimed steps, then `steps` timed
+    ones, each an rk4par step (the C + OpenMP restatement of rk4par/getrhs on
+    every host core, with the reference's atomic deposit) and, every
+    isteps4diff-th step, inner2Outer + the diffraction step (numpy
+    restatement with scipy's threaded FFT) + outer2Inner over isteps4diff
+    steps.  Wall-clock time around the timed steps; nothing is sampled or
+    extrapolated.  A step whose macroparticle left the inner window is
+    retried after the window is recomputed, as UndSection does."""
     from oracle import oracle as O
     from tests.oracle_bridge import oracle_beam, oracle_config
 
     cores = os.cpu_count() or 1
     O.set_threads(cores)
-    cfg = oracle_config(w.params)
-    budget = seconds
-    samples = []
-    for frac in (1.0 / 64, 1.0 / 32):
-        n = max(1024, int(w.np * frac))
-        beam = oracle_beam({k: v[:n] for k, v in w.beam.items()})
-        beam.chi[:] = beam.chi * (w.np / n)
-        nix, niy = O.get_in_node(cfg, beam.x, beam.y)
-        re, im = (a.copy() for a in w.field)
-        wr, wi = O.outer_to_inner(cfg, re, im, nix, niy)
-        taper = O.Taper(w.params.n2col0, w.params.n2col0, w.params.undgrad)
-        t0 = time.perf_counter()
-        steps = 0
-        szl = 0.0
-        while steps < 2 or (time.perf_counter() - t0 < budget / 4 and steps < 8):
-            O.rk4_step(cfg, taper, szl, w.h, beam, wr, wi, nix, niy)
-            szl += w.h
-            steps += 1
-        samples.append((n, (time.perf_counter() - t0) / steps))
-    (n1, t1), (n2, t2) = samples
-    b = max(0.0, (t2 - t1) / (n2 - n1))
-    a = max(0.0, t1 - b * n1)
-    t_rk4 = a + b * w.np
-    re, im = (a_.copy() for a_ in w.field)
-    t_diff = 0.0
-    if w.qdiffraction:
-        try:
-            import scipy.fft as sfft
+    fftmod = None
+    try:
+        import scipy.fft as sfft
 
-            class _F:  # numpy.fft interface over scipy's threaded FFT
-                @staticmethod
-                def fftn(x):
-                    return sfft.fftn(x, workers=cores)
+        class _F:  # numpy.fft interface over scipy's threaded FFT
+            @staticmethod
+            def fftn(x):
+                return sfft.fftn(x, workers=cores)
 
-                @staticmethod
-                def ifftn(x):
-                    return sfft.ifftn(x, workers=cores)
-            fftmod = _F
-        except Exception:
-            fftmod = None
-        t0 = time.perf_counter()
-        O.diffract(cfg, re, im, w.isteps4diff * w.h, fft=fftmod)
-        t_diff = time.perf_counter() - t0
-    per_step = t_rk4 + (t_diff / w.isteps4diff if w.qdiffraction else 0.0)
+            @staticmethod
+            def ifftn(x):
+                return sfft.ifftn(x, workers=cores)
+        fftmod = _F
+    except Exception:
+        pass
+    p = w.params
+    cfg = oracle_config(p)
+    beam = oracle_beam(w.beam)
+    re, im = (np.array(a, dtype=np.float64) for a in w.field)
+    st = {"win": O.get_in_node(cfg, beam.x, beam.y), "szl": 0.0, "i": 0, "diff": 0,
+          "retries": 0}
+    st["w"] = O.outer_to_inner(cfg, re, im, *st["win"])
+    taper = O.Taper(p.n2col0, p.n2col0, p.undgrad)
+
+    def step():
+        for _ in range(4):
+            t = O.Taper(taper.n2col, taper.n2col0, taper.undgrad)
+            rc = O.rk4_step(cfg, taper, st["szl"], w.h, beam, *st["w"], *st["win"])
+            if rc == 0:
+                break
+            if rc & 2:
+                raise RuntimeError("oracle: a macroparticle left the temporal mesh")
+            taper.update(t)
+            st["retries"] += 1
+            O.inner_to_outer(cfg, re, im, *st["w"], *st["win"])
+            st["win"] = O.get_in_node(cfg, beam.x, beam.y)
+            st["w"] = O.outer_to_inner(cfg, re, im, *st["win"])
+        else:
+            raise RuntimeError("oracle: the window retries did not hold the beam")
+        st["szl"] += w.h
+        st["i"] += 1
+        if w.qdiffraction and st["i"] % w.isteps4diff == 0:
+            O.inner_to_outer(cfg, re, im, *st["w"], *st["win"])
+            O.diffract(cfg, re, im, w.isteps4diff * w.h, fft=fftmod)
+            st["w"] = O.outer_to_inner(cfg, re, im, *st["win"])
+            st["diff"] += 1
+
+    for _ in range(warmup):
+        step()
+    d0 = st["diff"]
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    sec = time.perf_counter() - t0
+    return {"seconds": sec, "steps": steps, "warmup": warmup, "cores": cores,
+            "diffraction_calls": st["diff"] - d0, "retries": st["retries"],
+            "window": [int(v) for v in st["win"]], "value": w.np * steps / sec}
+
+
+def cpu_baseline(w):
+    """The oracle on one diffraction block of the workload (one warm-up step,
+    then the next isteps4diff steps with their diffraction call) on the host
+    cores: a bounded sample of the same work, timed as it is (no
+    extrapolation)."""
+    r = oracle_steps(w, w.isteps4diff, 1)
     return {
-        "value": w.np / per_step, "unit": UNIT, "cores": cores, "kind": "port",
-        "sample": (f"CPU restatement (oracle/, C+OpenMP {cores} threads, numpy/scipy FFT): "
-                   f"RK4 steps at Np={n1} and {n2} on the full mesh fitted to a+b*Np "
-                   f"(a={a:.3f}s, b={b:.3e}s) and one diffraction ({t_diff:.1f}s) every "
-                   f"{w.isteps4diff} steps, extrapolated to Np={w.np}"),
+        "value": r["value"], "unit": UNIT, "cores": r["cores"], "kind": "port",
+        "sample": (f"CPU restatement (oracle/: C+OpenMP RK4 on {r['cores']} threads, numpy "
+                   f"diffraction with scipy's threaded FFT) on the full workload "
+                   f"({w.np} macroparticles, full mesh): {r['steps']} RK4 steps and "
+                   f"{r['diffraction_calls']} diffraction call after 1 warm-up step, "
+                   f"{r['seconds']:.2f} s"),
+    }
+
+
+def workload_config(w, win, world):
+    """The `config` of both arms' lines (the same keys and values)."""
+    p = w.params
+    return {
+        "workload": w.name, "macroparticles": w.np, "mesh": [p.nx, p.ny, p.nz2],
+        "inner_window": [int(v) for v in win], "steps_per_period": 24,
+        "diffraction_every": w.isteps4diff,
+        "precision": "fp64 (value); mixed in 'mixed'",
+        "parallelism": f"replicas x{world}",
+        "l2": "inputs larger than L2 (particle state 470 MB, field 1.09 GB per array pair)",
     }
 
 
@@ -624,13 +666,7 @@ def run_gpu(args, rank, world):
         "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded beam and zero seed field; no dataset)",
-        "config": {
-            "workload": w.name, "macroparticles": n, "mesh": [p.nx, p.ny, p.nz2],
-            "inner_window": list(win), "steps_per_period": 24, "diffraction_every": every,
-            "precision": "fp64 (value); mixed in 'mixed'",
-            "parallelism": f"replicas x{world}",
-            "l2": "inputs larger than L2 (particle state 470 MB, field 1.09 GB per array pair)",
-        },
+        "config": workload_config(w, win, world),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "steps": args.e2e_steps,
                 "diffraction_calls": e2e_diff_calls, "window_changes": window_changes,
@@ -697,24 +733,34 @@ def run_gpu(args, rank, world):
     return rec
 
 
-def run_reference(args):
+def run_reference(args, world):
+    """The reference arm: the CPU implementation of the path on the host
+    cores, on the GPU arm's workload, schedule, metric and config.  The
+    reference is Fortran + MPI + FFTW-MPI + parallel HDF5 with no toolchain
+    here or on the GPU host image, so its CPU restatement (oracle/) runs in
+    its place: W warm-up and K timed steps on the full beam and mesh."""
     from puffin_gb300 import configs
-    w = configs.config2(np_=args.np)
-    cb = cpu_baseline(w, args.cpu_seconds)
+    w = configs.config2(np_=args.np, nz2=args.nz2)
+    r = oracle_steps(w, args.steps, args.warmup)
+    v = r["value"]
     return {
-        "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": 0,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * w.np / cb["value"],
+        "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * r["seconds"] / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded beam and zero seed field; no dataset)",
-        "config": {"workload": w.name, "macroparticles": w.np, "mesh": [129, 129, 4096],
-                   "precision": "fp64", "parallelism": "host cores"},
+        "config": workload_config(w, r["window"], world),
         "impl": "reference",
-        "cpu_baseline": cb,
-        "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
-                "d2h_bytes_per_step": 0},
+        "cpu_baseline": {
+            "value": v, "unit": UNIT, "cores": r["cores"], "kind": "port",
+            "sample": (f"the whole timed run: {args.steps} RK4 steps with "
+                       f"{r['diffraction_calls']} diffraction calls after {args.warmup} "
+                       f"warm-up steps on the full workload ({r['seconds']:.1f} s)")},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "retries": r["retries"],
         "note": ("the reference is Fortran + MPI + FFTW-MPI + parallel HDF5 and no Fortran "
                  "toolchain exists here or on the GPU host image, so the CPU restatement "
-                 "in oracle/ is timed in its place"),
+                 "in oracle/ (C + OpenMP RK4 with the reference's atomic deposit, numpy "
+                 "diffraction) is timed in its place; the CUDA library is not loaded"),
     }
 
 
@@ -724,7 +770,7 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
         if rank == 0:
-            print(json.dumps(run_reference(args)), flush=True)
+            print(json.dumps(run_reference(args, world)), flush=True)
         return
     if args.batch_only:
         import torch
@@ -741,8 +787,7 @@ def main():
     if rank == 0:
         if not args.no_cpu_baseline:
             from puffin_gb300 import configs
-            w = configs.config2(np_=args.np)
-            rec["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds)
+            rec["cpu_baseline"] = cpu_baseline(configs.config2(np_=args.np, nz2=args.nz2))
         print(json.dumps(rec), flush=True)
     if world > 1:
         import torch

@@ -55,7 +55,10 @@ typedef enum {
   PF_TIMEOUT = 5,         /* a bounded device-side wait gave up */
   PF_NO_DEVICE = 6,
   PF_OVERFLOW = 7,        /* a deposit exceeded the fixed-point range */
-  PF_STATE = 8            /* call order error (e.g. step before set_particles) */
+  PF_STATE = 8,           /* call order error (e.g. step before set_particles) */
+  PF_NOT_FINITE = 9       /* a NaN or infinity in a macroparticle's stage state, in the
+                             field it gathered or in the inner-window field; state left
+                             unchanged (the reference does not check) */
 } pf_status;
 
 typedef enum {
@@ -380,9 +383,12 @@ int pf_abi_version(void);
  * PF_NOALLOC_MAX_NODES, else PF_BAD_ARG.  Calls share that array: calls that
  * overlap on the GPU (different streams, several host threads) race.  The
  * first call on a device looks up the array's device address with that device
- * current; make it before any stream capture.  stream may be NULL (the
- * default stream).  Returns as pf_rk4_step; on PF_OUT_OF_WINDOW the state is
- * left unchanged. */
+ * current and keeps it for the process's life, so a cudaDeviceReset or a
+ * non-primary context on that device is not supported.  Every call waits for
+ * its stream (it reads the deposit scale and the status word back), so it
+ * must not be called while that stream is being captured.  stream may be NULL
+ * (the default stream).  Returns as pf_rk4_step; on PF_OUT_OF_WINDOW the
+ * caller's arrays are left unchanged. */
 #define PF_NOALLOC_MAX_PARTICLES 32768
 #define PF_NOALLOC_MAX_NODES 32768
 int pf_rk4_step_noalloc(const pf_params *p, double *n2col, double *n2col0, double szl,

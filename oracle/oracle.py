@@ -925,3 +925,44 @@ def generate_beam(z2m, ne, dz2, nseq, mean, sig, noise, seed, chi_per_electron):
         u = _uniform01(seed, i, 63)
         z = np.where(moved, z + (u - 0.5) * dz2 / np.sqrt(nk), z)
     return Beam(cols[0], cols[1], z, cols[2], cols[3], cols[4], nk * chi_per_electron)
+
+
+# ---------------------------------------------------------------------------
+# Known-answer formulas of the reference (puffin/lib/utilities/base_functions.f90),
+# pinned by its own unit tests (test/testFFunctions.pf), and the linear FEL
+# theory that the scaled units are built on.  The GPU tests compare a seed
+# propagated through the diffraction step and the exponential gain of cold
+# beams against them.
+# ---------------------------------------------------------------------------
+def gain_length(lam_w: float, rho: float) -> float:
+    """GainLength (base_functions.f90:448-462): the gain length
+    l_g = lambda_w / (4 pi rho) that scales zbar = z / l_g, with the
+    module's single-precision pi (puffin_constants.f90:22)."""
+    return lam_w / (4.0 * PUFFIN_PI * rho)
+
+
+def raleigh_length(rho: float, sigma: float) -> float:
+    """RaleighLength (base_functions.f90:514-525): sigma^2 / (2 rho), the
+    Rayleigh range in zbar of a seed whose field amplitude is
+    exp(-x^2 / (2 sigma^2)) (the gaussian() envelope of getSeed,
+    setup_calcs.f90:1507-1514)."""
+    return sigma ** 2 / (2.0 * rho)
+
+
+def diffraction_length(z: float, zr: float, sigma: float) -> float:
+    """DiffractionLength (base_functions.f90:489-507):
+    sqrt(2 ((z / zR)^2 + 1)) 6 sigma, a transverse extent that grows with z as
+    the width of a Gaussian beam, sqrt(1 + (z / zR)^2)."""
+    return math.sqrt(2.0 * ((z / zr) ** 2 + 1.0)) * 6.0 * sigma
+
+
+def cold_beam_power_growth(nodes_per_wavelength: int) -> float:
+    """e-foldings of the radiated power per unit zbar of a cold, resonant beam
+    in the exponential regime: sqrt(3) in the 1D high-gain theory (field
+    amplitude exp(sqrt(3)/2 zbar); so the power gain length is
+    gain_length / sqrt(3)), times the attenuation of linear (trilinear)
+    interpolation on a mesh of n nodes per resonant wavelength: gather and
+    deposit each multiply the coupling at the resonant wavenumber by
+    sinc^2(pi / n), and the growth rate goes as the coupling to the 1/3."""
+    x = math.pi / nodes_per_wavelength
+    return math.sqrt(3.0) * (math.sin(x) / x) ** (4.0 / 3.0)

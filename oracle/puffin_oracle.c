@@ -238,6 +238,9 @@ int or_rhs(const or_params *p, const or_stage *st, int64_t np,
   /* interpolation weights and node lists (getInterps_3D / _1D) */
 #pragma omp parallel for schedule(static) reduction(|:status)
   for (int64_t i = 0; i < np; ++i) {
+    /* floor for the node as for the weights (system_interpolation.f90:45-58);
+       the reference's p_nodes uses truncating int() (rhs.f90:174-178), which
+       agrees for every non-negative argument -- the inputs it defines */
     double z2n = floor(z2[i] / dz2) + 1.0;
     double locz2 = z2[i] - (z2n - 1.0) * dz2;
     int64_t iz = (int64_t)z2n; /* 1-based */

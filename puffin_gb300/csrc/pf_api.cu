@@ -222,9 +222,7 @@ static void free_window(pf_handle *h) {
   h->window_valid = false;
 }
 
-static int alloc_particles(pf_handle *h, int64_t n) {
-  if (n <= h->cap) return PF_OK;
-  free_particles(h);
+static int alloc_particles_raw(pf_handle *h, int64_t n) {
   const size_t b = sizeof(double) * (size_t)std::max<int64_t>(n, 1);
   for (int bb = 0; bb < 2; ++bb)
     for (int j = 0; j < 6; ++j) PF_CUDA(cudaMalloc(&h->y[bb][j], b));
@@ -238,24 +236,50 @@ static int alloc_particles(pf_handle *h, int64_t n) {
     PF_CUDA(cudaMalloc(&h->chi_f, sizeof(float) * (size_t)std::max<int64_t>(n, 1)));
     PF_CUDA(cudaMalloc(&h->base4, sizeof(float4) * (size_t)std::max<int64_t>(n, 1)));
   }
+  return PF_OK;
+}
+
+// On an allocation failure the handle is left without particles (PF_STATE
+// until the next successful pf_set_particles) and stays destroyable.
+static int alloc_particles(pf_handle *h, int64_t n) {
+  if (n <= h->cap) return PF_OK;
+  free_particles(h);
+  h->np = 0;
+  h->particles_set = false;
+  const int rc = alloc_particles_raw(h, n);
+  if (rc) {
+    free_particles(h);
+    return rc;
+  }
   h->cap = n;
   return PF_OK;
 }
 
+static int alloc_window_raw(pf_handle *h, int64_t nw) {
+  const size_t b = sizeof(double) * (size_t)nw;
+  if (h->p.precision == PF_MIXED) {
+    void **c32[] = {&h->w32, &h->as32, &h->d0_32, &h->d12_32, &h->acc32};
+    for (auto p : c32) PF_CUDA(cudaMalloc(p, b));  // float2 per node
+    PF_CUDA(cudaMemsetAsync(h->acc32, 0, b, h->stream));
+  } else {
+    double **ptrs[] = {&h->wr, &h->wi, &h->asr, &h->asi, &h->d0r, &h->d0i, &h->d12r, &h->d12i};
+    for (auto p : ptrs) PF_CUDA(cudaMalloc(p, b));
+    PF_CUDA(cudaMalloc(&h->acc, 4 * b));
+    PF_CUDA(cudaMemsetAsync(h->acc, 0, 4 * b, h->stream));
+  }
+  return PF_OK;
+}
+
+// On an allocation failure the handle is left without a window (PF_STATE
+// until the particles are set again) and stays destroyable.
 static int alloc_window(pf_handle *h, int nix, int niy) {
   const int64_t nw = (int64_t)nix * niy * h->npl;
   if (nw > h->wcap) {
     free_window(h);
-    const size_t b = sizeof(double) * (size_t)nw;
-    if (h->p.precision == PF_MIXED) {
-      void **c32[] = {&h->w32, &h->as32, &h->d0_32, &h->d12_32, &h->acc32};
-      for (auto p : c32) PF_CUDA(cudaMalloc(p, b));  // float2 per node
-      PF_CUDA(cudaMemsetAsync(h->acc32, 0, b, h->stream));
-    } else {
-      double **ptrs[] = {&h->wr, &h->wi, &h->asr, &h->asi, &h->d0r, &h->d0i, &h->d12r, &h->d12i};
-      for (auto p : ptrs) PF_CUDA(cudaMalloc(p, b));
-      PF_CUDA(cudaMalloc(&h->acc, 4 * b));
-      PF_CUDA(cudaMemsetAsync(h->acc, 0, 4 * b, h->stream));
+    const int rc = alloc_window_raw(h, nw);
+    if (rc) {
+      free_window(h);
+      return rc;
     }
     h->wcap = nw;
   }
@@ -326,6 +350,15 @@ int pf_window_from_particles(pf_handle *h, int *nix, int *niy) {
     };
     double smaxx = fabs(unkey(r[0])), sminx = fabs(unkey(r[1]));
     double smaxy = fabs(unkey(r[2])), sminy = fabs(unkey(r[3]));
+    if (!(std::isfinite(smaxx) && std::isfinite(sminx) && std::isfinite(smaxy) &&
+          std::isfinite(sminy))) {
+      h->err = "a macroparticle's transverse position is not finite";
+      return PF_NOT_FINITE;
+    }
+    if (!(std::max(smaxx, sminx) / p.dx < 1.0e9 && std::max(smaxy, sminy) / p.dy < 1.0e9)) {
+      h->err = "transverse grid not large enough for the inner window";
+      return PF_OUT_OF_WINDOW;
+    }
     long imaxx = (long)ceil(smaxx / p.dx), iminx = (long)floor(sminx / p.dx);
     long imaxy = (long)ceil(smaxy / p.dy), iminy = (long)floor(sminy / p.dy);
     ix = (int)((std::max(imaxx, iminx) + 3) * 2);
@@ -370,12 +403,7 @@ static int choose_window(pf_handle *h, bool grow_only) {
   return set_window(h, nix, niy);
 }
 
-static int status_to_rc(unsigned int st) {
-  if (st & ST_OVERFLOW) return PF_OVERFLOW;
-  if (st & ST_OUT_OF_Z2) return PF_OUT_OF_Z2;
-  if (st & ST_OUT_OF_WINDOW) return PF_OUT_OF_WINDOW;
-  return PF_OK;
-}
+static int status_to_rc(unsigned int st) { return pf_status_of(st); }
 
 // ---------------------------------------------------------------------------
 extern "C" {
@@ -922,6 +950,7 @@ int pf_rk4_step(pf_handle *h, double szl, double hstep) {
   if (rc == PF_OUT_OF_Z2) h->err = "a macroparticle's z2 node lies outside the temporal mesh";
   if (rc == PF_OUT_OF_WINDOW) h->err = "a macroparticle left the inner transverse window";
   if (rc == PF_OVERFLOW) h->err = "deposit contribution beyond the fixed-point range";
+  if (rc == PF_NOT_FINITE) h->err = "a non-finite value in a macroparticle's state or in the field";
   return rc;
 }
 

@@ -4,10 +4,35 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
 #include <string>
 #include <vector>
 
 #include "../../include/puffgpu.h"
+
+// One-time set-up per device: CUDA keeps kernel attributes (such as the
+// dynamic shared-memory limit) per device, so handles on several devices of
+// one process each need them set on their own device.  pf_device_once runs
+// f() once for the current device and returns its result on every call.
+constexpr int PF_MAX_DEVICES = 64;
+struct PfDeviceOnce {
+  std::mutex m;
+  bool done[PF_MAX_DEVICES] = {};
+  cudaError_t err[PF_MAX_DEVICES] = {};
+};
+template <typename F>
+cudaError_t pf_device_once(PfDeviceOnce &o, F &&f) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= PF_MAX_DEVICES) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> g(o.m);
+  if (!o.done[dev]) {
+    o.err[dev] = f();
+    o.done[dev] = true;
+  }
+  return o.err[dev];
+}
 
 // Puffin's global pi is a default-kind (single precision) literal
 // (puffin/lib/common/puffin_constants.f90:22).  GetKValues uses its own
@@ -20,7 +45,22 @@ enum : unsigned int {
   ST_OUT_OF_WINDOW = 1u,
   ST_OUT_OF_Z2 = 2u,
   ST_OVERFLOW = 4u,
+  ST_NOT_FINITE = 8u,
 };
+
+// pf_status of a device status word (the most severe condition first).
+inline int pf_status_of(unsigned int st) {
+  if (st & ST_NOT_FINITE) return PF_NOT_FINITE;
+  if (st & ST_OVERFLOW) return PF_OVERFLOW;
+  if (st & ST_OUT_OF_Z2) return PF_OUT_OF_Z2;
+  if (st & ST_OUT_OF_WINDOW) return PF_OUT_OF_WINDOW;
+  return PF_OK;
+}
+
+// Finite test from the exponent bits (integer operations, off the FP64 pipe).
+__device__ __forceinline__ bool pf_finite(double v) {
+  return (__double2hiint(v) & 0x7ff00000) != 0x7ff00000;
+}
 
 // Undulator b-field coefficients for one RK4 stage.  Every stage-uniform
 // sub-expression of bfields.f90 is evaluated once on the host, left to right
@@ -308,10 +348,14 @@ void pf_stage_coefficients(const pf_params &p, double sz, double n2col, int plac
 void pf_taper_stage(pf_handle *h, double sz, double *n2col, int *place);
 double pf_taper_profile_at(const std::vector<double> &z, const std::vector<double> &a, double sz);
 
+// A failed call's error is also taken off the runtime's last-error state, so
+// that an allocation failure, which leaves the context usable, is not
+// reported again by the next launch check.
 #define PF_CUDA(call)                                                     \
   do {                                                                    \
     cudaError_t e_ = (call);                                              \
     if (e_ != cudaSuccess) {                                              \
+      (void)cudaGetLastError();                                           \
       h->err = std::string(#call) + ": " + cudaGetErrorString(e_);        \
       return PF_CUDA_ERR;                                                 \
     }                                                                     \

@@ -191,6 +191,10 @@ __device__ __forceinline__ void stage_particle(const StageArgs &a, const int64_t
   }
   const double X = s[0], Y = s[1], Z2 = s[2], PX = s[3], PY = s[4], G = s[5];
   const double chi = a.chi[i];
+  // a NaN or infinity in the stage state stops the step (PF_NOT_FINITE)
+  if (!(pf_finite(X) && pf_finite(Y) && pf_finite(Z2) && pf_finite(PX) && pf_finite(PY) &&
+        pf_finite(G)))
+    atomicOr(a.status, ST_NOT_FINITE);
 
   // getP2 (gamma_to_p2.f90:84-85).  1 - u loses ~7 digits, so u and the
   // square root and reciprocal that follow keep IEEE division/sqrt and the
@@ -308,6 +312,7 @@ __device__ __forceinline__ void stage_particle(const StageArgs &a, const int64_t
       fr = w[c] * __ldg(a.ar + node[c]) + fr;
       fi = w[c] * __ldg(a.ai + node[c]) + fi;
     }
+    if (!(pf_finite(fr) && pf_finite(fi))) atomicOr(a.status, ST_NOT_FINITE);
     // deposit (getSource)
     if (a.field_evolve) {
       // (chi/dV3) (1 + eta p2) p / Gamma
@@ -501,6 +506,9 @@ __device__ __forceinline__ void node_update(const NodeArgs &a, const int64_t n,
     e0i = a.d0i[n];
   }
   const unsigned st = (STAGE == 4) ? *a.status : 0u;
+  // a non-finite field value stops the step before stage 4 commits
+  if (STAGE == 1 && !(pf_finite(wr) && pf_finite(wi)))
+    atomicOr(const_cast<unsigned int *>(a.status), ST_NOT_FINITE);
   const double dr = fix_to_double(lr, hr, inv_scale);
   const double di = fix_to_double(li, hi, inv_scale);
   // the four accumulator words of a node are cleared right after their
@@ -746,15 +754,20 @@ static int launch_stage(pf_handle *h, int stage, StageArgs &a) {
   size_t smem = 0;
   const bool dense = dense_mode(h, &smem);
   const int64_t dblocks = (h->np + FT_PPB - 1) / FT_PPB;
-  static bool attr_set = false;
-  if (dense && !attr_set) {
-    const void *fns[] = {(const void *)k_stage<1, false, true>, (const void *)k_stage<2, false, true>,
-                         (const void *)k_stage<3, false, true>, (const void *)k_stage<4, false, true>,
-                         (const void *)k_stage<1, true, true>,  (const void *)k_stage<2, true, true>,
-                         (const void *)k_stage<3, true, true>,  (const void *)k_stage<4, true, true>};
-    for (const void *f : fns)
-      PF_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
-    attr_set = true;
+  static PfDeviceOnce attr_once;  // the attribute is per device
+  if (dense) {
+    PF_CUDA(pf_device_once(attr_once, [] {
+      const void *fns[] = {(const void *)k_stage<1, false, true>, (const void *)k_stage<2, false, true>,
+                           (const void *)k_stage<3, false, true>, (const void *)k_stage<4, false, true>,
+                           (const void *)k_stage<1, true, true>,  (const void *)k_stage<2, true, true>,
+                           (const void *)k_stage<3, true, true>,  (const void *)k_stage<4, true, true>};
+      for (const void *f : fns) {
+        const cudaError_t e =
+            cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
+        if (e != cudaSuccess) return e;
+      }
+      return cudaSuccess;
+    }));
   }
   pf_prof_begin(h, PROF_STAGE);
 #define PF_STAGE_CASE(S)                                                                   \
@@ -905,15 +918,16 @@ size_t pf_stage_tile_smem(const pf_handle *h) {
 
 cudaError_t pf_stage_batch(cudaStream_t st, int stage, bool tile, const StageArgs *args,
                            const BatchTile *tiles, int ntiles, int grid, int threads, size_t smem) {
-  static std::once_flag once;
-  static cudaError_t attr = cudaSuccess;
-  std::call_once(once, [] {
+  static PfDeviceOnce attr_once;  // the attribute is per device
+  const cudaError_t attr = pf_device_once(attr_once, [] {
     const void *fns[] = {(const void *)k_stage_batch<1, true>, (const void *)k_stage_batch<2, true>,
                          (const void *)k_stage_batch<3, true>, (const void *)k_stage_batch<4, true>};
+    cudaError_t err = cudaSuccess;
     for (const void *f : fns) {
       const cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
-      if (e != cudaSuccess) attr = e;
+      if (e != cudaSuccess) err = e;
     }
+    return err;
   });
   if (attr != cudaSuccess) return attr;
   if (ntiles <= 0) return cudaSuccess;
@@ -1046,8 +1060,12 @@ int pf_rk4_fp64(pf_handle *h, double szl, double hstep, unsigned int *status_out
 // leaves its contents behind, so each call clears what must start at zero (the
 // deposit accumulators and the status word); two calls that overlap on the GPU
 // (e.g. on different streams) race on it.  The first call on a device looks up
-// the array's device address (cudaGetSymbolAddress) with that device current;
-// make that first call before any stream capture.
+// the array's device address (cudaGetSymbolAddress) with that device current
+// and keeps it for the life of the process, so the device's primary context
+// must stay the one in use: a cudaDeviceReset, or a caller-made non-primary
+// context, is not supported.  Every call waits for its stream twice (after the
+// deposit-scale reduction and after the status read), so no call may be made
+// while its stream is being captured into a CUDA graph.
 namespace {
 
 constexpr int64_t NA_NP = PF_NOALLOC_MAX_PARTICLES;
@@ -1256,11 +1274,7 @@ extern "C" int pf_rk4_step_noalloc(const pf_params *p, double *n2col, double *n2
   if (cudaMemcpyAsync(&hst, status, sizeof(hst), cudaMemcpyDeviceToHost, st) != cudaSuccess)
     return PF_CUDA_ERR;
   if (cudaStreamSynchronize(st) != cudaSuccess) return PF_CUDA_ERR;
-  if (hst != 0u) {
-    if (hst & ST_OVERFLOW) return PF_OVERFLOW;
-    if (hst & ST_OUT_OF_Z2) return PF_OUT_OF_Z2;
-    return PF_OUT_OF_WINDOW;  // state left unchanged, as the reference
-  }
+  if (hst != 0u) return pf_status_of(hst);  // state left unchanged, as the reference
   double *dst[6] = {x, y, z2, px, py, gam};
   for (int j = 0; j < 6 && np > 0; ++j)
     if (cudaMemcpyAsync(dst[j], ynext[j], sizeof(double) * (size_t)np, cudaMemcpyDeviceToDevice,

@@ -345,6 +345,9 @@ __device__ __forceinline__ void mixed_block(const MixArgs &a, const int64_t i0, 
       X = fmaf(a.cstate_f, kin[0], X);
       Y = fmaf(a.cstate_f, kin[1], Y);
     }
+    // a NaN or infinity in the stage state stops the step (PF_NOT_FINITE)
+    if (!(pf_finite(zs) && pf_finite(gs) && isfinite(X + Y + PX + PY)))
+      atomicOr(a.status, ST_NOT_FINITE);
     const float Gf = d2f_rn(gs);
     // 1/Gamma: FP32 reciprocal and one FP64 Newton step (relative error ~1e-14)
     const float rGf = __frcp_rn(Gf);
@@ -426,6 +429,7 @@ __device__ __forceinline__ void mixed_block(const MixArgs &a, const int64_t i0, 
         fi = zw1 * (w0 * c0.y + w1 * c1.y + w2 * c2.y + w3 * c3.y) +
              zw2 * (w0 * c4.y + w1 * c5.y + w2 * c6.y + w3 * c7.y);
       }
+      if (!isfinite(fr + fi)) atomicOr(a.status, ST_NOT_FINITE);
       if (a.field_evolve) {
         // deposit (chi/dV3) (1 + eta p2)/Gamma p w_c to the 8 (2 on 1D) nodes
         const float dw = a.chi_f[i] * a.inv_dV3 * qrG;
@@ -569,6 +573,8 @@ __device__ __forceinline__ void node_update_mixed(const MixNodeArgs &a, const in
   if (STAGE == 3 || STAGE == 4) e12 = a.d12[n];
   if (STAGE == 4) d0 = a.d0[n];
   const unsigned st = (STAGE == 4) ? *a.status : 0u;
+  // a non-finite field value stops the step before stage 4 commits
+  if (STAGE == 1 && !isfinite(w.x + w.y)) atomicOr(const_cast<unsigned int *>(a.status), ST_NOT_FINITE);
   if (STAGE == 1) {
     a.d0[n] = d;
     a.as[n] = make_float2(w.x + a.coef * d.x, w.y + a.coef * d.y);
@@ -835,9 +841,9 @@ void pf_mixed_fill_nodes(pf_handle *h, int stage, double hstep, unsigned *status
 }
 
 static cudaError_t mixed_attrs() {
-  static std::once_flag once;
-  static cudaError_t attr = cudaSuccess;
-  std::call_once(once, [] {
+  static PfDeviceOnce attr_once;  // the attribute is per device
+  return pf_device_once(attr_once, [] {
+    cudaError_t attr = cudaSuccess;
     // the tile may exceed the 48 KB default of dynamic shared memory
     const void *fns[] = {(const void *)k_stage_mixed<1, false>, (const void *)k_stage_mixed<2, false>,
                          (const void *)k_stage_mixed<3, false>, (const void *)k_stage_mixed<4, false>,
@@ -849,8 +855,8 @@ static cudaError_t mixed_attrs() {
       const cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
       if (e != cudaSuccess) attr = e;
     }
+    return attr;
   });
-  return attr;
 }
 
 cudaError_t pf_mixed_stage_batch(cudaStream_t st, int stage, const void *args,

@@ -13,11 +13,12 @@ import numpy as np
 from . import _build
 
 PF_OK, PF_OUT_OF_WINDOW, PF_OUT_OF_Z2, PF_BAD_ARG, PF_CUDA_ERR, PF_TIMEOUT, \
-    PF_NO_DEVICE, PF_OVERFLOW, PF_STATE = range(9)
+    PF_NO_DEVICE, PF_OVERFLOW, PF_STATE, PF_NOT_FINITE = range(10)
 STATUS_NAMES = {
     PF_OK: "PF_OK", PF_OUT_OF_WINDOW: "PF_OUT_OF_WINDOW", PF_OUT_OF_Z2: "PF_OUT_OF_Z2",
     PF_BAD_ARG: "PF_BAD_ARG", PF_CUDA_ERR: "PF_CUDA_ERR", PF_TIMEOUT: "PF_TIMEOUT",
     PF_NO_DEVICE: "PF_NO_DEVICE", PF_OVERFLOW: "PF_OVERFLOW", PF_STATE: "PF_STATE",
+    PF_NOT_FINITE: "PF_NOT_FINITE",
 }
 UND_PUFFIN, UND_HELICAL, UND_PLANEPOLE, UND_CURVED = 0, 1, 2, 3
 MESH_TEMPORAL, MESH_PERIODIC = 0, 1
@@ -162,9 +163,26 @@ def load(build_if_missing: bool = False):
     return L
 
 
+# The values pf_default_params writes (the reference's defaults; every other
+# field is zero).  Held here as well so that a workload can be described
+# without loading the CUDA library -- the CPU timing of the oracle does not
+# load it.  tests/test_abi.py checks that the two agree field by field.
+DEFAULTS = {
+    "rho": 0.01, "aw": 1.0, "gamma_r": 100.0, "fx": 1.0, "fy": 1.0, "szfe": 1.0e30,
+    "n2col0": 1.0, "dx": 1.0, "dy": 1.0, "dz2": 1.0, "sbeta": 1.0,
+    "sfilt_frac": float(np.float32(0.3)), "sperwaves": -1.0,
+    "und_type": UND_PUFFIN, "mesh_type": MESH_TEMPORAL, "nx": 1, "ny": 1, "nz2": 2,
+    "nbx": 16, "nby": 16, "nbz2": 37, "field_evolve": 1, "electrons_evolve": 1,
+    "coupling": 1, "qfilter": 1, "redist_every": 60, "precision": FP64,
+}
+
+
 def default_params(**overrides) -> Params:
+    """pf_default_params' values (DEFAULTS) with the given overrides; does
+    not load the library."""
     p = Params()
-    load().pf_default_params(ctypes.byref(p))
+    for k, v in DEFAULTS.items():
+        setattr(p, k, v)
     for k, v in overrides.items():
         if not hasattr(p, k):
             raise KeyError(k)

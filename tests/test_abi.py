@@ -48,6 +48,30 @@ def test_defaults_follow_reference():
     assert p.redist_every == 60 and p.qfilter == 1 and p.sbeta == 1.0
 
 
+def test_python_defaults_equal_the_library_defaults():
+    """lib.DEFAULTS (used to describe workloads without loading the CUDA
+    library) holds exactly what pf_default_params writes."""
+    lib = L.load()
+    got = L.Params()
+    lib.pf_default_params(ctypes.byref(got))
+    want = P.default_params()
+    for name, _ in L.Params._fields_:
+        assert getattr(got, name) == getattr(want, name), name
+
+
+def test_describing_a_workload_does_not_load_the_cuda_library():
+    import subprocess
+    import sys
+    code = ("import sys; from puffin_gb300 import configs, lib; "
+            "w = configs.config2(np_=4096, nz2=64); "
+            "assert lib._lib is None; "
+            "maps = open('/proc/self/maps').read(); "
+            "sys.exit(1 if 'libpuffgpu' in maps else 0)")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", code], cwd=root, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
 def test_create_rejects_bad_params_without_touching_a_device():
     lib = L.load()
     p = P.default_params(eta=0.0)

@@ -137,7 +137,18 @@ def test_cell_edges_and_periodic_images():
     """The cell index and fraction come from the bits of the scaled
     coordinate: macroparticles exactly on cell boundaries (transverse and
     z2), at negative z2 and beyond the first period of the periodic mesh
-    (their images), against the oracle's floor arithmetic at 1e-12."""
+    (their images), against the oracle's floor arithmetic at 1e-12.
+
+    Which behaviour this pins: on cell boundaries at non-negative
+    coordinates it is the reference's own -- there its node index from
+    truncating int() (rhs.f90:174-178) and its weights from floor
+    (system_interpolation.f90:45-58) agree.  Negative z2 and z2 beyond the
+    first period are inputs the reference does not define (int() and floor
+    part ways and its node index leaves the mesh); here the periodic mesh
+    reads them as their images, plane modulo nz2 - 1, which is where the
+    reference's own wrap (para_field.f90:212-215) puts them.  On the
+    temporal mesh z2 < 0 returns PF_OUT_OF_Z2 (a deliberate deviation: the
+    reference neither checks nor defines it)."""
     w = configs.config1(np_=4096, seed=5, nsteps=2)
     p = w.params
     beam = {k: v.copy() for k, v in w.beam.items()}
