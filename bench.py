@@ -75,8 +75,8 @@ def parse():
     ap.add_argument("--np3", type=int, default=2 ** 24,
                     help="macroparticles of the mixed-vs-FP64 leg on the config-1 mesh (0: skip)")
     ap.add_argument("--steps3", type=int, default=32)
-    ap.add_argument("--fidelity-np", type=int, default=2 ** 20,
-                    help="macroparticles of the mixed-vs-FP64 saturation leg (0: skip)")
+    ap.add_argument("--fidelity-np", type=int, default=2 ** 22,
+                    help="macroparticles of the mixed-vs-FP64 run to saturation (0: skip)")
     ap.add_argument("--fidelity-steps", type=int, default=6000)
     ap.add_argument("--batch-n", type=int, default=128,
                     help="instances of the batched form (0: skip the leg)")
@@ -91,6 +91,8 @@ def parse():
     ap.add_argument("--adjoint-steps", type=int, default=3000,
                     help="steps of the adjoint leg on the 33x33x128 periodic mesh (0: skip); "
                          "3000 is the adjoint form's full run")
+    ap.add_argument("--adjoint-fd-steps", default="3000,1000",
+                    help="horizons (steps) of the adjoint's finite-difference check ('' : none)")
     return ap.parse_args()
 
 
@@ -379,9 +381,14 @@ def whole_job_rate(units_per_rank, steps, world, ms):
 def adjoint_leg(args, dev):
     """The adjoint form: periodic 33 x 33 x 128 mesh (129 nodes, 128 unique
     planes), 2^18 macroparticles, Gaussian seed of waist 1.0 on the resonant
-    carrier, a 16-point taper profile, checkpoints every 64 steps; the forward
+    carrier at power 1e-3 of saturation (|A|^2 of about 1 in the scaled
+    units), a 16-point taper profile, checkpoints every 64 steps; the forward
     run with checkpoints, then the backward pass (recompute + adjoint), timed
-    with CUDA events on the library's stream."""
+    with CUDA events on the library's stream.  Then the gradient against
+    central finite differences with steps of 1e-6 (relative for the seed
+    amplitude, absolute for the taper points and the chirp) on all 18
+    components, at the full run and at the shorter horizons of
+    --adjoint-fd-steps."""
     import torch
 
     import puffin_gb300 as P
@@ -396,31 +403,75 @@ def adjoint_leg(args, dev):
     g = np.exp(-(xs[None, :] ** 2 + ys[:, None] ** 2) / 2.0).ravel()
     ph = np.arange(nz2) * p.dz2 / (2.0 * p.rho)
     seed = ((np.cos(ph)[:, None] * g[None, :]).ravel(), (np.sin(ph)[:, None] * g[None, :]).ravel())
-    taper_z = np.linspace(0.0, w.nsteps * w.h, 16)
-    alpha = np.ones(16)
+    amp, chirp = math.sqrt(1e-3), 0.0
+    out = {}
     with P.Puffin(p) as sim:
         sim.set_particles(*(w.beam[k] for k in P.PARTICLE_KEYS))
-        sim.set_taper_profile(taper_z, alpha)
         stream = torch.cuda.ExternalStream(sim.stream_handle, device=dev)
-        run = lambda: sim.adjoint_forward(w.nsteps, w.isteps4diff, True, w.h, 64, seed[0], seed[1],
-                                          1e-2, 0.0)
-        run()                                    # warm-up (plans, allocations)
+
+        def energy(nsteps, alpha, a, c):
+            sim.set_taper_profile(np.linspace(0.0, nsteps * w.h, 16), alpha)
+            return sim.adjoint_forward(nsteps, w.isteps4diff, True, w.h, 64, seed[0], seed[1],
+                                       a, c)
+
+        alpha0 = np.ones(16)
+        energy(w.nsteps, alpha0, amp, chirp)        # warm-up (plans, allocations)
         sim.adjoint_backward(16)
         e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
         torch.cuda.synchronize()
         e[0].record(stream)
-        energy = run()
+        e0 = energy(w.nsteps, alpha0, amp, chirp)
         e[1].record(stream)
         gt, gs, gc = sim.adjoint_backward(16)
         e[2].record(stream)
         torch.cuda.synchronize()
         fwd, bwd = e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])
-    return {
-        "workload": w.name, "macroparticles": w.np, "mesh": [nx, ny, nz2], "steps": w.nsteps,
-        "checkpoint_every": 64, "forward_ms": fwd, "backward_ms": bwd,
-        "backward_over_forward": bwd / fwd, "energy": energy,
-        "grad_seed_amp": gs, "grad_chirp": gc, "grad_taper_norm": float(np.linalg.norm(gt)),
-    }
+        out = {
+            "workload": w.name, "macroparticles": w.np, "mesh": [nx, ny, nz2],
+            "steps": w.nsteps, "checkpoint_every": 64, "seed_amplitude": amp,
+            "forward_ms": fwd, "backward_ms": bwd, "backward_over_forward": bwd / fwd,
+            "energy": e0, "grad_seed_amp": gs, "grad_chirp": gc,
+            "grad_taper_norm": float(np.linalg.norm(gt)),
+        }
+        checks = []
+        for nsteps in [int(v) for v in args.adjoint_fd_steps.split(",") if v.strip()]:
+            t0 = time.perf_counter()
+            energy(nsteps, alpha0, amp, chirp)
+            g_t, g_s, g_c = sim.adjoint_backward(16)
+            adj = list(g_t) + [g_s, g_c]
+            num = []
+            for k in range(18):
+                if k < 16:
+                    d = 1e-6
+                    ap, am = alpha0.copy(), alpha0.copy()
+                    ap[k] += d
+                    am[k] -= d
+                    num.append((energy(nsteps, ap, amp, chirp) - energy(nsteps, am, amp, chirp))
+                               / (2 * d))
+                elif k == 16:
+                    d = 1e-6 * amp
+                    num.append((energy(nsteps, alpha0, amp + d, chirp)
+                                - energy(nsteps, alpha0, amp - d, chirp)) / (2 * d))
+                else:
+                    d = 1e-6
+                    num.append((energy(nsteps, alpha0, amp, chirp + d)
+                                - energy(nsteps, alpha0, amp, chirp - d)) / (2 * d))
+            adj, num = np.array(adj), np.array(num)
+            big = np.abs(num) >= 1e-3 * np.max(np.abs(num))
+            rel = np.abs(adj - num) / np.maximum(np.abs(num), 1e-300)
+            checks.append({
+                "steps": nsteps, "zbar": nsteps * w.h,
+                "max_rel_error": float(np.max(rel[big])),
+                "within_1e-4": bool(np.max(rel[big]) <= 1e-4),
+                "components_checked": int(np.count_nonzero(big)),
+                "rel_error": [float(v) for v in rel],
+                "adjoint": [float(v) for v in adj], "differences": [float(v) for v in num],
+                "seconds": time.perf_counter() - t0,
+            })
+        out["finite_difference_checks"] = checks
+        out["fd_note"] = ("central differences, steps 1e-6 (seed amplitude: 1e-6 relative); "
+                          "components below 1e-3 of the largest are listed but not counted")
+    return out
 
 
 def fidelity_leg(args, dev):
@@ -441,10 +492,20 @@ def fidelity_leg(args, dev):
         w.params.precision = prec
         w.params.device = dev
         t0 = time.perf_counter()
-        curves[name] = fel.power_curve(w.params, w.beam, w.field, w.h, args.fidelity_steps)
+        curves[name] = fel.power_curve(w.params, w.beam, w.field, w.h, args.fidelity_steps,
+                                       timings=True)
         t[name] = time.perf_counter() - t0
     z = curves["fp64"][0]
     cmp = fel.compare(z, curves["fp64"][1], curves["mixed"][1])
+    # time per step over the whole run and over its last 10 % (the
+    # saturated, bunched beam), wall clock around each 16-step call
+    nlast = max(1, len(z) // 10)
+    per_step = {}
+    for name in ("fp64", "mixed"):
+        ts = curves[name][2]
+        per_step[name] = {"all_ms": 1e3 * float(ts.sum()) / (16 * len(ts)),
+                          "first_10pct_ms": 1e3 * float(ts[:nlast].sum()) / (16 * nlast),
+                          "last_10pct_ms": 1e3 * float(ts[-nlast:].sum()) / (16 * nlast)}
     return {
         "workload": "config-1 mesh run to saturation (periodic helical 21x21x64, rho 0.005)",
         "macroparticles": args.fidelity_np, "steps": args.fidelity_steps,
@@ -455,6 +516,12 @@ def fidelity_leg(args, dev):
         "targets": {"gain_length_rel": 5e-3, "saturated_power_rel": 1e-2},
         "within_targets": bool(abs(cmp["gain_length"]["rel_diff"]) <= 5e-3
                                and abs(cmp["saturated_energy"]["rel_diff"]) <= 1e-2),
+        "ms_per_step": per_step,
+        "speedup_mixed_vs_fp64": {
+            "all": per_step["fp64"]["all_ms"] / per_step["mixed"]["all_ms"],
+            "last_10pct": per_step["fp64"]["last_10pct_ms"] / per_step["mixed"]["last_10pct_ms"]},
+        "macroparticle_steps_per_s_last_10pct": {
+            k: args.fidelity_np / (1e-3 * v["last_10pct_ms"]) for k, v in per_step.items()},
         "wall_seconds": t,
     }
 

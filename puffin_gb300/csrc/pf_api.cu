@@ -471,6 +471,7 @@ int pf_create(const pf_params *p, pf_handle **out) {
   h->npl = (p->mesh_type == PF_MESH_PERIODIC) ? p->nz2 - 1 : p->nz2;
   h->nouter = (int64_t)p->nx * p->ny * p->nz2;
   auto fail = [&](cudaError_t e, const char *what) {
+    (void)cudaGetLastError();  // an allocation failure leaves the context usable
     g_err = std::string("pf_create: ") + what + ": " + cudaGetErrorString(e);
     pf_destroy(h);
     return PF_CUDA_ERR;

@@ -589,10 +589,12 @@ __device__ __forceinline__ void node_update_mixed(const MixNodeArgs &a, const in
       a.w[n] = make_float2(w.x + a.h6 * (d0.x + d.x + 2.f * e12.x), w.y + a.h6 * (d0.y + d.y + 2.f * e12.y));
   }
   // The accumulator is cleared last, with zeros computed from the loaded
-  // value (d - d is +0 for the finite sums of a run): a store of a constant
-  // to an address whose load is still in flight is several times slower on
-  // this GPU than the same store issued once the load has returned.
-  a.acc[n] = make_float2(d.x - d.x, d.y - d.y);
+  // value (its sign bit alone: a signed zero, also for a NaN left by a
+  // failed step): a store of a constant to an address whose load is still in
+  // flight is several times slower on this GPU than the same store issued
+  // once the load has returned.
+  a.acc[n] = make_float2(__int_as_float(__float_as_int(d.x) & (int)0x80000000),
+                         __int_as_float(__float_as_int(d.y) & (int)0x80000000));
 }
 
 template <int STAGE>

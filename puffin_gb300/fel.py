@@ -15,22 +15,32 @@ from . import lib as L
 from .puffin import PARTICLE_KEYS, Puffin
 
 
-def power_curve(params, beam, field, h: float, nsteps: int, every: int = 16):
+def power_curve(params, beam, field, h: float, nsteps: int, every: int = 16,
+                timings: bool = False):
     """Runs the module from (beam, field) in calls of `every` steps with
-    diffraction every `every` steps; returns (zbar, energy) after each call."""
+    diffraction every `every` steps; returns (zbar, energy) after each call,
+    and with `timings` also the wall-clock seconds of each call (the steps'
+    host and device time: each call ends with the device idle)."""
+    import time
+
     p = params
     nuniq = p.nz2 - 1 if p.mesh_type == L.MESH_PERIODIC else p.nz2
     n = p.nx * p.ny * nuniq
-    zs, es = [], []
+    zs, es, ts = [], [], []
     with Puffin(p) as sim:
         sim.set_particles(*(beam[k] for k in PARTICLE_KEYS))
         sim.set_field(*field)
         szl = 0.0
         for _ in range(nsteps // every):
+            t0 = time.perf_counter()
             szl = sim.und_section(every, every, True, h, szl)
+            sim.sync()
+            ts.append(time.perf_counter() - t0)
             fr, fi = sim.get_field()
             es.append(float(np.sum(fr[:n] ** 2 + fi[:n] ** 2)) * p.dx * p.dy * p.dz2)
             zs.append(szl)
+    if timings:
+        return np.array(zs), np.array(es), np.array(ts)
     return np.array(zs), np.array(es)
 
 

@@ -42,4 +42,8 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    # the reference project's checkout: first argument or PUFFIN_REFERENCE
+    src = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PUFFIN_REFERENCE")
+    if not src:
+        sys.exit("usage: make_golden.py <reference checkout> (or set PUFFIN_REFERENCE)")
+    main(src)

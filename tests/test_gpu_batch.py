@@ -189,3 +189,55 @@ def test_temporal_and_mixed_eager_batch():
     assert np.all(st == 0)
     for i, (g, w) in enumerate(zip(got, want)):
         _assert_same(g, w, False, f"instance {i}")
+
+
+def _oracle_instances():
+    """A sample of the batched form's own instance mixes: a 17^2 helical and a
+    65^2 planepole periodic instance from the recipe, and a 33^2 instance of
+    the recipe turned into a temporal mesh (its beam inside the mesh)."""
+    ws = configs.config5(n_inst=48, seed=21, nsteps=NSTEPS, np_range=(2 ** 11, 2 ** 12))
+    pick = {}
+    for w in ws:
+        key = (w.params.nx, w.params.und_type)
+        if key == (33, P.UND_HELICAL) and w.params.nz2 - 1 != 128:
+            continue   # the temporal one needs room for the 37-node z2 absorbing ends
+        if key in ((17, P.UND_HELICAL), (65, P.UND_PLANEPOLE), (33, P.UND_HELICAL)) \
+                and key not in pick:
+            pick[key] = w
+    assert len(pick) == 3
+    t = pick[(33, P.UND_HELICAL)]
+    p = t.params
+    p.mesh_type = P.MESH_TEMPORAL
+    p.nz2 = p.nz2 - 1
+    lz2 = (p.nz2 - 1) * p.dz2
+    t.beam["z2"] = 0.2 * lz2 + 0.6 * (t.beam["z2"] - t.beam["z2"].min()) / np.ptp(t.beam["z2"]) * lz2
+    n = p.nx * p.ny * p.nz2
+    t.field = (np.zeros(n), np.zeros(n))
+    return [pick[(17, P.UND_HELICAL)], pick[(65, P.UND_PLANEPOLE)], t]
+
+
+def test_batch_instances_match_the_oracle():
+    """The batch against the oracle's UndSection (undulator.f90:106-331) on
+    instances of the batched form's own mixes, at pf_run's single-instance
+    tolerance (1e-9): the batch is checked against the restatement of the
+    reference, not only against the library's own single-instance path."""
+    from oracle import oracle as O
+    from tests.oracle_bridge import assert_beam_close, oracle_beam, oracle_config
+    ws = _oracle_instances()
+    got, st, _ = _batch_run(ws)
+    assert np.all(st == 0)
+    for i, w in enumerate(ws):
+        cfg = oracle_config(w.params)
+        beam = oracle_beam(w.beam)
+        rng = np.random.default_rng(int(w.np))
+        n = len(w.field[0])
+        re, im = 1e-3 * rng.standard_normal(n), 1e-3 * rng.standard_normal(n)   # as _make
+        r = O.undulator_run(cfg, beam, re, im, w.h, NSTEPS, EVERY, True,
+                            redist_every=w.params.redist_every)
+        assert r.status == 0 and r.steps == NSTEPS, i
+        (gp, (gfr, gfi), gc), gz = got[i]
+        assert gc == r.csteps
+        assert_beam_close(gp, beam, rtol=1e-9, atol=1e-12)
+        scale = max(np.max(np.abs(re)), np.max(np.abs(im)))
+        np.testing.assert_allclose(gfr, re, rtol=0, atol=1e-9 * scale, err_msg=f"instance {i}")
+        np.testing.assert_allclose(gfi, im, rtol=0, atol=1e-9 * scale, err_msg=f"instance {i}")

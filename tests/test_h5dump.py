@@ -8,10 +8,12 @@ import pytest
 from puffin_gb300 import h5dump as H
 
 GOLD = os.path.join(os.path.dirname(__file__), "golden", "f1main_expected.npz")
-REF = "/root/reference/test/expected"
+# the reference project's checkout, when there is one (its test/expected dumps)
+REF = os.path.join(os.environ.get("PUFFIN_REFERENCE", ""), "test", "expected")
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="the reference's dump files are not here")
+@pytest.mark.skipif(not os.environ.get("PUFFIN_REFERENCE") or not os.path.isdir(REF),
+                    reason="set PUFFIN_REFERENCE to the reference checkout to read its dumps")
 def test_reads_reference_dumps():
     g = np.load(GOLD)
     beam, attrs = H.read_particles(os.path.join(REF, "f1main_expected_electrons.h5"))
