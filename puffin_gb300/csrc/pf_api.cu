@@ -637,36 +637,95 @@ __global__ void k_iota32(int32_t *p, int64_t n) {
   if (t < n) p[t] = (int32_t)t;
 }
 
-// one atomic per distinct plane of a warp (the arrays are mostly z2-ordered)
-__device__ __forceinline__ int warp_plane_add(int *cnt, int plane, bool on) {
-  const unsigned act = __ballot_sync(0xffffffffu, on);
-  if (!on) return 0;
-  const unsigned peers = __match_any_sync(act, plane);
-  const int leader = __ffs(peers) - 1;
-  const int lane = threadIdx.x & 31;
-  const int rank = __popc(peers & ((1u << lane) - 1u));
-  int base = 0;
-  if (lane == leader) base = atomicAdd(cnt + plane, __popc(peers));
-  base = __shfl_sync(peers, base, leader);
-  return base + rank;
+// Stable counting sort over the z2 planes.  The macroparticles are cut into
+// chunks of consecutive slots, one warp per chunk: (1) each chunk counts its
+// planes; (2) an exclusive scan of the counts in (plane, chunk) order gives
+// every chunk the first slot of each plane it holds; (3) each chunk writes its
+// macroparticles in order, a warp-wide rank among equal planes per round of
+// 32.  Slots keep their relative order within a plane, so the result depends
+// only on the input order: the same every run.
+constexpr int SORT_SCAN_TILE = 4096;  // ints per block of the scan
+
+__global__ void __launch_bounds__(32) k_chunk_count(const double *z2, int64_t n, int64_t chunk,
+                                                    double inv_dz2, int npl, int periodic,
+                                                    int *tab, int64_t nchunks) {
+  extern __shared__ int hist[];
+  const int64_t c = blockIdx.x;
+  for (int k = threadIdx.x; k < npl; k += 32) hist[k] = 0;
+  __syncwarp();
+  const int64_t i0 = c * chunk, i1 = min(n, i0 + chunk);
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += 32)
+    atomicAdd(hist + sort_plane(z2[i], inv_dz2, npl, periodic), 1);
+  __syncwarp();
+  for (int k = threadIdx.x; k < npl; k += 32) tab[(int64_t)k * nchunks + c] = hist[k];
 }
 
-__global__ void k_plane_count(const double *z2, int64_t n, double inv_dz2, int npl, int periodic,
-                              int *cnt) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const bool on = t < n;
-  const int p = on ? sort_plane(z2[t], inv_dz2, npl, periodic) : 0;
-  warp_plane_add(cnt, p, on);
-}
-
-__global__ void k_plane_scan(int *cnt, int npl) {  // exclusive, one thread
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+// exclusive scan of 4096-int tiles in place; tile totals to sums[blockIdx.x]
+__global__ void __launch_bounds__(256) k_scan_tiles(int *v, int64_t n, int *sums) {
+  __shared__ int warp_tot[8];
+  const int64_t base = (int64_t)blockIdx.x * SORT_SCAN_TILE + (int64_t)threadIdx.x * 16;
+  int x[16];
   int run = 0;
-  for (int k = 0; k < npl; ++k) {
-    const int c = cnt[k];
-    cnt[k] = run;
-    run += c;
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    x[k] = (base + k < n) ? v[base + k] : 0;
+    run += x[k];
   }
+  // exclusive scan of the per-thread totals across the block
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int inc = run;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += t;
+  }
+  if (lane == 31) warp_tot[w] = inc;
+  __syncthreads();
+  int woff = 0, tot = 0;
+  for (int k = 0; k < 8; ++k) {
+    if (k < w) woff += warp_tot[k];
+    tot += warp_tot[k];
+  }
+  int acc = woff + inc - run;
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    if (base + k < n) v[base + k] = acc;
+    acc += x[k];
+  }
+  if (threadIdx.x == 0) sums[blockIdx.x] = tot;
+}
+
+// exclusive scan of the tile totals (one block, in order)
+__global__ void __launch_bounds__(1024) k_scan_sums(int *sums, int m) {
+  __shared__ int carry;
+  __shared__ int warp_tot[32];
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int b = 0; b < m; b += 1024) {
+    const int i = b + threadIdx.x;
+    const int x = (i < m) ? sums[i] : 0;
+    int inc = x;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += t;
+    }
+    if (lane == 31) warp_tot[w] = inc;
+    __syncthreads();
+    int woff = 0, tot = 0;
+    for (int k = 0; k < 32; ++k) {
+      if (k < w) woff += warp_tot[k];
+      tot += warp_tot[k];
+    }
+    if (i < m) sums[i] = carry + woff + inc - x;
+    __syncthreads();
+    if (threadIdx.x == 0) carry += tot;
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(256) k_scan_add(int *v, int64_t n, const int *sums) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) v[i] += sums[i / SORT_SCAN_TILE];
 }
 
 struct SortArrays {
@@ -676,16 +735,36 @@ struct SortArrays {
   int32_t *perm_dst;
 };
 
-__global__ void k_plane_scatter(const SortArrays a, int64_t n, double inv_dz2, int npl,
-                                int periodic, int *off) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const bool on = t < n;
-  const int p = on ? sort_plane(a.src[2][t], inv_dz2, npl, periodic) : 0;
-  const int pos = warp_plane_add(off, p, on);
-  if (!on) return;
+__global__ void __launch_bounds__(32) k_chunk_scatter(const SortArrays a, int64_t n, int64_t chunk,
+                                                      double inv_dz2, int npl, int periodic,
+                                                      const int *tab, int64_t nchunks) {
+  extern __shared__ int run[];
+  const int64_t c = blockIdx.x;
+  for (int k = threadIdx.x; k < npl; k += 32) run[k] = tab[(int64_t)k * nchunks + c];
+  __syncwarp();
+  const int lane = threadIdx.x;
+  const unsigned lt = (1u << lane) - 1u;
+  const int64_t i0 = c * chunk, i1 = min(n, i0 + chunk);
+  for (int64_t r = i0; r < i1; r += 32) {
+    const int64_t t = r + lane;
+    const bool on = t < i1;
+    const unsigned act = __ballot_sync(0xffffffffu, on);
+    int pos = 0, p = 0;
+    unsigned peers = 0;
+    if (on) {
+      p = sort_plane(a.src[2][t], inv_dz2, npl, periodic);
+      peers = __match_any_sync(act, p);
+      pos = run[p] + __popc(peers & lt);
+    }
+    __syncwarp();
+    if (on && lane == 31 - __clz(peers)) run[p] += __popc(peers);  // the group's last lane
+    __syncwarp();
+    if (on) {
 #pragma unroll
-  for (int j = 0; j < 7; ++j) a.dst[j][pos] = a.src[j][t];
-  a.perm_dst[pos] = a.perm_src[t];
+      for (int j = 0; j < 7; ++j) a.dst[j][pos] = a.src[j][t];
+      a.perm_dst[pos] = a.perm_src[t];
+    }
+  }
 }
 
 __global__ void k_unpermute(const double *src, const int32_t *perm, double *dst, int64_t n) {
@@ -700,25 +779,48 @@ int pf_sort_z2(pf_handle *h) {
   if (!h->sort_z2 || h->np < ((int64_t)1 << 15) || h->p.one_d || h->npl < 2) return PF_OK;
   if (h->np >= ((int64_t)1 << 31)) return PF_OK;
   const int npl = (int)h->npl;
+  if ((size_t)npl * sizeof(int) > (size_t)200 * 1024) return PF_OK;  // plane table per warp
   const int periodic = (h->p.mesh_type == PF_MESH_PERIODIC);
   const double inv_dz2 = 1.0 / h->p.dz2;
   const int64_t n = h->np;
+  // chunks of at least 1024 slots, about 4096 of them, the count table
+  // (npl x chunks ints) at most 64 MB
+  int64_t chunk = std::max<int64_t>(1024, (n + 4095) / 4096);
+  while ((n + chunk - 1) / chunk * (int64_t)npl > ((int64_t)16 << 20)) chunk *= 2;
+  const int64_t nchunks = (n + chunk - 1) / chunk;
+  const int64_t ntab = nchunks * npl;
+  const int64_t ntiles = (ntab + SORT_SCAN_TILE - 1) / SORT_SCAN_TILE;
+  const size_t need = (size_t)(ntab + ntiles);
   if (!h->perm) PF_CUDA(cudaMalloc(&h->perm, sizeof(int32_t) * (size_t)h->cap));
+  if (h->plane_cap < (int64_t)need) {
+    cudaFree(h->plane_off);
+    h->plane_off = nullptr;
+    PF_CUDA(cudaMalloc(&h->plane_off, sizeof(int) * need));
+    h->plane_cap = (int64_t)need;
+  }
   if (!h->permuted) {
     k_iota32<<<grid_for(n, 256), 256, 0, h->stream>>>(h->perm, n);
     PF_LAUNCHED(h);
   }
-  if (h->plane_cap < npl) {
-    cudaFree(h->plane_off);
-    h->plane_off = nullptr;
-    PF_CUDA(cudaMalloc(&h->plane_off, sizeof(int) * (size_t)npl));
-    h->plane_cap = npl;
-  }
-  PF_CUDA(cudaMemsetAsync(h->plane_off, 0, sizeof(int) * (size_t)npl, h->stream));
-  k_plane_count<<<grid_for(n, 256), 256, 0, h->stream>>>(h->y[h->cur][2], n, inv_dz2, npl,
-                                                         periodic, h->plane_off);
+  const size_t smem = sizeof(int) * (size_t)npl;
+  static PfDeviceOnce attr_once;  // the attribute is per device
+  PF_CUDA(pf_device_once(attr_once, [] {
+    cudaError_t e = cudaFuncSetAttribute(k_chunk_count, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         200 * 1024);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_chunk_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               200 * 1024);
+    return e;
+  }));
+  int *tab = h->plane_off, *sums = h->plane_off + ntab;
+  k_chunk_count<<<(unsigned)nchunks, 32, smem, h->stream>>>(h->y[h->cur][2], n, chunk, inv_dz2,
+                                                            npl, periodic, tab, nchunks);
   PF_LAUNCHED(h);
-  k_plane_scan<<<1, 32, 0, h->stream>>>(h->plane_off, npl);
+  k_scan_tiles<<<(unsigned)ntiles, 256, 0, h->stream>>>(tab, ntab, sums);
+  PF_LAUNCHED(h);
+  k_scan_sums<<<1, 1024, 0, h->stream>>>(sums, (int)ntiles);
+  PF_LAUNCHED(h);
+  k_scan_add<<<grid_for(ntab, 256), 256, 0, h->stream>>>(tab, ntab, sums);
   PF_LAUNCHED(h);
   SortArrays a;
   const int nxt = 1 - h->cur;
@@ -730,8 +832,8 @@ int pf_sort_z2(pf_handle *h) {
   a.dst[6] = h->k1[0];
   a.perm_src = h->perm;
   a.perm_dst = reinterpret_cast<int32_t *>(h->ka[0]);
-  k_plane_scatter<<<grid_for(n, 256), 256, 0, h->stream>>>(a, n, inv_dz2, npl, periodic,
-                                                           h->plane_off);
+  k_chunk_scatter<<<(unsigned)nchunks, 32, smem, h->stream>>>(a, n, chunk, inv_dz2, npl, periodic,
+                                                              tab, nchunks);
   PF_LAUNCHED(h);
   const size_t b = sizeof(double) * (size_t)n;
   for (int j = 0; j < 6; ++j)

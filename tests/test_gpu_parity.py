@@ -551,3 +551,23 @@ def test_run_with_z2_ordering_matches_step_by_step(precision):
     else:
         assert_beam_close(got, oracle_beam(want), rtol=1e-5, atol=1e-7)
         field_close(gf, wf, 1e-4)
+
+
+def test_z2_ordering_is_the_same_every_run():
+    """The z2 ordering inside pf_run is a stable counting sort (the slots of
+    a plane keep their order), so the device order after a run depends on
+    the input only: reductions over the macroparticles in device order, such
+    as correctTrans's chi-weighted means (acc_lattice.f90:601-623), give the
+    same bits in two identical runs."""
+    w = configs.config1(np_=3 * 2 ** 15, seed=44, nsteps=130)
+    field = random_field(w.params, 6, amp=1e-2)
+    outs = []
+    for _ in range(2):
+        with P.Puffin(w.params) as sim:
+            sim.set_particles(*(w.beam[k] for k in P.PARTICLE_KEYS))
+            sim.set_field(*field)
+            sim.und_section(130, 10, True, w.h)
+            sim.correctTrans()
+            outs.append(sim.get_particles())
+    for k in P.PARTICLE_KEYS:
+        np.testing.assert_array_equal(outs[0][k], outs[1][k], err_msg=k)
