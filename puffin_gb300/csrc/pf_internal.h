@@ -203,6 +203,11 @@ struct pf_handle {
   int *plane_off = nullptr;
   int64_t plane_cap = 0, last_sort = 0;
   bool permuted = false, sort_z2 = true;
+  // macroparticle-stages the mixed stage kernels deposited past their shared
+  // tile since the last ordering (d_status[1], read with the status word): a
+  // bunched beam loses its z2 order within steps, and pf_run re-orders it
+  // once this passes a threshold
+  uint64_t tile_misses = 0;
 
   // mixed precision: interleaved complex-float outer mesh and window arrays
   void *oc32 = nullptr;

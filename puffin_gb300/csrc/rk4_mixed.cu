@@ -58,7 +58,11 @@ constexpr int MX_THREADS = 512;
 constexpr int MX_PPT = 8;  // macroparticles per thread, at most
 // the unsigned low words of the exact tile hold up to 4096 parts below 2^20
 static_assert(MX_THREADS * MX_PPT <= 4096, "tile low words could carry");
-constexpr int MX_TILE_PLANES = 3;
+// planes of the shared deposit tile: as many as fit MX_TILE_BYTES (three
+// 512-thread blocks per SM), at least 3, at most MX_TILE_PLANES_MAX
+constexpr int MX_TILE_PLANES_MIN = 3;
+constexpr int MX_TILE_PLANES_MAX = 8;
+constexpr size_t MX_TILE_BYTES = 72 * 1024;
 
 struct BFieldF {
   int type, place, one_d, focusing, tcase;
@@ -97,6 +101,8 @@ struct MixArgs {
   int nix, niy;
   int64_t npl, nz2;
   int periodic, one_d, tile;
+  int tplanes;          // planes of the shared tile
+  unsigned *misses;     // non-null: count of macroparticle-stages deposited past the tile
   double halfx, halfy, inv_dx, inv_dy, inv_dz2;
   double inv_g02, aw2, inv_eta, eta;
   float inv_dV3, sInv2rho, dxc, eta_k2, kn2col, n2col, rho2;
@@ -271,7 +277,7 @@ template <int STAGE, bool ONED>
 __device__ __forceinline__ void mixed_block(const MixArgs &a, const int64_t i0, const int64_t i1,
                                             const int ppt, float *tile, int &s_pzlo) {
   const int ntr = a.nix * a.niy;
-  const int tile_n = MX_TILE_PLANES * ntr;
+  const int tile_n = a.tplanes * ntr;
   // [re hi | im hi | re lo | im lo], tile_n words each
   int *thi_r = reinterpret_cast<int *>(tile);
   int *thi_i = thi_r + tile_n;
@@ -306,6 +312,7 @@ __device__ __forceinline__ void mixed_block(const MixArgs &a, const int64_t i0, 
     __syncthreads();
   }
   const int pzlo = a.tile ? s_pzlo : 0;
+  unsigned nmiss = 0;  // this thread's macroparticle-stages deposited past the tile
 
 #pragma unroll 1
   for (int q = 0; q < ppt; ++q) {
@@ -435,9 +442,15 @@ __device__ __forceinline__ void mixed_block(const MixArgs &a, const int64_t i0, 
         const float dw = a.chi_f[i] * a.inv_dV3 * qrG;
         const float sr = dw * PX, si = dw * PY;
         const int nc = ONED ? 2 : 8;
-        const int tp0 = pz0 - pzlo, tp1 = pz1 - pzlo;
-        if (a.tile && (unsigned)tp0 < (unsigned)MX_TILE_PLANES &&
-            (unsigned)tp1 < (unsigned)MX_TILE_PLANES && fabsf(sr) < a.tile_vmax &&
+        // tile planes from the origin, modulo the periodic mesh (a block
+        // of macroparticles may straddle its end)
+        int tp0 = pz0 - pzlo, tp1 = pz1 - pzlo;
+        if (a.periodic) {
+          tp0 += (tp0 < 0) ? (int)a.npl : 0;
+          tp1 += (tp1 < 0) ? (int)a.npl : 0;
+        }
+        if (a.tile && (unsigned)tp0 < (unsigned)a.tplanes &&
+            (unsigned)tp1 < (unsigned)a.tplanes && fabsf(sr) < a.tile_vmax &&
             fabsf(si) < a.tile_vmax) {
           // the common case: both planes in the tile, and every corner's
           // |w s| <= |s| fits the tile's range (0 <= w <= 1)
@@ -462,6 +475,7 @@ __device__ __forceinline__ void mixed_block(const MixArgs &a, const int64_t i0, 
             tile_add(thi_i + ti, tlo_i + ti, __float2int_rz(w * sis));
           }
         } else {
+        ++nmiss;
 #pragma unroll
         for (int c = 0; c < 8; ++c) {
           if (c >= nc) break;
@@ -479,8 +493,9 @@ __device__ __forceinline__ void mixed_block(const MixArgs &a, const int64_t i0, 
             node = b0 + cx + (int64_t)cy * a.nix;
           }
           const float vr = w * sr, vi = w * si;
-          const int tp = plane - pzlo;
-          if (a.tile && tp >= 0 && tp < MX_TILE_PLANES && fabsf(vr) < a.tile_vmax &&
+          int tp = plane - pzlo;
+          if (a.periodic && tp < 0) tp += (int)a.npl;
+          if (a.tile && tp >= 0 && tp < a.tplanes && fabsf(vr) < a.tile_vmax &&
               fabsf(vi) < a.tile_vmax) {
             const int ti = tp * ntr + (int)node;
             tile_add(thi_r + ti, tlo_r + ti, f2fix(vr, a.fix_scale));
@@ -547,17 +562,24 @@ __device__ __forceinline__ void mixed_block(const MixArgs &a, const int64_t i0, 
     }
   }
 
+  if (a.misses) {
+    const unsigned m = __reduce_add_sync(0xffffffffu, nmiss);
+    if ((threadIdx.x & 31) == 0 && m) atomicAdd(a.misses, m);
+  }
   if (a.tile) {
     __syncthreads();
     if (pzlo != INT_MAX) {
       // (hi 2^20 + lo) 2^-E in FP32 (the accumulators are FP32)
       const float shi = ldexpf(1.f, 20 - a.fixE), slo = ldexpf(1.f, -a.fixE);
       for (int t = threadIdx.x; t < tile_n; t += MX_THREADS) {
-        const int plane = pzlo + t / ntr;
-        if (plane >= a.npl) break;
+        int plane = pzlo + t / ntr;
+        if (plane >= a.npl) {  // past the end: the periodic mesh's first planes
+          if (!a.periodic) break;
+          plane -= (int)a.npl;
+        }
         const float2 v = make_float2(fmaf((float)thi_r[t], shi, (float)tlo_r[t] * slo),
                                      fmaf((float)thi_i[t], shi, (float)tlo_i[t] * slo));
-        if (v.x != 0.f || v.y != 0.f) global_add(a.acc + (int64_t)plane * ntr + (t - (plane - pzlo) * ntr), v);
+        if (v.x != 0.f || v.y != 0.f) global_add(a.acc + (int64_t)plane * ntr + (t % ntr), v);
       }
     }
   }
@@ -704,6 +726,8 @@ void pf_step_coefficients_f(pf_handle *h, double szl, double hstep, void *out_) 
 size_t pf_step_coefficients_f_bytes() { return 4 * sizeof(StageCoefF); }
 
 // Stage arguments of the handle's state that do not change between stages.
+static int mixed_tile_planes(const pf_handle *h);
+
 static void fill_mix_args(pf_handle *h, MixArgs &a, double hstep) {
   const pf_params &p = h->p;
   memset(&a, 0, sizeof(a));
@@ -766,6 +790,8 @@ static void fill_mix_args(pf_handle *h, MixArgs &a, double hstep) {
   // the tile needs a window that fits shared memory and a scale 2^E that is
   // a normal float (beams with any usable charge weights)
   a.tile = (pf_mixed_tile_smem(h) > 0 && a.fixE >= -126 && a.fixE <= 127) ? 1 : 0;
+  a.tplanes = std::max(1, mixed_tile_planes(h));
+  a.misses = h->d_status + 1;
 }
 
 // Per-stage fields: the state and slope arrays of stage s for buffer cur.
@@ -814,9 +840,16 @@ static void fill_mix_nodes(pf_handle *h, MixNodeArgs &n, int s, double hstep) {
   n.status = h->d_status;
 }
 
+// planes of the shared tile for the handle's window (0: it does not fit)
+static int mixed_tile_planes(const pf_handle *h) {
+  const size_t per_plane = (size_t)4 * h->nix * h->niy * sizeof(int);
+  if (per_plane == 0 || (size_t)MX_TILE_PLANES_MIN * per_plane > 96 * 1024) return 0;
+  const int fit = (int)(MX_TILE_BYTES / per_plane);
+  return std::min(MX_TILE_PLANES_MAX, std::max(MX_TILE_PLANES_MIN, fit));
+}
+
 size_t pf_mixed_tile_smem(const pf_handle *h) {
-  const size_t bytes = (size_t)4 * MX_TILE_PLANES * h->nix * h->niy * sizeof(int);
-  return bytes <= 96 * 1024 ? bytes : 0;
+  return (size_t)mixed_tile_planes(h) * 4 * h->nix * h->niy * sizeof(int);
 }
 
 size_t pf_mixed_stage_args_bytes() { return sizeof(MixArgs); }
@@ -828,6 +861,7 @@ void pf_mixed_fill_stage(pf_handle *h, int stage, int cur, double hstep, int til
   fill_mix_args(h, a, hstep);
   mix_stage_pointers(h, a, stage, cur, hstep);
   a.tile = (tile && a.tile) ? 1 : 0;
+  a.misses = nullptr;  // batched instances keep their order (no z2 re-ordering)
   a.ppt = MX_PPT;
   a.coef_tab = coef_tab;
   a.step_ctr = step_ctr;
@@ -901,7 +935,8 @@ int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_ou
   const int nxt = h->cur ^ 1;
   // status_out == nullptr: enqueue only (a step of an asynchronous block;
   // the caller clears the status word once per block and reads it after)
-  if (status_out) PF_CUDA(cudaMemsetAsync(h->d_status, 0, sizeof(unsigned int), h->stream));
+  // the status word and the tile-miss count (d_status[1])
+  if (status_out) PF_CUDA(cudaMemsetAsync(h->d_status, 0, 2 * sizeof(unsigned int), h->stream));
 
   MixArgs a;
   fill_mix_args(h, a, hstep);
@@ -968,11 +1003,12 @@ int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_ou
     h->cur = nxt;  // committed optimistically; the block is replayed if it failed
     return PF_OK;
   }
-  PF_CUDA(cudaMemcpyAsync(h->h_status, h->d_status, sizeof(unsigned int), cudaMemcpyDeviceToHost,
-                          h->stream));
+  PF_CUDA(cudaMemcpyAsync(h->h_status, h->d_status, 2 * sizeof(unsigned int),
+                          cudaMemcpyDeviceToHost, h->stream));
   PF_CUDA(cudaStreamSynchronize(h->stream));
   pf_prof_flush(h);
   *status_out = *h->h_status;
+  h->tile_misses += h->h_status[1];
   if (*status_out == 0u) h->cur = nxt;
   return PF_OK;
 }
