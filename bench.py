@@ -91,8 +91,9 @@ def parse():
     ap.add_argument("--adjoint-steps", type=int, default=3000,
                     help="steps of the adjoint leg on the 33x33x128 periodic mesh (0: skip); "
                          "3000 is the adjoint form's full run")
-    ap.add_argument("--adjoint-fd-steps", default="3000,1000",
-                    help="horizons (steps) of the adjoint's finite-difference check ('' : none)")
+    ap.add_argument("--adjoint-fd", default="3000:1e-6,3000:1e-7,1000:1e-6",
+                    help="steps:step-size pairs of the adjoint's central-difference checks "
+                         "('' : none)")
     return ap.parse_args()
 
 
@@ -387,8 +388,9 @@ def adjoint_leg(args, dev):
     with CUDA events on the library's stream.  Then the gradient against
     central finite differences with steps of 1e-6 (relative for the seed
     amplitude, absolute for the taper points and the chirp) on all 18
-    components, at the full run and at the shorter horizons of
-    --adjoint-fd-steps."""
+    components, at the horizons and step sizes of --adjoint-fd (two step
+    sizes at one horizon show how far the differences themselves have
+    converged)."""
     import torch
 
     import puffin_gb300 as P
@@ -433,34 +435,36 @@ def adjoint_leg(args, dev):
             "energy": e0, "grad_seed_amp": gs, "grad_chirp": gc,
             "grad_taper_norm": float(np.linalg.norm(gt)),
         }
-        checks = []
-        for nsteps in [int(v) for v in args.adjoint_fd_steps.split(",") if v.strip()]:
-            t0 = time.perf_counter()
-            energy(nsteps, alpha0, amp, chirp)
-            g_t, g_s, g_c = sim.adjoint_backward(16)
-            adj = list(g_t) + [g_s, g_c]
+        def differences(nsteps, d):
             num = []
             for k in range(18):
                 if k < 16:
-                    d = 1e-6
                     ap, am = alpha0.copy(), alpha0.copy()
                     ap[k] += d
                     am[k] -= d
                     num.append((energy(nsteps, ap, amp, chirp) - energy(nsteps, am, amp, chirp))
                                / (2 * d))
                 elif k == 16:
-                    d = 1e-6 * amp
-                    num.append((energy(nsteps, alpha0, amp + d, chirp)
-                                - energy(nsteps, alpha0, amp - d, chirp)) / (2 * d))
+                    da = d * amp
+                    num.append((energy(nsteps, alpha0, amp + da, chirp)
+                                - energy(nsteps, alpha0, amp - da, chirp)) / (2 * da))
                 else:
-                    d = 1e-6
                     num.append((energy(nsteps, alpha0, amp, chirp + d)
                                 - energy(nsteps, alpha0, amp, chirp - d)) / (2 * d))
-            adj, num = np.array(adj), np.array(num)
+            return np.array(num)
+
+        checks = []
+        for spec in [v for v in args.adjoint_fd.split(",") if v.strip()]:
+            nsteps, d = (int(spec.split(":")[0]), float(spec.split(":")[1]))
+            t0 = time.perf_counter()
+            energy(nsteps, alpha0, amp, chirp)
+            g_t, g_s, g_c = sim.adjoint_backward(16)
+            adj = np.array(list(g_t) + [g_s, g_c])
+            num = differences(nsteps, d)
             big = np.abs(num) >= 1e-3 * np.max(np.abs(num))
             rel = np.abs(adj - num) / np.maximum(np.abs(num), 1e-300)
             checks.append({
-                "steps": nsteps, "zbar": nsteps * w.h,
+                "steps": nsteps, "zbar": nsteps * w.h, "fd_step": d,
                 "max_rel_error": float(np.max(rel[big])),
                 "within_1e-4": bool(np.max(rel[big]) <= 1e-4),
                 "components_checked": int(np.count_nonzero(big)),
@@ -468,9 +472,19 @@ def adjoint_leg(args, dev):
                 "adjoint": [float(v) for v in adj], "differences": [float(v) for v in num],
                 "seconds": time.perf_counter() - t0,
             })
+        # the differences' own convergence where two step sizes ran at one horizon
+        for a in checks:
+            for b in checks:
+                if a["steps"] == b["steps"] and a["fd_step"] > b["fd_step"]:
+                    na, nb = np.array(a["differences"]), np.array(b["differences"])
+                    big = np.abs(nb) >= 1e-3 * np.max(np.abs(nb))
+                    spread = np.abs(na - nb) / np.maximum(np.abs(nb), 1e-300)
+                    a.setdefault("fd_spread_vs_smaller_step", float(np.max(spread[big])))
         out["finite_difference_checks"] = checks
-        out["fd_note"] = ("central differences, steps 1e-6 (seed amplitude: 1e-6 relative); "
-                          "components below 1e-3 of the largest are listed but not counted")
+        out["fd_note"] = ("central differences with the stated step (seed amplitude: relative "
+                          "to the amplitude); components below 1e-3 of the largest are listed "
+                          "but not counted; fd_spread_vs_smaller_step is the largest relative "
+                          "change of the differences themselves between the two step sizes")
     return out
 
 

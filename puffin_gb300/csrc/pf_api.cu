@@ -1282,15 +1282,26 @@ int pf_sched_after_step(pf_handle *h, RunSched &s, int istep) {
     const int r = pf_wrap_z2(h);
     if (r) return r;
   }
-  // re-order at the wrap cadence, and sooner when more than 2 % of the
-  // macroparticle-stages since the last ordering missed their block's tile
+  // re-order at the wrap cadence, and (mixed precision, whose stage kernel
+  // deposits through a shared tile of a few z2 planes per block) sooner when
+  // more than 2 % of the macroparticles would miss their block's tile: a
+  // bunched beam near saturation loses its z2 order within a few steps.
+  // Checked after every block of steps, or every fourth step of a run that
+  // goes step by step.
   const int64_t since = h->csteps - h->last_sort;
-  const bool disordered = since > 0 && (double)h->tile_misses > 0.02 * 4.0 * (double)h->np * (double)since;
+  bool disordered = false;
+  if (h->sort_z2 && h->p.precision == PF_MIXED && since > 0 && h->np >= ((int64_t)1 << 15) &&
+      (h->csteps - h->last_check >= 4 || h->csteps < h->last_check)) {
+    h->last_check = h->csteps;
+    double frac = 0.0;
+    const int r = pf_mixed_order_misses(h, &frac);
+    if (r) return r;
+    disordered = frac > 0.02;
+  }
   if (since >= s.redist || since < 0 || disordered) {
     const int r = pf_sort_z2(h);
     if (r) return r;
     h->last_sort = h->csteps;
-    h->tile_misses = 0;
   }
   if (s.steps_done) *s.steps_done = istep;
   return PF_OK;
@@ -1355,7 +1366,7 @@ int pf_run(pf_handle *h, int32_t nsteps, int32_t isteps4diff, int32_t qdiffracti
     const int cur0 = h->cur;
     rc = pf_block_snapshot(h, true);
     if (rc) return rc;
-    PF_CUDA(cudaMemsetAsync(h->d_status, 0, 2 * sizeof(unsigned int), h->stream));
+    PF_CUDA(cudaMemsetAsync(h->d_status, 0, sizeof(unsigned int), h->stream));
     const int len = last - istep + 1;
     bool wrap_inside = false;
     for (int k = 1; k < len; ++k) wrap_inside |= ((csteps0 + k) % redist == 0);
@@ -1381,11 +1392,10 @@ int pf_run(pf_handle *h, int32_t nsteps, int32_t isteps4diff, int32_t qdiffracti
       }
       h->g_warm = true;  // kernel attributes are set: later blocks may be captured
     }
-    PF_CUDA(cudaMemcpyAsync(h->h_status, h->d_status, 2 * sizeof(unsigned int),
+    PF_CUDA(cudaMemcpyAsync(h->h_status, h->d_status, sizeof(unsigned int),
                             cudaMemcpyDeviceToHost, h->stream));
     PF_CUDA(cudaStreamSynchronize(h->stream));
     pf_prof_flush(h);
-    h->tile_misses += h->h_status[1];
     if (*h->h_status == 0u) {
       rc = pf_sched_after_step(h, sc, last);  // last step's position, diffraction and wrap
       if (rc) return rc;

@@ -201,13 +201,9 @@ struct pf_handle {
   // holds the caller's macroparticle perm[k] while `permuted`
   int32_t *perm = nullptr;
   int *plane_off = nullptr;
-  int64_t plane_cap = 0, last_sort = 0;
+  int64_t plane_cap = 0, last_sort = 0, last_check = 0;
   bool permuted = false, sort_z2 = true;
-  // macroparticle-stages the mixed stage kernels deposited past their shared
-  // tile since the last ordering (d_status[1], read with the status word): a
-  // bunched beam loses its z2 order within steps, and pf_run re-orders it
-  // once this passes a threshold
-  uint64_t tile_misses = 0;
+
 
   // mixed precision: interleaved complex-float outer mesh and window arrays
   void *oc32 = nullptr;
@@ -313,6 +309,9 @@ cudaError_t pf_mixed_nodes_batch(cudaStream_t st, int stage, const void *args,
                                  int *step_ctr);
 // mixed-precision RK4 step
 int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_out);
+// fraction of the macroparticles whose deposit would miss their mixed stage
+// block's shared tile (the z2 order a bunched beam loses within steps)
+int pf_mixed_order_misses(pf_handle *h, double *frac);
 // stage-coefficient table entries of one step (4 entries), FP64 and FP32 forms
 void pf_step_coefficients(pf_handle *h, double szl, double hstep, StageCoef *out);
 void pf_step_coefficients_f(pf_handle *h, double szl, double hstep, void *out);

@@ -58,10 +58,11 @@ constexpr int MX_THREADS = 512;
 constexpr int MX_PPT = 8;  // macroparticles per thread, at most
 // the unsigned low words of the exact tile hold up to 4096 parts below 2^20
 static_assert(MX_THREADS * MX_PPT <= 4096, "tile low words could carry");
-// planes of the shared deposit tile: as many as fit MX_TILE_BYTES (three
-// 512-thread blocks per SM), at least 3, at most MX_TILE_PLANES_MAX
-constexpr int MX_TILE_PLANES_MIN = 3;
-constexpr int MX_TILE_PLANES_MAX = 8;
+// planes of the shared deposit tile: 3, or 8 where eight fit MX_TILE_BYTES
+// (three 512-thread blocks per SM); a compile-time count keeps the kernel
+// within its 40 registers
+constexpr int MX_TILE_PLANES = 3;
+constexpr int MX_TILE_PLANES_WIDE = 8;
 constexpr size_t MX_TILE_BYTES = 72 * 1024;
 
 struct BFieldF {
@@ -101,8 +102,6 @@ struct MixArgs {
   int nix, niy;
   int64_t npl, nz2;
   int periodic, one_d, tile;
-  int tplanes;          // planes of the shared tile
-  unsigned *misses;     // non-null: count of macroparticle-stages deposited past the tile
   double halfx, halfy, inv_dx, inv_dy, inv_dz2;
   double inv_g02, aw2, inv_eta, eta;
   float inv_dV3, sInv2rho, dxc, eta_k2, kn2col, n2col, rho2;
@@ -273,11 +272,11 @@ __device__ __forceinline__ bool cell_split(double t, int &ip, float &fr) {
 // One block's macroparticles i0 + q MX_THREADS + threadIdx.x (q < ppt,
 // below i1).  Every thread of the block calls it (it holds block barriers
 // when the tile is on).
-template <int STAGE, bool ONED>
+template <int STAGE, bool ONED, int TP>
 __device__ __forceinline__ void mixed_block(const MixArgs &a, const int64_t i0, const int64_t i1,
                                             const int ppt, float *tile, int &s_pzlo) {
   const int ntr = a.nix * a.niy;
-  const int tile_n = a.tplanes * ntr;
+  const int tile_n = TP * ntr;
   // [re hi | im hi | re lo | im lo], tile_n words each
   int *thi_r = reinterpret_cast<int *>(tile);
   int *thi_i = thi_r + tile_n;
@@ -312,7 +311,6 @@ __device__ __forceinline__ void mixed_block(const MixArgs &a, const int64_t i0, 
     __syncthreads();
   }
   const int pzlo = a.tile ? s_pzlo : 0;
-  unsigned nmiss = 0;  // this thread's macroparticle-stages deposited past the tile
 
 #pragma unroll 1
   for (int q = 0; q < ppt; ++q) {
@@ -442,15 +440,11 @@ __device__ __forceinline__ void mixed_block(const MixArgs &a, const int64_t i0, 
         const float dw = a.chi_f[i] * a.inv_dV3 * qrG;
         const float sr = dw * PX, si = dw * PY;
         const int nc = ONED ? 2 : 8;
-        // tile planes from the origin, modulo the periodic mesh (a block
-        // of macroparticles may straddle its end)
-        int tp0 = pz0 - pzlo, tp1 = pz1 - pzlo;
-        if (a.periodic) {
-          tp0 += (tp0 < 0) ? (int)a.npl : 0;
-          tp1 += (tp1 < 0) ? (int)a.npl : 0;
-        }
-        if (a.tile && (unsigned)tp0 < (unsigned)a.tplanes &&
-            (unsigned)tp1 < (unsigned)a.tplanes && fabsf(sr) < a.tile_vmax &&
+        // tile planes from the origin (a block straddling the end of the
+        // periodic mesh takes the per-corner path below, which wraps)
+        const int tp0 = pz0 - pzlo, tp1 = pz1 - pzlo;
+        if (a.tile && (unsigned)tp0 < (unsigned)TP &&
+            (unsigned)tp1 < (unsigned)TP && fabsf(sr) < a.tile_vmax &&
             fabsf(si) < a.tile_vmax) {
           // the common case: both planes in the tile, and every corner's
           // |w s| <= |s| fits the tile's range (0 <= w <= 1)
@@ -475,7 +469,6 @@ __device__ __forceinline__ void mixed_block(const MixArgs &a, const int64_t i0, 
             tile_add(thi_i + ti, tlo_i + ti, __float2int_rz(w * sis));
           }
         } else {
-        ++nmiss;
 #pragma unroll
         for (int c = 0; c < 8; ++c) {
           if (c >= nc) break;
@@ -495,7 +488,7 @@ __device__ __forceinline__ void mixed_block(const MixArgs &a, const int64_t i0, 
           const float vr = w * sr, vi = w * si;
           int tp = plane - pzlo;
           if (a.periodic && tp < 0) tp += (int)a.npl;
-          if (a.tile && tp >= 0 && tp < a.tplanes && fabsf(vr) < a.tile_vmax &&
+          if (a.tile && tp >= 0 && tp < TP && fabsf(vr) < a.tile_vmax &&
               fabsf(vi) < a.tile_vmax) {
             const int ti = tp * ntr + (int)node;
             tile_add(thi_r + ti, tlo_r + ti, f2fix(vr, a.fix_scale));
@@ -562,10 +555,6 @@ __device__ __forceinline__ void mixed_block(const MixArgs &a, const int64_t i0, 
     }
   }
 
-  if (a.misses) {
-    const unsigned m = __reduce_add_sync(0xffffffffu, nmiss);
-    if ((threadIdx.x & 31) == 0 && m) atomicAdd(a.misses, m);
-  }
   if (a.tile) {
     __syncthreads();
     if (pzlo != INT_MAX) {
@@ -627,12 +616,13 @@ __global__ void __launch_bounds__(256) k_nodes_mixed(const MixNodeArgs a) {
   if (STAGE == 4 && a.step_ctr && n == 0) *a.step_ctr += 1;
 }
 
-template <int STAGE, bool ONED>
+template <int STAGE, bool ONED, int TP = MX_TILE_PLANES>
 __global__ void __launch_bounds__(MX_THREADS, 3) k_stage_mixed(const MixArgs a) {
   extern __shared__ __align__(16) float tile[];
   __shared__ int s_pzlo;
   const int64_t i0 = (int64_t)blockIdx.x * (MX_THREADS * a.ppt);
-  mixed_block<STAGE, ONED>(a, i0, min(a.np, i0 + (int64_t)MX_THREADS * a.ppt), a.ppt, tile, s_pzlo);
+  mixed_block<STAGE, ONED, TP>(a, i0, min(a.np, i0 + (int64_t)MX_THREADS * a.ppt), a.ppt, tile,
+                               s_pzlo);
 }
 
 // Batched mixed stage over (instance, macroparticle range) tiles of at most
@@ -658,7 +648,7 @@ __global__ void __launch_bounds__(MX_THREADS, 3) k_stage_mixed_batch(const MixAr
       __syncthreads();
     }
     const int ppt = (int)((tl.end - tl.begin + MX_THREADS - 1) / MX_THREADS);
-    mixed_block<STAGE, false>(sa, tl.begin, tl.end, ppt, tile, s_pzlo);
+    mixed_block<STAGE, false, MX_TILE_PLANES>(sa, tl.begin, tl.end, ppt, tile, s_pzlo);
   }
 }
 
@@ -726,8 +716,6 @@ void pf_step_coefficients_f(pf_handle *h, double szl, double hstep, void *out_) 
 size_t pf_step_coefficients_f_bytes() { return 4 * sizeof(StageCoefF); }
 
 // Stage arguments of the handle's state that do not change between stages.
-static int mixed_tile_planes(const pf_handle *h);
-
 static void fill_mix_args(pf_handle *h, MixArgs &a, double hstep) {
   const pf_params &p = h->p;
   memset(&a, 0, sizeof(a));
@@ -790,8 +778,6 @@ static void fill_mix_args(pf_handle *h, MixArgs &a, double hstep) {
   // the tile needs a window that fits shared memory and a scale 2^E that is
   // a normal float (beams with any usable charge weights)
   a.tile = (pf_mixed_tile_smem(h) > 0 && a.fixE >= -126 && a.fixE <= 127) ? 1 : 0;
-  a.tplanes = std::max(1, mixed_tile_planes(h));
-  a.misses = h->d_status + 1;
 }
 
 // Per-stage fields: the state and slope arrays of stage s for buffer cur.
@@ -840,16 +826,20 @@ static void fill_mix_nodes(pf_handle *h, MixNodeArgs &n, int s, double hstep) {
   n.status = h->d_status;
 }
 
-// planes of the shared tile for the handle's window (0: it does not fit)
-static int mixed_tile_planes(const pf_handle *h) {
-  const size_t per_plane = (size_t)4 * h->nix * h->niy * sizeof(int);
-  if (per_plane == 0 || (size_t)MX_TILE_PLANES_MIN * per_plane > 96 * 1024) return 0;
-  const int fit = (int)(MX_TILE_BYTES / per_plane);
-  return std::min(MX_TILE_PLANES_MAX, std::max(MX_TILE_PLANES_MIN, fit));
+// shared bytes of the 3-plane tile (0: it does not fit); the batched kernel
+// and the default of the single-instance kernel
+size_t pf_mixed_tile_smem(const pf_handle *h) {
+  const size_t bytes = (size_t)4 * MX_TILE_PLANES * h->nix * h->niy * sizeof(int);
+  return bytes <= 96 * 1024 ? bytes : 0;
 }
 
-size_t pf_mixed_tile_smem(const pf_handle *h) {
-  return (size_t)mixed_tile_planes(h) * 4 * h->nix * h->niy * sizeof(int);
+// planes of the single-instance kernel's tile: 8 where they fit
+// MX_TILE_BYTES (small windows, such as the 21 x 21 of the config-1 mesh:
+// a bunched beam's blocks spread over several planes), else 3
+static int mixed_tile_planes(const pf_handle *h) {
+  const size_t per_plane = (size_t)4 * h->nix * h->niy * sizeof(int);
+  return (size_t)MX_TILE_PLANES_WIDE * per_plane <= MX_TILE_BYTES ? MX_TILE_PLANES_WIDE
+                                                                 : MX_TILE_PLANES;
 }
 
 size_t pf_mixed_stage_args_bytes() { return sizeof(MixArgs); }
@@ -861,7 +851,6 @@ void pf_mixed_fill_stage(pf_handle *h, int stage, int cur, double hstep, int til
   fill_mix_args(h, a, hstep);
   mix_stage_pointers(h, a, stage, cur, hstep);
   a.tile = (tile && a.tile) ? 1 : 0;
-  a.misses = nullptr;  // batched instances keep their order (no z2 re-ordering)
   a.ppt = MX_PPT;
   a.coef_tab = coef_tab;
   a.step_ctr = step_ctr;
@@ -885,6 +874,14 @@ static cudaError_t mixed_attrs() {
                          (const void *)k_stage_mixed<3, false>, (const void *)k_stage_mixed<4, false>,
                          (const void *)k_stage_mixed<1, true>,  (const void *)k_stage_mixed<2, true>,
                          (const void *)k_stage_mixed<3, true>,  (const void *)k_stage_mixed<4, true>,
+                         (const void *)k_stage_mixed<1, false, MX_TILE_PLANES_WIDE>,
+                         (const void *)k_stage_mixed<2, false, MX_TILE_PLANES_WIDE>,
+                         (const void *)k_stage_mixed<3, false, MX_TILE_PLANES_WIDE>,
+                         (const void *)k_stage_mixed<4, false, MX_TILE_PLANES_WIDE>,
+                         (const void *)k_stage_mixed<1, true, MX_TILE_PLANES_WIDE>,
+                         (const void *)k_stage_mixed<2, true, MX_TILE_PLANES_WIDE>,
+                         (const void *)k_stage_mixed<3, true, MX_TILE_PLANES_WIDE>,
+                         (const void *)k_stage_mixed<4, true, MX_TILE_PLANES_WIDE>,
                          (const void *)k_stage_mixed_batch<1>,  (const void *)k_stage_mixed_batch<2>,
                          (const void *)k_stage_mixed_batch<3>,  (const void *)k_stage_mixed_batch<4>};
     for (const void *f : fns) {
@@ -928,6 +925,87 @@ cudaError_t pf_mixed_nodes_batch(cudaStream_t st, int stage, const void *args,
   return cudaGetLastError();
 }
 
+// Macroparticles per thread of the single-instance stage kernel: six (3072
+// per block), eight for beams dense along z2 (a block then still spans a
+// fraction of a plane; six and eight measured best for the config-2 and the
+// config-1-mesh 2^24 beams), fewer when the beam is too small to give every
+// SM two blocks.
+static int mixed_ppt(const pf_handle *h) {
+  const int64_t per_plane = h->np / std::max<int64_t>(1, (int64_t)h->npl);
+  const int64_t want = (per_plane >= (int64_t)16 * MX_THREADS) ? MX_PPT : 6;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(want, h->np / ((int64_t)152 * 2 * MX_THREADS)));
+}
+
+namespace {
+// Macroparticles of the stage kernel's blocks (as the kernel cuts them)
+// whose z2 cell lies outside the fast path of their block's shared tile:
+// the lowest plane the block starts from is estimated as the kernel does,
+// and a macroparticle counts when its two planes are not both in the tile.
+__global__ void __launch_bounds__(MX_THREADS) k_order_misses(const double *z2, int64_t np, int ppt,
+                                                             double inv_dz2, int npl, int periodic,
+                                                             int tp, unsigned *count) {
+  __shared__ int s_lo;
+  __shared__ unsigned s_cnt;
+  const int64_t i0 = (int64_t)blockIdx.x * MX_THREADS * ppt;
+  const int64_t i1 = min(np, i0 + (int64_t)MX_THREADS * ppt);
+  if (threadIdx.x == 0) {
+    s_lo = INT_MAX;
+    s_cnt = 0;
+  }
+  __syncthreads();
+  long long kmin = LLONG_MAX;
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += MX_THREADS)
+    kmin = min(kmin, __double_as_longlong(z2[i]));
+  for (int o = 16; o > 0; o >>= 1) kmin = min(kmin, __shfl_xor_sync(0xffffffffu, kmin, o));
+  if ((threadIdx.x & 31) == 0 && kmin != LLONG_MAX) {
+    double fz = floor(__longlong_as_double(kmin) * inv_dz2);
+    if (fabs(fz) < 1.0e9) {
+      if (periodic) fz = fmax(fz - npl * floor(fz / npl), 0.0);
+      atomicMin(&s_lo, (int)fz);
+    }
+  }
+  __syncthreads();
+  unsigned miss = 0;
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += MX_THREADS) {
+    double fz = floor(z2[i] * inv_dz2);
+    if (!(fabs(fz) < 1.0e9)) {
+      ++miss;
+      continue;
+    }
+    if (periodic) fz = fz - npl * floor(fz / npl);
+    const int t = (int)fz - s_lo;
+    if (!(t >= 0 && t + 1 < tp && !(periodic && (int)fz + 1 == npl))) ++miss;
+  }
+  for (int o = 16; o > 0; o >>= 1) miss += __shfl_xor_sync(0xffffffffu, miss, o);
+  if ((threadIdx.x & 31) == 0 && miss) atomicAdd(&s_cnt, miss);
+  __syncthreads();
+  if (threadIdx.x == 0 && s_cnt) atomicAdd(count, s_cnt);
+}
+}  // namespace
+
+// Fraction of the macroparticles (current state) whose deposits would miss
+// their stage block's shared tile; 0 when the stage kernel uses no tile.
+int pf_mixed_order_misses(pf_handle *h, double *frac) {
+  *frac = 0.0;
+  MixArgs a;
+  fill_mix_args(h, a, 0.0);
+  if (!a.tile || h->np == 0 || h->p.one_d) return PF_OK;
+  const int ppt = mixed_ppt(h);
+  const int64_t per_block = (int64_t)MX_THREADS * ppt;
+  const unsigned g = (unsigned)((h->np + per_block - 1) / per_block);
+  unsigned *cnt = h->d_status + 1;
+  PF_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned), h->stream));
+  k_order_misses<<<g, MX_THREADS, 0, h->stream>>>(h->y[h->cur][2], h->np, ppt, 1.0 / h->p.dz2,
+                                                  (int)h->npl, h->p.mesh_type == PF_MESH_PERIODIC,
+                                                  mixed_tile_planes(h), cnt);
+  PF_LAUNCHED(h);
+  PF_CUDA(cudaMemcpyAsync(h->h_status + 1, cnt, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                          h->stream));
+  PF_CUDA(cudaStreamSynchronize(h->stream));
+  *frac = (double)h->h_status[1] / (double)h->np;
+  return PF_OK;
+}
+
 int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_out) {
   const pf_params &p = h->p;
   const double hh = hstep * 0.5, szh = szl + hh;
@@ -935,8 +1013,7 @@ int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_ou
   const int nxt = h->cur ^ 1;
   // status_out == nullptr: enqueue only (a step of an asynchronous block;
   // the caller clears the status word once per block and reads it after)
-  // the status word and the tile-miss count (d_status[1])
-  if (status_out) PF_CUDA(cudaMemsetAsync(h->d_status, 0, 2 * sizeof(unsigned int), h->stream));
+  if (status_out) PF_CUDA(cudaMemsetAsync(h->d_status, 0, sizeof(unsigned int), h->stream));
 
   MixArgs a;
   fill_mix_args(h, a, hstep);
@@ -944,19 +1021,16 @@ int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_ou
     a.coef_tab = h->coef_dev;
     a.step_ctr = h->step_ctr;
   }
-  const size_t smem = a.tile ? pf_mixed_tile_smem(h) : 0;
+  const bool wide = a.tile && mixed_tile_planes(h) == MX_TILE_PLANES_WIDE;
+  const size_t smem = !a.tile ? 0
+                      : wide ? (size_t)4 * MX_TILE_PLANES_WIDE * h->nix * h->niy * sizeof(int)
+                             : pf_mixed_tile_smem(h);
   MixNodeArgs n;
   fill_mix_nodes(h, n, 1, hstep);
   if (h->capturing) n.step_ctr = h->step_ctr;
 
   PF_CUDA(mixed_attrs());
-  // six macroparticles per thread (3072 per block), eight for beams dense
-  // along z2 (a block then still spans a fraction of a plane; six and eight
-  // measured best for the config-2 and the config-1-mesh 2^24 beams), fewer
-  // when the beam is too small to give every SM two blocks
-  const int64_t per_plane = h->np / std::max<int64_t>(1, (int64_t)h->npl);
-  const int64_t want = (per_plane >= (int64_t)16 * MX_THREADS) ? MX_PPT : 6;
-  a.ppt = (int)std::max<int64_t>(1, std::min<int64_t>(want, h->np / ((int64_t)152 * 2 * MX_THREADS)));
+  a.ppt = mixed_ppt(h);
   const int64_t per_block = (int64_t)MX_THREADS * a.ppt;
   const unsigned pg = (unsigned)std::max<int64_t>(1, (h->np + per_block - 1) / per_block);
   const unsigned ng = (unsigned)std::max<int64_t>(1, (h->nwin + 255) / 256);
@@ -975,7 +1049,10 @@ int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_ou
       pf_prof_begin(h, PROF_STAGE);
 #define PF_MIX_CASE(S)                                                                 \
   case S:                                                                              \
-    if (oned) k_stage_mixed<S, true><<<pg, MX_THREADS, smem, h->stream>>>(a);          \
+    if (wide) {                                                                        \
+      if (oned) k_stage_mixed<S, true, MX_TILE_PLANES_WIDE><<<pg, MX_THREADS, smem, h->stream>>>(a); \
+      else k_stage_mixed<S, false, MX_TILE_PLANES_WIDE><<<pg, MX_THREADS, smem, h->stream>>>(a);     \
+    } else if (oned) k_stage_mixed<S, true><<<pg, MX_THREADS, smem, h->stream>>>(a);   \
     else k_stage_mixed<S, false><<<pg, MX_THREADS, smem, h->stream>>>(a);              \
     break;
       switch (s) {
@@ -1003,12 +1080,11 @@ int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_ou
     h->cur = nxt;  // committed optimistically; the block is replayed if it failed
     return PF_OK;
   }
-  PF_CUDA(cudaMemcpyAsync(h->h_status, h->d_status, 2 * sizeof(unsigned int),
-                          cudaMemcpyDeviceToHost, h->stream));
+  PF_CUDA(cudaMemcpyAsync(h->h_status, h->d_status, sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                          h->stream));
   PF_CUDA(cudaStreamSynchronize(h->stream));
   pf_prof_flush(h);
   *status_out = *h->h_status;
-  h->tile_misses += h->h_status[1];
   if (*status_out == 0u) h->cur = nxt;
   return PF_OK;
 }
