@@ -1,0 +1,100 @@
+// Paired-FP32 ("double-float") real numbers for the FP64 path's FFTs.
+//
+// GB300 issues FP64 at 1/64 of its FP32 rate, and the FP64 diffraction is
+// bound by that pipe (the 43-point butterflies of the 129-point transforms).
+// A value held as an unevaluated sum hi + lo of two floats (|lo| <= ulp(hi)/2)
+// carries 48 significand bits; sums and products are formed with FP32
+// operations only, using the error-free transformations TwoSum (Knuth) and
+// TwoProd through the fused multiply-add, the classical double-float
+// arithmetic (Dekker 1971; the "sloppy" addition of Hida, Li and Bailey's
+// double-double library, applied to floats).  Each operation is exact to
+// about 2^-46 relative, so a 129-point transform keeps about 1e-13 of the
+// field scale, where the reference's FFTW keeps about 1e-16: far inside the
+// 1e-10 at which the reference's own tests compare runs.  The results do not
+// depend on the order of anything (every butterfly's operations are fixed),
+// so runs stay bit-reproducible.
+//
+// Conversions to and from FP64 happen once per element and pass (loads of
+// the split FP64 field, stores of the result); the float halves are taken
+// with integer operations on the bit patterns and one FP64 subtraction.
+#pragma once
+
+#include <stdint.h>
+
+struct pf_dd {
+  float hi, lo;
+  pf_dd() = default;
+  __host__ __device__ constexpr pf_dd(float h, float l) : hi(h), lo(l) {}
+  __host__ __device__ constexpr pf_dd(int v) : hi((float)v), lo(0.f) {}
+  __host__ __device__ constexpr pf_dd(double v)
+      : hi((float)v), lo((float)(v - (double)(float)v)) {}
+};
+
+__device__ __forceinline__ pf_dd dd_fast_two_sum(float a, float b) {  // |a| >= |b|
+  const float s = a + b;
+  return pf_dd(s, b - (s - a));
+}
+
+__device__ __forceinline__ pf_dd operator+(pf_dd a, pf_dd b) {
+  const float s = a.hi + b.hi;
+  const float bb = s - a.hi;
+  float e = (a.hi - (s - bb)) + (b.hi - bb);  // TwoSum error of the high parts
+  e += a.lo + b.lo;
+  return dd_fast_two_sum(s, e);
+}
+__device__ __forceinline__ pf_dd operator-(pf_dd a) { return pf_dd(-a.hi, -a.lo); }
+__device__ __forceinline__ pf_dd operator-(pf_dd a, pf_dd b) { return a + (-b); }
+
+__device__ __forceinline__ pf_dd operator*(pf_dd a, pf_dd b) {
+  const float p = a.hi * b.hi;
+  float e = __fmaf_rn(a.hi, b.hi, -p);  // TwoProd error
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return dd_fast_two_sum(p, e);
+}
+
+// a * b + c with one normalisation
+__device__ __forceinline__ pf_dd fma(pf_dd a, pf_dd b, pf_dd c) {
+  const float p = a.hi * b.hi;
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  const float s = p + c.hi;
+  const float bb = s - p;
+  float t = (p - (s - bb)) + (c.hi - bb);
+  t += e + c.lo;
+  return dd_fast_two_sum(s, t);
+}
+
+__device__ __forceinline__ pf_dd operator/(pf_dd a, pf_dd b) {
+  const float q1 = __fdiv_rn(a.hi, b.hi);
+  const pf_dd r = a - b * pf_dd(q1, 0.f);
+  const float q2 = __fdiv_rn(r.hi, b.hi);
+  return dd_fast_two_sum(q1, q2);
+}
+
+// FP64 <-> pair, with integer operations for the float halves
+__device__ __forceinline__ float dd_d2f_rn(double d) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  const unsigned sign = hi & 0x80000000u;
+  const int e = (int)((hi >> 20) & 0x7ffu) - 896;
+  if (e <= 0) return __uint_as_float(sign);             // below FP32's normal range
+  if (e >= 255) return __uint_as_float(sign | 0x7f800000u);
+  const unsigned mag = ((unsigned)e << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+  return __uint_as_float(sign | (mag + ((lo >> 28) & 1u)));
+}
+__device__ __forceinline__ double dd_f2d(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned sign = u & 0x80000000u;
+  const unsigned e = (u >> 23) & 0xffu;
+  if (e == 0u) return __hiloint2double((int)sign, 0);
+  const unsigned ed = (e == 255u) ? 2047u : e + 896u;
+  const unsigned m = u & 0x7fffffu;
+  return __hiloint2double((int)(sign | (ed << 20) | (m >> 3)), (int)(m << 29));
+}
+__device__ __forceinline__ pf_dd dd_from_double(double v) {
+  const float h = dd_d2f_rn(v);
+  return pf_dd(h, dd_d2f_rn(v - dd_f2d(h)));
+}
+__device__ __forceinline__ double dd_to_double(pf_dd v) { return dd_f2d(v.hi) + dd_f2d(v.lo); }

@@ -31,37 +31,55 @@
 #include <string>
 #include <vector>
 
+#include "dd_real.cuh"
 #include "pf_internal.h"
 
 #define FFT_T double
+#define FFT_IO double
 #define FFT_NS fft64
 #define FFT_REAL_IS_FLOAT 0
 #include "fft_kernels.cuh"
 #undef FFT_T
+#undef FFT_IO
+#undef FFT_NS
+#undef FFT_REAL_IS_FLOAT
+// the FP64 field transformed in paired-FP32 arithmetic (dd_real.cuh)
+#define FFT_T pf_dd
+#define FFT_IO double
+#define FFT_NS fftdd
+#define FFT_REAL_IS_FLOAT 0
+#include "fft_kernels.cuh"
+#undef FFT_T
+#undef FFT_IO
 #undef FFT_NS
 #undef FFT_REAL_IS_FLOAT
 #define FFT_T float
+#define FFT_IO float
 #define FFT_NS fft32
 #define FFT_REAL_IS_FLOAT 1
 #include "fft_kernels.cuh"
 #undef FFT_T
+#undef FFT_IO
 #undef FFT_NS
 #undef FFT_REAL_IS_FLOAT
 
 struct DiffPlan {
   fft64::Plan *p64 = nullptr;
+  fftdd::Plan *pdd = nullptr;
   fft32::Plan *p32 = nullptr;
 };
 
 void pf_diff_destroy(DiffPlan *d) {
   if (!d) return;
   if (d->p64) fft64::destroy(d->p64);
+  if (d->pdd) fftdd::destroy(d->pdd);
   if (d->p32) fft32::destroy(d->p32);
   delete d;
 }
 
 int pf_diffract_outer(pf_handle *h, double dz) {
   if (!h->diff) h->diff = new DiffPlan();
+  if (h->fft_pairs) return fftdd::diffract(h, h->diff->pdd, h->or_, h->oi_, nullptr, dz);
   return fft64::diffract(h, h->diff->p64, h->or_, h->oi_, nullptr, dz);
 }
 

@@ -5,6 +5,16 @@
 namespace FFT_NS {
 
 typedef FFT_T real;
+typedef FFT_IO io_real;  // element type of the split re/im field in HBM
+constexpr bool REAL_IS_DD = std::is_same<real, pf_dd>::value;
+
+__device__ __forceinline__ double to_io(double v) { return v; }
+__device__ __forceinline__ float to_io(float v) { return v; }
+__device__ __forceinline__ double to_io(pf_dd v) { return dd_to_double(v); }
+__device__ __forceinline__ double conv_in(double v, double *) { return v; }
+__device__ __forceinline__ float conv_in(float v, float *) { return v; }
+__device__ __forceinline__ pf_dd conv_in(double v, pf_dd *) { return dd_from_double(v); }
+__device__ __forceinline__ real from_io(io_real v) { return conv_in(v, (real *)nullptr); }
 
 
 struct cplx {
@@ -68,8 +78,8 @@ enum { MID_NONE = 0, MID_PROP = 1, MID_DAMP = 2, MID_SPLIT = 3, MID_RECOMB = 4,
 struct FftArgs {
   cplx *A;
   cplx *anb;
-  const real *re_in, *im_in;    // split input (first pass)
-  real *re_out, *im_out;        // split output (last pass)
+  const io_real *re_in, *im_in;  // split input (first pass)
+  io_real *re_out, *im_out;      // split output (last pass)
   const cplx *tw_f, *tw_b;      // per-pass twiddles, forward and backward
   AxisPlan ax;
   AxisPlan ay;   // the y axis, for the transverse-plane kernel (ax is then x)
@@ -106,10 +116,24 @@ __device__ __forceinline__ void cp_async_wait_all() {
 // element pos of the pass input into shared slot dst
 __device__ __forceinline__ void load_async(cplx *dst, const FftArgs &a, int64_t pos) {
   if (a.load_split) {
-    cp_async<sizeof(real)>(&dst->r, a.re_in + pos);
-    cp_async<sizeof(real)>(&dst->i, a.im_in + pos);
+    static_assert(sizeof(io_real) == sizeof(real), "a split element fills its slot");
+    cp_async<sizeof(io_real)>(&dst->r, a.re_in + pos);
+    cp_async<sizeof(io_real)>(&dst->i, a.im_in + pos);
   } else {
     cp_async<sizeof(cplx)>(dst, a.A + pos);
+  }
+}
+
+// Paired-FP32 arithmetic: a slot filled from the split FP64 field holds the
+// FP64 bits; the thread that loaded it converts it in place after the wait.
+__device__ __forceinline__ void fix_loaded(cplx *slot, const FftArgs &a) {
+  if constexpr (REAL_IS_DD) {
+    if (a.load_split) {
+      const double r = *reinterpret_cast<const double *>(&slot->r);
+      const double i = *reinterpret_cast<const double *>(&slot->i);
+      slot->r = conv_in(r, (real *)nullptr);
+      slot->i = conv_in(i, (real *)nullptr);
+    }
   }
 }
 
@@ -566,13 +590,14 @@ __device__ __forceinline__ cplx mid_op(const FftArgs &a, int64_t pos, int x, int
 
 __device__ __forceinline__ void store(const FftArgs &a, int64_t pos, cplx v) {
   if (a.store_split) {
-    a.re_out[pos] = v.r;
-    a.im_out[pos] = v.i;
+    const io_real vr = to_io(v.r), vi = to_io(v.i);
+    a.re_out[pos] = vr;
+    a.im_out[pos] = vi;
     if (a.mirror) {
       const int64_t plane = (int64_t)a.T.nx * a.T.ny;
       if (pos < plane) {
-        a.re_out[pos + plane * a.T.nz] = v.r;
-        a.im_out[pos + plane * a.T.nz] = v.i;
+        a.re_out[pos + plane * a.T.nz] = vr;
+        a.im_out[pos + plane * a.T.nz] = vi;
       }
     }
   } else {
@@ -610,6 +635,12 @@ __global__ void __launch_bounds__(NTHREADS, (sizeof(real) == 8) ? 3 : 1) k_fft(c
     load_async(smem + l * n + j, a, pos);
   }
   cp_async_wait_all();
+  if constexpr (REAL_IS_DD) {
+    for (int t = tid; t < nl * n; t += NTHREADS) {
+      const int l = (p.stride == 1) ? t / n : t % nl, j = (p.stride == 1) ? t - (t / n) * n : t / nl;
+      fix_loaded(smem + l * n + j, a);
+    }
+  }
   __syncthreads();
   {
     cplx *res = run_transform(smem, other, scratch, a, nl, a.dir);
@@ -660,7 +691,7 @@ __global__ void k_elementwise(const FftArgs a) {
   if (t >= n) return;
   const int x = (int)(t % T.nx), y = (int)((t / T.nx) % T.ny);
   const int z = (int)(t / ((int64_t)T.nx * T.ny));
-  cplx v = a.load_split ? cplx{a.re_in[t], a.im_in[t]} : a.A[t];
+  cplx v = a.load_split ? cplx{from_io(a.re_in[t]), from_io(a.im_in[t])} : a.A[t];
   v = mid_op(a, t, x, y, z, v);
   store(a, t, v);
 }
@@ -868,6 +899,8 @@ __global__ void __launch_bounds__(PT, 1) k_fft_plane(const FftArgs a) {
   const int64_t off = (int64_t)z * plane;
   for (int t = threadIdx.x; t < plane; t += PT) load_async(buf + t, a, off + t);
   cp_async_wait_all();
+  if constexpr (REAL_IS_DD)
+    for (int t = threadIdx.x; t < plane; t += PT) fix_loaded(buf + t, a);
   __syncthreads();
   xy_transform<NX, NY>(buf, a, a.dir != 0);
   if (a.mid != MID_NONE) {
@@ -941,6 +974,9 @@ __global__ void __launch_bounds__(PT, (sizeof(real) == 4) ? 4 : 3) k_z4(const Ff
   if (on)
     for (int j = j0; j < M; j += JS) load_async(buf + j * G + l, a, pos_of(j));
   cp_async_wait_all();
+  if constexpr (REAL_IS_DD)
+    if (on)
+      for (int j = j0; j < M; j += JS) fix_loaded(buf + j * G + l, a);
   __syncthreads();
   // FP32 (LSU-bound): the twiddles and the propagator / damping are applied
   // as the last radix pass writes its outputs (Z4Twiddle, Z4Mid); FP64
@@ -1397,12 +1433,12 @@ static int plane_pass(pf_handle *h, Plan *d, FftArgs a) {
   return PF_OK;
 }
 
-static void base_args(pf_handle *h, Plan *d, real *re, real *im, cplx *oc, FftArgs &a);
+static void base_args(pf_handle *h, Plan *d, io_real *re, io_real *im, cplx *oc, FftArgs &a);
 static int run_schedule(pf_handle *h, Plan *d, const FftArgs &a, bool split, bool adjoint);
 
 // Diffract the outer mesh: split real/imaginary arrays (re, im) or, when
 // those are null, the interleaved complex mesh oc (nz2 planes either way).
-static int diffract(pf_handle *h, Plan *&plan, real *re, real *im, cplx *oc, double dz) {
+static int diffract(pf_handle *h, Plan *&plan, io_real *re, io_real *im, cplx *oc, double dz) {
   const pf_params &p = h->p;
   if (!plan) {
     int rc = build_plan(h, plan);
@@ -1421,7 +1457,7 @@ static int diffract(pf_handle *h, Plan *&plan, real *re, real *im, cplx *oc, dou
   return run_schedule(h, d, a, split, false);
 }
 
-static void base_args(pf_handle *h, Plan *d, real *re, real *im, cplx *oc, FftArgs &a) {
+static void base_args(pf_handle *h, Plan *d, io_real *re, io_real *im, cplx *oc, FftArgs &a) {
   const pf_params &p = h->p;
   memset(&a, 0, sizeof(a));
   a.A = d->A;
@@ -1521,7 +1557,7 @@ static int run_schedule(pf_handle *h, Plan *d, const FftArgs &a, bool split, boo
 // over -dz (the filter and D are real), so the adjoint is
 // Prop^H(Abs^H(v)) with Abs^H(v) = m (B D F v / N) + (1 - m) v.  The periodic
 // mirror plane is not written.
-static int diffract_adjoint(pf_handle *h, Plan *&plan, real *re, real *im, double dz) {
+static int diffract_adjoint(pf_handle *h, Plan *&plan, io_real *re, io_real *im, double dz) {
   const pf_params &p = h->p;
   if (!plan) {
     int rc = build_plan(h, plan);

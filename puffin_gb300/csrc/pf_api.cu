@@ -1434,6 +1434,16 @@ int pf_set_taper_profile(pf_handle *h, int32_t n, const double *z, const double 
   return PF_OK;
 }
 
+int pf_set_fft_arithmetic(pf_handle *h, int32_t mode) {
+  if (!h || (mode != PF_FFT_FP64 && mode != PF_FFT_PAIRED_FP32)) return PF_BAD_ARG;
+  if (h->p.precision == PF_MIXED) {
+    h->err = "pf_set_fft_arithmetic: the mixed-precision path transforms in FP32";
+    return PF_BAD_ARG;
+  }
+  h->fft_pairs = (mode == PF_FFT_PAIRED_FP32);
+  return PF_OK;
+}
+
 int pf_set_launch_mode(pf_handle *h, int32_t mode) {
   if (!h || mode < 0 || mode > 2) return PF_BAD_ARG;
   h->launch_mode = mode;

@@ -253,6 +253,8 @@ struct pf_handle {
   unsigned int *h_status = nullptr;  // pinned
 
   DiffPlan *diff = nullptr;
+  // FP64 path: diffraction FFTs in paired-FP32 arithmetic (pf_set_fft_arithmetic)
+  bool fft_pairs = false;
 
   // optional per-kernel-class timing
   bool prof = false;

@@ -23,6 +23,7 @@ STATUS_NAMES = {
 UND_PUFFIN, UND_HELICAL, UND_PLANEPOLE, UND_CURVED = 0, 1, 2, 3
 MESH_TEMPORAL, MESH_PERIODIC = 0, 1
 FP64, MIXED = 0, 1
+FFT_FP64, FFT_PAIRED_FP32 = 0, 1
 
 _DOUBLES = ("rho", "eta", "kappa", "aw", "gamma_r", "fx", "fy", "kx_und", "ky_und",
             "kbxsf", "kbysf", "szfs", "szfe", "n2col0", "undgrad", "dx", "dy", "dz2",
@@ -56,7 +57,7 @@ SYMBOLS = (
     "pf_batch_tune", "pf_batch_get_shape", "pf_batch_set_shape", "pf_batch_use_graphs",
     "pf_batch_launches", "pf_batch_stream", "pf_batch_last_error", "pf_set_window_field",
     "pf_get_window_field", "pf_set_window_field_dev", "pf_get_window_field_dev",
-    "pf_window_nodes",
+    "pf_window_nodes", "pf_set_fft_arithmetic",
 )
 NOALLOC_MAX_PARTICLES = 32768
 NOALLOC_MAX_NODES = 32768
@@ -125,6 +126,7 @@ def load(build_if_missing: bool = False):
         "pf_step_count": (i64, [H]),
         "pf_set_taper_profile": (ctypes.c_int, [H, i32, ctypes.c_void_p, ctypes.c_void_p]),
         "pf_set_launch_mode": (ctypes.c_int, [H, i32]),
+        "pf_set_fft_arithmetic": (ctypes.c_int, [H, i32]),
         "pf_generate_beam": (ctypes.c_int, [H, i64, ctypes.c_void_p, ctypes.c_void_p, f64, i32,
                                             ctypes.c_void_p, ctypes.c_void_p, i32,
                                             ctypes.c_uint64, f64]),

@@ -227,6 +227,11 @@ class Puffin:
             raise ValueError("z and alpha need the same length")
         self._check(self._lib.pf_set_taper_profile(self._h, len(z), z.ctypes.data, a.ctypes.data))
 
+    def set_fft_arithmetic(self, mode: int):
+        """FP64 path: diffraction FFTs in FP64 (lib.FFT_FP64) or in paired
+        FP32 arithmetic (lib.FFT_PAIRED_FP32; see pf_set_fft_arithmetic)."""
+        self._check(self._lib.pf_set_fft_arithmetic(self._h, int(mode)))
+
     def set_launch_mode(self, mode: int):
         """0 step by step, 1 asynchronous step blocks, 2 blocks as CUDA graphs."""
         self._check(self._lib.pf_set_launch_mode(self._h, int(mode)))

@@ -571,3 +571,37 @@ def test_z2_ordering_is_the_same_every_run():
             outs.append(sim.get_particles())
     for k in P.PARTICLE_KEYS:
         np.testing.assert_array_equal(outs[0][k], outs[1][k], err_msg=k)
+
+
+@pytest.mark.parametrize("mesh", ["periodic", (17, 21, 4096), (129, 129, 8), (129, 17, 1536),
+                                  (17, 33, 600), (33, 33, 64), (65, 65, 32), (17, 17, 2048)])
+def test_paired_fp32_diffraction_matches_oracle(mesh):
+    """The FP64 path's diffraction with its FFTs in paired-FP32 arithmetic
+    (pf_set_fft_arithmetic): every kernel form against the oracle's FP64
+    diffraction step to 2e-12 of the field scale, and two calls in a row
+    give the same bits."""
+    rho = 0.005
+    lamr = 4.0 * configs.PUFFIN_PI * rho
+    if mesh == "periodic":
+        p = P.default_params(rho=rho, eta=1e-5, kappa=0.2, nx=21, ny=21, nz2=65, dx=0.2, dy=0.2,
+                             dz2=lamr / 16, mesh_type=P.MESH_PERIODIC, sperwaves=4.0)
+    else:
+        nx, ny, nz2 = mesh
+        p = P.default_params(rho=rho, eta=1e-5, kappa=0.2, nx=nx, ny=ny, nz2=nz2, dx=0.3,
+                             dy=0.25, dz2=lamr / 16, mesh_type=P.MESH_TEMPORAL)
+    field = random_field(p, 13, amp=1.0)
+    if mesh == "periodic":
+        n = p.nx * p.ny
+        field[0][-n:] = field[0][:n]
+        field[1][-n:] = field[1][:n]
+    outs = []
+    for _ in range(2):
+        with P.Puffin(p) as sim:
+            sim.set_fft_arithmetic(P.lib.FFT_PAIRED_FP32)
+            sim.set_field(*field)
+            sim.diffractIM(0.31)
+            outs.append(sim.get_field())
+    re, im = (a.copy() for a in field)
+    O.diffract(oracle_config(p), re, im, 0.31)
+    field_close(outs[0], (re, im), 2e-12)
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
