@@ -267,7 +267,8 @@ def workload_config(w, win, world):
 
 
 # ---------------------------------------------------------------------------
-def _time_path(args, dev, precision, world, workload="config2", steps=None, warmup=None):
+def _time_path(args, dev, precision, world, workload="config2", steps=None, warmup=None,
+               fft_arithmetic=None):
     """Run a workload on one precision path: W warm-up steps, then K timed
     steps (CUDA events on the library's stream).  Returns timings, the
     per-kernel-class device times, the final radiated power sum |A|^2 and the
@@ -288,6 +289,8 @@ def _time_path(args, dev, precision, world, workload="config2", steps=None, warm
     p.device = dev
     p.precision = precision
     sim = P.Puffin(p)
+    if fft_arithmetic is not None:
+        sim.set_fft_arithmetic(fft_arithmetic)
     sim.set_particles(*(w.beam[k] for k in P.PARTICLE_KEYS))
     sim.set_field(*w.field)
     win = sim.window
@@ -699,6 +702,12 @@ def run_gpu(args, rank, world):
     e2e_diff_calls = n_diff
     sim.close()
 
+    # the same FP64 leg with the diffraction FFTs in FP64 arithmetic (the
+    # default transforms in paired FP32, pf_set_fft_arithmetic)
+    r64f = _time_path(args, dev, P.FP64, world, fft_arithmetic=L.FFT_FP64)
+    r64f["sim"].close()
+    (r64f_ms,) = max_over_ranks([r64f["ms"]], world, f"cuda:{dev}")
+
     rmx = None
     c3 = None
     if not args.no_mixed:
@@ -754,7 +763,13 @@ def run_gpu(args, rank, world):
                 "per_step": "the six evolving particle arrays and the inner-window "
                             "field, in and out (chi handed in once before the steps); "
                             "the outer field in and out around each diffraction call"},
-        "gpu_launches": r64["launches"] + (rmx["launches"] if rmx else 0)
+        "fft_arithmetic": {
+            "value_leg": "paired FP32 (48-bit significands; the field stays FP64 in HBM)",
+            "fp64_arithmetic": {"value": whole_job_rate(n, args.steps, world, r64f_ms),
+                                "ms_per_step": r64f_ms / args.steps,
+                                "fft_ms": r64f["kernel"]["fft"][0]},
+            "paired_fp32_fft_ms": r64["kernel"]["fft"][0]},
+        "gpu_launches": r64["launches"] + r64f["launches"] + (rmx["launches"] if rmx else 0)
         + (c3["fp64"]["launches"] + c3["mixed"]["launches"] if c3 else 0),
         "kernel_ms": kern,
         "roofline": {"kernel": "k_stage (fused FP64 RK4 stage)", "bound": "hbm",

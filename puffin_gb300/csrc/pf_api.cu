@@ -469,6 +469,7 @@ int pf_create(const pf_params *p, pf_handle **out) {
   h->n2col0 = p->n2col0;
   h->undgrad = p->undgrad;
   h->npl = (p->mesh_type == PF_MESH_PERIODIC) ? p->nz2 - 1 : p->nz2;
+  h->fft_pairs = (p->precision == PF_FP64);  // pf_set_fft_arithmetic: paired FP32 by default
   h->nouter = (int64_t)p->nx * p->ny * p->nz2;
   auto fail = [&](cudaError_t e, const char *what) {
     (void)cudaGetLastError();  // an allocation failure leaves the context usable
