@@ -609,9 +609,10 @@ __device__ __forceinline__ void store(const FftArgs &a, int64_t pos, cplx v) {
   }
 }
 
-// resident blocks per SM of the line kernel: FP64 3 (80 registers), FP32 1;
-// paired FP32 needs more registers per value in flight: 2
-constexpr int KFFT_MINB = REAL_IS_DD ? 2 : (sizeof(real) == 8) ? 3 : 1;
+// resident blocks per SM of the line kernel: 3 for the 8-byte reals (FP64
+// and paired FP32, 80 registers; the paired form spills a few words, and
+// measured 8 % slower at two blocks and 128 registers), 1 for FP32
+constexpr int KFFT_MINB = (sizeof(real) == 8) ? 3 : 1;
 __global__ void __launch_bounds__(NTHREADS, KFFT_MINB) k_fft(const FftArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx *smem_all = reinterpret_cast<cplx *>(smem_raw);
