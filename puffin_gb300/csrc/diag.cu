@@ -98,28 +98,49 @@ __global__ void k_bunching(const double *z2, const double *chi, int64_t np, int 
   }
   __syncthreads();
   const int base = s_base;
+  // The z2-ordered macroparticles of a warp fall in one or two slices: their
+  // contributions are summed across the warp first, one pass per distinct
+  // slice (a butterfly over all 32 lanes of the members' values), and one
+  // lane per slice adds the sums to the block's bins -- shared FP64 atomics
+  // to one address from every lane would serialise.  Every lane of the warp
+  // takes part (a macroparticle without a slice contributes nothing).
+  auto add = [&](int slot, double vr, double vi, double vd) {
+    const int lane = threadIdx.x & 31;
+    unsigned todo = __ballot_sync(0xffffffffu, slot >= 0);
+    while (todo) {
+      const int leader = __ffs(todo) - 1;
+      const int ls = __shfl_sync(0xffffffffu, slot, leader);
+      const bool member = (slot == ls);
+      double sr = member ? vr : 0.0, si = member ? vi : 0.0, sdv = member ? vd : 0.0;
+      for (int o = 16; o > 0; o >>= 1) {
+        sr += __shfl_xor_sync(0xffffffffu, sr, o);
+        si += __shfl_xor_sync(0xffffffffu, si, o);
+        sdv += __shfl_xor_sync(0xffffffffu, sdv, o);
+      }
+      todo &= ~__ballot_sync(0xffffffffu, member);
+      if (lane != leader) continue;
+      const int b = ls - base;
+      if (b >= 0 && b < BUNCH_BINS) {
+        atomicAdd(s_r + b, sr);
+        atomicAdd(s_i + b, si);
+        if (sdv != 0.0) atomicAdd(s_d + b, sdv);
+      } else {
+        atomicAdd(br + ls, sr);
+        atomicAdd(bi + ls, si);
+        if (sdv != 0.0) atomicAdd(sd + ls, sdv);
+      }
+    }
+  };
+  double sn = 0.0, cs = 0.0, w0 = 0.0;
   if (ok) {
     const double ph = (double)harmonic * z / (2.0 * rho);
-    double sn, cs;
     sincos(ph, &sn, &cs);
-    const double w0 = (is * S - z) / S;
-    auto add = [&](int slot, double vr, double vi, double vd) {
-      const int b = slot - base;
-      if (b >= 0 && b < BUNCH_BINS) {
-        atomicAdd(s_r + b, vr);
-        atomicAdd(s_i + b, vi);
-        if (vd != 0.0) atomicAdd(s_d + b, vd);
-      } else {
-        atomicAdd(br + slot, vr);
-        atomicAdd(bi + slot, vi);
-        if (vd != 0.0) atomicAdd(sd + slot, vd);
-      }
-    };
-    add(is - 1, c * cs * w0, c * sn * w0, c);
-    if (!periodic) {
-      const double w1 = -((is - 1) * S - z) / S;
-      add(is, c * cs * w1, c * sn * w1, 0.0);  // slice is+1 (the arrays hold nslices+1)
-    }
+    w0 = (is * S - z) / S;
+  }
+  add(ok ? is - 1 : -1, c * cs * w0, c * sn * w0, c);
+  if (!periodic) {
+    const double w1 = ok ? -((is - 1) * S - z) / S : 0.0;
+    add(ok ? is : -1, c * cs * w1, c * sn * w1, 0.0);  // slice is+1 (the arrays hold nslices+1)
   }
   __syncthreads();
   if (base == INT_MAX) return;
