@@ -488,6 +488,58 @@ def adjoint_leg(args, dev):
                           "to the amplitude); components below 1e-3 of the largest are listed "
                           "but not counted; fd_spread_vs_smaller_step is the largest relative "
                           "change of the differences themselves between the two step sizes")
+
+    # the same run on a mixed-precision handle: the recorded forward runs the
+    # mixed stage kernels and the FP32 diffraction, the adjoint keeps their
+    # precision split; its gradient is checked against the FP64 forward's
+    # differences above (a step of 1e-6 of a taper value is below the FP32
+    # resolution of the mixed coefficients)
+    pm = P.Params.from_buffer_copy(p)
+    pm.precision = P.MIXED
+    with P.Puffin(pm) as sim:
+        sim.set_particles(*(w.beam[k] for k in P.PARTICLE_KEYS))
+        stream = torch.cuda.ExternalStream(sim.stream_handle, device=dev)
+
+        def energy_m(nsteps, alpha, a, c):
+            sim.set_taper_profile(np.linspace(0.0, nsteps * w.h, 16), alpha)
+            return sim.adjoint_forward(nsteps, w.isteps4diff, True, w.h, 64, seed[0], seed[1],
+                                       a, c)
+
+        energy_m(w.nsteps, alpha0, amp, chirp)      # warm-up
+        sim.adjoint_backward(16)
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        torch.cuda.synchronize()
+        e[0].record(stream)
+        em = energy_m(w.nsteps, alpha0, amp, chirp)
+        e[1].record(stream)
+        sim.adjoint_backward(16)
+        e[2].record(stream)
+        torch.cuda.synchronize()
+        mfwd, mbwd = e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])
+        mixed = {
+            "forward_ms": mfwd, "backward_ms": mbwd, "backward_over_forward": mbwd / mfwd,
+            "forward_speedup_vs_fp64": fwd / mfwd, "backward_speedup_vs_fp64": bwd / mbwd,
+            "energy": em, "energy_rel_vs_fp64": abs(em - e0) / abs(e0),
+        }
+        vs = []
+        for chk in checks:
+            energy_m(chk["steps"], alpha0, amp, chirp)
+            g_t, g_s, g_c = sim.adjoint_backward(16)
+            adj = np.array(list(g_t) + [g_s, g_c])
+            num = np.array(chk["differences"])
+            a64 = np.array(chk["adjoint"])
+            big = np.abs(num) >= 1e-3 * np.max(np.abs(num))
+            rel = np.abs(adj - num) / np.maximum(np.abs(num), 1e-300)
+            rel64 = np.abs(adj - a64) / np.maximum(np.abs(a64), 1e-300)
+            vs.append({
+                "steps": chk["steps"], "fd_step": chk["fd_step"],
+                "max_rel_error_vs_fp64_differences": float(np.max(rel[big])),
+                "within_1e-4": bool(np.max(rel[big]) <= 1e-4),
+                "max_rel_diff_vs_fp64_adjoint": float(np.max(rel64[big])),
+                "adjoint": [float(v) for v in adj],
+            })
+        mixed["finite_difference_checks"] = vs
+    out["mixed"] = mixed
     return out
 
 

@@ -267,15 +267,19 @@ int pf_init_undulator(pf_handle *h, int32_t und_type, double fx, double fy, doub
                       double kbysf, double mf, double taper, int32_t nsteps, double hstep,
                       int32_t und_ends);
 
-/* Adjoint of the RK4 / diffraction run (FP64 path), with checkpoint and
- * recompute.  pf_adjoint_forward runs nsteps steps the way pf_run does
- * (UndSection's loop, undulator.f90:182-333; no window retries: the window
- * must hold the beam for the whole run) from the handle's particles with the
- * energy chirp gamma += chirp (z2 - <z2>) applied and the initial field
- * seed_amp * (seed_re, seed_im) (outer mesh), under the taper profile set by
- * pf_set_taper_profile, keeping the state every checkpoint_every steps; it
- * returns the final pulse energy E = dx dy dz2 sum |A|^2 over the outer mesh
- * (unique z2 planes).  pf_adjoint_backward then returns denergy * dE/d(the
+/* Adjoint of the RK4 / diffraction run, with checkpoint and recompute, on
+ * an FP64 or a mixed-precision handle.  On a mixed handle the run records
+ * the mixed stage kernels and the FP32 diffraction, and the adjoint keeps
+ * their split: the field adjoint in FP32 complex; the particle adjoint, the
+ * RK4 combination and the z2 (phase) adjoint in FP64; the rest of each
+ * stage's vector-Jacobian product in FP32.  pf_adjoint_forward runs nsteps steps
+ * the way pf_run does (UndSection's loop, undulator.f90:182-333; no window
+ * retries: the window must hold the beam for the whole run) from the
+ * handle's particles with the energy chirp gamma += chirp (z2 - <z2>)
+ * applied and the initial field seed_amp * (seed_re, seed_im) (outer mesh),
+ * under the taper profile set by pf_set_taper_profile, keeping the state
+ * every checkpoint_every steps; it returns the final pulse energy
+ * E = dx dy dz2 sum |A|^2 over the outer mesh (unique z2 planes).  pf_adjoint_backward then returns denergy * dE/d(the
  * ntaper profile values), dE/d(seed_amp) and dE/d(chirp), recomputing each
  * segment of checkpoint_every steps once.  Both leave the handle's
  * particles at the unchirped beam; the field must be set again before other

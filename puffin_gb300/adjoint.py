@@ -2,7 +2,7 @@
 ``torch.autograd.Function``.
 
 ``pulse_energy(sim, alpha, seed_amp, chirp, ...)`` runs the RK4/diffraction
-run on the handle ``sim`` (FP64) with the taper profile ``alpha`` at the
+run on the handle ``sim`` (FP64 or mixed precision) with the taper profile ``alpha`` at the
 control points ``taper_z``, the initial field ``seed_amp * seed`` and the
 energy chirp ``chirp``, and returns the pulse energy as a 0-d float64 tensor.
 Its backward pass is the hand-written adjoint of the interpolate-push-deposit-

@@ -21,6 +21,8 @@
 
 #include <stdint.h>
 
+#include "fp_convert.cuh"
+
 struct pf_dd {
   float hi, lo;
   pf_dd() = default;
@@ -74,27 +76,8 @@ __device__ __forceinline__ pf_dd operator/(pf_dd a, pf_dd b) {
 }
 
 // FP64 <-> pair, with integer operations for the float halves
-__device__ __forceinline__ float dd_d2f_rn(double d) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
-  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
-  const unsigned sign = hi & 0x80000000u;
-  const int e = (int)((hi >> 20) & 0x7ffu) - 896;
-  if (e <= 0) return __uint_as_float(sign);             // below FP32's normal range
-  if (e >= 255) return __uint_as_float(sign | 0x7f800000u);
-  const unsigned mag = ((unsigned)e << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
-  return __uint_as_float(sign | (mag + ((lo >> 28) & 1u)));
-}
-__device__ __forceinline__ double dd_f2d(float f) {
-  const unsigned u = __float_as_uint(f);
-  const unsigned sign = u & 0x80000000u;
-  const unsigned e = (u >> 23) & 0xffu;
-  if (e == 0u) return __hiloint2double((int)sign, 0);
-  const unsigned ed = (e == 255u) ? 2047u : e + 896u;
-  const unsigned m = u & 0x7fffffu;
-  return __hiloint2double((int)(sign | (ed << 20) | (m >> 3)), (int)(m << 29));
-}
 __device__ __forceinline__ pf_dd dd_from_double(double v) {
-  const float h = dd_d2f_rn(v);
-  return pf_dd(h, dd_d2f_rn(v - dd_f2d(h)));
+  const float h = d2f_rn(v);
+  return pf_dd(h, d2f_rn(v - f2d(h)));
 }
-__device__ __forceinline__ double dd_to_double(pf_dd v) { return dd_f2d(v.hi) + dd_f2d(v.lo); }
+__device__ __forceinline__ double dd_to_double(pf_dd v) { return f2d(v.hi) + f2d(v.lo); }

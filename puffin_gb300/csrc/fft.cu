@@ -90,5 +90,10 @@ int pf_diffract_outer_c32(pf_handle *h, void *outer, double dz) {
 
 int pf_diffract_adjoint_split(pf_handle *h, double *re, double *im, double dz) {
   if (!h->diff) h->diff = new DiffPlan();
-  return fft64::diffract_adjoint(h, h->diff->p64, re, im, dz);
+  return fft64::diffract_adjoint(h, h->diff->p64, re, im, nullptr, dz);
+}
+
+int pf_diffract_adjoint_c32(pf_handle *h, void *outer, double dz) {
+  if (!h->diff) h->diff = new DiffPlan();
+  return fft32::diffract_adjoint(h, h->diff->p32, nullptr, nullptr, (fft32::cplx *)outer, dz);
 }

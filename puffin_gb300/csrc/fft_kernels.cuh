@@ -1554,14 +1554,16 @@ static int run_schedule(pf_handle *h, Plan *d, const FftArgs &a, bool split, boo
 }
 
 // Adjoint (with respect to the real inner product sum re*re' + im*im') of
-// one diffraction step over dz on split re/im arrays of the outer mesh.  The
+// one diffraction step over dz on split re/im arrays of the outer mesh or,
+// when those are null, on the interleaved complex mesh oc in place.  The
 // step is A -> Abs(Prop(A)) with Prop = B P F / N (P the propagator and
 // high-pass filter) and Abs(A) = B D F (m A) / N + (1 - m) A (D the damping,
 // m the mask); FFTW's B is the adjoint of F, P's adjoint is the propagator
 // over -dz (the filter and D are real), so the adjoint is
 // Prop^H(Abs^H(v)) with Abs^H(v) = m (B D F v / N) + (1 - m) v.  The periodic
 // mirror plane is not written.
-static int diffract_adjoint(pf_handle *h, Plan *&plan, io_real *re, io_real *im, double dz) {
+static int diffract_adjoint(pf_handle *h, Plan *&plan, io_real *re, io_real *im, cplx *oc,
+                            double dz) {
   const pf_params &p = h->p;
   if (!plan) {
     int rc = build_plan(h, plan);
@@ -1569,7 +1571,8 @@ static int diffract_adjoint(pf_handle *h, Plan *&plan, io_real *re, io_real *im,
   }
   Plan *d = plan;
   FftArgs a;
-  base_args(h, d, re, im, nullptr, a);
+  const bool split = (re != nullptr);
+  base_args(h, d, re, im, oc, a);
   a.mirror = 0;
   const int64_t ntab = (int64_t)(d->nx + d->ny) * d->nz;
   k_tables<<<(unsigned)((ntab + 255) / 256), 256, 0, h->stream>>>(
@@ -1578,14 +1581,14 @@ static int diffract_adjoint(pf_handle *h, Plan *&plan, io_real *re, io_real *im,
   // A = v, A_nb = (1 - m) v
   {
     FftArgs b = a;
-    b.load_split = 1;
+    b.load_split = split ? 1 : 0;
     b.store_split = 0;
     b.mid = MID_ADJ_SPLIT;
     const unsigned g = (unsigned)((d->n + 255) / 256);
     k_elementwise<<<g, 256, 0, h->stream>>>(b);
     PF_LAUNCHED(h);
   }
-  return run_schedule(h, d, a, true, true);
+  return run_schedule(h, d, a, split, true);
 }
 
 }  // namespace FFT_NS

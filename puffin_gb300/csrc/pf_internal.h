@@ -314,6 +314,27 @@ int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_ou
 // fraction of the macroparticles whose deposit would miss their mixed stage
 // block's shared tile (the z2 order a bunched beam loses within steps)
 int pf_mixed_order_misses(pf_handle *h, double *frac);
+// One stage of the mixed step on explicit arrays (the adjoint's recorded
+// forward), with pf_rk4_mixed's stage roles: stage 1 writes kout (k1),
+// stage 2 kacc (k2), stage 3 kout (k3) and kacc = kin + k3, stage 4 ynext =
+// y + h/6 (k1 + k4 + 2 kacc).  Slope arrays hold FP32 values, except index 2
+// (z2), which is FP64; the stage field is one float2 per window node, and
+// the deposit goes to the handle's accumulator.
+struct PfMixRec {
+  const double *y[6];
+  const void *as;
+  void *kin[6], *kout[6], *kacc[6], *k1[6];
+  double *ynext[6];
+};
+int pf_mixed_stage_rec(pf_handle *h, int stage, double hstep, double sz, const PfMixRec &r);
+// the mixed stage kernel's constants for the handle (its adjoint uses them)
+struct PfMixConst {
+  double aw2g, g02, inv_eta, inv_dz2;
+  double ser[7];
+  float ser_r1, ser_r2, inv_dx_f, inv_dy_f, hx_dx, hy_dy, eta_f, inv_dV3, sInv2rho, dxc, eta_k2,
+      rho2;
+};
+void pf_mixed_constants(pf_handle *h, PfMixConst *c);
 // stage-coefficient table entries of one step (4 entries), FP64 and FP32 forms
 void pf_step_coefficients(pf_handle *h, double szl, double hstep, StageCoef *out);
 void pf_step_coefficients_f(pf_handle *h, double szl, double hstep, void *out);
@@ -347,6 +368,9 @@ int pf_sched_eager_step(pf_handle *h, RunSched &s, int istep);
 int pf_diffract_adjoint_split(pf_handle *h, double *re, double *im, double dz);
 // diffraction of an interleaved complex-float outer mesh (mixed precision)
 int pf_diffract_outer_c32(pf_handle *h, void *outer, double dz);
+// adjoint of one FP32 diffraction step on an interleaved complex-float outer
+// mesh (the unique planes; the periodic mirror plane is not written)
+int pf_diffract_adjoint_c32(pf_handle *h, void *outer, double dz);
 void pf_diff_destroy(DiffPlan *d);
 
 void pf_stage_coefficients(const pf_params &p, double sz, double n2col, int place,

@@ -50,6 +50,7 @@
 #include <climits>
 #include <mutex>
 
+#include "mixed_common.cuh"
 #include "pf_internal.h"
 
 namespace {
@@ -64,11 +65,6 @@ static_assert(MX_THREADS * MX_PPT <= 4096, "tile low words could carry");
 constexpr int MX_TILE_PLANES = 3;
 constexpr int MX_TILE_PLANES_WIDE = 8;
 constexpr size_t MX_TILE_BYTES = 72 * 1024;
-
-struct BFieldF {
-  int type, place, one_d, focusing, tcase;
-  float bx0, by0, focx, focy, S, C, c1, ux, uy, u3, fx, fy, kx, ky, kxky, czs, cze, szt;
-};
 
 struct MixArgs {
   const void *coef_tab;  // non-null: StageCoefF at [*step_ctr * 4 + stage - 1]
@@ -124,49 +120,6 @@ struct StageCoefF {
   float n2col, kn2col;
 };
 
-__device__ __forceinline__ void bfield_f(const BFieldF &b, float x, float y, float &bx, float &by,
-                                         float &bz) {
-  const float pi = (float)PF_PUFFIN_PI;
-  bx = b.bx0;
-  by = b.by0;
-  bz = 0.f;
-  if (b.type == PF_UND_CURVED) {
-    const float shx = sinhf(b.kx * x), shy = sinhf(b.ky * y);
-    const float chx = coshf(b.kx * x), chy = coshf(b.ky * y);
-    if (b.place == 0) {
-      bx = b.kxky * shx * shy * b.szt / 4.f / pi * b.S;
-      by = chx * chy * b.szt / 4.f / pi * b.S;
-      bz = b.czs * chx * shy * b.u3 * b.C;
-    } else if (b.place == 2) {
-      bx = b.kxky * shx * shy * b.u3 * b.S;
-      by = chx * chy * b.u3 * b.S;
-      bz = b.cze * chx * shy * b.u3 * b.C;
-    } else {
-      bx = b.kxky * shx * shy * b.S;
-      by = chx * chy * b.S;
-      bz = b.cze * chx * shy * b.C;
-    }
-    if (b.one_d) bz = 0.f;
-  } else if (b.type == PF_UND_PLANEPOLE) {
-    if (!b.one_d) {
-      const float sh = sinhf(b.c1 * y);
-      bz = (b.place == 1) ? sh * b.C : sh * b.u3 * b.C;
-    }
-  } else if (!b.one_d) {
-    const bool hel = (b.type == PF_UND_HELICAL);
-    if (b.place == 1) {
-      bz = hel ? b.c1 * (-(x * b.S) + y * b.C) : b.c1 * (-(b.fx * x * b.S) + b.fy * y * b.C);
-    } else {
-      const float t = (b.tcase == 0) ? 0.f : -(b.ux * x * b.S);
-      bz = t + b.uy * y * b.C;
-    }
-  }
-  if (b.focusing) {
-    bx = b.focx * y + bx;
-    by = -(b.focy * x) + by;
-  }
-}
-
 // v * 2^E truncated toward zero (scale = 2^E, so the product is exact);
 // the caller guarantees |v * 2^E| < 2^31
 __device__ __forceinline__ int f2fix(float v, float scale) { return __float2int_rz(v * scale); }
@@ -179,95 +132,8 @@ __device__ __forceinline__ void tile_add(int *hi, unsigned *lo, int r) {
   atomicAdd(lo, (unsigned)r & 0xFFFFFu);
 }
 
-__device__ __forceinline__ void global_add(float2 *a, float2 v) {
-  atomicAdd(&a->x, v.x);
-  atomicAdd(&a->y, v.y);
-}
-
-// FP32 -> FP64, exact, with integer operations.  Zero and FP32 subnormals
-// give a signed zero (slopes that small are below every tolerance here);
-// infinities and NaNs map to infinities and NaNs.
-__device__ __forceinline__ double f2d(float f) {
-  const unsigned u = __float_as_uint(f);
-  const unsigned sign = u & 0x80000000u;
-  const unsigned e = (u >> 23) & 0xffu;
-  if (e == 0u) return __hiloint2double((int)sign, 0);
-  const unsigned ed = (e == 255u) ? 2047u : e + 896u;  // rebias 127 -> 1023
-  const unsigned m = u & 0x7fffffu;
-  return __hiloint2double((int)(sign | (ed << 20) | (m >> 3)), (int)(m << 29));
-}
-
-// FP64 -> FP32 rounded to nearest (ties away from zero) with integer
-// operations; magnitudes below FP32's normal range give a signed zero and
-// above it an infinity.
-__device__ __forceinline__ float d2f_rn(double d) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
-  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
-  const unsigned sign = hi & 0x80000000u;
-  const int e = (int)((hi >> 20) & 0x7ffu) - 896;
-  if (e <= 0) return __uint_as_float(sign);
-  if (e >= 255) return __uint_as_float(sign | 0x7f800000u);
-  const unsigned mag = ((unsigned)e << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
-  return __uint_as_float(sign | (mag + ((lo >> 28) & 1u)));  // a carry rounds into the exponent
-}
-
-// p2 = (1/sqrt(1 - u) - 1) / eta from the binomial series with the 1/eta
-// folded into the coefficients c[k] = C(2k+2, k+1) / 4^(k+1) / eta:
-// three terms for u < 2e-6, five for u < 1e-4, seven for u < 1e-3 (the
-// truncation stays below 1e-17 of the result), the closed form above
-__device__ __forceinline__ double p2_series(double u, const double *c, double inv_eta, float r1,
-                                            float r2) {
-  if (u < 2.0e-6) {
-    // u c0 (1 + (c1/c0) u + (c2/c0) u^2) with the correction (below 2e-6) in
-    // FP32: its rounding is below 1e-13 of p2; two FP64 operations
-    const float uf = d2f_rn(u);
-    const float corr = uf * fmaf(r2, uf, r1);
-    const double uc = u * c[0];
-    return fma(uc, f2d(corr), uc);
-  }
-  if (u < 1.0e-4) {
-    double s = c[4];
-    s = fma(s, u, c[3]);
-    s = fma(s, u, c[2]);
-    s = fma(s, u, c[1]);
-    s = fma(s, u, c[0]);
-    return u * s;
-  }
-  if (u < 1.0e-3) {
-    double s = c[6];
-#pragma unroll
-    for (int k = 5; k >= 0; --k) s = fma(s, u, c[k]);
-    return u * s;
-  }
-  return (1.0 / sqrt(1.0 - u) - 1.0) * inv_eta;
-}
-
-// Cell index and FP32 fraction of t >= 0 taken from the bits of t (integer
-// operations only); false for t < 0 or t >= 2^30, which the caller handles
-// in FP64.
-__device__ __forceinline__ bool cell_split(double t, int &ip, float &fr) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(t);
-  const int e = (int)((b >> 52) & 0x7ffull) - 1023;
-  if ((b >> 63) || e > 29) return false;
-  if (e < 0) {
-    ip = 0;
-    fr = d2f_rn(t);
-    return true;
-  }
-  const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
-  const int sh = 52 - e;
-  ip = (int)(m >> sh);
-  const unsigned long long fb = m & ((1ull << sh) - 1ull);  // fraction * 2^sh
-  if (fb == 0ull) {
-    fr = 0.f;
-    return true;
-  }
-  const int lz = __clzll((long long)fb);
-  const int ex = (63 - lz) - sh;  // fraction = 1.xxx * 2^ex, ex < 0
-  const unsigned mant = (unsigned)((fb << (lz + 1)) >> 41);  // 23 bits below the leading one
-  fr = __uint_as_float((unsigned)(ex + 127) << 23 | mant);
-  return true;
-}
+// one vector reduction (both components) per node in global memory
+__device__ __forceinline__ void global_add(float2 *a, float2 v) { atomicAdd(a, v); }
 
 // One block's macroparticles i0 + q MX_THREADS + threadIdx.x (q < ppt,
 // below i1).  Every thread of the block calls it (it holds block barriers
@@ -666,34 +532,6 @@ __global__ void __launch_bounds__(256) k_nodes_mixed_batch(const MixNodeArgs *__
 }
 
 
-BFieldF to_float(const BFieldCoef &b) {
-  BFieldF f;
-  f.type = b.type;
-  f.place = b.place;
-  f.one_d = b.one_d;
-  f.focusing = b.focusing;
-  f.tcase = b.tcase;
-  f.bx0 = (float)b.bx0;
-  f.by0 = (float)b.by0;
-  f.focx = (float)b.focx;
-  f.focy = (float)b.focy;
-  f.S = (float)b.S;
-  f.C = (float)b.C;
-  f.c1 = (float)b.c1;
-  f.ux = (float)b.ux;
-  f.uy = (float)b.uy;
-  f.u3 = (float)b.u3;
-  f.fx = (float)b.fx;
-  f.fy = (float)b.fy;
-  f.kx = (float)b.kx;
-  f.ky = (float)b.ky;
-  f.kxky = (float)b.kxky;
-  f.czs = (float)b.czs;
-  f.cze = (float)b.cze;
-  f.szt = (float)b.szt;
-  return f;
-}
-
 }  // namespace
 
 // FP32 stage-coefficient entries of one step (advances the taper state)
@@ -1006,6 +844,35 @@ int pf_mixed_order_misses(pf_handle *h, double *frac) {
   return PF_OK;
 }
 
+// k_stage_mixed<stage> over pg blocks in the tile form the handle's window takes
+static void launch_mixed_stage(pf_handle *h, int s, const MixArgs &a, unsigned pg, size_t smem,
+                               bool wide, bool oned) {
+#define PF_MIX_CASE(S)                                                                 \
+  case S:                                                                              \
+    if (wide) {                                                                        \
+      if (oned) k_stage_mixed<S, true, MX_TILE_PLANES_WIDE><<<pg, MX_THREADS, smem, h->stream>>>(a); \
+      else k_stage_mixed<S, false, MX_TILE_PLANES_WIDE><<<pg, MX_THREADS, smem, h->stream>>>(a);     \
+    } else if (oned) k_stage_mixed<S, true><<<pg, MX_THREADS, smem, h->stream>>>(a);   \
+    else k_stage_mixed<S, false><<<pg, MX_THREADS, smem, h->stream>>>(a);              \
+    break;
+  switch (s) {
+    PF_MIX_CASE(1)
+    PF_MIX_CASE(2)
+    PF_MIX_CASE(3)
+    PF_MIX_CASE(4)
+  }
+#undef PF_MIX_CASE
+}
+
+// shared bytes of the stage kernel's tile for the handle's window, and
+// whether it is the eight-plane form
+static size_t mixed_stage_smem(const pf_handle *h, const MixArgs &a, bool *wide) {
+  *wide = a.tile && mixed_tile_planes(h) == MX_TILE_PLANES_WIDE;
+  return !a.tile ? 0
+         : *wide ? (size_t)4 * MX_TILE_PLANES_WIDE * h->nix * h->niy * sizeof(int)
+                 : pf_mixed_tile_smem(h);
+}
+
 int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_out) {
   const pf_params &p = h->p;
   const double hh = hstep * 0.5, szh = szl + hh;
@@ -1021,10 +888,8 @@ int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_ou
     a.coef_tab = h->coef_dev;
     a.step_ctr = h->step_ctr;
   }
-  const bool wide = a.tile && mixed_tile_planes(h) == MX_TILE_PLANES_WIDE;
-  const size_t smem = !a.tile ? 0
-                      : wide ? (size_t)4 * MX_TILE_PLANES_WIDE * h->nix * h->niy * sizeof(int)
-                             : pf_mixed_tile_smem(h);
+  bool wide = false;
+  const size_t smem = mixed_stage_smem(h, a, &wide);
   MixNodeArgs n;
   fill_mix_nodes(h, n, 1, hstep);
   if (h->capturing) n.step_ctr = h->step_ctr;
@@ -1047,21 +912,7 @@ int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_ou
     mix_stage_pointers(h, a, s, h->cur, hstep);
     if (h->np > 0) {
       pf_prof_begin(h, PROF_STAGE);
-#define PF_MIX_CASE(S)                                                                 \
-  case S:                                                                              \
-    if (wide) {                                                                        \
-      if (oned) k_stage_mixed<S, true, MX_TILE_PLANES_WIDE><<<pg, MX_THREADS, smem, h->stream>>>(a); \
-      else k_stage_mixed<S, false, MX_TILE_PLANES_WIDE><<<pg, MX_THREADS, smem, h->stream>>>(a);     \
-    } else if (oned) k_stage_mixed<S, true><<<pg, MX_THREADS, smem, h->stream>>>(a);   \
-    else k_stage_mixed<S, false><<<pg, MX_THREADS, smem, h->stream>>>(a);              \
-    break;
-      switch (s) {
-        PF_MIX_CASE(1)
-        PF_MIX_CASE(2)
-        PF_MIX_CASE(3)
-        PF_MIX_CASE(4)
-      }
-#undef PF_MIX_CASE
+      launch_mixed_stage(h, s, a, pg, smem, wide, oned);
       pf_prof_end(h);
       PF_LAUNCHED(h);
     }
@@ -1087,4 +938,76 @@ int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_ou
   *status_out = *h->h_status;
   if (*status_out == 0u) h->cur = nxt;
   return PF_OK;
+}
+
+// One stage of the mixed step on explicit arrays (the adjoint's recorded
+// forward): the stage roles and arithmetic of pf_rk4_mixed, the b-field and
+// taper of position sz.
+int pf_mixed_stage_rec(pf_handle *h, int stage, double hstep, double sz, const PfMixRec &r) {
+  if (h->np == 0) return PF_OK;
+  const pf_params &p = h->p;
+  const double hh = hstep * 0.5;
+  const double stage_c[4] = {0.0, hh, hh, hstep};
+  MixArgs a;
+  fill_mix_args(h, a, hstep);
+  double n2col;
+  int place;
+  pf_taper_stage(h, sz, &n2col, &place);
+  BFieldCoef bf;
+  pf_stage_coefficients(p, sz, n2col, place, &bf);
+  a.bf = to_float(bf);
+  a.n2col = (float)n2col;
+  a.kn2col = (float)(p.kappa * n2col);
+  a.x = r.y[0];
+  a.y = r.y[1];
+  a.z2 = r.y[2];
+  a.px = r.y[3];
+  a.py = r.y[4];
+  a.gam = r.y[5];
+  a.base4 = h->base4;
+  a.cstate = stage_c[stage - 1];
+  a.cstate_f = (float)stage_c[stage - 1];
+  a.as = (const float2 *)r.as;
+  for (int j = 0; j < 6; ++j) {
+    a.kin_f[j] = (const float *)r.kin[j];
+    a.kout_f[j] = (float *)r.kout[j];
+    a.kacc_f[j] = (float *)r.kacc[j];
+    a.k1_f[j] = (const float *)r.k1[j];
+    a.ynext[j] = r.ynext[j];
+  }
+  a.kin_z = (const double *)r.kin[2];
+  a.kout_z = (double *)r.kout[2];
+  a.kacc_z = (double *)r.kacc[2];
+  a.k1_z = (const double *)r.k1[2];
+  PF_CUDA(mixed_attrs());
+  a.ppt = mixed_ppt(h);
+  const int64_t per_block = (int64_t)MX_THREADS * a.ppt;
+  const unsigned pg = (unsigned)std::max<int64_t>(1, (h->np + per_block - 1) / per_block);
+  bool wide = false;
+  const size_t smem = mixed_stage_smem(h, a, &wide);
+  launch_mixed_stage(h, stage, a, pg, smem, wide, p.one_d != 0);
+  PF_LAUNCHED(h);
+  return PF_OK;
+}
+
+void pf_mixed_constants(pf_handle *h, PfMixConst *c) {
+  MixArgs a;
+  fill_mix_args(h, a, 0.0);
+  c->aw2g = a.aw2g;
+  c->g02 = a.g02;
+  c->inv_eta = a.inv_eta;
+  c->inv_dz2 = a.inv_dz2;
+  for (int k = 0; k < 7; ++k) c->ser[k] = a.ser[k];
+  c->ser_r1 = a.ser_r1;
+  c->ser_r2 = a.ser_r2;
+  c->inv_dx_f = a.inv_dx_f;
+  c->inv_dy_f = a.inv_dy_f;
+  c->hx_dx = a.hx_dx;
+  c->hy_dy = a.hy_dy;
+  c->eta_f = a.eta_f;
+  c->inv_dV3 = a.inv_dV3;
+  c->sInv2rho = a.sInv2rho;
+  c->dxc = a.dxc;
+  c->eta_k2 = a.eta_k2;
+  c->rho2 = a.rho2;
 }

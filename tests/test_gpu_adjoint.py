@@ -1,13 +1,17 @@
-"""Adjoint of the RK4/diffraction run (FP64) against central finite
-differences of the forward run, and the forward of the adjoint driver
-against pf_run on the same inputs.
+"""Adjoint of the RK4/diffraction run against central finite differences of
+the FP64 forward run, and the forward of the adjoint driver against pf_run
+on the same inputs, for FP64 and mixed-precision handles.
 
 Workload: the config-1 mesh (periodic, helical, 21 x 21 x 64 unique planes),
 4096 macroparticles, 32 steps with diffraction every 8 and checkpoints every
 8, a 16-point taper profile, a Gaussian seed (waist 1.0) at amplitude 1e-2
-and an energy chirp.  Tolerance (the adjoint form's target): the adjoint gradient within
-1e-4 relative of central differences with steps of 1e-6, for every component
-larger than 1e-3 of the largest.
+and an energy chirp.  Tolerance (the adjoint form's target): the adjoint
+gradient within 1e-4 relative of central differences with steps of 1e-6, for
+every component larger than 1e-3 of the largest.  The mixed-precision
+adjoint is checked against the FP64 forward's differences: a step of 1e-6
+of a taper value is below the FP32 resolution of the mixed forward's
+coefficients (2^-24 relative), so its own energy cannot be differenced at
+that step.
 """
 import numpy as np
 import pytest
@@ -38,6 +42,46 @@ def _setup():
     return w, (seed_re, seed_im), taper_z, alpha
 
 
+def _mixed(params):
+    q = P.Params.from_buffer_copy(params)
+    q.precision = P.MIXED
+    return q
+
+
+def _run_energy(params, w, seed, taper_z, alpha, amp, chirp):
+    """Pulse energy of the same run through pf_run (und_section)."""
+    beam = {k: v.copy() for k, v in w.beam.items()}
+    beam["gam"] = beam["gam"] + chirp * (beam["z2"] - np.sum(beam["z2"]) / len(beam["z2"]))
+    with P.Puffin(params) as sim:
+        sim.set_particles(*(beam[k] for k in P.PARTICLE_KEYS))
+        sim.set_field(amp * seed[0], amp * seed[1])
+        sim.set_taper_profile(taper_z, alpha)
+        sim.und_section(NSTEPS, EVERY, True, w.h)
+        fr, fi = sim.get_field()
+    p = w.params
+    n = p.nx * p.ny * (p.nz2 - 1)  # unique planes of the periodic mesh
+    return p.dx * p.dy * p.dz2 * float(np.sum(fr[:n] ** 2 + fi[:n] ** 2))
+
+
+def _fd_checks(sim, w, seed, taper_z, alpha, amp, chirp):
+    """(name, central difference) of the energy on the handle sim."""
+    def fd(f, x, d):
+        return (f(x + d) - f(x - d)) / (2.0 * d)
+
+    out = [
+        ("seed_amp", fd(lambda a: _energy(sim, w, seed, taper_z, alpha, a, chirp),
+                        amp, 1e-6 * amp)),
+        ("chirp", fd(lambda c: _energy(sim, w, seed, taper_z, alpha, amp, c), chirp, 1e-6)),
+    ]
+    for k in (1, 6, 11, 15):
+        def e_k(v, k=k):
+            a = alpha.copy()
+            a[k] = v
+            return _energy(sim, w, seed, taper_z, a, amp, chirp)
+        out.append((f"taper[{k}]", fd(e_k, alpha[k], 1e-6)))
+    return out
+
+
 def _energy(sim, w, seed, taper_z, alpha, amp, chirp):
     sim.set_taper_profile(taper_z, alpha)
     return sim.adjoint_forward(NSTEPS, EVERY, True, w.h, K, seed[0], seed[1], amp, chirp)
@@ -49,17 +93,7 @@ def test_adjoint_forward_matches_pf_run():
     with P.Puffin(w.params) as sim:
         sim.set_particles(*(w.beam[k] for k in P.PARTICLE_KEYS))
         e_adj = _energy(sim, w, seed, taper_z, alpha, amp, chirp)
-    beam = {k: v.copy() for k, v in w.beam.items()}
-    beam["gam"] = beam["gam"] + chirp * (beam["z2"] - np.sum(beam["z2"]) / len(beam["z2"]))
-    with P.Puffin(w.params) as sim:
-        sim.set_particles(*(beam[k] for k in P.PARTICLE_KEYS))
-        sim.set_field(amp * seed[0], amp * seed[1])
-        sim.set_taper_profile(taper_z, alpha)
-        sim.und_section(NSTEPS, EVERY, True, w.h)
-        fr, fi = sim.get_field()
-    p = w.params
-    n = p.nx * p.ny * (p.nz2 - 1)  # unique planes of the periodic mesh
-    e_run = p.dx * p.dy * p.dz2 * float(np.sum(fr[:n] ** 2 + fi[:n] ** 2))
+    e_run = _run_energy(w.params, w, seed, taper_z, alpha, amp, chirp)
     assert e_adj == pytest.approx(e_run, rel=1e-9)
 
 
@@ -71,27 +105,53 @@ def test_adjoint_gradient_matches_central_differences():
         e0 = _energy(sim, w, seed, taper_z, alpha, amp, chirp)
         g_taper, g_amp, g_chirp = sim.adjoint_backward(len(alpha))
         assert e0 > 0.0
-
-        def fd(f, x, d):
-            return (f(x + d) - f(x - d)) / (2.0 * d)
-
-        checks = [
-            ("seed_amp", g_amp, fd(lambda a: _energy(sim, w, seed, taper_z, alpha, a, chirp),
-                                   amp, 1e-6 * amp)),
-            ("chirp", g_chirp, fd(lambda c: _energy(sim, w, seed, taper_z, alpha, amp, c),
-                                  chirp, 1e-6)),
-        ]
-        for k in (1, 6, 11, 15):
-            def e_k(v, k=k):
-                a = alpha.copy()
-                a[k] = v
-                return _energy(sim, w, seed, taper_z, a, amp, chirp)
-            checks.append((f"taper[{k}]", g_taper[k], fd(e_k, alpha[k], 1e-6)))
-    scale = max(abs(c[2]) for c in checks)
-    for name, adj, num in checks:
-        if abs(num) < 1e-3 * scale:
+        num = _fd_checks(sim, w, seed, taper_z, alpha, amp, chirp)
+    adj = {"seed_amp": g_amp, "chirp": g_chirp}
+    adj.update({f"taper[{k}]": g_taper[k] for k in range(len(alpha))})
+    scale = max(abs(v) for _, v in num)
+    for name, v in num:
+        if abs(v) < 1e-3 * scale:
             continue
-        assert abs(adj - num) <= 1e-4 * abs(num), f"{name}: adjoint {adj!r} vs differences {num!r}"
+        assert abs(adj[name] - v) <= 1e-4 * abs(v), f"{name}: adjoint {adj[name]!r} vs differences {v!r}"
+
+
+def test_mixed_adjoint_forward_matches_pf_run():
+    """The mixed adjoint's recorded forward runs the mixed stage kernels and
+    the FP32 diffraction: its energy is pf_run's on a mixed handle, to the
+    rounding of the FP32 float atomics (deposits outside the shared tiles)."""
+    w, seed, taper_z, alpha = _setup()
+    amp, chirp = 1e-2, 0.05
+    with P.Puffin(_mixed(w.params)) as sim:
+        sim.set_particles(*(w.beam[k] for k in P.PARTICLE_KEYS))
+        e_adj = _energy(sim, w, seed, taper_z, alpha, amp, chirp)
+    e_run = _run_energy(_mixed(w.params), w, seed, taper_z, alpha, amp, chirp)
+    e_64 = _run_energy(w.params, w, seed, taper_z, alpha, amp, chirp)
+    assert e_adj == pytest.approx(e_run, rel=1e-5)
+    assert e_adj == pytest.approx(e_64, rel=1e-4)
+
+
+def test_mixed_adjoint_gradient_matches_fp64_differences():
+    w, seed, taper_z, alpha = _setup()
+    amp, chirp = 1e-2, 0.05
+    with P.Puffin(_mixed(w.params)) as sim:
+        sim.set_particles(*(w.beam[k] for k in P.PARTICLE_KEYS))
+        assert _energy(sim, w, seed, taper_z, alpha, amp, chirp) > 0.0
+        g_taper, g_amp, g_chirp = sim.adjoint_backward(len(alpha))
+        # the backward pass leaves the handle usable for another run
+        e_again = _energy(sim, w, seed, taper_z, alpha, amp, chirp)
+        g2 = sim.adjoint_backward(len(alpha))
+    np.testing.assert_allclose(g2[0], g_taper, rtol=1e-5, atol=1e-5 * np.max(np.abs(g_taper)))
+    assert e_again > 0.0
+    with P.Puffin(w.params) as sim:
+        sim.set_particles(*(w.beam[k] for k in P.PARTICLE_KEYS))
+        num = _fd_checks(sim, w, seed, taper_z, alpha, amp, chirp)
+    adj = {"seed_amp": g_amp, "chirp": g_chirp}
+    adj.update({f"taper[{k}]": g_taper[k] for k in range(len(alpha))})
+    scale = max(abs(v) for _, v in num)
+    for name, v in num:
+        if abs(v) < 1e-3 * scale:
+            continue
+        assert abs(adj[name] - v) <= 1e-4 * abs(v), f"{name}: mixed adjoint {adj[name]!r} vs FP64 differences {v!r}"
 
 
 def test_autograd_function():
