@@ -12,7 +12,8 @@ merged diffraction call (dz = 8 h), exactly as UndSection schedules them.
 * e2e    -- the same metric through the C ABI with host buffers, in the
             reference's data flow: every step copies the particles and the
             inner-window field (the arrays rk4par advances) in from pinned
-            host memory and reads them back; around each diffraction call the
+            host memory and reads them back (pf_rk4_step_host, the copies
+            overlapped with the step); around each diffraction call the
             outer field goes in and comes back as well (inner2Outer /
             diffractIM / outer2Inner);
 * roofline -- the dominant kernel (the fused RK4 stage kernel) timed live
@@ -692,10 +693,11 @@ def run_gpu(args, rank, world):
 
     # end to end through the C ABI with host buffers, in UndSection's data
     # flow: every step hands in the six evolving particle arrays (chi, which
-    # rk4par never changes, is handed in once before the steps) and the
-    # inner-window field (the arrays rk4par advances) from pinned host memory
-    # and reads them back; the outer field goes in before and comes back
-    # after each diffraction call (every 8th step)
+    # rk4par never changes, stays the handle's) and the inner-window field
+    # (the arrays rk4par advances) from pinned host memory and takes them
+    # back, in one pf_rk4_step_host call that overlaps the copies with the
+    # step; the outer field goes in before and comes back after each
+    # diffraction call (every 8th step), with the window after it
     n = w.np
     pin = {k: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy() for k in P.PARTICLE_KEYS}
     fre = torch.empty(sim.n_outer, dtype=torch.float64, pin_memory=True).numpy()
@@ -708,8 +710,6 @@ def run_gpu(args, rank, world):
     fim[:] = i_
     lib = L.load()
     ptrs = [pin[k].ctypes.data for k in P.PARTICLE_KEYS]
-    # the window that the host state needs (set_particles may grow it once)
-    assert lib.pf_set_particles(sim._h, n, *ptrs) == 0
     nw = sim.n_window
     wre = torch.empty(nw, dtype=torch.float64, pin_memory=True).numpy()
     wim = torch.empty(nw, dtype=torch.float64, pin_memory=True).numpy()
@@ -727,20 +727,25 @@ def run_gpu(args, rank, world):
         diff = (state64["i"] + 1) % every == 0
         if diff:
             assert lib.pf_set_field(sim._h, fre.ctypes.data, fim.ctypes.data) == 0
-        assert lib.pf_set_window_field(sim._h, wre.ctypes.data, wim.ctypes.data) == 0
-        assert lib.pf_set_particles(sim._h, n, *ptrs[:6], None) == 0   # chi kept
-        step()
-        if lib.pf_window_nodes(sim._h) != nw:
-            # the particles needed a larger window (pf_set_particles) or a
-            # retry redistributed them: the handle re-made the window from its
-            # own field, and the driver reads it back at the new size
+        rc = lib.pf_rk4_step_host(sim._h, state64["szl"], w.h, *ptrs[:6], wre.ctypes.data,
+                                  wim.ctypes.data)
+        if rc == L.PF_OUT_OF_WINDOW:
+            # the reference's retry: a new window from the particles (the
+            # arrays came back as they went in), read back at its size
+            assert lib.pf_redistribute(sim._h) == 0
             nw = lib.pf_window_nodes(sim._h)
             wre = torch.empty(nw, dtype=torch.float64, pin_memory=True).numpy()
             wim = torch.empty(nw, dtype=torch.float64, pin_memory=True).numpy()
+            assert lib.pf_get_window_field(sim._h, wre.ctypes.data, wim.ctypes.data) == 0
             window_changes += 1
-        assert lib.pf_get_particles(sim._h, *ptrs[:6], None) == 0
-        assert lib.pf_get_window_field(sim._h, wre.ctypes.data, wim.ctypes.data) == 0
+            rc = lib.pf_rk4_step_host(sim._h, state64["szl"], w.h, *ptrs[:6], wre.ctypes.data,
+                                      wim.ctypes.data)
+        assert rc == 0, rc
+        state64["szl"] += w.h
+        state64["i"] += 1
         if diff:
+            sim.diffractIM(every * w.h)
+            assert lib.pf_get_window_field(sim._h, wre.ctypes.data, wim.ctypes.data) == 0
             assert lib.pf_get_field(sim._h, fre.ctypes.data, fim.ctypes.data) == 0
             n_diff += 1
     t1.record(stream)
@@ -750,7 +755,7 @@ def run_gpu(args, rank, world):
     e2e_ms = max(t0.elapsed_time(t1), 1e-9)
     k_e2e = max(1, args.e2e_steps)
     h2d = (6 * 8 * n + 2 * 8 * nw) + 2 * 8 * sim.n_outer * n_diff / k_e2e
-    d2h = (6 * 8 * n + 2 * 8 * nw) + 2 * 8 * sim.n_outer * n_diff / k_e2e
+    d2h = (6 * 8 * n + 2 * 8 * nw) + (2 * 8 * sim.n_outer + 2 * 8 * nw) * n_diff / k_e2e
     e2e_diff_calls = n_diff
     sim.close()
 
@@ -813,8 +818,12 @@ def run_gpu(args, rank, world):
                 "d2h_bytes_per_step": d2h, "steps": args.e2e_steps,
                 "diffraction_calls": e2e_diff_calls, "window_changes": window_changes,
                 "per_step": "the six evolving particle arrays and the inner-window "
-                            "field, in and out (chi handed in once before the steps); "
-                            "the outer field in and out around each diffraction call"},
+                            "field, in and out through pf_rk4_step_host (the copies "
+                            "overlapped with the step; chi stays the handle's); the "
+                            "outer field in and out around each diffraction call, and "
+                            "the window out again after it",
+                "api": "pf_rk4_step_host + pf_set_field / pf_diffract / "
+                       "pf_get_window_field / pf_get_field"},
         "fft_arithmetic": {
             "value_leg": "paired FP32 (48-bit significands; the field stays FP64 in HBM)",
             "fp64_arithmetic": {"value": whole_job_rate(n, args.steps, world, r64f_ms),

@@ -19,6 +19,7 @@
  *
  * Reference interfaces replaced (file:line inside the Puffin project):
  *   pf_rk4_step      rk4par(sZ, h, qD)        puffin/lib/interaction/puffin_mpi_RK4.f90:38
+ *   pf_rk4_step_host rk4par with the driver's host arrays (sElX_G.., ac_rfield_in)
  *                    -> derivs                puffin/lib/interaction/derivative.f90:36
  *                    -> getrhs                puffin/lib/interaction/rhs.f90:60
  *   pf_diffract      inner2Outer + diffractIM(sStep, qD, qOK) + outer2Inner
@@ -181,6 +182,22 @@ int pf_get_window(const pf_handle *h, int32_t *nix, int32_t *niy);
 /* One rk4par step at local zbar szl with step size h.  Returns PF_OK, or
  * PF_OUT_OF_WINDOW / PF_OUT_OF_Z2 with the state unchanged. */
 int pf_rk4_step(pf_handle *h, double szl, double hstep);
+
+/* One rk4par step with the driver's arrays in host memory (FP64 handles):
+ * the six evolving particle arrays (pf_get_particles' order; chi stays the
+ * handle's, as rk4par never changes it) and the inner-window field
+ * (pf_window_nodes() values each) are read, advanced by one step and written
+ * back.  The same as pf_set_window_field + pf_set_particles(..., chi NULL)
+ * + pf_rk4_step + pf_get_particles + pf_get_window_field, without choosing
+ * the window again: the copies in and out run on a second stream,
+ * overlapped with the step's kernels (the particles in chunks), so page-
+ * locked host arrays are copied while the step computes.  Returns PF_OK, or
+ * PF_OUT_OF_WINDOW / PF_OUT_OF_Z2 / PF_OVERFLOW / PF_NOT_FINITE with the
+ * host arrays and the handle's state holding the step's input (then
+ * pf_redistribute and pf_get_window_field give the driver the new window,
+ * as the reference's retry does). */
+int pf_rk4_step_host(pf_handle *h, double szl, double hstep, double *x, double *y, double *z2,
+                     double *px, double *py, double *gam, double *wre, double *wim);
 
 /* getInNode + getLocalFieldIndices: recompute the inner window from the
  * particles and apply the periodic z2 wrap. */

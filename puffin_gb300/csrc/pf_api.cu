@@ -509,6 +509,9 @@ int pf_destroy(pf_handle *h) {
     cudaEventDestroy(e.a);
     cudaEventDestroy(e.b);
   }
+  if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
+  for (cudaEvent_t e : h->copy_events) cudaEventDestroy(e);
+  if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
   free_particles(h);
   free_window(h);
   pf_diff_destroy(h->diff);
@@ -535,6 +538,21 @@ int pf_destroy(pf_handle *h) {
 
 __global__ void k_unpermute(const double *src, const int32_t *perm, double *dst, int64_t n);
 
+// chi (and its FP32 copy) of a z2-ordered handle back in the caller's
+// order, for new particle arrays in that order that keep chi
+static int unpermute_chi(pf_handle *h) {
+  const int64_t n = h->np;
+  k_unpermute<<<grid_for(n, 256), 256, 0, h->stream>>>(h->chi, h->perm, h->kb[0], n);
+  PF_LAUNCHED(h);
+  PF_CUDA(cudaMemcpyAsync(h->chi, h->kb[0], sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice,
+                          h->stream));
+  if (h->chi_f) {
+    k_to_f32<<<grid_for(n, 256), 256, 0, h->stream>>>(h->chi_f, h->chi, n);
+    PF_LAUNCHED(h);
+  }
+  return PF_OK;
+}
+
 static int set_particles_impl(pf_handle *h, int64_t n, const double *const src[7],
                               cudaMemcpyKind kind) {
   if (!h || n < 0) return PF_BAD_ARG;
@@ -552,16 +570,8 @@ static int set_particles_impl(pf_handle *h, int64_t n, const double *const src[7
   int rc = alloc_particles(h, n);
   if (rc) return rc;
   if (h->permuted && src[6] == nullptr && n > 0 && n == h->np) {
-    // the kept chi goes back to the caller's order with the new arrays
-    cudaSetDevice(h->dev);
-    k_unpermute<<<grid_for(n, 256), 256, 0, h->stream>>>(h->chi, h->perm, h->kb[0], n);
-    PF_LAUNCHED(h);
-    PF_CUDA(cudaMemcpyAsync(h->chi, h->kb[0], sizeof(double) * (size_t)n,
-                            cudaMemcpyDeviceToDevice, h->stream));
-    if (h->chi_f) {
-      k_to_f32<<<grid_for(n, 256), 256, 0, h->stream>>>(h->chi_f, h->chi, n);
-      PF_LAUNCHED(h);
-    }
+    rc = unpermute_chi(h);  // the kept chi goes back to the caller's order
+    if (rc) return rc;
   }
   h->permuted = false;
   h->np = n;
@@ -1050,6 +1060,39 @@ int pf_rk4_step(pf_handle *h, double szl, double hstep) {
   int rc = (h->p.precision == PF_MIXED) ? pf_rk4_mixed(h, szl, hstep, &st)
                                          : pf_rk4_fp64(h, szl, hstep, &st);
   if (rc) return rc;
+  rc = status_to_rc(st);
+  if (rc == PF_OUT_OF_Z2) h->err = "a macroparticle's z2 node lies outside the temporal mesh";
+  if (rc == PF_OUT_OF_WINDOW) h->err = "a macroparticle left the inner transverse window";
+  if (rc == PF_OVERFLOW) h->err = "deposit contribution beyond the fixed-point range";
+  if (rc == PF_NOT_FINITE) h->err = "a non-finite value in a macroparticle's state or in the field";
+  return rc;
+}
+
+int pf_rk4_step_host(pf_handle *h, double szl, double hstep, double *x, double *y, double *z2,
+                     double *px, double *py, double *gam, double *wre, double *wim) {
+  if (!h || !x || !y || !z2 || !px || !py || !gam || !wre || !wim) return PF_BAD_ARG;
+  if (!h->particles_set || h->nwin == 0 || h->np == 0) {
+    h->err = "pf_rk4_step_host: particles not set";
+    return PF_STATE;
+  }
+  if (h->p.precision != PF_FP64) {
+    h->err = "pf_rk4_step_host runs on FP64 handles (mixed: pf_set_particles, "
+             "pf_set_window_field, pf_rk4_step and the getters)";
+    return PF_BAD_ARG;
+  }
+  cudaSetDevice(h->dev);
+  // the arrays come in the caller's order: a z2-ordered handle's chi
+  // follows them back
+  if (h->permuted) {
+    const int rc = unpermute_chi(h);
+    if (rc) return rc;
+    h->permuted = false;
+  }
+  double *const host[6] = {x, y, z2, px, py, gam};
+  unsigned int st = 0;
+  int rc = pf_rk4_fp64_host(h, szl, hstep, host, wre, wim, &st);
+  if (rc) return rc;
+  h->window_valid = true;
   rc = status_to_rc(st);
   if (rc == PF_OUT_OF_Z2) h->err = "a macroparticle's z2 node lies outside the temporal mesh";
   if (rc == PF_OUT_OF_WINDOW) h->err = "a macroparticle left the inner transverse window";

@@ -256,6 +256,10 @@ struct pf_handle {
   // FP64 path: diffraction FFTs in paired-FP32 arithmetic (pf_set_fft_arithmetic)
   bool fft_pairs = false;
 
+  // the host-array step (pf_rk4_step_host): a copy stream and its events
+  cudaStream_t copy_stream = nullptr;
+  std::vector<cudaEvent_t> copy_events;
+
   // optional per-kernel-class timing
   bool prof = false;
   std::vector<ProfEvent> prof_pending;
@@ -273,6 +277,11 @@ void pf_prof_flush(pf_handle *h);
 
 // fp64 RK4 step on the device; returns the device status word.
 int pf_rk4_fp64(pf_handle *h, double szl, double hstep, unsigned int *status_out);
+// the same step with the particles and the window field in host memory,
+// copied in and out around it and overlapped with its kernels; returns the
+// status word (the host arrays hold the step's input again when it is set)
+int pf_rk4_fp64_host(pf_handle *h, double szl, double hstep, double *const host[6], double *wre,
+                     double *wim, unsigned int *status_out);
 // building blocks of the FP64 step for other drivers (the adjoint)
 void pf_fill_stage_args(pf_handle *h, StageArgs &a, double h6);
 int pf_launch_stage(pf_handle *h, int stage, StageArgs &a);   // k_stage<stage>

@@ -746,14 +746,16 @@ static bool dense_mode(const pf_handle *h, size_t *smem) {
   return h->np >= (int64_t)8 * h->npl * ntr && bytes <= 96 * 1024;
 }
 
+// k_stage<stage> over the a.np macroparticles a points to (the handle's
+// beam, or a range of it), in the deposit mode the handle's beam takes
 static int launch_stage(pf_handle *h, int stage, StageArgs &a) {
   const int threads = 256;
-  const int64_t blocks = (h->np + threads - 1) / threads;
+  const int64_t blocks = (a.np + threads - 1) / threads;
   if (blocks == 0) return PF_OK;
   const bool oned = h->p.one_d != 0;
   size_t smem = 0;
   const bool dense = dense_mode(h, &smem);
-  const int64_t dblocks = (h->np + FT_PPB - 1) / FT_PPB;
+  const int64_t dblocks = (a.np + FT_PPB - 1) / FT_PPB;
   static PfDeviceOnce attr_once;  // the attribute is per device
   if (dense) {
     PF_CUDA(pf_device_once(attr_once, [] {
@@ -1039,6 +1041,129 @@ int pf_rk4_fp64(pf_handle *h, double szl, double hstep, unsigned int *status_out
   pf_prof_flush(h);
   *status_out = *h->h_status;
   if (*status_out == 0u) h->cur = nxt;
+  return PF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// The step with the driver's arrays in host memory (rk4par as the
+// reference's driver calls it, every step handing in and taking back the
+// particle arrays and the inner-window field).  The copies run on a second
+// stream and overlap the kernels: the window field goes in first (every
+// macroparticle of stage 1 gathers from it), the particles in chunks that
+// stage 1 starts on as each arrives, and stage 4's output leaves chunk by
+// chunk as it is written, the window field after the last node update.  The
+// deposit is an integer sum, so the chunked stages give the bits of the
+// whole-beam launches.  When the status word is set (a macroparticle out of
+// the window or the mesh, an overflow, a non-finite value) the host arrays
+// receive the step's input again and the device state is the step's input.
+int pf_rk4_fp64_host(pf_handle *h, double szl, double hstep, double *const host[6], double *wre,
+                     double *wim, unsigned int *status_out) {
+  const pf_params &p = h->p;
+  const double hh = hstep * 0.5, h6 = hstep / 6.0, szh = szl + hh;
+  const double stage_sz[4] = {szl, szh, szh, szl + hstep};
+  const double stage_c[4] = {0.0, hh, hh, hstep};
+  const int cur = h->cur, nxt = cur ^ 1;
+  const int64_t np = h->np;
+  // chunks of at least 2^20 macroparticles (48 MB of state), at most 16
+  const int64_t chunk = std::max<int64_t>((int64_t)1 << 20, (np + 15) / 16);
+  const int nch = (int)std::max<int64_t>(1, (np + chunk - 1) / chunk);
+  if (!h->copy_stream)
+    PF_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+  while ((int)h->copy_events.size() < 2 * nch + 1) {
+    cudaEvent_t e;
+    PF_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    h->copy_events.push_back(e);
+  }
+  cudaEvent_t *ev_in = h->copy_events.data(), *ev_out = ev_in + nch, ev_w = ev_in[2 * nch];
+  cudaStream_t cs = h->copy_stream, st = h->stream;
+  const size_t wb = (size_t)h->nwin * sizeof(double);
+
+  PF_CUDA(cudaMemsetAsync(h->d_status, 0, sizeof(unsigned int), st));
+  PF_CUDA(cudaMemcpyAsync(h->wr, wre, wb, cudaMemcpyHostToDevice, st));
+  PF_CUDA(cudaMemcpyAsync(h->wi, wim, wb, cudaMemcpyHostToDevice, st));
+  for (int c = 0; c < nch; ++c) {
+    const int64_t off = c * chunk, len = std::min(chunk, np - off);
+    for (int j = 0; j < 6; ++j)
+      PF_CUDA(cudaMemcpyAsync(h->y[cur][j] + off, host[j] + off, (size_t)len * sizeof(double),
+                              cudaMemcpyHostToDevice, cs));
+    PF_CUDA(cudaEventRecord(ev_in[c], cs));
+  }
+
+  StageArgs a;
+  pf_fill_stage_args(h, a, h6);
+  NodeArgs n;
+  pf_fill_node_args(h, n, hstep);
+  // the stage arguments of macroparticles [off, off + len)
+  auto range = [](const StageArgs &b, int64_t off, int64_t len) {
+    StageArgs r = b;
+    r.x += off;
+    r.y += off;
+    r.z2 += off;
+    r.px += off;
+    r.py += off;
+    r.gam += off;
+    r.chi += off;
+    for (int j = 0; j < 6; ++j) {
+      if (r.kin[j]) r.kin[j] += off;
+      if (r.kout[j]) r.kout[j] += off;
+      if (r.kacc[j]) r.kacc[j] += off;
+      if (r.k1[j]) r.k1[j] += off;
+      if (r.ynext[j]) r.ynext[j] += off;
+    }
+    r.np = len;
+    return r;
+  };
+  for (int s = 1; s <= 4; ++s) {
+    double n2col;
+    int place;
+    pf_taper_stage(h, stage_sz[s - 1], &n2col, &place);
+    a.n2col = n2col;
+    a.kn2col = p.kappa * n2col;
+    pf_stage_coefficients(p, stage_sz[s - 1], n2col, place, &a.bf);
+    a.cstate = stage_c[s - 1];
+    pf_stage_pointers(h, a, s, cur);
+    if (s == 1 || s == 4) {
+      for (int c = 0; c < nch; ++c) {
+        const int64_t off = c * chunk, len = std::min(chunk, np - off);
+        if (s == 1) PF_CUDA(cudaStreamWaitEvent(st, ev_in[c], 0));
+        StageArgs r = range(a, off, len);
+        int rc = launch_stage(h, s, r);
+        if (rc) return rc;
+        if (s == 4) {
+          // this chunk's new state leaves while the next chunks run
+          PF_CUDA(cudaEventRecord(ev_out[c], st));
+          PF_CUDA(cudaStreamWaitEvent(cs, ev_out[c], 0));
+          for (int j = 0; j < 6; ++j)
+            PF_CUDA(cudaMemcpyAsync(host[j] + off, h->y[nxt][j] + off,
+                                    (size_t)len * sizeof(double), cudaMemcpyDeviceToHost, cs));
+        }
+      }
+    } else {
+      int rc = launch_stage(h, s, a);
+      if (rc) return rc;
+    }
+    n.coef = (s == 3) ? hstep : hh;
+    int rc = launch_nodes(h, s, n);
+    if (rc) return rc;
+  }
+  PF_CUDA(cudaMemcpyAsync(wre, h->wr, wb, cudaMemcpyDeviceToHost, st));
+  PF_CUDA(cudaMemcpyAsync(wim, h->wi, wb, cudaMemcpyDeviceToHost, st));
+  PF_CUDA(cudaMemcpyAsync(h->h_status, h->d_status, sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                          st));
+  PF_CUDA(cudaEventRecord(ev_w, st));
+  PF_CUDA(cudaStreamWaitEvent(cs, ev_w, 0));
+  PF_CUDA(cudaStreamSynchronize(cs));
+  *status_out = *h->h_status;
+  if (*status_out == 0u) {
+    h->cur = nxt;
+    return PF_OK;
+  }
+  // a failed step: the window field was left as it came in (stage 4's node
+  // update commits nothing once the status is set); the particles go back
+  for (int j = 0; j < 6; ++j)
+    PF_CUDA(cudaMemcpyAsync(host[j], h->y[cur][j], (size_t)np * sizeof(double),
+                            cudaMemcpyDeviceToHost, st));
+  PF_CUDA(cudaStreamSynchronize(st));
   return PF_OK;
 }
 

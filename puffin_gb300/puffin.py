@@ -194,6 +194,25 @@ class Puffin:
 
     rk4_step = rk4par
 
+    def rk4par_host(self, szl: float, h: float, particles: dict, window: tuple) -> bool:
+        """One RK4 step on the driver's host arrays (pf_rk4_step_host): the
+        float64 arrays particles["x"] .. particles["gam"] and the window field
+        (re, im), advanced in place, the copies overlapped with the step.
+        False (arrays and state as they came in) if a particle left the
+        window or the mesh."""
+        arrs = [particles[k] for k in PARTICLE_KEYS[:6]] + list(window)
+        for a in arrs:
+            if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags.c_contiguous):
+                raise ValueError("rk4par_host takes C-contiguous float64 numpy arrays")
+        if any(a.size != self.n_particles for a in arrs[:6]):
+            raise ValueError("particle arrays must hold the handle's macroparticles")
+        if any(a.size != self.n_window for a in arrs[6:]):
+            raise ValueError(f"window field arrays must hold {self.n_window} values")
+        rc = self._check(self._lib.pf_rk4_step_host(self._h, float(szl), float(h),
+                                                    *[a.ctypes.data for a in arrs]),
+                         allow=(L.PF_OUT_OF_WINDOW, L.PF_OUT_OF_Z2))
+        return rc == L.PF_OK
+
     def redistribute(self):
         self._check(self._lib.pf_redistribute(self._h))
 

@@ -1,0 +1,110 @@
+"""pf_rk4_step_host: rk4par on the driver's host arrays, the copies in and
+out overlapped with the step's kernels (the particles in chunks of 2^20),
+against the device-resident sequence it replaces (set_window_field +
+set_particles with chi kept + rk4par + get_particles + get_window_field):
+bit for bit in FP64, for one chunk and for several; a macroparticle that
+leaves the window leaves the host arrays and the handle's state as they
+came in."""
+import numpy as np
+import pytest
+import torch
+
+import puffin_gb300 as P
+from puffin_gb300 import configs
+
+pytestmark = pytest.mark.gpu
+KEYS = P.PARTICLE_KEYS[:6]
+
+
+def _pinned(a):
+    t = torch.empty(a.size, dtype=torch.float64, pin_memory=True).numpy()
+    t[:] = a
+    return t
+
+
+def _field(p, seed):
+    rng = np.random.default_rng(seed)
+    n = p.nx * p.ny * p.nz2
+    return 1e-3 * rng.standard_normal(n), 1e-3 * rng.standard_normal(n)
+
+
+@pytest.mark.parametrize("np_", [3000, (1 << 21) + 12345])
+def test_host_step_matches_resident_steps(np_):
+    w = configs.config1(np_=np_, seed=5)
+    field = _field(w.params, 5)
+    with P.Puffin(w.params) as a, P.Puffin(w.params) as b:
+        for sim in (a, b):
+            sim.set_particles(*(w.beam[k] for k in P.PARTICLE_KEYS))
+            sim.set_field(*field)
+        parts = {k: _pinned(w.beam[k]) for k in KEYS}
+        wre, wim = (_pinned(v) for v in a.get_window_field())
+        szl = 0.0
+        for _ in range(3):
+            assert a.rk4par_host(szl, w.h, parts, (wre, wim))
+            assert b.rk4par(szl, w.h)
+            szl += w.h
+        got_b = b.get_particles()
+        wb = b.get_window_field()
+        got_a = a.get_particles()
+    for k in KEYS:
+        np.testing.assert_array_equal(parts[k], got_b[k], err_msg=k)
+        np.testing.assert_array_equal(got_a[k], got_b[k], err_msg=k)
+    np.testing.assert_array_equal(wre, wb[0])
+    np.testing.assert_array_equal(wim, wb[1])
+    assert not np.array_equal(parts["z2"], w.beam["z2"])  # the steps moved the beam
+
+
+def test_host_step_failure_leaves_arrays_and_state():
+    w = configs.config1(np_=(1 << 21) + 7, seed=6)
+    field = _field(w.params, 6)
+    with P.Puffin(w.params) as sim:
+        sim.set_particles(*(w.beam[k] for k in P.PARTICLE_KEYS))
+        sim.set_field(*field)
+        parts = {k: _pinned(w.beam[k]) for k in KEYS}
+        wre, wim = (_pinned(v) for v in sim.get_window_field())
+        # a macroparticle of the second chunk far outside the transverse window
+        parts["x"][(1 << 20) + 5] = 1.0e3
+        before = {k: v.copy() for k, v in parts.items()}
+        w_before = (wre.copy(), wim.copy())
+        assert not sim.rk4par_host(0.0, w.h, parts, (wre, wim))
+        got = sim.get_particles()
+    for k in KEYS:
+        np.testing.assert_array_equal(parts[k], before[k], err_msg=k)
+        np.testing.assert_array_equal(got[k], before[k], err_msg=k)
+    np.testing.assert_array_equal(wre, w_before[0])
+    np.testing.assert_array_equal(wim, w_before[1])
+
+
+def test_host_step_after_z2_ordering_keeps_chi_with_the_caller_order():
+    """After pf_run has z2-ordered the handle, host arrays in the caller's
+    order take chi back to that order: the step equals a fresh handle's."""
+    w = configs.config1(np_=1 << 16, seed=7)
+    field = _field(w.params, 7)
+    with P.Puffin(w.params) as a, P.Puffin(w.params) as b:
+        for sim in (a, b):
+            sim.set_particles(*(w.beam[k] for k in P.PARTICLE_KEYS))
+            sim.set_field(*field)
+        szl = a.und_section(120, 16, True, w.h, 0.0)   # z2-orders the beam at the wrap cadence
+        state = a.get_particles()
+        fr, fi = a.get_field()
+        b.set_particles(*(state[k] for k in P.PARTICLE_KEYS))
+        b.set_field(fr, fi)
+        parts = {k: _pinned(state[k]) for k in KEYS}
+        wre, wim = (_pinned(v) for v in a.get_window_field())
+        assert a.rk4par_host(szl, w.h, parts, (wre, wim))
+        assert b.rk4par(szl, w.h)
+        got_b = b.get_particles()
+    for k in KEYS:
+        np.testing.assert_allclose(parts[k], got_b[k], rtol=0, atol=0, err_msg=k)
+
+
+def test_host_step_rejects_mixed_handles():
+    w = configs.config1(np_=3000, seed=8)
+    q = P.Params.from_buffer_copy(w.params)
+    q.precision = P.MIXED
+    with P.Puffin(q) as sim:
+        sim.set_particles(*(w.beam[k] for k in P.PARTICLE_KEYS))
+        parts = {k: np.ascontiguousarray(w.beam[k], dtype=np.float64) for k in KEYS}
+        wre, wim = (np.ascontiguousarray(v) for v in sim.get_window_field())
+        with pytest.raises(RuntimeError):
+            sim.rk4par_host(0.0, w.h, parts, (wre, wim))
