@@ -722,11 +722,16 @@ def run_gpu(args, rank, world):
         torch.distributed.barrier()
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
+    # wall time per call class (every call returns with its work done)
+    e2e_parts = {"set_field": 0.0, "step_host": 0.0, "diffract_and_get": 0.0}
     t0.record(stream)
     for _ in range(max(0, args.e2e_steps)):
         diff = (state64["i"] + 1) % every == 0
+        tp = time.perf_counter()
         if diff:
             assert lib.pf_set_field(sim._h, fre.ctypes.data, fim.ctypes.data) == 0
+        tq = time.perf_counter()
+        e2e_parts["set_field"] += tq - tp
         rc = lib.pf_rk4_step_host(sim._h, state64["szl"], w.h, *ptrs[:6], wre.ctypes.data,
                                   wim.ctypes.data)
         if rc == L.PF_OUT_OF_WINDOW:
@@ -741,6 +746,8 @@ def run_gpu(args, rank, world):
             rc = lib.pf_rk4_step_host(sim._h, state64["szl"], w.h, *ptrs[:6], wre.ctypes.data,
                                       wim.ctypes.data)
         assert rc == 0, rc
+        tr = time.perf_counter()
+        e2e_parts["step_host"] += tr - tq
         state64["szl"] += w.h
         state64["i"] += 1
         if diff:
@@ -748,6 +755,7 @@ def run_gpu(args, rank, world):
             assert lib.pf_get_window_field(sim._h, wre.ctypes.data, wim.ctypes.data) == 0
             assert lib.pf_get_field(sim._h, fre.ctypes.data, fim.ctypes.data) == 0
             n_diff += 1
+        e2e_parts["diffract_and_get"] += time.perf_counter() - tr
     t1.record(stream)
     torch.cuda.synchronize()
     if world > 1:
@@ -823,7 +831,9 @@ def run_gpu(args, rank, world):
                             "outer field in and out around each diffraction call, and "
                             "the window out again after it",
                 "api": "pf_rk4_step_host + pf_set_field / pf_diffract / "
-                       "pf_get_window_field / pf_get_field"},
+                       "pf_get_window_field / pf_get_field",
+                "ms_per_step_by_call": {k: 1e3 * v / max(1, args.e2e_steps)
+                                        for k, v in e2e_parts.items()}},
         "fft_arithmetic": {
             "value_leg": "paired FP32 (48-bit significands; the field stays FP64 in HBM)",
             "fp64_arithmetic": {"value": whole_job_rate(n, args.steps, world, r64f_ms),
