@@ -696,8 +696,9 @@ def run_gpu(args, rank, world):
     # rk4par never changes, stays the handle's) and the inner-window field
     # (the arrays rk4par advances) from pinned host memory and takes them
     # back, in one pf_rk4_step_host call that overlaps the copies with the
-    # step; the outer field goes in before and comes back after each
-    # diffraction call (every 8th step), with the window after it
+    # step; every 8th step inner2Outer + diffractIM + outer2Inner take the
+    # outer field and the window in and back (pf_diffract_host, the outer
+    # field's copies overlapped with the transforms)
     n = w.np
     pin = {k: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy() for k in P.PARTICLE_KEYS}
     fre = torch.empty(sim.n_outer, dtype=torch.float64, pin_memory=True).numpy()
@@ -723,15 +724,11 @@ def run_gpu(args, rank, world):
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
     # wall time per call class (every call returns with its work done)
-    e2e_parts = {"set_field": 0.0, "step_host": 0.0, "diffract_and_get": 0.0}
+    e2e_parts = {"step_host": 0.0, "diffract_host": 0.0}
     t0.record(stream)
     for _ in range(max(0, args.e2e_steps)):
         diff = (state64["i"] + 1) % every == 0
-        tp = time.perf_counter()
-        if diff:
-            assert lib.pf_set_field(sim._h, fre.ctypes.data, fim.ctypes.data) == 0
         tq = time.perf_counter()
-        e2e_parts["set_field"] += tq - tp
         rc = lib.pf_rk4_step_host(sim._h, state64["szl"], w.h, *ptrs[:6], wre.ctypes.data,
                                   wim.ctypes.data)
         if rc == L.PF_OUT_OF_WINDOW:
@@ -751,18 +748,17 @@ def run_gpu(args, rank, world):
         state64["szl"] += w.h
         state64["i"] += 1
         if diff:
-            sim.diffractIM(every * w.h)
-            assert lib.pf_get_window_field(sim._h, wre.ctypes.data, wim.ctypes.data) == 0
-            assert lib.pf_get_field(sim._h, fre.ctypes.data, fim.ctypes.data) == 0
+            assert lib.pf_diffract_host(sim._h, every * w.h, fre.ctypes.data, fim.ctypes.data,
+                                        wre.ctypes.data, wim.ctypes.data) == 0
             n_diff += 1
-        e2e_parts["diffract_and_get"] += time.perf_counter() - tr
+        e2e_parts["diffract_host"] += time.perf_counter() - tr
     t1.record(stream)
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
     e2e_ms = max(t0.elapsed_time(t1), 1e-9)
     k_e2e = max(1, args.e2e_steps)
-    h2d = (6 * 8 * n + 2 * 8 * nw) + 2 * 8 * sim.n_outer * n_diff / k_e2e
+    h2d = (6 * 8 * n + 2 * 8 * nw) + (2 * 8 * sim.n_outer + 2 * 8 * nw) * n_diff / k_e2e
     d2h = (6 * 8 * n + 2 * 8 * nw) + (2 * 8 * sim.n_outer + 2 * 8 * nw) * n_diff / k_e2e
     e2e_diff_calls = n_diff
     sim.close()
@@ -828,10 +824,9 @@ def run_gpu(args, rank, world):
                 "per_step": "the six evolving particle arrays and the inner-window "
                             "field, in and out through pf_rk4_step_host (the copies "
                             "overlapped with the step; chi stays the handle's); the "
-                            "outer field in and out around each diffraction call, and "
-                            "the window out again after it",
-                "api": "pf_rk4_step_host + pf_set_field / pf_diffract / "
-                       "pf_get_window_field / pf_get_field",
+                            "outer field and the window in and out around each "
+                            "diffraction call through pf_diffract_host",
+                "api": "pf_rk4_step_host + pf_diffract_host",
                 "ms_per_step_by_call": {k: 1e3 * v / max(1, args.e2e_steps)
                                         for k, v in e2e_parts.items()}},
         "fft_arithmetic": {

@@ -20,6 +20,8 @@
  * Reference interfaces replaced (file:line inside the Puffin project):
  *   pf_rk4_step      rk4par(sZ, h, qD)        puffin/lib/interaction/puffin_mpi_RK4.f90:38
  *   pf_rk4_step_host rk4par with the driver's host arrays (sElX_G.., ac_rfield_in)
+ *   pf_diffract_host inner2Outer + diffractIM + outer2Inner with the driver's
+ *                    host arrays (ac_rfield, ac_rfield_in)
  *                    -> derivs                puffin/lib/interaction/derivative.f90:36
  *                    -> getrhs                puffin/lib/interaction/rhs.f90:60
  *   pf_diffract      inner2Outer + diffractIM(sStep, qD, qOK) + outer2Inner
@@ -198,6 +200,17 @@ int pf_rk4_step(pf_handle *h, double szl, double hstep);
  * as the reference's retry does). */
 int pf_rk4_step_host(pf_handle *h, double szl, double hstep, double *x, double *y, double *z2,
                      double *px, double *py, double *gam, double *wre, double *wim);
+
+/* inner2Outer + diffractIM + outer2Inner with the driver's arrays in host
+ * memory (FP64 handles): the outer field (nx * ny * nz2 values each) and,
+ * when the handle has a window, the inner-window field (pf_window_nodes()
+ * values each) are read and written in place, as pf_set_field +
+ * pf_set_window_field + pf_diffract + pf_get_field + pf_get_window_field
+ * would, with the outer field's copies overlapped with the transforms
+ * (copied in and out by ranges of z2 planes while the first and the last
+ * pass run on the others). */
+int pf_diffract_host(pf_handle *h, double dz, double *ore, double *oim, double *wre,
+                     double *wim);
 
 /* getInNode + getLocalFieldIndices: recompute the inner window from the
  * particles and apply the periodic z2 wrap. */

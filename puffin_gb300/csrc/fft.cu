@@ -28,6 +28,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -86,6 +87,15 @@ int pf_diffract_outer(pf_handle *h, double dz) {
 int pf_diffract_outer_c32(pf_handle *h, void *outer, double dz) {
   if (!h->diff) h->diff = new DiffPlan();
   return fft32::diffract(h, h->diff->p32, nullptr, nullptr, (fft32::cplx *)outer, dz);
+}
+
+int pf_diffract_outer_ranges(pf_handle *h, double dz, const std::vector<int64_t> &zcut,
+                             const std::function<int(int)> &before,
+                             const std::function<int(int)> &after) {
+  if (!h->diff) h->diff = new DiffPlan();
+  if (h->fft_pairs)
+    return fftdd::diffract_ranges(h, h->diff->pdd, h->or_, h->oi_, dz, zcut, before, after);
+  return fft64::diffract_ranges(h, h->diff->p64, h->or_, h->oi_, dz, zcut, before, after);
 }
 
 int pf_diffract_adjoint_split(pf_handle *h, double *re, double *im, double dz) {

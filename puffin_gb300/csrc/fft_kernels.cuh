@@ -54,7 +54,8 @@ struct AxisPlan {
   int64_t stride;   // element stride along the axis
   int64_t inner;    // base(L) = L % inner + (L / inner) * ostride
   int64_t ostride;
-  int64_t nlines;
+  int64_t nlines;   // the line kernel runs lines [line0, nlines)
+  int64_t line0;
   int lpb;
   int axis;         // 0 x, 1 y, 2 z
   int pfa;          // 1: n = 129 = 3 * 43 as a prime-factor transform (k_fft)
@@ -618,7 +619,7 @@ __global__ void __launch_bounds__(NTHREADS, KFFT_MINB) k_fft(const FftArgs a) {
   cplx *smem_all = reinterpret_cast<cplx *>(smem_raw);
   const AxisPlan &p = a.ax;
   const int n = p.n;
-  const int64_t L0 = (int64_t)blockIdx.x * p.lpb;
+  const int64_t L0 = p.line0 + (int64_t)blockIdx.x * p.lpb;
   const int nl = (int)min((int64_t)p.lpb, p.nlines - L0);
   const int tid = threadIdx.x;
   cplx *smem = smem_all;
@@ -1548,6 +1549,86 @@ static int run_schedule(pf_handle *h, Plan *d, const FftArgs &a, bool split, boo
     // the mirror plane is written by the last pass only
     b.mirror = a.mirror && s.store_split;
     const int rc = fft_pass(h, d, b, s.axis);
+    if (rc) return rc;
+  }
+  return PF_OK;
+}
+
+// The diffraction step of diffract() on split re/im arrays, with the first
+// and the last pass over x cut into ranges of z2 planes [zcut[c],
+// zcut[c + 1]) (an x line lies in one plane: line y + ny z): before(c) runs
+// before the first pass reads range c, after(c) once the last pass has
+// written it (range 0 also carries the periodic mirror plane).  The other
+// passes run whole.  Meshes whose transverse passes are one plane kernel
+// run whole too: every before() first, every after() at the end.
+static int diffract_ranges(pf_handle *h, Plan *&plan, io_real *re, io_real *im, double dz,
+                           const std::vector<int64_t> &zcut,
+                           const std::function<int(int)> &before,
+                           const std::function<int(int)> &after) {
+  const pf_params &p = h->p;
+  if (!plan) {
+    int rc = build_plan(h, plan);
+    if (rc) return rc;
+  }
+  Plan *d = plan;
+  const int nch = (int)zcut.size() - 1;
+  if (d->plane || d->ax[0].n == 1) {
+    for (int c = 0; c < nch; ++c) {
+      const int rc = before(c);
+      if (rc) return rc;
+    }
+    int rc = diffract(h, plan, re, im, nullptr, dz);
+    for (int c = 0; c < nch && rc == PF_OK; ++c) rc = after(c);
+    return rc;
+  }
+  FftArgs a;
+  base_args(h, d, re, im, nullptr, a);
+  const int64_t ntab = (int64_t)(d->nx + d->ny) * d->nz;
+  pf_prof_begin(h, PROF_DIFF);
+  k_tables<<<(unsigned)((ntab + 255) / 256), 256, 0, h->stream>>>(
+      d->px, d->py, d->dxt, d->dyt, d->kx, d->ky, d->kz, d->nx, d->ny, d->nz, dz, dz, p.sbeta);
+  pf_prof_end(h);
+  PF_LAUNCHED(h);
+  // x lines of the planes of range c
+  auto x_range = [&](FftArgs b, int c) {
+    b.ax = d->ax[0];
+    b.ax.line0 = (int64_t)d->ny * zcut[c];
+    b.ax.nlines = (int64_t)d->ny * zcut[c + 1];
+    const int64_t blocks = (b.ax.nlines - b.ax.line0 + b.ax.lpb - 1) / b.ax.lpb;
+    if (blocks <= 0) return PF_OK;
+    pf_prof_begin(h, PROF_FFT);
+    k_fft<<<(unsigned)blocks, NTHREADS, d->smem[0], h->stream>>>(b);
+    pf_prof_end(h);
+    PF_LAUNCHED(h);
+    return PF_OK;
+  };
+  struct Step {
+    int axis, dir, mid, second, load_split, store_split;
+  };
+  const Step steps[9] = {
+      {0, 0, MID_NONE, 0, 1, 0},   {1, 0, MID_NONE, 0, 0, 0}, {2, 0, MID_PROP, 1, 0, 0},
+      {1, 1, MID_NONE, 0, 0, 0},   {0, 1, MID_SPLIT, 1, 0, 0}, {1, 0, MID_NONE, 0, 0, 0},
+      {2, 0, MID_DAMP, 1, 0, 0},   {1, 1, MID_NONE, 0, 0, 0}, {0, 1, MID_RECOMB, 0, 0, 1},
+  };
+  for (int k = 0; k < 9; ++k) {
+    const Step &st = steps[k];
+    FftArgs b = a;
+    b.dir = st.dir;
+    b.mid = st.mid;
+    b.second = st.second;
+    b.load_split = st.load_split;
+    b.store_split = st.store_split;
+    b.mirror = a.mirror && st.store_split;
+    int rc = PF_OK;
+    if (k == 0 || k == 8) {
+      for (int c = 0; c < nch && rc == PF_OK; ++c) {
+        if (k == 0) rc = before(c);
+        if (rc == PF_OK) rc = x_range(b, c);
+        if (k == 8 && rc == PF_OK) rc = after(c);
+      }
+    } else {
+      rc = fft_pass(h, d, b, st.axis);
+    }
     if (rc) return rc;
   }
   return PF_OK;

@@ -1101,6 +1101,99 @@ int pf_rk4_step_host(pf_handle *h, double szl, double hstep, double *x, double *
   return rc;
 }
 
+// inner2Outer + diffractIM + outer2Inner with the driver's arrays in host
+// memory (FP64 handles): the window field goes in first; the outer field
+// goes in by ranges of z2 planes on the copy stream, each range's window
+// planes are copied into it and the first x pass runs on it as it arrives;
+// the last x pass writes the outer field range by range and each range goes
+// out while the next is computed; the window field comes back from the
+// diffracted field last.
+int pf_diffract_host(pf_handle *h, double dz, double *ore, double *oim, double *wre,
+                     double *wim) {
+  if (!h || !ore || !oim) return PF_BAD_ARG;
+  if (h->p.precision != PF_FP64) {
+    h->err = "pf_diffract_host runs on FP64 handles (mixed: pf_set_field, pf_diffract, "
+             "pf_get_field)";
+    return PF_BAD_ARG;
+  }
+  // the driver's window arrays are the window state whenever there is one
+  const bool win = h->nwin > 0;
+  if (win && (!wre || !wim)) return PF_BAD_ARG;
+  cudaSetDevice(h->dev);
+  const pf_params &p = h->p;
+  const bool periodic = (p.mesh_type == PF_MESH_PERIODIC);
+  const int64_t plane = (int64_t)p.nx * p.ny;
+  const int64_t nzf = periodic ? p.nz2 - 1 : p.nz2;  // planes the transforms run over
+  const int nch = (int)std::max<int64_t>(1, std::min<int64_t>(8, nzf));
+  std::vector<int64_t> zcut((size_t)nch + 1);
+  for (int c = 0; c <= nch; ++c) zcut[c] = nzf * c / nch;
+  if (!h->copy_stream) PF_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+  while ((int)h->copy_events.size() < 2 * nch + 1) {
+    cudaEvent_t e;
+    PF_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    h->copy_events.push_back(e);
+  }
+  cudaEvent_t *ev_in = h->copy_events.data(), *ev_out = ev_in + nch, ev_end = ev_in[2 * nch];
+  cudaStream_t cs = h->copy_stream, st = h->stream;
+  const size_t wb = (size_t)h->nwin * sizeof(double);
+  if (win) {
+    PF_CUDA(cudaMemcpyAsync(h->wr, wre, wb, cudaMemcpyHostToDevice, st));
+    PF_CUDA(cudaMemcpyAsync(h->wi, wim, wb, cudaMemcpyHostToDevice, st));
+  }
+  for (int c = 0; c < nch; ++c) {
+    const size_t off = (size_t)(zcut[c] * plane), n = (size_t)((zcut[c + 1] - zcut[c]) * plane);
+    PF_CUDA(cudaMemcpyAsync(h->or_ + off, ore + off, n * sizeof(double), cudaMemcpyHostToDevice, cs));
+    PF_CUDA(cudaMemcpyAsync(h->oi_ + off, oim + off, n * sizeof(double), cudaMemcpyHostToDevice, cs));
+    PF_CUDA(cudaEventRecord(ev_in[c], cs));
+  }
+  const int64_t wplane = (int64_t)h->nix * h->niy;
+  auto before = [&](int c) -> int {
+    PF_CUDA(cudaStreamWaitEvent(st, ev_in[c], 0));
+    if (win) {  // inner2Outer of the range's planes (range 0 also writes the mirror plane)
+      const int64_t z0 = zcut[c], nz = zcut[c + 1] - zcut[c];
+      k_window_copy<<<grid_for(wplane * nz, 256), 256, 0, st>>>(
+          h->wr + z0 * wplane, h->wi + z0 * wplane, h->or_ + z0 * plane, h->oi_ + z0 * plane,
+          h->nix, h->niy, nz, p.nx, p.ny, p.nz2, 1, (periodic && c == 0) ? 1 : 0);
+      PF_LAUNCHED(h);
+    }
+    return PF_OK;
+  };
+  auto after = [&](int c) -> int {
+    PF_CUDA(cudaEventRecord(ev_out[c], st));
+    PF_CUDA(cudaStreamWaitEvent(cs, ev_out[c], 0));
+    const size_t off = (size_t)(zcut[c] * plane), n = (size_t)((zcut[c + 1] - zcut[c]) * plane);
+    PF_CUDA(cudaMemcpyAsync(ore + off, h->or_ + off, n * sizeof(double), cudaMemcpyDeviceToHost, cs));
+    PF_CUDA(cudaMemcpyAsync(oim + off, h->oi_ + off, n * sizeof(double), cudaMemcpyDeviceToHost, cs));
+    if (periodic && c == 0) {  // the mirror plane, written with plane 0
+      const size_t mo = (size_t)((p.nz2 - 1) * plane);
+      PF_CUDA(cudaMemcpyAsync(ore + mo, h->or_ + mo, (size_t)plane * sizeof(double),
+                              cudaMemcpyDeviceToHost, cs));
+      PF_CUDA(cudaMemcpyAsync(oim + mo, h->oi_ + mo, (size_t)plane * sizeof(double),
+                              cudaMemcpyDeviceToHost, cs));
+    }
+    return PF_OK;
+  };
+  int rc = pf_diffract_outer_ranges(h, dz, zcut, before, after);
+  if (rc) {
+    cudaStreamSynchronize(cs);
+    cudaStreamSynchronize(st);
+    return rc;
+  }
+  if (win) {  // outer2Inner, then the window goes out
+    k_window_copy<<<grid_for(h->nwin, 256), 256, 0, st>>>(h->wr, h->wi, h->or_, h->oi_, h->nix,
+                                                         h->niy, h->npl, p.nx, p.ny, p.nz2, 0, 0);
+    PF_LAUNCHED(h);
+    PF_CUDA(cudaMemcpyAsync(wre, h->wr, wb, cudaMemcpyDeviceToHost, st));
+    PF_CUDA(cudaMemcpyAsync(wim, h->wi, wb, cudaMemcpyDeviceToHost, st));
+    h->window_valid = true;
+  }
+  PF_CUDA(cudaEventRecord(ev_end, st));
+  PF_CUDA(cudaStreamWaitEvent(cs, ev_end, 0));
+  PF_CUDA(cudaStreamSynchronize(cs));
+  pf_prof_flush(h);
+  return PF_OK;
+}
+
 int pf_wrap_z2(pf_handle *h) {
   if (!h) return PF_BAD_ARG;
   if (h->p.mesh_type != PF_MESH_PERIODIC || h->np == 0) return PF_OK;

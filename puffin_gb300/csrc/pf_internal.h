@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <functional>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -354,6 +355,12 @@ int pf_outer_to_inner(pf_handle *h);
 int pf_inner_to_outer(pf_handle *h);
 // diffraction
 int pf_diffract_outer(pf_handle *h, double dz);
+// the FP64 outer mesh's diffraction with the first and last x passes cut
+// into ranges of z2 planes [zcut[c], zcut[c + 1]): before(c) runs before the
+// first pass reads range c, after(c) once the last pass has written it
+int pf_diffract_outer_ranges(pf_handle *h, double dz, const std::vector<int64_t> &zcut,
+                             const std::function<int(int)> &before,
+                             const std::function<int(int)> &after);
 // inner2Outer + diffraction + outer2Inner queued on the handle's stream
 int pf_diffract_enqueue(pf_handle *h, double dz);
 // save (restore) the particles and the window field of an asynchronous block

@@ -46,7 +46,7 @@ SYMBOLS = (
     "pf_default_params", "pf_create", "pf_destroy", "pf_set_particles", "pf_get_particles",
     "pf_set_particles_dev", "pf_get_particles_dev", "pf_num_particles", "pf_set_field",
     "pf_get_field", "pf_set_field_dev", "pf_get_field_dev", "pf_set_taper", "pf_get_taper",
-    "pf_get_window", "pf_rk4_step", "pf_rk4_step_host", "pf_redistribute", "pf_wrap_z2", "pf_diffract", "pf_run",
+    "pf_get_window", "pf_rk4_step", "pf_rk4_step_host", "pf_diffract_host", "pf_redistribute", "pf_wrap_z2", "pf_diffract", "pf_run",
     "pf_sync", "pf_kernel_launches", "pf_last_error", "pf_abi_version", "pf_get_stream",
     "pf_profile", "pf_profile_read", "pf_rk4_step_noalloc", "pf_power", "pf_num_slices",
     "pf_bunching", "pf_spectrum", "pf_step_count", "pf_set_step_count", "pf_drift",
@@ -109,6 +109,7 @@ def load(build_if_missing: bool = False):
         "pf_window_nodes": (i64, [H]),
         "pf_rk4_step": (ctypes.c_int, [H, f64, f64]),
         "pf_rk4_step_host": (ctypes.c_int, [H, f64, f64] + [ctypes.c_void_p] * 8),
+        "pf_diffract_host": (ctypes.c_int, [H, f64] + [ctypes.c_void_p] * 4),
         "pf_redistribute": (ctypes.c_int, [H]),
         "pf_wrap_z2": (ctypes.c_int, [H]),
         "pf_diffract": (ctypes.c_int, [H, f64]),

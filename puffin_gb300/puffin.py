@@ -213,6 +213,20 @@ class Puffin:
                          allow=(L.PF_OUT_OF_WINDOW, L.PF_OUT_OF_Z2))
         return rc == L.PF_OK
 
+    def diffractIM_host(self, dz: float, outer: tuple, window: tuple):
+        """inner2Outer + diffractIM + outer2Inner on the driver's host arrays
+        (pf_diffract_host): the outer field (re, im) and the window field
+        (re, im), C-contiguous float64, updated in place."""
+        arrs = list(outer) + list(window)
+        for a in arrs:
+            if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags.c_contiguous):
+                raise ValueError("diffractIM_host takes C-contiguous float64 numpy arrays")
+        if any(a.size != self.n_outer for a in arrs[:2]):
+            raise ValueError(f"outer field arrays must hold {self.n_outer} values")
+        if any(a.size != self.n_window for a in arrs[2:]):
+            raise ValueError(f"window field arrays must hold {self.n_window} values")
+        self._check(self._lib.pf_diffract_host(self._h, float(dz), *[a.ctypes.data for a in arrs]))
+
     def redistribute(self):
         self._check(self._lib.pf_redistribute(self._h))
 

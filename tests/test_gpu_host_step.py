@@ -1,8 +1,10 @@
-"""pf_rk4_step_host: rk4par on the driver's host arrays, the copies in and
-out overlapped with the step's kernels (the particles in chunks of 2^20),
-against the device-resident sequence it replaces (set_window_field +
-set_particles with chi kept + rk4par + get_particles + get_window_field):
-bit for bit in FP64, for one chunk and for several; a macroparticle that
+"""pf_rk4_step_host and pf_diffract_host: rk4par and inner2Outer +
+diffractIM + outer2Inner on the driver's host arrays, the copies in and out
+overlapped with the kernels (the particles in chunks of 2^20 or more, the
+outer field by ranges of z2 planes), against the device-resident sequences
+they replace (set_window_field + set_particles with chi kept + rk4par +
+get_particles + get_window_field; set_field + set_window_field + diffractIM
++ get_field + get_window_field): bit for bit in FP64; a macroparticle that
 leaves the window leaves the host arrays and the handle's state as they
 came in."""
 import numpy as np
@@ -11,6 +13,7 @@ import torch
 
 import puffin_gb300 as P
 from puffin_gb300 import configs
+from puffin_gb300 import lib as L
 
 pytestmark = pytest.mark.gpu
 KEYS = P.PARTICLE_KEYS[:6]
@@ -62,7 +65,7 @@ def test_host_step_failure_leaves_arrays_and_state():
         sim.set_field(*field)
         parts = {k: _pinned(w.beam[k]) for k in KEYS}
         wre, wim = (_pinned(v) for v in sim.get_window_field())
-        # a macroparticle of the second chunk far outside the transverse window
+        # a macroparticle of a later chunk far outside the transverse window
         parts["x"][(1 << 20) + 5] = 1.0e3
         before = {k: v.copy() for k, v in parts.items()}
         w_before = (wre.copy(), wim.copy())
@@ -108,3 +111,52 @@ def test_host_step_rejects_mixed_handles():
         wre, wim = (np.ascontiguousarray(v) for v in sim.get_window_field())
         with pytest.raises(RuntimeError):
             sim.rk4par_host(0.0, w.h, parts, (wre, wim))
+
+
+@pytest.mark.parametrize("periodic", [False, True])
+@pytest.mark.parametrize("arith", ["paired", "fp64"])
+def test_host_diffraction_matches_set_diffract_get(periodic, arith):
+    """pf_diffract_host (the outer field in and out by ranges of z2 planes,
+    overlapped with the first and last x passes) against pf_set_field +
+    pf_set_window_field + pf_diffract + pf_get_field + pf_get_window_field,
+    bit for bit, on a 129 x 129 mesh (line kernels cut into plane ranges)."""
+    w = configs.config2(np_=20000, nz2=65)
+    p = P.Params.from_buffer_copy(w.params)
+    if periodic:
+        p.mesh_type = P.MESH_PERIODIC
+    mode = {"paired": L.FFT_PAIRED_FP32, "fp64": L.FFT_FP64}[arith]
+    rng = np.random.default_rng(11)
+    n = p.nx * p.ny * p.nz2
+    ore0, oim0 = 1e-3 * rng.standard_normal(n), 1e-3 * rng.standard_normal(n)
+    with P.Puffin(p) as a, P.Puffin(p) as b:
+        for sim in (a, b):
+            sim.set_fft_arithmetic(mode)
+            sim.set_particles(*(w.beam[k] for k in P.PARTICLE_KEYS))
+            sim.set_field(ore0, oim0)
+        wre0, wim0 = a.get_window_field()
+        wre0 = wre0 + 1e-4 * rng.standard_normal(wre0.size)   # the driver's window differs
+        wim0 = wim0 + 1e-4 * rng.standard_normal(wim0.size)
+        ore, oim = _pinned(ore0), _pinned(oim0)
+        wre, wim = _pinned(wre0), _pinned(wim0)
+        a.diffractIM_host(8 * w.h, (ore, oim), (wre, wim))
+        b.set_window_field(wre0, wim0)
+        b.diffractIM(8 * w.h)
+        fr, fi = b.get_field()
+        gr, gi = b.get_window_field()
+    np.testing.assert_array_equal(ore, fr)
+    np.testing.assert_array_equal(oim, fi)
+    np.testing.assert_array_equal(wre, gr)
+    np.testing.assert_array_equal(wim, gi)
+    assert not np.array_equal(ore, ore0)
+
+
+def test_host_diffraction_rejects_mixed_handles():
+    w = configs.config1(np_=3000, seed=9)
+    q = P.Params.from_buffer_copy(w.params)
+    q.precision = P.MIXED
+    with P.Puffin(q) as sim:
+        sim.set_particles(*(w.beam[k] for k in P.PARTICLE_KEYS))
+        n = q.nx * q.ny * q.nz2
+        wre, wim = (np.ascontiguousarray(v) for v in sim.get_window_field())
+        with pytest.raises(RuntimeError):
+            sim.diffractIM_host(w.h, (np.zeros(n), np.zeros(n)), (wre, wim))
