@@ -677,28 +677,27 @@ def batch_leg(args, dev):
     return out
 
 
-def run_gpu(args, rank, world):
+def e2e_run(r, args, world):
+    """The step loop end to end through the C ABI with host buffers, in
+    UndSection's data flow, continuing the state of the timed leg r: every
+    step hands in the six evolving particle arrays (chi, which rk4par never
+    changes, stays the handle's) and the inner-window field (the arrays
+    rk4par advances) from pinned host memory and takes them back, in one
+    pf_rk4_step_host call that overlaps the copies with the step; every 8th
+    step inner2Outer + diffractIM + outer2Inner take the outer field and the
+    window in and back (FP64: pf_diffract_host, the outer field's copies
+    overlapped with the transforms; mixed: pf_set_field, pf_set_window_field,
+    pf_diffract, pf_get_field, pf_get_window_field).  CUDA events on the
+    library's stream around args.e2e_steps steps, after one untimed block of
+    steps with its diffraction call."""
     import torch
 
     import puffin_gb300 as P
     from puffin_gb300 import lib as L
 
-    dev = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(dev)
-    r64 = _time_path(args, dev, P.FP64, world)
-    w, sim, step, stream, win = r64["w"], r64["sim"], r64["step"], r64["stream"], r64["win"]
-    p = w.params
-    ms = r64["ms"]
+    w, sim, state, stream = r["w"], r["sim"], r["state"], r["stream"]
     every = w.isteps4diff
-
-    # end to end through the C ABI with host buffers, in UndSection's data
-    # flow: every step hands in the six evolving particle arrays (chi, which
-    # rk4par never changes, stays the handle's) and the inner-window field
-    # (the arrays rk4par advances) from pinned host memory and takes them
-    # back, in one pf_rk4_step_host call that overlaps the copies with the
-    # step; every 8th step inner2Outer + diffractIM + outer2Inner take the
-    # outer field and the window in and back (pf_diffract_host, the outer
-    # field's copies overlapped with the transforms)
+    mixed = sim.params.precision == P.MIXED
     n = w.np
     pin = {k: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy() for k in P.PARTICLE_KEYS}
     fre = torch.empty(sim.n_outer, dtype=torch.float64, pin_memory=True).numpy()
@@ -715,21 +714,27 @@ def run_gpu(args, rank, world):
     wre = torch.empty(nw, dtype=torch.float64, pin_memory=True).numpy()
     wim = torch.empty(nw, dtype=torch.float64, pin_memory=True).numpy()
     assert lib.pf_get_window_field(sim._h, wre.ctypes.data, wim.ctypes.data) == 0
-    state64 = r64["state"]
     n_diff = 0
     window_changes = 0
-    torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
     # wall time per call class (every call returns with its work done)
-    e2e_parts = {"step_host": 0.0, "diffract_host": 0.0}
-    t0.record(stream)
-    for _ in range(max(0, args.e2e_steps)):
-        diff = (state64["i"] + 1) % every == 0
+    parts = {"step_host": 0.0, "diffract": 0.0}
+    # one block of steps with its diffraction call untimed first: the fresh
+    # pinned host buffers' first copies and the calls' one-time work
+    n_warm = every if args.e2e_steps > 0 else 0
+    for it in range(n_warm + max(0, args.e2e_steps)):
+        if it == n_warm:
+            torch.cuda.synchronize()
+            if world > 1:
+                torch.distributed.barrier()
+            n_diff = 0
+            window_changes = 0
+            parts = {k: 0.0 for k in parts}
+            t0.record(stream)
+        diff = (state["i"] + 1) % every == 0
         tq = time.perf_counter()
-        rc = lib.pf_rk4_step_host(sim._h, state64["szl"], w.h, *ptrs[:6], wre.ctypes.data,
+        rc = lib.pf_rk4_step_host(sim._h, state["szl"], w.h, *ptrs[:6], wre.ctypes.data,
                                   wim.ctypes.data)
         if rc == L.PF_OUT_OF_WINDOW:
             # the reference's retry: a new window from the particles (the
@@ -740,27 +745,59 @@ def run_gpu(args, rank, world):
             wim = torch.empty(nw, dtype=torch.float64, pin_memory=True).numpy()
             assert lib.pf_get_window_field(sim._h, wre.ctypes.data, wim.ctypes.data) == 0
             window_changes += 1
-            rc = lib.pf_rk4_step_host(sim._h, state64["szl"], w.h, *ptrs[:6], wre.ctypes.data,
+            rc = lib.pf_rk4_step_host(sim._h, state["szl"], w.h, *ptrs[:6], wre.ctypes.data,
                                       wim.ctypes.data)
         assert rc == 0, rc
         tr = time.perf_counter()
-        e2e_parts["step_host"] += tr - tq
-        state64["szl"] += w.h
-        state64["i"] += 1
+        parts["step_host"] += tr - tq
+        state["szl"] += w.h
+        state["i"] += 1
         if diff:
-            assert lib.pf_diffract_host(sim._h, every * w.h, fre.ctypes.data, fim.ctypes.data,
-                                        wre.ctypes.data, wim.ctypes.data) == 0
+            if mixed:
+                assert lib.pf_set_field(sim._h, fre.ctypes.data, fim.ctypes.data) == 0
+                assert lib.pf_set_window_field(sim._h, wre.ctypes.data, wim.ctypes.data) == 0
+                sim.diffractIM(every * w.h)
+                assert lib.pf_get_field(sim._h, fre.ctypes.data, fim.ctypes.data) == 0
+                assert lib.pf_get_window_field(sim._h, wre.ctypes.data, wim.ctypes.data) == 0
+            else:
+                assert lib.pf_diffract_host(sim._h, every * w.h, fre.ctypes.data,
+                                            fim.ctypes.data, wre.ctypes.data,
+                                            wim.ctypes.data) == 0
             n_diff += 1
-        e2e_parts["diffract_host"] += time.perf_counter() - tr
+        parts["diffract"] += time.perf_counter() - tr
+    if args.e2e_steps <= 0:
+        t0.record(stream)
     t1.record(stream)
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
-    e2e_ms = max(t0.elapsed_time(t1), 1e-9)
     k_e2e = max(1, args.e2e_steps)
     h2d = (6 * 8 * n + 2 * 8 * nw) + (2 * 8 * sim.n_outer + 2 * 8 * nw) * n_diff / k_e2e
     d2h = (6 * 8 * n + 2 * 8 * nw) + (2 * 8 * sim.n_outer + 2 * 8 * nw) * n_diff / k_e2e
-    e2e_diff_calls = n_diff
+    return {"ms": max(t0.elapsed_time(t1), 1e-9), "h2d": h2d, "d2h": d2h, "n_diff": n_diff,
+            "window_changes": window_changes, "nw": nw,
+            "parts": {k: 1e3 * v / k_e2e for k, v in parts.items()}}
+
+
+def run_gpu(args, rank, world):
+    import torch
+
+    import puffin_gb300 as P
+    from puffin_gb300 import lib as L
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    r64 = _time_path(args, dev, P.FP64, world)
+    w, sim, step, stream, win = r64["w"], r64["sim"], r64["step"], r64["stream"], r64["win"]
+    p = w.params
+    ms = r64["ms"]
+    every = w.isteps4diff
+
+    n = w.np
+    e2e = e2e_run(r64, args, world)
+    e2e_ms, h2d, d2h = e2e["ms"], e2e["h2d"], e2e["d2h"]
+    e2e_diff_calls, window_changes, e2e_parts = e2e["n_diff"], e2e["window_changes"], e2e["parts"]
+    nw = e2e["nw"]
     sim.close()
 
     # the same FP64 leg with the diffraction FFTs in FP64 arithmetic (the
@@ -770,9 +807,11 @@ def run_gpu(args, rank, world):
     (r64f_ms,) = max_over_ranks([r64f["ms"]], world, f"cuda:{dev}")
 
     rmx = None
+    e2e_mx = None
     c3 = None
     if not args.no_mixed:
         rmx = _time_path(args, dev, P.MIXED, world)
+        e2e_mx = e2e_run(rmx, args, world) if args.e2e_steps > 0 else None
         rmx["sim"].close()
         if args.np3 > 0:
             c3 = {}
@@ -784,6 +823,8 @@ def run_gpu(args, rank, world):
     fid = fidelity_leg(args, dev) if args.fidelity_np > 0 and not args.no_mixed else None
     adj = adjoint_leg(args, dev) if args.adjoint_steps > 0 else None
     bat = batch_leg(args, dev) if args.batch_n > 0 else None
+    if rmx and e2e_mx:
+        (e2e_mx["ms"],) = max_over_ranks([e2e_mx["ms"]], world, f"cuda:{dev}")
     ms, e2e_ms, mx_ms, c3_64_ms, c3_mx_ms = max_over_ranks(
         [ms, e2e_ms, rmx["ms"] if rmx else 0.0, c3["fp64"]["ms"] if c3 else 0.0,
          c3["mixed"]["ms"] if c3 else 0.0], world, f"cuda:{dev}")
@@ -827,8 +868,7 @@ def run_gpu(args, rank, world):
                             "outer field and the window in and out around each "
                             "diffraction call through pf_diffract_host",
                 "api": "pf_rk4_step_host + pf_diffract_host",
-                "ms_per_step_by_call": {k: 1e3 * v / max(1, args.e2e_steps)
-                                        for k, v in e2e_parts.items()}},
+                "ms_per_step_by_call": e2e_parts},
         "fft_arithmetic": {
             "value_leg": "paired FP32 (48-bit significands; the field stays FP64 in HBM)",
             "fp64_arithmetic": {"value": whole_job_rate(n, args.steps, world, r64f_ms),
@@ -868,6 +908,15 @@ def run_gpu(args, rank, world):
                          "peak": peak, "unit": "GB/s", "frac": m_ach / peak},
             "clocks": rmx["clocks"],
         }
+        if e2e_mx:
+            rec["mixed"]["e2e"] = {
+                "value": whole_job_rate(n, args.e2e_steps, world, e2e_mx["ms"]), "unit": UNIT,
+                "h2d_bytes_per_step": e2e_mx["h2d"], "d2h_bytes_per_step": e2e_mx["d2h"],
+                "steps": args.e2e_steps, "diffraction_calls": e2e_mx["n_diff"],
+                "speedup_vs_fp64_e2e": e2e_ms / e2e_mx["ms"],
+                "api": "pf_rk4_step_host + pf_set_field / pf_set_window_field / pf_diffract / "
+                       "pf_get_field / pf_get_window_field",
+                "ms_per_step_by_call": e2e_mx["parts"]}
     if fid:
         rec["mixed_fidelity"] = fid
     if adj:

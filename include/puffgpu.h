@@ -185,7 +185,7 @@ int pf_get_window(const pf_handle *h, int32_t *nix, int32_t *niy);
  * PF_OUT_OF_WINDOW / PF_OUT_OF_Z2 with the state unchanged. */
 int pf_rk4_step(pf_handle *h, double szl, double hstep);
 
-/* One rk4par step with the driver's arrays in host memory (FP64 handles):
+/* One rk4par step with the driver's arrays in host memory:
  * the six evolving particle arrays (pf_get_particles' order; chi stays the
  * handle's, as rk4par never changes it) and the inner-window field
  * (pf_window_nodes() values each) are read, advanced by one step and written
@@ -193,7 +193,9 @@ int pf_rk4_step(pf_handle *h, double szl, double hstep);
  * + pf_rk4_step + pf_get_particles + pf_get_window_field, without choosing
  * the window again: the copies in and out run on a second stream,
  * overlapped with the step's kernels (the particles in chunks), so page-
- * locked host arrays are copied while the step computes.  Returns PF_OK, or
+ * locked host arrays are copied while the step computes (on mixed
+ * handles the window field is converted to and from its complex-float form
+ * on the device, as pf_set/get_window_field do).  Returns PF_OK, or
  * PF_OUT_OF_WINDOW / PF_OUT_OF_Z2 / PF_OVERFLOW / PF_NOT_FINITE with the
  * host arrays and the handle's state holding the step's input (then
  * pf_redistribute and pf_get_window_field give the driver the new window,

@@ -1075,11 +1075,6 @@ int pf_rk4_step_host(pf_handle *h, double szl, double hstep, double *x, double *
     h->err = "pf_rk4_step_host: particles not set";
     return PF_STATE;
   }
-  if (h->p.precision != PF_FP64) {
-    h->err = "pf_rk4_step_host runs on FP64 handles (mixed: pf_set_particles, "
-             "pf_set_window_field, pf_rk4_step and the getters)";
-    return PF_BAD_ARG;
-  }
   cudaSetDevice(h->dev);
   // the arrays come in the caller's order: a z2-ordered handle's chi
   // follows them back
@@ -1090,7 +1085,8 @@ int pf_rk4_step_host(pf_handle *h, double szl, double hstep, double *x, double *
   }
   double *const host[6] = {x, y, z2, px, py, gam};
   unsigned int st = 0;
-  int rc = pf_rk4_fp64_host(h, szl, hstep, host, wre, wim, &st);
+  int rc = (h->p.precision == PF_MIXED) ? pf_rk4_mixed_host(h, szl, hstep, host, wre, wim, &st)
+                                         : pf_rk4_fp64_host(h, szl, hstep, host, wre, wim, &st);
   if (rc) return rc;
   h->window_valid = true;
   rc = status_to_rc(st);

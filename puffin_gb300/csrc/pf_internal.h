@@ -283,6 +283,8 @@ int pf_rk4_fp64(pf_handle *h, double szl, double hstep, unsigned int *status_out
 // status word (the host arrays hold the step's input again when it is set)
 int pf_rk4_fp64_host(pf_handle *h, double szl, double hstep, double *const host[6], double *wre,
                      double *wim, unsigned int *status_out);
+int pf_rk4_mixed_host(pf_handle *h, double szl, double hstep, double *const host[6], double *wre,
+                      double *wim, unsigned int *status_out);
 // building blocks of the FP64 step for other drivers (the adjoint)
 void pf_fill_stage_args(pf_handle *h, StageArgs &a, double h6);
 int pf_launch_stage(pf_handle *h, int stage, StageArgs &a);   // k_stage<stage>

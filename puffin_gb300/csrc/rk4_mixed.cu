@@ -940,6 +940,161 @@ int pf_rk4_mixed(pf_handle *h, double szl, double hstep, unsigned int *status_ou
   return PF_OK;
 }
 
+namespace {
+// FP64 split window field <-> the interleaved complex-float window, as
+// pf_set_window_field and pf_get_window_field convert it
+__global__ void k_win_in_c32(float2 *w, const double *re, const double *im, int64_t n) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) w[t] = make_float2((float)re[t], (float)im[t]);
+}
+__global__ void k_win_out_c32(const float2 *w, double *re, double *im, int64_t n) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) {
+    const float2 v = w[t];
+    re[t] = (double)v.x;
+    im[t] = (double)v.y;
+  }
+}
+}  // namespace
+
+// The mixed step with the driver's arrays in host memory: the copies of
+// pf_rk4_fp64_host (the window field first, the particles by chunks that
+// stage 1 starts on as they arrive, stage 4's output leaving chunk by
+// chunk), the window field converted to and from its complex-float form
+// on the device through the staging buffer.
+int pf_rk4_mixed_host(pf_handle *h, double szl, double hstep, double *const host[6], double *wre,
+                      double *wim, unsigned int *status_out) {
+  const pf_params &p = h->p;
+  const double hh = hstep * 0.5, szh = szl + hh;
+  const double stage_sz[4] = {szl, szh, szh, szl + hstep};
+  const int cur = h->cur, nxt = cur ^ 1;
+  const int64_t np = h->np, nw = h->nwin;
+  const int64_t chunk = std::max<int64_t>((int64_t)1 << 20, (np + 15) / 16);
+  const int nch = (int)std::max<int64_t>(1, (np + chunk - 1) / chunk);
+  if (!h->copy_stream)
+    PF_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+  while ((int)h->copy_events.size() < 2 * nch + 1) {
+    cudaEvent_t e;
+    PF_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    h->copy_events.push_back(e);
+  }
+  if (!h->staging) PF_CUDA(cudaMalloc(&h->staging, 2 * sizeof(double) * (size_t)h->nouter));
+  cudaEvent_t *ev_in = h->copy_events.data(), *ev_out = ev_in + nch, ev_w = ev_in[2 * nch];
+  cudaStream_t cs = h->copy_stream, st = h->stream;
+  const size_t wb = (size_t)nw * sizeof(double);
+  const unsigned gw = (unsigned)std::max<int64_t>(1, (nw + 255) / 256);
+
+  PF_CUDA(cudaMemsetAsync(h->d_status, 0, sizeof(unsigned int), st));
+  PF_CUDA(cudaMemcpyAsync(h->staging, wre, wb, cudaMemcpyHostToDevice, st));
+  PF_CUDA(cudaMemcpyAsync(h->staging + nw, wim, wb, cudaMemcpyHostToDevice, st));
+  k_win_in_c32<<<gw, 256, 0, st>>>((float2 *)h->w32, h->staging, h->staging + nw, nw);
+  PF_LAUNCHED(h);
+  for (int c = 0; c < nch; ++c) {
+    const int64_t off = c * chunk, len = std::min(chunk, np - off);
+    for (int j = 0; j < 6; ++j)
+      PF_CUDA(cudaMemcpyAsync(h->y[cur][j] + off, host[j] + off, (size_t)len * sizeof(double),
+                              cudaMemcpyHostToDevice, cs));
+    PF_CUDA(cudaEventRecord(ev_in[c], cs));
+  }
+
+  MixArgs a;
+  fill_mix_args(h, a, hstep);
+  bool wide = false;
+  const size_t smem = mixed_stage_smem(h, a, &wide);
+  MixNodeArgs n;
+  fill_mix_nodes(h, n, 1, hstep);
+  PF_CUDA(mixed_attrs());
+  a.ppt = mixed_ppt(h);
+  const int64_t per_block = (int64_t)MX_THREADS * a.ppt;
+  const bool oned = p.one_d != 0;
+  // the stage arguments of macroparticles [off, off + len)
+  auto range = [](const MixArgs &b, int64_t off, int64_t len) {
+    MixArgs r = b;
+    r.x += off;
+    r.y += off;
+    r.z2 += off;
+    r.px += off;
+    r.py += off;
+    r.gam += off;
+    r.chi_f += off;
+    r.base4 += off;
+    for (int j = 0; j < 6; ++j) {
+      if (r.kin_f[j]) r.kin_f[j] += off;
+      if (r.kout_f[j]) r.kout_f[j] += off;
+      if (r.kacc_f[j]) r.kacc_f[j] += off;
+      if (r.k1_f[j]) r.k1_f[j] += off;
+      if (r.ynext[j]) r.ynext[j] += off;
+    }
+    if (r.kin_z) r.kin_z += off;
+    if (r.kout_z) r.kout_z += off;
+    if (r.kacc_z) r.kacc_z += off;
+    if (r.k1_z) r.k1_z += off;
+    r.np = len;
+    return r;
+  };
+  for (int s = 1; s <= 4; ++s) {
+    double n2col;
+    int place;
+    pf_taper_stage(h, stage_sz[s - 1], &n2col, &place);
+    BFieldCoef bf;
+    pf_stage_coefficients(p, stage_sz[s - 1], n2col, place, &bf);
+    a.bf = to_float(bf);
+    a.n2col = (float)n2col;
+    a.kn2col = (float)(p.kappa * n2col);
+    mix_stage_pointers(h, a, s, cur, hstep);
+    if (np > 0) {
+      if (s == 1 || s == 4) {
+        for (int c = 0; c < nch; ++c) {
+          const int64_t off = c * chunk, len = std::min(chunk, np - off);
+          if (s == 1) PF_CUDA(cudaStreamWaitEvent(st, ev_in[c], 0));
+          const MixArgs r = range(a, off, len);
+          launch_mixed_stage(h, s, r, (unsigned)((len + per_block - 1) / per_block), smem, wide,
+                             oned);
+          PF_LAUNCHED(h);
+          if (s == 4) {
+            PF_CUDA(cudaEventRecord(ev_out[c], st));
+            PF_CUDA(cudaStreamWaitEvent(cs, ev_out[c], 0));
+            for (int j = 0; j < 6; ++j)
+              PF_CUDA(cudaMemcpyAsync(host[j] + off, h->y[nxt][j] + off,
+                                      (size_t)len * sizeof(double), cudaMemcpyDeviceToHost, cs));
+          }
+        }
+      } else {
+        launch_mixed_stage(h, s, a, (unsigned)std::max<int64_t>(1, (np + per_block - 1) / per_block),
+                           smem, wide, oned);
+        PF_LAUNCHED(h);
+      }
+    }
+    n.coef = (float)((s == 3) ? hstep : hh);
+    switch (s) {
+      case 1: k_nodes_mixed<1><<<gw, 256, 0, st>>>(n); break;
+      case 2: k_nodes_mixed<2><<<gw, 256, 0, st>>>(n); break;
+      case 3: k_nodes_mixed<3><<<gw, 256, 0, st>>>(n); break;
+      default: k_nodes_mixed<4><<<gw, 256, 0, st>>>(n); break;
+    }
+    PF_LAUNCHED(h);
+  }
+  k_win_out_c32<<<gw, 256, 0, st>>>((const float2 *)h->w32, h->staging, h->staging + nw, nw);
+  PF_LAUNCHED(h);
+  PF_CUDA(cudaMemcpyAsync(wre, h->staging, wb, cudaMemcpyDeviceToHost, st));
+  PF_CUDA(cudaMemcpyAsync(wim, h->staging + nw, wb, cudaMemcpyDeviceToHost, st));
+  PF_CUDA(cudaMemcpyAsync(h->h_status, h->d_status, sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                          st));
+  PF_CUDA(cudaEventRecord(ev_w, st));
+  PF_CUDA(cudaStreamWaitEvent(cs, ev_w, 0));
+  PF_CUDA(cudaStreamSynchronize(cs));
+  *status_out = *h->h_status;
+  if (*status_out == 0u) {
+    h->cur = nxt;
+    return PF_OK;
+  }
+  for (int j = 0; j < 6; ++j)
+    PF_CUDA(cudaMemcpyAsync(host[j], h->y[cur][j], (size_t)np * sizeof(double),
+                            cudaMemcpyDeviceToHost, st));
+  PF_CUDA(cudaStreamSynchronize(st));
+  return PF_OK;
+}
+
 // One stage of the mixed step on explicit arrays (the adjoint's recorded
 // forward): the stage roles and arithmetic of pf_rk4_mixed, the b-field and
 // taper of position sz.

@@ -195,9 +195,10 @@ class Puffin:
     rk4_step = rk4par
 
     def rk4par_host(self, szl: float, h: float, particles: dict, window: tuple) -> bool:
-        """One RK4 step on the driver's host arrays (pf_rk4_step_host): the
-        float64 arrays particles["x"] .. particles["gam"] and the window field
-        (re, im), advanced in place, the copies overlapped with the step.
+        """One RK4 step on the driver's host arrays (pf_rk4_step_host; FP64
+        and mixed handles): the float64 arrays particles["x"] ..
+        particles["gam"] and the window field (re, im), advanced in place,
+        the copies overlapped with the step.
         False (arrays and state as they came in) if a particle left the
         window or the mesh."""
         arrs = [particles[k] for k in PARTICLE_KEYS[:6]] + list(window)

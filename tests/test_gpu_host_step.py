@@ -101,16 +101,33 @@ def test_host_step_after_z2_ordering_keeps_chi_with_the_caller_order():
         np.testing.assert_allclose(parts[k], got_b[k], rtol=0, atol=0, err_msg=k)
 
 
-def test_host_step_rejects_mixed_handles():
-    w = configs.config1(np_=3000, seed=8)
+def test_host_step_mixed_matches_resident_steps():
+    """The mixed form (window field converted to and from complex float on
+    the device): the same steps as the five-call sequence, to the rounding
+    of the FP32 float atomics (chunked launches cut the stage blocks, and
+    so the split between shared tile and HBM deposits, differently)."""
+    w = configs.config1(np_=(1 << 21) + 12345, seed=8)
     q = P.Params.from_buffer_copy(w.params)
     q.precision = P.MIXED
-    with P.Puffin(q) as sim:
-        sim.set_particles(*(w.beam[k] for k in P.PARTICLE_KEYS))
-        parts = {k: np.ascontiguousarray(w.beam[k], dtype=np.float64) for k in KEYS}
-        wre, wim = (np.ascontiguousarray(v) for v in sim.get_window_field())
-        with pytest.raises(RuntimeError):
-            sim.rk4par_host(0.0, w.h, parts, (wre, wim))
+    field = _field(w.params, 8)
+    with P.Puffin(q) as a, P.Puffin(q) as b:
+        for sim in (a, b):
+            sim.set_particles(*(w.beam[k] for k in P.PARTICLE_KEYS))
+            sim.set_field(*field)
+        parts = {k: _pinned(w.beam[k]) for k in KEYS}
+        wre, wim = (_pinned(v) for v in a.get_window_field())
+        szl = 0.0
+        for _ in range(3):
+            assert a.rk4par_host(szl, w.h, parts, (wre, wim))
+            assert b.rk4par(szl, w.h)
+            szl += w.h
+        got_b = b.get_particles()
+        wb = b.get_window_field()
+    for k in KEYS:
+        np.testing.assert_allclose(parts[k], got_b[k], rtol=1e-9, atol=1e-12, err_msg=k)
+    scale = max(np.max(np.abs(wb[0])), np.max(np.abs(wb[1])))
+    np.testing.assert_allclose(wre, wb[0], rtol=0, atol=1e-5 * scale)
+    np.testing.assert_allclose(wim, wb[1], rtol=0, atol=1e-5 * scale)
 
 
 @pytest.mark.parametrize("periodic", [False, True])
