@@ -123,8 +123,10 @@ def test_host_step_mixed_matches_resident_steps():
             szl += w.h
         got_b = b.get_particles()
         wb = b.get_window_field()
+    # the FP32 slopes of macroparticles whose deposits rounded differently
+    # differ by FP32 roundings (3e-8 relative) times the step
     for k in KEYS:
-        np.testing.assert_allclose(parts[k], got_b[k], rtol=1e-9, atol=1e-12, err_msg=k)
+        np.testing.assert_allclose(parts[k], got_b[k], rtol=1e-7, atol=1e-8, err_msg=k)
     scale = max(np.max(np.abs(wb[0])), np.max(np.abs(wb[1])))
     np.testing.assert_allclose(wre, wb[0], rtol=0, atol=1e-5 * scale)
     np.testing.assert_allclose(wim, wb[1], rtol=0, atol=1e-5 * scale)
