@@ -685,9 +685,9 @@ def e2e_run(r, args, world):
     rk4par advances) from pinned host memory and takes them back, in one
     pf_rk4_step_host call that overlaps the copies with the step; every 8th
     step inner2Outer + diffractIM + outer2Inner take the outer field and the
-    window in and back (FP64: pf_diffract_host, the outer field's copies
-    overlapped with the transforms; mixed: pf_set_field, pf_set_window_field,
-    pf_diffract, pf_get_field, pf_get_window_field).  CUDA events on the
+    window in and back in one pf_diffract_host call, the outer field's copies
+    overlapped with the transforms (a mixed handle converts the FP64 arrays
+    to and from its complex-float field on the device).  CUDA events on the
     library's stream around args.e2e_steps steps, after one untimed block of
     steps with its diffraction call."""
     import torch
@@ -697,7 +697,6 @@ def e2e_run(r, args, world):
 
     w, sim, state, stream = r["w"], r["sim"], r["state"], r["stream"]
     every = w.isteps4diff
-    mixed = sim.params.precision == P.MIXED
     n = w.np
     pin = {k: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy() for k in P.PARTICLE_KEYS}
     fre = torch.empty(sim.n_outer, dtype=torch.float64, pin_memory=True).numpy()
@@ -753,16 +752,8 @@ def e2e_run(r, args, world):
         state["szl"] += w.h
         state["i"] += 1
         if diff:
-            if mixed:
-                assert lib.pf_set_field(sim._h, fre.ctypes.data, fim.ctypes.data) == 0
-                assert lib.pf_set_window_field(sim._h, wre.ctypes.data, wim.ctypes.data) == 0
-                sim.diffractIM(every * w.h)
-                assert lib.pf_get_field(sim._h, fre.ctypes.data, fim.ctypes.data) == 0
-                assert lib.pf_get_window_field(sim._h, wre.ctypes.data, wim.ctypes.data) == 0
-            else:
-                assert lib.pf_diffract_host(sim._h, every * w.h, fre.ctypes.data,
-                                            fim.ctypes.data, wre.ctypes.data,
-                                            wim.ctypes.data) == 0
+            assert lib.pf_diffract_host(sim._h, every * w.h, fre.ctypes.data, fim.ctypes.data,
+                                        wre.ctypes.data, wim.ctypes.data) == 0
             n_diff += 1
         parts["diffract"] += time.perf_counter() - tr
     if args.e2e_steps <= 0:
@@ -914,8 +905,7 @@ def run_gpu(args, rank, world):
                 "h2d_bytes_per_step": e2e_mx["h2d"], "d2h_bytes_per_step": e2e_mx["d2h"],
                 "steps": args.e2e_steps, "diffraction_calls": e2e_mx["n_diff"],
                 "speedup_vs_fp64_e2e": e2e_ms / e2e_mx["ms"],
-                "api": "pf_rk4_step_host + pf_set_field / pf_set_window_field / pf_diffract / "
-                       "pf_get_field / pf_get_window_field",
+                "api": "pf_rk4_step_host + pf_diffract_host",
                 "ms_per_step_by_call": e2e_mx["parts"]}
     if fid:
         rec["mixed_fidelity"] = fid

@@ -204,7 +204,9 @@ int pf_rk4_step_host(pf_handle *h, double szl, double hstep, double *x, double *
                      double *px, double *py, double *gam, double *wre, double *wim);
 
 /* inner2Outer + diffractIM + outer2Inner with the driver's arrays in host
- * memory (FP64 handles): the outer field (nx * ny * nz2 values each) and,
+ * memory (FP64 and mixed handles; a mixed handle converts them to and from
+ * its complex-float field on the device with pf_set_field's and
+ * pf_get_field's roundings): the outer field (nx * ny * nz2 values each) and,
  * when the handle has a window, the inner-window field (pf_window_nodes()
  * values each) are read and written in place, as pf_set_field +
  * pf_set_window_field + pf_diffract + pf_get_field + pf_get_window_field

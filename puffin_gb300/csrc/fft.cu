@@ -93,9 +93,14 @@ int pf_diffract_outer_ranges(pf_handle *h, double dz, const std::vector<int64_t>
                              const std::function<int(int)> &before,
                              const std::function<int(int)> &after) {
   if (!h->diff) h->diff = new DiffPlan();
+  if (h->p.precision == PF_MIXED)
+    return fft32::diffract_ranges(h, h->diff->p32, nullptr, nullptr, (fft32::cplx *)h->oc32, dz,
+                                  zcut, before, after);
   if (h->fft_pairs)
-    return fftdd::diffract_ranges(h, h->diff->pdd, h->or_, h->oi_, dz, zcut, before, after);
-  return fft64::diffract_ranges(h, h->diff->p64, h->or_, h->oi_, dz, zcut, before, after);
+    return fftdd::diffract_ranges(h, h->diff->pdd, h->or_, h->oi_, nullptr, dz, zcut, before,
+                                  after);
+  return fft64::diffract_ranges(h, h->diff->p64, h->or_, h->oi_, nullptr, dz, zcut, before,
+                                after);
 }
 
 int pf_diffract_adjoint_split(pf_handle *h, double *re, double *im, double dz) {

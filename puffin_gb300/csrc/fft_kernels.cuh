@@ -92,6 +92,7 @@ struct FftArgs {
   int mirror;    // periodic: also write plane nz (mirror of plane 0) of the output
   // four-step z2 transform: w_N^(b k1) at [k1 * N2 + b], forward and backward
   const cplx *tw4f, *tw4b;
+  int z0;        // the transverse-plane kernel runs planes z0 + blockIdx.x
 };
 
 __device__ __forceinline__ int64_t line_base(const AxisPlan &p, int64_t L) {
@@ -900,7 +901,7 @@ __global__ void __launch_bounds__(PT, 1) k_fft_plane(const FftArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx *buf = reinterpret_cast<cplx *>(smem_raw);
   constexpr int plane = NX * NY;
-  const int z = blockIdx.x;
+  const int z = a.z0 + blockIdx.x;
   const int64_t off = (int64_t)z * plane;
   for (int t = threadIdx.x; t < plane; t += PT) load_async(buf + t, a, off + t);
   cp_async_wait_all();
@@ -1554,15 +1555,15 @@ static int run_schedule(pf_handle *h, Plan *d, const FftArgs &a, bool split, boo
   return PF_OK;
 }
 
-// The diffraction step of diffract() on split re/im arrays, with the first
-// and the last pass over x cut into ranges of z2 planes [zcut[c],
-// zcut[c + 1]) (an x line lies in one plane: line y + ny z): before(c) runs
-// before the first pass reads range c, after(c) once the last pass has
-// written it (range 0 also carries the periodic mirror plane).  The other
-// passes run whole.  Meshes whose transverse passes are one plane kernel
-// run whole too: every before() first, every after() at the end.
-static int diffract_ranges(pf_handle *h, Plan *&plan, io_real *re, io_real *im, double dz,
-                           const std::vector<int64_t> &zcut,
+// The diffraction step of diffract() (split re/im arrays, or the
+// interleaved complex mesh oc when re is null), with the first and the last
+// transverse pass cut into ranges of z2 planes [zcut[c], zcut[c + 1]): the
+// x passes of the line kernels (an x line lies in one plane: line y + ny z)
+// or the plane kernel's passes.  before(c) runs before the first pass reads
+// range c, after(c) once the last pass has written it (range 0 also carries
+// the periodic mirror plane).  The other passes run whole.
+static int diffract_ranges(pf_handle *h, Plan *&plan, io_real *re, io_real *im, cplx *oc,
+                           double dz, const std::vector<int64_t> &zcut,
                            const std::function<int(int)> &before,
                            const std::function<int(int)> &after) {
   const pf_params &p = h->p;
@@ -1572,60 +1573,79 @@ static int diffract_ranges(pf_handle *h, Plan *&plan, io_real *re, io_real *im, 
   }
   Plan *d = plan;
   const int nch = (int)zcut.size() - 1;
-  if (d->plane || d->ax[0].n == 1) {
+  const bool split = (re != nullptr);
+  if (!d->plane && d->ax[0].n == 1) {  // no transverse pass to cut: run whole
     for (int c = 0; c < nch; ++c) {
       const int rc = before(c);
       if (rc) return rc;
     }
-    int rc = diffract(h, plan, re, im, nullptr, dz);
+    int rc = diffract(h, plan, re, im, oc, dz);
     for (int c = 0; c < nch && rc == PF_OK; ++c) rc = after(c);
     return rc;
   }
   FftArgs a;
-  base_args(h, d, re, im, nullptr, a);
+  base_args(h, d, re, im, oc, a);
   const int64_t ntab = (int64_t)(d->nx + d->ny) * d->nz;
   pf_prof_begin(h, PROF_DIFF);
   k_tables<<<(unsigned)((ntab + 255) / 256), 256, 0, h->stream>>>(
       d->px, d->py, d->dxt, d->dyt, d->kx, d->ky, d->kz, d->nx, d->ny, d->nz, dz, dz, p.sbeta);
   pf_prof_end(h);
   PF_LAUNCHED(h);
-  // x lines of the planes of range c
-  auto x_range = [&](FftArgs b, int c) {
-    b.ax = d->ax[0];
-    b.ax.line0 = (int64_t)d->ny * zcut[c];
-    b.ax.nlines = (int64_t)d->ny * zcut[c + 1];
-    const int64_t blocks = (b.ax.nlines - b.ax.line0 + b.ax.lpb - 1) / b.ax.lpb;
-    if (blocks <= 0) return PF_OK;
+  // the first or last transverse pass over the planes of range c
+  auto range_pass = [&](FftArgs b, int c) {
+    const int64_t z0 = zcut[c], z1 = zcut[c + 1];
+    if (z1 <= z0) return PF_OK;
     pf_prof_begin(h, PROF_FFT);
-    k_fft<<<(unsigned)blocks, NTHREADS, d->smem[0], h->stream>>>(b);
+    if (d->plane) {
+      b.ax = d->ax[0];
+      b.ay = d->ax[1];
+      b.z0 = (int)z0;
+      d->plane<<<(unsigned)(z1 - z0), PT, d->plane_smem, h->stream>>>(b);
+    } else {
+      b.ax = d->ax[0];
+      b.ax.line0 = (int64_t)d->ny * z0;
+      b.ax.nlines = (int64_t)d->ny * z1;
+      const int64_t blocks = (b.ax.nlines - b.ax.line0 + b.ax.lpb - 1) / b.ax.lpb;
+      k_fft<<<(unsigned)blocks, NTHREADS, d->smem[0], h->stream>>>(b);
+    }
     pf_prof_end(h);
     PF_LAUNCHED(h);
     return PF_OK;
   };
   struct Step {
-    int axis, dir, mid, second, load_split, store_split;
+    int transverse, axis, dir, mid, second, load_split, store_split;
   };
-  const Step steps[9] = {
-      {0, 0, MID_NONE, 0, 1, 0},   {1, 0, MID_NONE, 0, 0, 0}, {2, 0, MID_PROP, 1, 0, 0},
-      {1, 1, MID_NONE, 0, 0, 0},   {0, 1, MID_SPLIT, 1, 0, 0}, {1, 0, MID_NONE, 0, 0, 0},
-      {2, 0, MID_DAMP, 1, 0, 0},   {1, 1, MID_NONE, 0, 0, 0}, {0, 1, MID_RECOMB, 0, 0, 1},
+  // the schedules of run_schedule: five passes with the plane kernel, nine
+  // with the line kernels
+  const Step plane_steps[5] = {
+      {1, 0, 0, MID_NONE, 0, 1, 0}, {0, 2, 0, MID_PROP, 1, 0, 0}, {1, 0, 1, MID_SPLIT, 1, 0, 0},
+      {0, 2, 0, MID_DAMP, 1, 0, 0}, {1, 0, 1, MID_RECOMB, 0, 0, 1},
   };
-  for (int k = 0; k < 9; ++k) {
+  const Step line_steps[9] = {
+      {1, 0, 0, MID_NONE, 0, 1, 0},   {0, 1, 0, MID_NONE, 0, 0, 0}, {0, 2, 0, MID_PROP, 1, 0, 0},
+      {0, 1, 1, MID_NONE, 0, 0, 0},   {0, 0, 1, MID_SPLIT, 1, 0, 0}, {0, 1, 0, MID_NONE, 0, 0, 0},
+      {0, 2, 0, MID_DAMP, 1, 0, 0},   {0, 1, 1, MID_NONE, 0, 0, 0}, {1, 0, 1, MID_RECOMB, 0, 0, 1},
+  };
+  const Step *steps = d->plane ? plane_steps : line_steps;
+  const int nsteps = d->plane ? 5 : 9;
+  for (int k = 0; k < nsteps; ++k) {
     const Step &st = steps[k];
     FftArgs b = a;
     b.dir = st.dir;
     b.mid = st.mid;
     b.second = st.second;
-    b.load_split = st.load_split;
-    b.store_split = st.store_split;
+    b.load_split = split && st.load_split;
+    b.store_split = split && st.store_split;
     b.mirror = a.mirror && st.store_split;
     int rc = PF_OK;
-    if (k == 0 || k == 8) {
+    if (k == 0 || k == nsteps - 1) {
       for (int c = 0; c < nch && rc == PF_OK; ++c) {
         if (k == 0) rc = before(c);
-        if (rc == PF_OK) rc = x_range(b, c);
-        if (k == 8 && rc == PF_OK) rc = after(c);
+        if (rc == PF_OK) rc = range_pass(b, c);
+        if (k == nsteps - 1 && rc == PF_OK) rc = after(c);
       }
+    } else if (st.transverse) {
+      rc = plane_pass(h, d, b);
     } else {
       rc = fft_pass(h, d, b, st.axis);
     }

@@ -519,6 +519,7 @@ int pf_destroy(pf_handle *h) {
   cudaFree(h->oi_);
   cudaFree(h->oc32);
   cudaFree(h->staging);
+  cudaFree(h->wstage);
   cudaFree(h->diag);
   cudaFree(h->lat_scratch);
   cudaFree(h->snap);
@@ -1098,27 +1099,25 @@ int pf_rk4_step_host(pf_handle *h, double szl, double hstep, double *x, double *
 }
 
 // inner2Outer + diffractIM + outer2Inner with the driver's arrays in host
-// memory (FP64 handles): the window field goes in first; the outer field
-// goes in by ranges of z2 planes on the copy stream, each range's window
-// planes are copied into it and the first x pass runs on it as it arrives;
-// the last x pass writes the outer field range by range and each range goes
+// memory: the window field goes in first; the outer field goes in by ranges
+// of z2 planes on the copy stream, each range's window planes are copied
+// into it and the first transverse pass runs on it as it arrives; the last
+// transverse pass writes the outer field range by range and each range goes
 // out while the next is computed; the window field comes back from the
-// diffracted field last.
+// diffracted field last.  On a mixed handle the FP64 arrays are converted to
+// and from the complex-float field on the device (the outer field through
+// the staging buffer, the window through its own).
 int pf_diffract_host(pf_handle *h, double dz, double *ore, double *oim, double *wre,
                      double *wim) {
   if (!h || !ore || !oim) return PF_BAD_ARG;
-  if (h->p.precision != PF_FP64) {
-    h->err = "pf_diffract_host runs on FP64 handles (mixed: pf_set_field, pf_diffract, "
-             "pf_get_field)";
-    return PF_BAD_ARG;
-  }
   // the driver's window arrays are the window state whenever there is one
   const bool win = h->nwin > 0;
   if (win && (!wre || !wim)) return PF_BAD_ARG;
   cudaSetDevice(h->dev);
   const pf_params &p = h->p;
+  const bool mixed = (p.precision == PF_MIXED);
   const bool periodic = (p.mesh_type == PF_MESH_PERIODIC);
-  const int64_t plane = (int64_t)p.nx * p.ny;
+  const int64_t plane = (int64_t)p.nx * p.ny, no = h->nouter;
   const int64_t nzf = periodic ? p.nz2 - 1 : p.nz2;  // planes the transforms run over
   const int nch = (int)std::max<int64_t>(1, std::min<int64_t>(8, nzf));
   std::vector<int64_t> zcut((size_t)nch + 1);
@@ -1129,42 +1128,83 @@ int pf_diffract_host(pf_handle *h, double dz, double *ore, double *oim, double *
     PF_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     h->copy_events.push_back(e);
   }
+  // mixed: the FP64 outer field passes through the staging buffer (re then
+  // im, nouter each) and the window through its own, converted on the device
+  if (mixed && !h->staging) PF_CUDA(cudaMalloc(&h->staging, 2 * sizeof(double) * (size_t)no));
+  if (mixed && win && h->wstage_cap < h->nwin) {
+    cudaFree(h->wstage);
+    h->wstage = nullptr;
+    h->wstage_cap = 0;
+    PF_CUDA(cudaMalloc(&h->wstage, 2 * sizeof(double) * (size_t)h->nwin));
+    h->wstage_cap = h->nwin;
+  }
+  double *dre = mixed ? h->staging : h->or_, *dim = mixed ? h->staging + no : h->oi_;
+  float2 *oc = (float2 *)h->oc32, *w32 = (float2 *)h->w32;
   cudaEvent_t *ev_in = h->copy_events.data(), *ev_out = ev_in + nch, ev_end = ev_in[2 * nch];
   cudaStream_t cs = h->copy_stream, st = h->stream;
   const size_t wb = (size_t)h->nwin * sizeof(double);
   if (win) {
-    PF_CUDA(cudaMemcpyAsync(h->wr, wre, wb, cudaMemcpyHostToDevice, st));
-    PF_CUDA(cudaMemcpyAsync(h->wi, wim, wb, cudaMemcpyHostToDevice, st));
+    if (mixed) {
+      PF_CUDA(cudaMemcpyAsync(h->wstage, wre, wb, cudaMemcpyHostToDevice, st));
+      PF_CUDA(cudaMemcpyAsync(h->wstage + h->nwin, wim, wb, cudaMemcpyHostToDevice, st));
+      k_to_c32<<<grid_for(h->nwin, 256), 256, 0, st>>>(w32, h->wstage, h->wstage + h->nwin,
+                                                        h->nwin);
+      PF_LAUNCHED(h);
+    } else {
+      PF_CUDA(cudaMemcpyAsync(h->wr, wre, wb, cudaMemcpyHostToDevice, st));
+      PF_CUDA(cudaMemcpyAsync(h->wi, wim, wb, cudaMemcpyHostToDevice, st));
+    }
   }
   for (int c = 0; c < nch; ++c) {
     const size_t off = (size_t)(zcut[c] * plane), n = (size_t)((zcut[c + 1] - zcut[c]) * plane);
-    PF_CUDA(cudaMemcpyAsync(h->or_ + off, ore + off, n * sizeof(double), cudaMemcpyHostToDevice, cs));
-    PF_CUDA(cudaMemcpyAsync(h->oi_ + off, oim + off, n * sizeof(double), cudaMemcpyHostToDevice, cs));
+    PF_CUDA(cudaMemcpyAsync(dre + off, ore + off, n * sizeof(double), cudaMemcpyHostToDevice, cs));
+    PF_CUDA(cudaMemcpyAsync(dim + off, oim + off, n * sizeof(double), cudaMemcpyHostToDevice, cs));
     PF_CUDA(cudaEventRecord(ev_in[c], cs));
   }
   const int64_t wplane = (int64_t)h->nix * h->niy;
   auto before = [&](int c) -> int {
     PF_CUDA(cudaStreamWaitEvent(st, ev_in[c], 0));
+    const int64_t z0 = zcut[c], nz = zcut[c + 1] - zcut[c];
+    if (mixed) {
+      k_to_c32<<<grid_for(nz * plane, 256), 256, 0, st>>>(oc + z0 * plane, dre + z0 * plane,
+                                                           dim + z0 * plane, nz * plane);
+      PF_LAUNCHED(h);
+    }
     if (win) {  // inner2Outer of the range's planes (range 0 also writes the mirror plane)
-      const int64_t z0 = zcut[c], nz = zcut[c + 1] - zcut[c];
-      k_window_copy<<<grid_for(wplane * nz, 256), 256, 0, st>>>(
-          h->wr + z0 * wplane, h->wi + z0 * wplane, h->or_ + z0 * plane, h->oi_ + z0 * plane,
-          h->nix, h->niy, nz, p.nx, p.ny, p.nz2, 1, (periodic && c == 0) ? 1 : 0);
+      const int mirror = (periodic && c == 0) ? 1 : 0;
+      if (mixed)
+        k_window_copy_c32<<<grid_for(wplane * nz, 256), 256, 0, st>>>(
+            w32 + z0 * wplane, oc + z0 * plane, h->nix, h->niy, nz, p.nx, p.ny, p.nz2, 1, mirror);
+      else
+        k_window_copy<<<grid_for(wplane * nz, 256), 256, 0, st>>>(
+            h->wr + z0 * wplane, h->wi + z0 * wplane, h->or_ + z0 * plane, h->oi_ + z0 * plane,
+            h->nix, h->niy, nz, p.nx, p.ny, p.nz2, 1, mirror);
       PF_LAUNCHED(h);
     }
     return PF_OK;
   };
   auto after = [&](int c) -> int {
+    const int64_t z0 = zcut[c], nz = zcut[c + 1] - zcut[c];
+    if (mixed) {
+      k_from_c32<<<grid_for(nz * plane, 256), 256, 0, st>>>(oc + z0 * plane, dre + z0 * plane,
+                                                             dim + z0 * plane, nz * plane);
+      PF_LAUNCHED(h);
+      if (periodic && c == 0) {
+        const int64_t mo = (p.nz2 - 1) * plane;
+        k_from_c32<<<grid_for(plane, 256), 256, 0, st>>>(oc + mo, dre + mo, dim + mo, plane);
+        PF_LAUNCHED(h);
+      }
+    }
     PF_CUDA(cudaEventRecord(ev_out[c], st));
     PF_CUDA(cudaStreamWaitEvent(cs, ev_out[c], 0));
-    const size_t off = (size_t)(zcut[c] * plane), n = (size_t)((zcut[c + 1] - zcut[c]) * plane);
-    PF_CUDA(cudaMemcpyAsync(ore + off, h->or_ + off, n * sizeof(double), cudaMemcpyDeviceToHost, cs));
-    PF_CUDA(cudaMemcpyAsync(oim + off, h->oi_ + off, n * sizeof(double), cudaMemcpyDeviceToHost, cs));
+    const size_t off = (size_t)(z0 * plane), n = (size_t)(nz * plane);
+    PF_CUDA(cudaMemcpyAsync(ore + off, dre + off, n * sizeof(double), cudaMemcpyDeviceToHost, cs));
+    PF_CUDA(cudaMemcpyAsync(oim + off, dim + off, n * sizeof(double), cudaMemcpyDeviceToHost, cs));
     if (periodic && c == 0) {  // the mirror plane, written with plane 0
       const size_t mo = (size_t)((p.nz2 - 1) * plane);
-      PF_CUDA(cudaMemcpyAsync(ore + mo, h->or_ + mo, (size_t)plane * sizeof(double),
+      PF_CUDA(cudaMemcpyAsync(ore + mo, dre + mo, (size_t)plane * sizeof(double),
                               cudaMemcpyDeviceToHost, cs));
-      PF_CUDA(cudaMemcpyAsync(oim + mo, h->oi_ + mo, (size_t)plane * sizeof(double),
+      PF_CUDA(cudaMemcpyAsync(oim + mo, dim + mo, (size_t)plane * sizeof(double),
                               cudaMemcpyDeviceToHost, cs));
     }
     return PF_OK;
@@ -1176,11 +1216,23 @@ int pf_diffract_host(pf_handle *h, double dz, double *ore, double *oim, double *
     return rc;
   }
   if (win) {  // outer2Inner, then the window goes out
-    k_window_copy<<<grid_for(h->nwin, 256), 256, 0, st>>>(h->wr, h->wi, h->or_, h->oi_, h->nix,
-                                                         h->niy, h->npl, p.nx, p.ny, p.nz2, 0, 0);
-    PF_LAUNCHED(h);
-    PF_CUDA(cudaMemcpyAsync(wre, h->wr, wb, cudaMemcpyDeviceToHost, st));
-    PF_CUDA(cudaMemcpyAsync(wim, h->wi, wb, cudaMemcpyDeviceToHost, st));
+    if (mixed) {
+      k_window_copy_c32<<<grid_for(h->nwin, 256), 256, 0, st>>>(w32, oc, h->nix, h->niy, h->npl,
+                                                               p.nx, p.ny, p.nz2, 0, 0);
+      PF_LAUNCHED(h);
+      k_from_c32<<<grid_for(h->nwin, 256), 256, 0, st>>>(w32, h->wstage, h->wstage + h->nwin,
+                                                          h->nwin);
+      PF_LAUNCHED(h);
+      PF_CUDA(cudaMemcpyAsync(wre, h->wstage, wb, cudaMemcpyDeviceToHost, st));
+      PF_CUDA(cudaMemcpyAsync(wim, h->wstage + h->nwin, wb, cudaMemcpyDeviceToHost, st));
+    } else {
+      k_window_copy<<<grid_for(h->nwin, 256), 256, 0, st>>>(h->wr, h->wi, h->or_, h->oi_, h->nix,
+                                                           h->niy, h->npl, p.nx, p.ny, p.nz2, 0,
+                                                           0);
+      PF_LAUNCHED(h);
+      PF_CUDA(cudaMemcpyAsync(wre, h->wr, wb, cudaMemcpyDeviceToHost, st));
+      PF_CUDA(cudaMemcpyAsync(wim, h->wi, wb, cudaMemcpyDeviceToHost, st));
+    }
     h->window_valid = true;
   }
   PF_CUDA(cudaEventRecord(ev_end, st));

@@ -210,6 +210,8 @@ struct pf_handle {
   void *oc32 = nullptr;
   void *w32 = nullptr, *as32 = nullptr, *d0_32 = nullptr, *d12_32 = nullptr, *acc32 = nullptr;
   double *staging = nullptr;  // FP64 staging for field transfers (2 * nouter)
+  double *wstage = nullptr;   // FP64 staging of the window field (2 * wstage_cap), mixed
+  int64_t wstage_cap = 0;
 
   // diagnostics scratch
   double *diag = nullptr;
@@ -357,9 +359,10 @@ int pf_outer_to_inner(pf_handle *h);
 int pf_inner_to_outer(pf_handle *h);
 // diffraction
 int pf_diffract_outer(pf_handle *h, double dz);
-// the FP64 outer mesh's diffraction with the first and last x passes cut
-// into ranges of z2 planes [zcut[c], zcut[c + 1]): before(c) runs before the
-// first pass reads range c, after(c) once the last pass has written it
+// the outer mesh's diffraction (FP64 split, or complex float on a mixed
+// handle) with the first and last transverse passes cut into ranges of z2
+// planes [zcut[c], zcut[c + 1]): before(c) runs before the first pass reads
+// range c, after(c) once the last pass has written it
 int pf_diffract_outer_ranges(pf_handle *h, double dz, const std::vector<int64_t> &zcut,
                              const std::function<int(int)> &before,
                              const std::function<int(int)> &after);

@@ -169,13 +169,60 @@ def test_host_diffraction_matches_set_diffract_get(periodic, arith):
     assert not np.array_equal(ore, ore0)
 
 
-def test_host_diffraction_rejects_mixed_handles():
-    w = configs.config1(np_=3000, seed=9)
-    q = P.Params.from_buffer_copy(w.params)
-    q.precision = P.MIXED
-    with P.Puffin(q) as sim:
-        sim.set_particles(*(w.beam[k] for k in P.PARTICLE_KEYS))
-        n = q.nx * q.ny * q.nz2
-        wre, wim = (np.ascontiguousarray(v) for v in sim.get_window_field())
-        with pytest.raises(RuntimeError):
-            sim.diffractIM_host(w.h, (np.zeros(n), np.zeros(n)), (wre, wim))
+@pytest.mark.parametrize("periodic", [False, True])
+def test_host_diffraction_mixed_matches_set_diffract_get(periodic):
+    """The mixed form (the FP64 arrays converted to and from the complex
+    float field on the device, range by range): bit for bit as the
+    five-call sequence, which converts with the same roundings."""
+    w = configs.config2(np_=20000, nz2=65)
+    p = P.Params.from_buffer_copy(w.params)
+    p.precision = P.MIXED
+    if periodic:
+        p.mesh_type = P.MESH_PERIODIC
+    rng = np.random.default_rng(13)
+    n = p.nx * p.ny * p.nz2
+    ore0, oim0 = 1e-3 * rng.standard_normal(n), 1e-3 * rng.standard_normal(n)
+    with P.Puffin(p) as a, P.Puffin(p) as b:
+        for sim in (a, b):
+            sim.set_particles(*(w.beam[k] for k in P.PARTICLE_KEYS))
+            sim.set_field(ore0, oim0)
+        wre0, wim0 = a.get_window_field()
+        wre0 = wre0 + 1e-4 * rng.standard_normal(wre0.size)
+        wim0 = wim0 + 1e-4 * rng.standard_normal(wim0.size)
+        ore, oim = _pinned(ore0), _pinned(oim0)
+        wre, wim = _pinned(wre0), _pinned(wim0)
+        for _ in range(2):  # the second call reuses the staging buffers
+            a.diffractIM_host(8 * w.h, (ore, oim), (wre, wim))
+        b.set_window_field(wre0, wim0)
+        b.diffractIM(8 * w.h)
+        b.set_field(*b.get_field())
+        b.set_window_field(*b.get_window_field())
+        b.diffractIM(8 * w.h)
+        fr, fi = b.get_field()
+        gr, gi = b.get_window_field()
+    np.testing.assert_array_equal(ore, fr)
+    np.testing.assert_array_equal(oim, fi)
+    np.testing.assert_array_equal(wre, gr)
+    np.testing.assert_array_equal(wim, gi)
+    assert not np.array_equal(ore, ore0)
+
+
+def test_host_diffraction_without_a_window():
+    """No particles, so no inner window: the call transforms the outer field
+    alone (window arguments may be NULL), as pf_set_field + pf_diffract +
+    pf_get_field do."""
+    w = configs.config2(np_=20000, nz2=65)
+    p = w.params
+    rng = np.random.default_rng(12)
+    n = p.nx * p.ny * p.nz2
+    ore0, oim0 = 1e-3 * rng.standard_normal(n), 1e-3 * rng.standard_normal(n)
+    lib = L.load()
+    with P.Puffin(p) as a, P.Puffin(p) as b:
+        ore, oim = _pinned(ore0), _pinned(oim0)
+        assert lib.pf_diffract_host(a._h, 8 * w.h, ore.ctypes.data, oim.ctypes.data, None,
+                                    None) == 0
+        b.set_field(ore0, oim0)
+        b.diffractIM(8 * w.h)
+        fr, fi = b.get_field()
+    np.testing.assert_array_equal(ore, fr)
+    np.testing.assert_array_equal(oim, fi)
