@@ -89,6 +89,8 @@ def parse():
                     help="skip the one-at-a-time comparison of the batched form")
     ap.add_argument("--no-batch-tune", action="store_true",
                     help="batched form with the default shapes (persistent grids)")
+    ap.add_argument("--no-dft-gemm", action="store_true",
+                    help="skip the measurement of the transverse DFT as tensor-core GEMMs")
     ap.add_argument("--adjoint-steps", type=int, default=3000,
                     help="steps of the adjoint leg on the 33x33x128 periodic mesh (0: skip); "
                          "3000 is the adjoint form's full run")
@@ -596,6 +598,114 @@ def fidelity_leg(args, dev):
     }
 
 
+def dft_gemm_leg(args, dev, fft_call_ms):
+    """The transverse 129-point DFT as a matrix product on the tensor cores,
+    measured beside the butterfly kernels of the mixed path (a measurement,
+    not a product path): the x transform of every row of the config-2
+    complex-float mesh (129 * nz2 rows of 129 interleaved complex values,
+    a real matrix of 258 columns) times the real form of the forward DFT
+    matrix (258 x 258), in TF32 with the split-precision scheme that keeps
+    FP32 accuracy (hi*hi + lo*hi + hi*lo, three products; hi keeps the
+    operand's top 10 significand bits, lo the rest), through cuBLAS.
+    Timed on the mesh's own layout (row stride 1032 bytes), on rows padded
+    to 264 columns, and on a 64-plane slice that stays in L2 (the tensor
+    rate for this shape); the error is against an FP64 product on sample
+    rows.  A 2D transform is two such products (x and y, the same work)."""
+    import torch
+
+    d = f"cuda:{dev}"
+    nx = 129
+    n2 = 2 * nx
+    nrow = nx * args.nz2
+    gen = torch.Generator(device=d)
+    gen.manual_seed(5)
+    x = 1e-3 * torch.randn(nrow, n2, device=d, generator=gen)
+    kk = torch.arange(nx, dtype=torch.float64)
+    th = 2.0 * math.pi * torch.outer(kk, kk) / nx
+    c, s = torch.cos(th), torch.sin(th)
+    b64 = torch.empty(n2, n2, dtype=torch.float64)
+    b64[0::2, 0::2] = c   # x_re -> y_re
+    b64[1::2, 0::2] = s   # x_im -> y_re
+    b64[0::2, 1::2] = -s  # x_re -> y_im
+    b64[1::2, 1::2] = c   # x_im -> y_im
+    b64 = b64.to(d)
+    b32 = b64.to(torch.float32)
+
+    def split(t):
+        hi = (t.view(torch.int32) & -8192).view(torch.float32)  # low 13 bits cleared
+        return hi, t - hi
+
+    def three(xh, xl, bh, bl, y):
+        torch.matmul(xh, bh, out=y)
+        y.addmm_(xl, bh)
+        y.addmm_(xh, bl)
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    old_tf32 = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = True
+    try:
+        out = {}
+        bh, bl = split(b32)
+        xh, xl = split(x)
+        y = torch.empty(nrow, n2, device=d)
+        flops = 3 * 2.0 * nrow * n2 * n2
+        t = timed(lambda: three(xh, xl, bh, bl, y), 5)
+        out["mesh_layout"] = {"ms": t, "tflops": flops / (t * 1e-3) / 1e12}
+        # accuracy on sample rows against an FP64 product
+        ns = 4096
+        ref = x[:ns].double() @ b64
+        scale = ref.abs().max().item()
+        err3 = (y[:ns].double() - ref).abs().max().item() / scale
+        err1 = ((x[:ns] @ b32).double() - ref).abs().max().item() / scale
+        # padded rows (a 16-byte multiple stride): the library's best case
+        pad = 264
+        xp = torch.zeros(nrow, pad, device=d)
+        xp[:, :n2] = x
+        bp = torch.zeros(pad, pad, device=d)
+        bp[:n2, :n2] = b32
+        del xh, xl, y
+        bph, bpl = split(bp)
+        xph, xpl = split(xp)
+        yp = torch.empty(nrow, pad, device=d)
+        t = timed(lambda: three(xph, xpl, bph, bpl, yp), 5)
+        out["padded_264"] = {"ms": t, "tflops": flops / (t * 1e-3) / 1e12}
+        # 256 planes: 33,024 rows, 105 MB of operands and result, in L2
+        m = nx * min(256, args.nz2)
+        xs_h, xs_l, ys = xph[:m].contiguous(), xpl[:m].contiguous(), yp[:m].contiguous()
+        t = timed(lambda: three(xs_h, xs_l, bph, bpl, ys), 50)
+        fl = 3 * 2.0 * m * n2 * n2
+        out["l2_resident_256_planes"] = {"ms": t, "tflops": fl / (t * 1e-3) / 1e12}
+        del xp, xph, xpl, yp
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = old_tf32
+    best = min(out["mesh_layout"]["ms"], out["padded_264"]["ms"])
+    out.update({
+        "what": "x transform of the 129x129x%d complex-float mesh as three TF32 GEMMs "
+                "(%d x 258 by 258 x 258, split precision) in cuBLAS" % (args.nz2, nrow),
+        "rel_error_three_products": err3,
+        "rel_error_one_tf32_product": err1,
+        "per_2d_transform_ms": 2 * best,
+        "butterfly_fft_call_ms": fft_call_ms,
+        "butterfly_note": "the mixed diffraction call runs four 2D transforms of this mesh "
+                          "(three passes of the in-place plane kernel) and its z2 passes in "
+                          "butterfly_fft_call_ms",
+    })
+    del x
+    torch.cuda.empty_cache()
+    return out
+
+
 def batch_leg(args, dev):
     """The batched form: args.batch_n independent periodic single-slice
     instances (macroparticles log-uniform in [2^14, 2^20], meshes
@@ -810,6 +920,13 @@ def run_gpu(args, rank, world):
                 c3[name] = _time_path(args, dev, prec, world, "config3", args.steps3, args.warmup)
                 c3[name]["sim"].close()
 
+    dgemm = None
+    if rmx and not args.no_dft_gemm:
+        every_mx = rmx["w"].isteps4diff
+        calls = sum(1 for i in range(args.warmup + 1, args.warmup + args.steps + 1)
+                    if i % every_mx == 0)
+        dgemm = dft_gemm_leg(args, dev, rmx["kernel"]["fft"][0] / max(1, calls))
+
     # the forms that hold many buffers run last
     fid = fidelity_leg(args, dev) if args.fidelity_np > 0 and not args.no_mixed else None
     adj = adjoint_leg(args, dev) if args.adjoint_steps > 0 else None
@@ -907,6 +1024,8 @@ def run_gpu(args, rank, world):
                 "speedup_vs_fp64_e2e": e2e_ms / e2e_mx["ms"],
                 "api": "pf_rk4_step_host + pf_diffract_host",
                 "ms_per_step_by_call": e2e_mx["parts"]}
+    if dgemm:
+        rec["dft_as_tensor_core_gemm"] = dgemm
     if fid:
         rec["mixed_fidelity"] = fid
     if adj:

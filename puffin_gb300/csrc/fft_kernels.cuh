@@ -1591,8 +1591,9 @@ static int diffract_ranges(pf_handle *h, Plan *&plan, io_real *re, io_real *im, 
       d->px, d->py, d->dxt, d->dyt, d->kx, d->ky, d->kz, d->nx, d->ny, d->nz, dz, dz, p.sbeta);
   pf_prof_end(h);
   PF_LAUNCHED(h);
-  // the first or last transverse pass over the planes of range c
-  auto range_pass = [&](FftArgs b, int c) {
+  // a transverse pass (the plane kernel, or the line kernel along x or y:
+  // x lines and y lines each lie in one plane) over the planes of range c
+  auto range_pass = [&](FftArgs b, int axis, int c) {
     const int64_t z0 = zcut[c], z1 = zcut[c + 1];
     if (z1 <= z0) return PF_OK;
     pf_prof_begin(h, PROF_FFT);
@@ -1602,11 +1603,12 @@ static int diffract_ranges(pf_handle *h, Plan *&plan, io_real *re, io_real *im, 
       b.z0 = (int)z0;
       d->plane<<<(unsigned)(z1 - z0), PT, d->plane_smem, h->stream>>>(b);
     } else {
-      b.ax = d->ax[0];
-      b.ax.line0 = (int64_t)d->ny * z0;
-      b.ax.nlines = (int64_t)d->ny * z1;
+      const int64_t per = axis == 0 ? d->ny : d->nx;  // lines per plane
+      b.ax = d->ax[axis];
+      b.ax.line0 = per * z0;
+      b.ax.nlines = per * z1;
       const int64_t blocks = (b.ax.nlines - b.ax.line0 + b.ax.lpb - 1) / b.ax.lpb;
-      k_fft<<<(unsigned)blocks, NTHREADS, d->smem[0], h->stream>>>(b);
+      k_fft<<<(unsigned)blocks, NTHREADS, d->smem[axis], h->stream>>>(b);
     }
     pf_prof_end(h);
     PF_LAUNCHED(h);
@@ -1628,8 +1630,7 @@ static int diffract_ranges(pf_handle *h, Plan *&plan, io_real *re, io_real *im, 
   };
   const Step *steps = d->plane ? plane_steps : line_steps;
   const int nsteps = d->plane ? 5 : 9;
-  for (int k = 0; k < nsteps; ++k) {
-    const Step &st = steps[k];
+  auto args_of = [&](const Step &st) {
     FftArgs b = a;
     b.dir = st.dir;
     b.mid = st.mid;
@@ -1637,21 +1638,28 @@ static int diffract_ranges(pf_handle *h, Plan *&plan, io_real *re, io_real *im, 
     b.load_split = split && st.load_split;
     b.store_split = split && st.store_split;
     b.mirror = a.mirror && st.store_split;
-    int rc = PF_OK;
-    if (k == 0 || k == nsteps - 1) {
-      for (int c = 0; c < nch && rc == PF_OK; ++c) {
-        if (k == 0) rc = before(c);
-        if (rc == PF_OK) rc = range_pass(b, c);
-        if (k == nsteps - 1 && rc == PF_OK) rc = after(c);
-      }
-    } else if (st.transverse) {
-      rc = plane_pass(h, d, b);
-    } else {
-      rc = fft_pass(h, d, b, st.axis);
-    }
-    if (rc) return rc;
+    return b;
+  };
+  // range by range: the first pass (x, or the plane kernel) as each range
+  // arrives and, on the line schedule, the y pass after it; the last y pass
+  // and the last pass before each range goes out.  The passes between run
+  // whole.
+  const int nedge = (!d->plane && d->ax[1].n > 1) ? 2 : 1;
+  int rc = PF_OK;
+  for (int c = 0; c < nch && rc == PF_OK; ++c) {
+    rc = before(c);
+    for (int k = 0; k < nedge && rc == PF_OK; ++k) rc = range_pass(args_of(steps[k]), steps[k].axis, c);
   }
-  return PF_OK;
+  for (int k = nedge; k < nsteps - nedge && rc == PF_OK; ++k) {
+    const Step &st = steps[k];
+    rc = st.transverse ? plane_pass(h, d, args_of(st)) : fft_pass(h, d, args_of(st), st.axis);
+  }
+  for (int c = 0; c < nch && rc == PF_OK; ++c) {
+    for (int k = nsteps - nedge; k < nsteps && rc == PF_OK; ++k)
+      rc = range_pass(args_of(steps[k]), steps[k].axis, c);
+    if (rc == PF_OK) rc = after(c);
+  }
+  return rc;
 }
 
 // Adjoint (with respect to the real inner product sum re*re' + im*im') of
