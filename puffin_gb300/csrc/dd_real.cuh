@@ -81,3 +81,47 @@ __device__ __forceinline__ pf_dd dd_from_double(double v) {
   return pf_dd(h, d2f_rn(v - f2d(h)));
 }
 __device__ __forceinline__ double dd_to_double(pf_dd v) { return f2d(v.hi) + f2d(v.lo); }
+
+// Sums x0 + sum_j a_j c_j of the FFTs' odd-prime butterflies.  For pairs the
+// sum is kept unnormalised: one float s takes the high parts of the products
+// (TwoSum on every addition) and a second float l gathers x0's low part, the
+// TwoSum errors and the TwoProd and cross-term errors of the products; one
+// TwoSum at the end normalises.  12 float operations per term against 15 for
+// a normalised pair multiply-add (Ogita, Rump and Oishi's cascaded summation,
+// applied to the dot product); l's own roundings are 2^-24 of the errors it
+// holds, about 2^-48 of the terms.  For float and double the accumulator is
+// the value with a fused multiply-add.
+struct pf_dd_acc {
+  float s, l;
+};
+__device__ __forceinline__ pf_dd_acc acc_start(pf_dd x) { return pf_dd_acc{x.hi, x.lo}; }
+__device__ __forceinline__ void acc_fma(pf_dd_acc &c, pf_dd a, pf_dd b) {
+  const float p = a.hi * b.hi;
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  const float s = c.s + p;
+  const float bb = s - c.s;
+  const float err = (c.s - (s - bb)) + (p - bb);
+  c.s = s;
+  c.l += err + e;
+}
+__device__ __forceinline__ pf_dd acc_end(pf_dd_acc c) {
+  const float s = c.s + c.l;
+  const float bb = s - c.s;
+  return pf_dd(s, (c.s - (s - bb)) + (c.l - bb));
+}
+__device__ __forceinline__ float acc_start(float x) { return x; }
+__device__ __forceinline__ void acc_fma(float &c, float a, float b) { c = __fmaf_rn(a, b, c); }
+__device__ __forceinline__ float acc_end(float c) { return c; }
+__device__ __forceinline__ double acc_start(double x) { return x; }
+__device__ __forceinline__ void acc_fma(double &c, double a, double b) { c = __fma_rn(a, b, c); }
+__device__ __forceinline__ double acc_end(double c) { return c; }
+template <class T>
+struct pf_acc_of {
+  using type = T;
+};
+template <>
+struct pf_acc_of<pf_dd> {
+  using type = pf_dd_acc;
+};

@@ -7,6 +7,7 @@ namespace FFT_NS {
 typedef FFT_T real;
 typedef FFT_IO io_real;  // element type of the split re/im field in HBM
 constexpr bool REAL_IS_DD = std::is_same<real, pf_dd>::value;
+typedef pf_acc_of<real>::type acc;  // sums of products in the odd-prime butterflies
 
 __device__ __forceinline__ double to_io(double v) { return v; }
 __device__ __forceinline__ float to_io(float v) { return v; }
@@ -254,7 +255,8 @@ __device__ __forceinline__ void odd_butterfly(const cplx *src, int nb, const cpl
   // the root index m = j*q mod R is uniform across the threads of a group
 #pragma unroll 1
   for (int q = g + 1; q <= H; q += G) {
-    cplx C = x0, S{(real)0, (real)0};
+    acc Cr = acc_start(x0.r), Ci = acc_start(x0.i);
+    acc Sr = acc_start((real)0), Si = acc_start((real)0);
     int m = 0;
 #pragma unroll
     for (int j = 1; j <= H; ++j) {
@@ -262,11 +264,12 @@ __device__ __forceinline__ void odd_butterfly(const cplx *src, int nb, const cpl
       if (m >= R) m -= R;
       const real c = c_roots[OFF + m].r;
       const real sn = c_roots[OFF + m].i;
-      C.r = fma(a[j - 1].r, c, C.r);
-      C.i = fma(a[j - 1].i, c, C.i);
-      S.r = fma(b[j - 1].r, sn, S.r);
-      S.i = fma(b[j - 1].i, sn, S.i);
+      acc_fma(Cr, a[j - 1].r, c);
+      acc_fma(Ci, a[j - 1].i, c);
+      acc_fma(Sr, b[j - 1].r, sn);
+      acc_fma(Si, b[j - 1].i, sn);
     }
+    const cplx C{acc_end(Cr), acc_end(Ci)}, S{acc_end(Sr), acc_end(Si)};
     if (!INV) {
       dst[q * ds] = cplx{C.r + S.i, C.i - S.r};
       dst[(R - q) * ds] = cplx{C.r - S.i, C.i + S.r};
@@ -324,7 +327,8 @@ __device__ __forceinline__ void odd_pass_shared(const cplx *in, cplx *out, int n
       }
 #pragma unroll 1
       for (int q = g + 1; q <= H; q += G) {
-        cplx C = x0, S{(real)0, (real)0};
+        acc Cr = acc_start(x0.r), Ci = acc_start(x0.i);
+        acc Sr = acc_start((real)0), Si = acc_start((real)0);
         int m = 0;
 #pragma unroll
         for (int jj = 1; jj <= H; ++jj) {
@@ -333,11 +337,12 @@ __device__ __forceinline__ void odd_pass_shared(const cplx *in, cplx *out, int n
           const real c = c_roots[OFF + m].r;
           const real sn = c_roots[OFF + m].i;
           const cplx av = ab[jj - 1], bv = ab[H + jj - 1];
-          C.r = fma(av.r, c, C.r);
-          C.i = fma(av.i, c, C.i);
-          S.r = fma(bv.r, sn, S.r);
-          S.i = fma(bv.i, sn, S.i);
+          acc_fma(Cr, av.r, c);
+          acc_fma(Ci, av.i, c);
+          acc_fma(Sr, bv.r, sn);
+          acc_fma(Si, bv.i, sn);
         }
+        const cplx C{acc_end(Cr), acc_end(Ci)}, S{acc_end(Sr), acc_end(Si)};
         if (!INV) {
           dst[q * Ns] = cplx{C.r + S.i, C.i - S.r};
           dst[(R - q) * Ns] = cplx{C.r - S.i, C.i + S.r};
@@ -463,7 +468,8 @@ __device__ __forceinline__ void pfa129_pass43(const cplx *in, cplx *out, int nl,
       }
 #pragma unroll 1
       for (int q = g + 1; q <= H; q += G) {
-        cplx C = x0, S{(real)0, (real)0};
+        acc Cr = acc_start(x0.r), Ci = acc_start(x0.i);
+        acc Sr = acc_start((real)0), Si = acc_start((real)0);
         int m = 0;
 #pragma unroll
         for (int jj = 1; jj <= H; ++jj) {
@@ -472,11 +478,12 @@ __device__ __forceinline__ void pfa129_pass43(const cplx *in, cplx *out, int nl,
           const real c = c_roots[OFF + m].r;
           const real sn = c_roots[OFF + m].i;
           const cplx av = ab[jj - 1], bv = ab[H + jj - 1];
-          C.r = fma(av.r, c, C.r);
-          C.i = fma(av.i, c, C.i);
-          S.r = fma(bv.r, sn, S.r);
-          S.i = fma(bv.i, sn, S.i);
+          acc_fma(Cr, av.r, c);
+          acc_fma(Ci, av.i, c);
+          acc_fma(Sr, bv.r, sn);
+          acc_fma(Si, bv.i, sn);
         }
+        const cplx C{acc_end(Cr), acc_end(Ci)}, S{acc_end(Sr), acc_end(Si)};
         const int kq = (k0 + 87 * q) % 129, kr = (k0 + 87 * (R - q)) % 129;
         if (!INV) {
           dst[kq] = cplx{C.r + S.i, C.i - S.r};
@@ -613,7 +620,8 @@ __device__ __forceinline__ void store(const FftArgs &a, int64_t pos, cplx v) {
 
 // resident blocks per SM of the line kernel: 3 for the 8-byte reals (FP64
 // and paired FP32, 80 registers; the paired form spills a few words, and
-// measured 8 % slower at two blocks and 128 registers), 1 for FP32
+// measured 8 % slower at two blocks and 128 registers, 2 % slower at four
+// blocks, 64 registers and 7 lines per block), 1 for FP32
 constexpr int KFFT_MINB = (sizeof(real) == 8) ? 3 : 1;
 __global__ void __launch_bounds__(NTHREADS, KFFT_MINB) k_fft(const FftArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -842,17 +850,19 @@ __device__ __forceinline__ void ip_pass(cplx *buf, int nl, int ls, int es, const
       // constant-bank operand
 #pragma unroll
       for (int q = 1; q <= H; ++q) {
-        cplx C = x0[b], S{(real)0, (real)0};
+        acc Cr = acc_start(x0[b].r), Ci = acc_start(x0[b].i);
+        acc Sr = acc_start((real)0), Si = acc_start((real)0);
 #pragma unroll
         for (int j = 1; j <= H; ++j) {
           const int m = (j * q) % R;
           const real c = c_roots[OFF + m].r;
           const real sn = c_roots[OFF + m].i;
-          C.r = fma(av[b][j - 1].r, c, C.r);
-          C.i = fma(av[b][j - 1].i, c, C.i);
-          S.r = fma(bv[b][j - 1].r, sn, S.r);
-          S.i = fma(bv[b][j - 1].i, sn, S.i);
+          acc_fma(Cr, av[b][j - 1].r, c);
+          acc_fma(Ci, av[b][j - 1].i, c);
+          acc_fma(Sr, bv[b][j - 1].r, sn);
+          acc_fma(Si, bv[b][j - 1].i, sn);
         }
+        const cplx C{acc_end(Cr), acc_end(Ci)}, S{acc_end(Sr), acc_end(Si)};
         if (!INV) {
           buf[slot(o + q * ds)] = cplx{C.r + S.i, C.i - S.r};
           buf[slot(o + (R - q) * ds)] = cplx{C.r - S.i, C.i + S.r};
