@@ -106,32 +106,50 @@ __device__ __forceinline__ bool split_cell(double t, int64_t &ip, double &fr) {
   return true;
 }
 
-// Exact conversion of c * 2^E (truncated toward zero) to a two's-complement
-// 128-bit integer (hi:lo).  Returns false when |c * 2^E| >= 2^maxexp.
-__device__ __forceinline__ bool to_fix(double c, int E, int maxexp, u64 &lo, u64 &hi) {
-  u64 b = (u64)__double_as_longlong(c);
-  int ex = (int)((b >> 52) & 0x7ffull);
+// A deposit factor unpacked once for mul_to_fix: significand with its hidden
+// bit, biased exponent (0: zero or subnormal, 0x7ff: not finite) and sign.
+struct FixOperand {
+  u64 m;
+  int e;
+  unsigned neg;
+};
+__device__ __forceinline__ FixOperand fix_operand(double v) {
+  const u64 b = (u64)__double_as_longlong(v);
+  return FixOperand{(b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull, (int)((b >> 52) & 0x7ffull),
+                    (unsigned)(b >> 63)};
+}
+
+// Exact product x * y * 2^E truncated toward zero as a two's-complement
+// 128-bit integer (hi:lo), with integer operations only: the 106-bit
+// product of the significands shifted onto the fixed-point grid, so the
+// product is never rounded to FP64 first and no FP64 operation is spent on
+// it.  Returns false when |x y 2^E| >= 2^maxexp (maxexp <= 126) or an
+// operand is not finite; a zero or subnormal operand gives 0.
+__device__ __forceinline__ bool mul_to_fix(const FixOperand &x, const FixOperand &y, int E,
+                                           int maxexp, u64 &lo, u64 &hi) {
   lo = 0;
   hi = 0;
-  if (ex == 0) return true;             // zero or subnormal: below resolution
-  if (ex == 0x7ff) return false;        // inf / nan
-  u64 m = (b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
-  int s = ex - 1075 + E;                // |c| * 2^E = m * 2^s
-  if (s + 53 > maxexp) return false;
-  if (s >= 64) {
-    hi = m << (s - 64);
-  } else if (s > 0) {
-    lo = m << s;
-    hi = m >> (64 - s);
-  } else if (s == 0) {
-    lo = m;
-  } else if (s > -53) {
-    lo = m >> (-s);
+  if (x.e == 0x7ff || y.e == 0x7ff) return false;
+  if (x.e == 0 || y.e == 0) return true;
+  const u64 plo = x.m * y.m, phi = __umul64hi(x.m, y.m);  // P < 2^106
+  const int sh = x.e + y.e - 2150 + E;                     // |x y| 2^E = P 2^sh
+  const int top = (phi >> 41) ? 106 : 105;                 // bit length of P
+  if (top + sh > maxexp) return false;
+  if (sh >= 0) {  // sh <= maxexp - 105 < 64
+    hi = sh ? (phi << sh) | (plo >> (64 - sh)) : phi;
+    lo = plo << sh;
   } else {
-    return true;
+    const int r = -sh;
+    if (r >= 106) return true;  // below the grid
+    if (r < 64) {
+      lo = (plo >> r) | (phi << (64 - r));
+      hi = phi >> r;
+    } else {
+      lo = phi >> (r - 64);
+    }
   }
-  if (b >> 63) {                         // negate
-    u64 nlo = ~lo + 1ull;
+  if (x.neg ^ y.neg) {  // negate
+    const u64 nlo = ~lo + 1ull;
     hi = ~hi + (lo == 0 ? 1ull : 0ull);
     lo = nlo;
   }
@@ -204,7 +222,9 @@ __device__ __forceinline__ void stage_particle(const StageArgs &a, const int64_t
   const double bb = 1.0 + a.aw * ((PX * PX) + (PY * PY));  // a.aw holds aw**2
   const double p2 = ((1.0 / sqrt(1.0 - aa * bb)) - 1.0) * a.inv_eta;
   const double q = 1.0 + a.eta * p2;
-  const double rG = 1.0 / G;
+  // 1/Gamma from aa = 1/(gamma0^2 Gamma^2): two products instead of a
+  // division, within 3 ulp (1/Gamma only scales well-conditioned terms)
+  const double rG = G * (a.gamma_r * aa);
   const double qrG = q * rG;
 
   // interpolation (getInterps_3D / getInterps_1D): cell index and fraction
@@ -317,8 +337,7 @@ __device__ __forceinline__ void stage_particle(const StageArgs &a, const int64_t
     if (a.field_evolve) {
       // (chi/dV3) (1 + eta p2) p / Gamma
       const double dw = chi * a.inv_dV3 * qrG;
-      const double sr = dw * PX;
-      const double si = dw * PY;
+      const FixOperand osr = fix_operand(dw * PX), osi = fix_operand(dw * PY);
       bool fits = true;
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
@@ -329,10 +348,11 @@ __device__ __forceinline__ void stage_particle(const StageArgs &a, const int64_t
           if (tp >= 0 && tp < FT_PLANES) ti = tp * t.ntr + (int)(node[c] - plane * t.ntr);
         }
         u64 lo, hi;
-        fits &= to_fix(w[c] * sr, a.fix_e, a.fix_maxexp, lo, hi);
+        const FixOperand ow = fix_operand(w[c]);
+        fits &= mul_to_fix(ow, osr, a.fix_e, a.fix_maxexp, lo, hi);
         if (TILE && ti >= 0) fix_add(t.lo_r, t.hi_r, ti, lo, hi);
         else fix_add(a.acc_lo_r, a.acc_hi_r, node[c], lo, hi);
-        fits &= to_fix(w[c] * si, a.fix_e, a.fix_maxexp, lo, hi);
+        fits &= mul_to_fix(ow, osi, a.fix_e, a.fix_maxexp, lo, hi);
         if (TILE && ti >= 0) fix_add(t.lo_i, t.hi_i, ti, lo, hi);
         else fix_add(a.acc_lo_i, a.acc_hi_i, node[c], lo, hi);
       }
