@@ -56,7 +56,7 @@ BYTES_PER_PARTICLE_STAGE = 104          # 56 B read + 48 B write (416 B per step
 # capture of k_stage<3> on 2^22 macroparticles over 129 x 129 x 2048 planes
 # (the config-2 density; the traffic grows with the macroparticles, the
 # window field is mostly read from L2)
-TRAFFIC_PER_PARTICLE_STAGE = 881.5e6 / 4194304
+TRAFFIC_PER_PARTICLE_STAGE = 881.0e6 / 4194304
 FLOPS_PER_PARTICLE_STAGE = 166          # ~664 FP64 flop per particle-step
 
 
