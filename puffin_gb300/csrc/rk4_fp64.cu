@@ -164,15 +164,46 @@ __device__ __forceinline__ void fix_add(u64 *lo_arr, u64 *hi_arr, int64_t n, u64
   if (add != 0) atomicAdd(hi_arr + n, add);
 }
 
-__device__ __forceinline__ double fix_to_double(u64 lo, u64 hi, double inv_scale) {
-  bool neg = (long long)hi < 0;
+// The 128-bit fixed-point sum (hi:lo) times 2^-E as the nearest double (ties
+// to even), with integer operations only: the leading 53 bits of the
+// magnitude, rounded on the bits below them, with the scale 2^-E folded into
+// the exponent.  Results outside the normal range (not reached by the scales
+// the beam sets) take the FP64 route.
+__device__ __forceinline__ double fix_to_double(u64 lo, u64 hi, int E) {
+  const bool neg = (long long)hi < 0;
   if (neg) {
     u64 nlo = ~lo + 1ull;
     hi = ~hi + (lo == 0 ? 1ull : 0ull);
     lo = nlo;
   }
-  double v = __ull2double_rn(hi) * 18446744073709551616.0 + __ull2double_rn(lo);
-  v = v * inv_scale;
+  if ((hi | lo) == 0ull) return 0.0;
+  const int lz = hi ? __clzll((long long)hi) : 64 + __clzll((long long)lo);
+  u64 nh, nl;  // the magnitude shifted so that its leading one is bit 127
+  if (lz >= 64) {
+    nh = lo << (lz - 64);
+    nl = 0ull;
+  } else if (lz > 0) {
+    nh = (hi << lz) | (lo >> (64 - lz));
+    nl = lo << lz;
+  } else {
+    nh = hi;
+    nl = lo;
+  }
+  int msb = 127 - lz;
+  u64 m = nh >> 11;  // 53 bits, the leading one at bit 52
+  const bool rb = (nh >> 10) & 1ull, sticky = ((nh & 0x3FFull) | nl) != 0ull;
+  if (rb && (sticky || (m & 1ull))) ++m;
+  if (m >> 53) {  // the rounding carried into a new leading bit
+    m >>= 1;
+    ++msb;
+  }
+  const int be = msb - E + 1023;
+  double v;
+  if (be > 0 && be < 2047) {
+    v = __longlong_as_double((long long)(((u64)be << 52) | (m & 0xFFFFFFFFFFFFFull)));
+  } else {
+    v = (__ull2double_rn(hi) * 18446744073709551616.0 + __ull2double_rn(lo)) * ldexp(1.0, -E);
+  }
   return neg ? -v : v;
 }
 
@@ -512,8 +543,7 @@ __global__ void __launch_bounds__(256, 4) k_stage_batch(const StageArgs *__restr
 // Every input of the node is loaded before the first store (the arrays
 // could alias as far as the compiler knows), so a thread waits for HBM once.
 template <int STAGE>
-__device__ __forceinline__ void node_update(const NodeArgs &a, const int64_t n,
-                                            const double inv_scale) {
+__device__ __forceinline__ void node_update(const NodeArgs &a, const int64_t n) {
   const u64 lr = a.acc_lo_r[n], hr = a.acc_hi_r[n], li = a.acc_lo_i[n], hi = a.acc_hi_i[n];
   const double wr = a.wr[n], wi = a.wi[n];
   double e0r = 0.0, e0i = 0.0, e12r = 0.0, e12i = 0.0;
@@ -529,8 +559,8 @@ __device__ __forceinline__ void node_update(const NodeArgs &a, const int64_t n,
   // a non-finite field value stops the step before stage 4 commits
   if (STAGE == 1 && !(pf_finite(wr) && pf_finite(wi)))
     atomicOr(const_cast<unsigned int *>(a.status), ST_NOT_FINITE);
-  const double dr = fix_to_double(lr, hr, inv_scale);
-  const double di = fix_to_double(li, hi, inv_scale);
+  const double dr = fix_to_double(lr, hr, a.fix_e);
+  const double di = fix_to_double(li, hi, a.fix_e);
   // the four accumulator words of a node are cleared right after their
   // conversion (measured faster here than clearing them after the other
   // stores)
@@ -562,10 +592,10 @@ __device__ __forceinline__ void node_update(const NodeArgs &a, const int64_t n,
 }
 
 template <int STAGE>
-__global__ void __launch_bounds__(256) k_nodes(const NodeArgs a, const double inv_scale) {
+__global__ void __launch_bounds__(256) k_nodes(const NodeArgs a) {
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= a.n) return;
-  node_update<STAGE>(a, n, inv_scale);
+  node_update<STAGE>(a, n);
   if (STAGE == 4 && a.step_ctr && n == 0) *a.step_ctr += 1;
 }
 
@@ -578,9 +608,8 @@ __global__ void __launch_bounds__(256) k_nodes_batch(const NodeArgs *__restrict_
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const BatchTile tl = tiles[t];
     const NodeArgs a = args[tl.inst];
-    const double inv_scale = ldexp(1.0, -a.fix_e);
     for (int64_t n = tl.begin + threadIdx.x; n < tl.end; n += blockDim.x)
-      node_update<STAGE>(a, n, inv_scale);
+      node_update<STAGE>(a, n);
   }
   if (STAGE == 4 && step_ctr && blockIdx.x == 0 && threadIdx.x == 0) *step_ctr += 1;
 }
@@ -818,13 +847,12 @@ static int launch_nodes(pf_handle *h, int stage, NodeArgs &n) {
   const int threads = 256;
   const int64_t blocks = (n.n + threads - 1) / threads;
   if (blocks == 0) return PF_OK;
-  const double inv_scale = ldexp(1.0, -h->fix_e);
   pf_prof_begin(h, PROF_NODES);
   switch (stage) {
-    case 1: k_nodes<1><<<(unsigned)blocks, threads, 0, h->stream>>>(n, inv_scale); break;
-    case 2: k_nodes<2><<<(unsigned)blocks, threads, 0, h->stream>>>(n, inv_scale); break;
-    case 3: k_nodes<3><<<(unsigned)blocks, threads, 0, h->stream>>>(n, inv_scale); break;
-    case 4: k_nodes<4><<<(unsigned)blocks, threads, 0, h->stream>>>(n, inv_scale); break;
+    case 1: k_nodes<1><<<(unsigned)blocks, threads, 0, h->stream>>>(n); break;
+    case 2: k_nodes<2><<<(unsigned)blocks, threads, 0, h->stream>>>(n); break;
+    case 3: k_nodes<3><<<(unsigned)blocks, threads, 0, h->stream>>>(n); break;
+    case 4: k_nodes<4><<<(unsigned)blocks, threads, 0, h->stream>>>(n); break;
   }
   pf_prof_end(h);
   PF_LAUNCHED(h);
@@ -1372,7 +1400,6 @@ extern "C" int pf_rk4_step_noalloc(const pf_params *p, double *n2col, double *n2
   nd.h6 = a.h6;
   nd.fix_e = fix_e;
   nd.status = status;
-  const double inv_scale = ldexp(1.0, -fix_e);
 
   const double hh = hstep * 0.5, szh = szl + hh;
   const double stage_sz[4] = {szl, szh, szh, szl + hstep};
@@ -1411,10 +1438,10 @@ extern "C" int pf_rk4_step_noalloc(const pf_params *p, double *n2col, double *n2
     }
     nd.coef = (s == 3) ? hstep : hh;
     switch (s) {
-      case 1: k_nodes<1><<<ng, 256, 0, st>>>(nd, inv_scale); break;
-      case 2: k_nodes<2><<<ng, 256, 0, st>>>(nd, inv_scale); break;
-      case 3: k_nodes<3><<<ng, 256, 0, st>>>(nd, inv_scale); break;
-      default: k_nodes<4><<<ng, 256, 0, st>>>(nd, inv_scale); break;
+      case 1: k_nodes<1><<<ng, 256, 0, st>>>(nd); break;
+      case 2: k_nodes<2><<<ng, 256, 0, st>>>(nd); break;
+      case 3: k_nodes<3><<<ng, 256, 0, st>>>(nd); break;
+      default: k_nodes<4><<<ng, 256, 0, st>>>(nd); break;
     }
     if (cudaGetLastError() != cudaSuccess) return PF_CUDA_ERR;
   }
