@@ -31,7 +31,8 @@ def _field(p, seed):
     return 1e-3 * rng.standard_normal(n), 1e-3 * rng.standard_normal(n)
 
 
-@pytest.mark.parametrize("np_", [3000, (1 << 21) + 12345])
+# one chunk; three chunks; five chunks, the last of 4321 macroparticles
+@pytest.mark.parametrize("np_", [3000, (1 << 21) + 12345, (1 << 22) + 4321])
 def test_host_step_matches_resident_steps(np_):
     w = configs.config1(np_=np_, seed=5)
     field = _field(w.params, 5)
