@@ -208,12 +208,15 @@ def test_host_diffraction_mixed_matches_set_diffract_get(periodic):
     assert not np.array_equal(ore, ore0)
 
 
-def test_host_diffraction_without_a_window():
+@pytest.mark.parametrize("mixed", [False, True])
+def test_host_diffraction_without_a_window(mixed):
     """No particles, so no inner window: the call transforms the outer field
     alone (window arguments may be NULL), as pf_set_field + pf_diffract +
     pf_get_field do."""
     w = configs.config2(np_=20000, nz2=65)
-    p = w.params
+    p = P.Params.from_buffer_copy(w.params)
+    if mixed:
+        p.precision = P.MIXED
     rng = np.random.default_rng(12)
     n = p.nx * p.ny * p.nz2
     ore0, oim0 = 1e-3 * rng.standard_normal(n), 1e-3 * rng.standard_normal(n)
