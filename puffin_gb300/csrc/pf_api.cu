@@ -1099,14 +1099,14 @@ int pf_rk4_step_host(pf_handle *h, double szl, double hstep, double *x, double *
 }
 
 // inner2Outer + diffractIM + outer2Inner with the driver's arrays in host
-// memory: the window field goes in first; the outer field goes in by ranges
-// of z2 planes on the copy stream, each range's window planes are copied
-// into it and the first transverse pass runs on it as it arrives; the last
-// transverse pass writes the outer field range by range and each range goes
-// out while the next is computed; the window field comes back from the
-// diffracted field last.  On a mixed handle the FP64 arrays are converted to
-// and from the complex-float field on the device (the outer field through
-// the staging buffer, the window through its own).
+// memory: the outer field and the window field go in by ranges of z2 planes
+// on the copy stream, each range's window planes are copied into it and the
+// first transverse passes run on it as it arrives; the last transverse
+// passes write the outer field range by range, the range's window planes
+// are taken from it, and the range goes out while the next is computed.  On
+// a mixed handle the FP64 arrays are converted to and from the complex-float
+// fields on the device (the outer field through the staging buffer, the
+// window through its own).
 int pf_diffract_host(pf_handle *h, double dz, double *ore, double *oim, double *wre,
                      double *wim) {
   if (!h || !ore || !oim) return PF_BAD_ARG;
@@ -1119,9 +1119,12 @@ int pf_diffract_host(pf_handle *h, double dz, double *ore, double *oim, double *
   const bool periodic = (p.mesh_type == PF_MESH_PERIODIC);
   const int64_t plane = (int64_t)p.nx * p.ny, no = h->nouter;
   const int64_t nzf = periodic ? p.nz2 - 1 : p.nz2;  // planes the transforms run over
-  const int nch = (int)std::max<int64_t>(1, std::min<int64_t>(8, nzf));
-  std::vector<int64_t> zcut((size_t)nch + 1);
-  for (int c = 0; c <= nch; ++c) zcut[c] = nzf * c / nch;
+  // eight ranges of z2 planes (ranges graded down to 1/20 of the planes at
+  // the ends measured no different)
+  const int64_t n8 = std::max<int64_t>(1, std::min<int64_t>(8, nzf));
+  std::vector<int64_t> zcut;
+  for (int64_t c = 0; c <= n8; ++c) zcut.push_back(nzf * c / n8);
+  const int nch = (int)zcut.size() - 1;
   if (!h->copy_stream) PF_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
   while ((int)h->copy_events.size() < 2 * nch + 1) {
     cudaEvent_t e;
@@ -1139,29 +1142,26 @@ int pf_diffract_host(pf_handle *h, double dz, double *ore, double *oim, double *
     h->wstage_cap = h->nwin;
   }
   double *dre = mixed ? h->staging : h->or_, *dim = mixed ? h->staging + no : h->oi_;
+  // the window's FP64 planes on the device (the window state itself, or its staging)
+  double *wdr = mixed ? h->wstage : h->wr, *wdi = mixed ? h->wstage + h->nwin : h->wi;
   float2 *oc = (float2 *)h->oc32, *w32 = (float2 *)h->w32;
   cudaEvent_t *ev_in = h->copy_events.data(), *ev_out = ev_in + nch, ev_end = ev_in[2 * nch];
   cudaStream_t cs = h->copy_stream, st = h->stream;
-  const size_t wb = (size_t)h->nwin * sizeof(double);
-  if (win) {
-    if (mixed) {
-      PF_CUDA(cudaMemcpyAsync(h->wstage, wre, wb, cudaMemcpyHostToDevice, st));
-      PF_CUDA(cudaMemcpyAsync(h->wstage + h->nwin, wim, wb, cudaMemcpyHostToDevice, st));
-      k_to_c32<<<grid_for(h->nwin, 256), 256, 0, st>>>(w32, h->wstage, h->wstage + h->nwin,
-                                                        h->nwin);
-      PF_LAUNCHED(h);
-    } else {
-      PF_CUDA(cudaMemcpyAsync(h->wr, wre, wb, cudaMemcpyHostToDevice, st));
-      PF_CUDA(cudaMemcpyAsync(h->wi, wim, wb, cudaMemcpyHostToDevice, st));
-    }
-  }
+  // window planes [z0, z0 + nz): wplane * nz values from wplane * z0 on
+  const int64_t wplane = (int64_t)h->nix * h->niy;
+  // in by ranges on the copy stream: the outer field's planes and the
+  // window's planes of each range
   for (int c = 0; c < nch; ++c) {
     const size_t off = (size_t)(zcut[c] * plane), n = (size_t)((zcut[c + 1] - zcut[c]) * plane);
     PF_CUDA(cudaMemcpyAsync(dre + off, ore + off, n * sizeof(double), cudaMemcpyHostToDevice, cs));
     PF_CUDA(cudaMemcpyAsync(dim + off, oim + off, n * sizeof(double), cudaMemcpyHostToDevice, cs));
+    if (win) {
+      const size_t wo = (size_t)(zcut[c] * wplane), wn = (size_t)((zcut[c + 1] - zcut[c]) * wplane);
+      PF_CUDA(cudaMemcpyAsync(wdr + wo, wre + wo, wn * sizeof(double), cudaMemcpyHostToDevice, cs));
+      PF_CUDA(cudaMemcpyAsync(wdi + wo, wim + wo, wn * sizeof(double), cudaMemcpyHostToDevice, cs));
+    }
     PF_CUDA(cudaEventRecord(ev_in[c], cs));
   }
-  const int64_t wplane = (int64_t)h->nix * h->niy;
   auto before = [&](int c) -> int {
     PF_CUDA(cudaStreamWaitEvent(st, ev_in[c], 0));
     const int64_t z0 = zcut[c], nz = zcut[c + 1] - zcut[c];
@@ -1169,6 +1169,11 @@ int pf_diffract_host(pf_handle *h, double dz, double *ore, double *oim, double *
       k_to_c32<<<grid_for(nz * plane, 256), 256, 0, st>>>(oc + z0 * plane, dre + z0 * plane,
                                                            dim + z0 * plane, nz * plane);
       PF_LAUNCHED(h);
+      if (win) {
+        k_to_c32<<<grid_for(nz * wplane, 256), 256, 0, st>>>(w32 + z0 * wplane, wdr + z0 * wplane,
+                                                              wdi + z0 * wplane, nz * wplane);
+        PF_LAUNCHED(h);
+      }
     }
     if (win) {  // inner2Outer of the range's planes (range 0 also writes the mirror plane)
       const int mirror = (periodic && c == 0) ? 1 : 0;
@@ -1185,6 +1190,20 @@ int pf_diffract_host(pf_handle *h, double dz, double *ore, double *oim, double *
   };
   auto after = [&](int c) -> int {
     const int64_t z0 = zcut[c], nz = zcut[c + 1] - zcut[c];
+    if (win) {  // outer2Inner of the range's planes
+      if (mixed) {
+        k_window_copy_c32<<<grid_for(wplane * nz, 256), 256, 0, st>>>(
+            w32 + z0 * wplane, oc + z0 * plane, h->nix, h->niy, nz, p.nx, p.ny, p.nz2, 0, 0);
+        PF_LAUNCHED(h);
+        k_from_c32<<<grid_for(nz * wplane, 256), 256, 0, st>>>(w32 + z0 * wplane, wdr + z0 * wplane,
+                                                                wdi + z0 * wplane, nz * wplane);
+      } else {
+        k_window_copy<<<grid_for(wplane * nz, 256), 256, 0, st>>>(
+            h->wr + z0 * wplane, h->wi + z0 * wplane, h->or_ + z0 * plane, h->oi_ + z0 * plane,
+            h->nix, h->niy, nz, p.nx, p.ny, p.nz2, 0, 0);
+      }
+      PF_LAUNCHED(h);
+    }
     if (mixed) {
       k_from_c32<<<grid_for(nz * plane, 256), 256, 0, st>>>(oc + z0 * plane, dre + z0 * plane,
                                                              dim + z0 * plane, nz * plane);
@@ -1207,6 +1226,11 @@ int pf_diffract_host(pf_handle *h, double dz, double *ore, double *oim, double *
       PF_CUDA(cudaMemcpyAsync(oim + mo, dim + mo, (size_t)plane * sizeof(double),
                               cudaMemcpyDeviceToHost, cs));
     }
+    if (win) {
+      const size_t wo = (size_t)(z0 * wplane), wn = (size_t)(nz * wplane);
+      PF_CUDA(cudaMemcpyAsync(wre + wo, wdr + wo, wn * sizeof(double), cudaMemcpyDeviceToHost, cs));
+      PF_CUDA(cudaMemcpyAsync(wim + wo, wdi + wo, wn * sizeof(double), cudaMemcpyDeviceToHost, cs));
+    }
     return PF_OK;
   };
   int rc = pf_diffract_outer_ranges(h, dz, zcut, before, after);
@@ -1215,26 +1239,7 @@ int pf_diffract_host(pf_handle *h, double dz, double *ore, double *oim, double *
     cudaStreamSynchronize(st);
     return rc;
   }
-  if (win) {  // outer2Inner, then the window goes out
-    if (mixed) {
-      k_window_copy_c32<<<grid_for(h->nwin, 256), 256, 0, st>>>(w32, oc, h->nix, h->niy, h->npl,
-                                                               p.nx, p.ny, p.nz2, 0, 0);
-      PF_LAUNCHED(h);
-      k_from_c32<<<grid_for(h->nwin, 256), 256, 0, st>>>(w32, h->wstage, h->wstage + h->nwin,
-                                                          h->nwin);
-      PF_LAUNCHED(h);
-      PF_CUDA(cudaMemcpyAsync(wre, h->wstage, wb, cudaMemcpyDeviceToHost, st));
-      PF_CUDA(cudaMemcpyAsync(wim, h->wstage + h->nwin, wb, cudaMemcpyDeviceToHost, st));
-    } else {
-      k_window_copy<<<grid_for(h->nwin, 256), 256, 0, st>>>(h->wr, h->wi, h->or_, h->oi_, h->nix,
-                                                           h->niy, h->npl, p.nx, p.ny, p.nz2, 0,
-                                                           0);
-      PF_LAUNCHED(h);
-      PF_CUDA(cudaMemcpyAsync(wre, h->wr, wb, cudaMemcpyDeviceToHost, st));
-      PF_CUDA(cudaMemcpyAsync(wim, h->wi, wb, cudaMemcpyDeviceToHost, st));
-    }
-    h->window_valid = true;
-  }
+  if (win) h->window_valid = true;
   PF_CUDA(cudaEventRecord(ev_end, st));
   PF_CUDA(cudaStreamWaitEvent(cs, ev_end, 0));
   PF_CUDA(cudaStreamSynchronize(cs));
