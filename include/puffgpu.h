@@ -210,9 +210,9 @@ int pf_rk4_step_host(pf_handle *h, double szl, double hstep, double *x, double *
  * when the handle has a window, the inner-window field (pf_window_nodes()
  * values each) are read and written in place, as pf_set_field +
  * pf_set_window_field + pf_diffract + pf_get_field + pf_get_window_field
- * would, with the outer field's copies overlapped with the transforms
- * (copied in and out by ranges of z2 planes while the first and the last
- * pass run on the others). */
+ * would, with the copies overlapped with the transforms (the outer field
+ * and the window copied in and out by ranges of z2 planes while the first
+ * and the last passes run on the others). */
 int pf_diffract_host(pf_handle *h, double dz, double *ore, double *oim, double *wre,
                      double *wim);
 
