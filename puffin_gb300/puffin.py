@@ -216,8 +216,10 @@ class Puffin:
 
     def diffractIM_host(self, dz: float, outer: tuple, window: tuple):
         """inner2Outer + diffractIM + outer2Inner on the driver's host arrays
-        (pf_diffract_host): the outer field (re, im) and the window field
-        (re, im), C-contiguous float64, updated in place."""
+        (pf_diffract_host; FP64 and mixed handles): the outer field (re, im)
+        and the window field (re, im), C-contiguous float64, updated in
+        place, their copies overlapped with the transforms by ranges of z2
+        planes."""
         arrs = list(outer) + list(window)
         for a in arrs:
             if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags.c_contiguous):
