@@ -120,6 +120,7 @@ struct StageArgs {
   int field_evolve, electrons_evolve, coupling;
   int fix_e;              // fixed-point scale exponent of the deposit
   int fix_maxexp;         // overflow guard: |contribution * 2^E| < 2^fix_maxexp
+  int tile_ppb;           // dense mode: macroparticles per block (set at launch)
   BFieldCoef bf;
   unsigned int *status;
 };
