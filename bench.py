@@ -67,8 +67,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=8)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--np", type=int, default=2 ** 23, help="macroparticles")
-    ap.add_argument("--e2e-steps", type=int, default=24,
-                    help="end-to-end steps (3 diffraction calls at the default cadence)")
+    ap.add_argument("--e2e-steps", type=int, default=48,
+                    help="end-to-end steps (6 diffraction calls at the default cadence)")
     ap.add_argument("--nz2", type=int, default=4096,
                     help="z2 nodes of the mesh (smaller only for profiling captures)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
