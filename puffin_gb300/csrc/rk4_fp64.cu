@@ -815,7 +815,19 @@ static int64_t dense_ppb(int64_t np, int64_t slots) {
 // k_stage<stage> over the a.np macroparticles a points to (the handle's
 // beam, or a range of it), in the deposit mode the handle's beam takes
 static int launch_stage(pf_handle *h, int stage, StageArgs &a) {
-  const int threads = 256;
+  // direct mode: blocks of 256 threads, halved down to 64 while the grid
+  // has fewer than eight blocks per SM, so that a small beam's warps spread
+  // over all SMs evenly (2^16 macroparticles: 256 blocks of 256 left 48 of
+  // 152 SMs one block and the others two)
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    nsm = std::max(1, nsm);
+  }
+  int threads = 256;
+  while (threads > 64 && (a.np + threads - 1) / threads < (int64_t)8 * nsm) threads /= 2;
   const int64_t blocks = (a.np + threads - 1) / threads;
   if (blocks == 0) return PF_OK;
   const bool oned = h->p.one_d != 0;
