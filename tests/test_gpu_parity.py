@@ -374,8 +374,10 @@ def test_deposit_is_bit_reproducible():
 
 def test_dense_beam_tiled_deposit():
     """2^18 macroparticles on the config-1 mesh (about ten per window cell)
-    select the shared-memory deposit tile: one RK4 step against the oracle
-    (rtol 1e-12) and bit-identical repeats."""
+    select the shared-memory deposit tile, in blocks sized to fill a wave
+    of resident blocks (342 blocks of 768 macroparticles, the last one
+    holding 256): one RK4 step against the oracle (rtol 1e-12) and
+    bit-identical repeats."""
     w = configs.config1(np_=2 ** 18, seed=9, nsteps=2)
     field = random_field(w.params, 5)
     outs = []
