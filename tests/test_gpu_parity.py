@@ -372,13 +372,15 @@ def test_deposit_is_bit_reproducible():
     np.testing.assert_array_equal(outs[0][1][1], outs[1][1][1])
 
 
-def test_dense_beam_tiled_deposit():
-    """2^18 macroparticles on the config-1 mesh (about ten per window cell)
-    select the shared-memory deposit tile, in blocks sized to fill a wave
-    of resident blocks (342 blocks of 768 macroparticles, the last one
-    holding 256): one RK4 step against the oracle (rtol 1e-12) and
-    bit-identical repeats."""
-    w = configs.config1(np_=2 ** 18, seed=9, nsteps=2)
+@pytest.mark.parametrize("npart", [2 ** 18, 3_500_000])
+def test_dense_beam_tiled_deposit(npart):
+    """Dense beams on the config-1 mesh select the shared-memory deposit
+    tile: 2^18 macroparticles (about ten per window cell) in blocks sized to
+    fill a wave of resident blocks (342 blocks of 768 macroparticles, the
+    last one holding 256), 3.5 M in the full blocks of 8192 (428 blocks,
+    94 % of a wave; the last one holding 2016).  One RK4 step against the
+    oracle (rtol 1e-12) and bit-identical repeats."""
+    w = configs.config1(np_=npart, seed=9, nsteps=2)
     field = random_field(w.params, 5)
     outs = []
     for _ in range(2):
@@ -389,7 +391,16 @@ def test_dense_beam_tiled_deposit():
         np.testing.assert_array_equal(outs[0][0][k], outs[1][0][k])
     np.testing.assert_array_equal(outs[0][1][0], outs[1][1][0])
     b, of, _ = run_oracle_steps(w.params, w.beam, field, w.h, 1, nix, niy)
-    assert_beam_close(outs[0][0], b, rtol=1e-12, atol=1e-15)
+    if npart < 10 ** 6:
+        assert_beam_close(outs[0][0], b, rtol=1e-12, atol=1e-15)
+    else:
+        # p2 = (1/sqrt(1 - u) - 1)/eta cancels seven digits (u ~ 4e-6 here),
+        # so an ulp of difference upstream flips its rounding for a few
+        # macroparticles in millions: 2^-52/u ~ 6e-11 of p2, h = 0.002 times
+        # that in z2, 1.1e-13 absolute (z2 near zero makes it large relative)
+        assert_beam_close(outs[0][0], b, rtol=1e-12, atol=1e-15,
+                          keys=("x", "y", "px", "py", "gam"))
+        np.testing.assert_allclose(outs[0][0]["z2"], b.z2, rtol=1e-12, atol=2e-13)
     field_close(outs[0][1], of, 1e-12)
 
 
