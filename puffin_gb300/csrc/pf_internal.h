@@ -309,6 +309,8 @@ size_t pf_stage_tile_smem(const pf_handle *h);
 // blocks of a kernel resident on the current device at once (grid < 0 of the
 // batched launchers: a persistent grid)
 int pf_resident_blocks(const void *kernel, int threads, size_t smem);
+// SM count of the current device (cached per device ordinal)
+int pf_sm_count();
 constexpr int PF_FT_PPB = 8192;  // largest dense-mode tile of the FP64 stage
 // batched mixed-precision launches (rk4_mixed.cu); the argument records are
 // opaque to the callers

@@ -18,6 +18,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 
 #include <climits>
@@ -819,13 +820,7 @@ static int launch_stage(pf_handle *h, int stage, StageArgs &a) {
   // has fewer than eight blocks per SM, so that a small beam's warps spread
   // over all SMs evenly (2^16 macroparticles: 256 blocks of 256 left 48 of
   // 152 SMs one block and the others two)
-  static int nsm = 0;
-  if (!nsm) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    nsm = std::max(1, nsm);
-  }
+  const int nsm = pf_sm_count();
   int threads = 256;
   while (threads > 64 && (a.np + threads - 1) / threads < (int64_t)8 * nsm) threads /= 2;
   const int64_t blocks = (a.np + threads - 1) / threads;
@@ -983,6 +978,20 @@ void pf_fill_node_args(pf_handle *h, NodeArgs &n, double hstep) {
   n.h6 = hstep / 6.0;
   n.fix_e = h->fix_e;
   n.status = h->d_status;
+}
+
+int pf_sm_count() {
+  static std::atomic<int> cache[64];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  int n = cache[dev].load(std::memory_order_relaxed);
+  if (n == 0) {
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    n = std::max(1, n);
+    cache[dev].store(n, std::memory_order_relaxed);
+  }
+  return n;
 }
 
 int pf_resident_blocks(const void *kernel, int threads, size_t smem) {

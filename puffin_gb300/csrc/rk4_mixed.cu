@@ -771,18 +771,11 @@ cudaError_t pf_mixed_nodes_batch(cudaStream_t st, int stage, const void *args,
 static int mixed_ppt(const pf_handle *h) {
   const int64_t per_plane = h->np / std::max<int64_t>(1, (int64_t)h->npl);
   const int64_t want = (per_plane >= (int64_t)16 * MX_THREADS) ? MX_PPT : 6;
-  int64_t ppt = std::max<int64_t>(1, std::min<int64_t>(want, h->np / ((int64_t)152 * 2 * MX_THREADS)));
+  int64_t ppt = std::max<int64_t>(1, std::min<int64_t>(want, h->np / ((int64_t)pf_sm_count() * 2 * MX_THREADS)));
   // fewer macroparticles per thread when the grid's waves of resident blocks
   // (three per SM) would be less than 85 % full: 2^22 macroparticles at 8
   // per thread made 2.25 waves, at 6 they make 3.0
-  static int nsm = 0;
-  if (!nsm) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    nsm = std::max(1, nsm);
-  }
-  const int64_t slots = (int64_t)3 * nsm, per = (int64_t)MX_THREADS;
+  const int64_t slots = (int64_t)3 * pf_sm_count(), per = (int64_t)MX_THREADS;
   const int64_t nb = (h->np + per * ppt - 1) / (per * ppt);
   const int64_t waves = std::max<int64_t>(1, (nb + slots - 1) / slots);
   if (nb < (int64_t)(0.85 * (double)(waves * slots)))
